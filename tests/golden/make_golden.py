@@ -1,0 +1,199 @@
+"""Generate the golden fixtures of the femmd2D timestep from the reference itself.
+
+Each case is a seeded scene (femmd_old_gb300.scene) replayed by the reference's
+own C++ classes, compiled from the reference sources (oracle/Makefile target
+``ref`` -> oracle/_ref/ref_harness).  The harness dumps setup arrays, cell and
+neighbour sets, forces, energies and trajectory snapshots; this script stores
+the scene command stream and every dump in tests/golden/<case>.npz.
+
+Run here, where the reference checkout exists:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from femmd_old_gb300 import scene as S  # noqa: E402
+import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+MESHES = os.environ.get("FEMMD_REF_MESHES", "/root/reference/femmd2D/meshes")
+
+
+def probes(sc: S.Scene, runs=(50, 200)) -> S.Scene:
+    sc.add("dump_setup").add("build_nn").add("dump_nn").add("calc_forces").add("dump_state")
+    for n in runs:
+        sc.add("run", n).add("dump_state")
+    sc.add("dump_nn")
+    return sc
+
+
+def case_lj_xy():
+    return probes(S.lj_fluid(n_side=16, seed_pos=11, seed_vel=12))
+
+
+def case_lj_multitype():
+    """Two types, per-particle sigma, asymmetric epsilon/cutoff tables."""
+    n_side, rho = 14, 0.7
+    n = n_side * n_side
+    L = math.sqrt(n / rho)
+    a = L / n_side
+    rng = np.random.Generator(np.random.PCG64(21))
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy"), -1).reshape(-1, 2)
+    pos = (ij + 0.5) * a + rng.uniform(-0.08, 0.08, size=(n, 2))
+    typ = (rng.uniform(size=n) < 0.4).astype(np.int32)
+    sig = np.where(typ == 1, 0.9, 1.05)
+    m = np.where(typ == 1, 0.8, 1.2)
+    vel = rng.normal(0, 0.8, size=(n, 2))
+    sc = S.Scene(meta=dict(workload="lj_multitype"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.004).add("set_numTypes", 2)
+    sc.add("set_pair_potential", [1.0, 0.7, 0.7, 1.3], [2.5, 1.8, 1.8, S.WCA_RC],
+           [S.lj_shift(2.5), S.lj_shift(1.8), S.lj_shift(1.8), 1.0])
+    sc.add("set_skin", 0.35)
+    sc.add("add_particles", pos[:, 0], pos[:, 1], vel[:, 0], vel[:, 1], m, sig, typ)
+    sc.add("init_neighbor_list")
+    return probes(sc)
+
+
+def _slab(pbc, seed):
+    n_side = 12
+    L = 16.0
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy"), -1).reshape(-1, 2)
+    pos = 2.0 + (ij + 0.5) * (12.0 / n_side) + rng.uniform(-0.05, 0.05, size=(n_side * n_side, 2))
+    vel = rng.normal(0, 0.3, size=pos.shape)
+    sc = S.Scene(meta=dict(workload=f"slab_pbc{pbc}"))
+    sc.add("init", L, L).add("PBC", pbc).add("set_dt", 0.003).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [2.5], [S.lj_shift(2.5)])
+    sc.add("set_skin", 0.3)
+    n = pos.shape[0]
+    sc.add("add_particles", pos[:, 0], pos[:, 1], vel[:, 0], vel[:, 1], np.ones(n), np.ones(n),
+           np.zeros(n, np.int32))
+    sc.add("init_neighbor_list")
+    return probes(sc, runs=(20, 40))
+
+
+def case_lj_xpbc():
+    return _slab(1, 31)
+
+
+def case_lj_nopbc():
+    return _slab(0, 32)
+
+
+def case_tiny_box():
+    """Box of two cells per axis: the 3x3 stencil visits cells twice and the
+    reference's list holds duplicates (applyCellBC always wraps)."""
+    n_side = 6
+    L = 6.0
+    rng = np.random.Generator(np.random.PCG64(41))
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy"), -1).reshape(-1, 2)
+    pos = (ij + 0.5) * (L / n_side) + rng.uniform(-0.05, 0.05, size=(36, 2))
+    vel = rng.normal(0, 0.5, size=pos.shape)
+    sc = S.Scene(meta=dict(workload="tiny_box"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [2.5], [S.lj_shift(2.5)])
+    sc.add("set_skin", 0.3)
+    sc.add("add_particles", pos[:, 0], pos[:, 1], vel[:, 0], vel[:, 1], np.ones(36), np.ones(36),
+           np.zeros(36, np.int32))
+    sc.add("init_neighbor_list")
+    return probes(sc, runs=(30,))
+
+
+def case_susp_all():
+    return probes(S.suspension(n_side=3, rings=3, bonds="all", T=0.5, center_jitter=0.3), runs=(100, 300))
+
+
+def case_susp_boundary():
+    return probes(S.suspension(n_side=3, rings=3, bonds="boundary", T=0.5, center_jitter=0.3, seeds=(13, 14, 15)),
+                  runs=(100, 300))
+
+
+def case_susp_refdisk():
+    v, t = S.load_mesh(os.path.join(MESHES, "diskVertices.txt"), os.path.join(MESHES, "diskTriangles.txt"))
+    sc = S.suspension(n_side=3, radius=4.0, mesh=(v * 8.0, t), bonds="all", T=0.3, center_jitter=0.2, phi=0.4)
+    return probes(sc, runs=(100, 200))
+
+
+def case_susp_crossing():
+    """Disks drifting across the periodic boundary: FEA unwrap and
+    minimum-image bond paths.  Rest lengths come from unwrapped positions."""
+    verts, tris = S.hex_disk_mesh(3.0, 3, jitter=0.02, seed=51)
+    nv = verts.shape[0]
+    L = 20.0
+    sc = S.Scene(meta=dict(workload="susp_crossing"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [S.WCA_RC], [1.0]).add("set_skin", 0.3)
+    sc.add("set_kBond", 80.0).add("set_youngs_modulus", 40.0).add("set_poisson_ratio", 0.3)
+    sc.add("set_elastomer_bonds", 1)
+    centers = [(16.8, 10.0), (10.0, 16.8), (4.0, 4.0)]
+    for c in centers:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 0, 0, 1.0, float(nv), True)
+    sc.add("init_neighbor_list")
+    vel = np.zeros((3 * nv, 2), np.float32)
+    vel[:nv, 0] = 6.0
+    vel[nv:2 * nv, 1] = 6.0
+    vel[2 * nv:, :] = -6.0
+    sc.add("set_velocities_array", vel)
+    return probes(sc, runs=(200, 300))
+
+
+def case_susp_mixed():
+    """Elastomers first, then free LJ particles of a second type."""
+    verts, tris = S.hex_disk_mesh(3.0, 3, jitter=0.02, seed=61)
+    nv = verts.shape[0]
+    L = 24.0
+    rng = np.random.Generator(np.random.PCG64(62))
+    sc = S.Scene(meta=dict(workload="susp_mixed"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.003).add("set_numTypes", 2)
+    sc.add("set_pair_potential", [1.0, 1.0, 1.0, 1.0], [2.5, S.WCA_RC, S.WCA_RC, S.WCA_RC],
+           [S.lj_shift(2.5), 1.0, 1.0, 1.0])
+    sc.add("set_skin", 0.3).add("set_kBond", 100.0).add("set_youngs_modulus", 50.0)
+    for c in [(6.0, 6.0), (18.0, 6.0), (6.0, 18.0), (18.0, 18.0)]:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 1, 0, 1.0, float(nv), True)
+    centers = np.array([(6.0, 6.0), (18.0, 6.0), (6.0, 18.0), (18.0, 18.0)])
+    g = (np.stack(np.meshgrid(np.arange(20), np.arange(20), indexing="xy"), -1).reshape(-1, 2) + 0.5) * (L / 20)
+    d = g[:, None, :] - centers[None]
+    d -= L * np.round(d / L)
+    keep = ((d ** 2).sum(-1) > 4.2 ** 2).all(1)
+    p = g[keep] + rng.uniform(-0.05, 0.05, size=(int(keep.sum()), 2))
+    n = p.shape[0]
+    v = rng.normal(0, 1.0, size=(n, 2))
+    sc.add("add_particles", p[:, 0], p[:, 1], v[:, 0], v[:, 1], np.ones(n), np.ones(n), np.zeros(n, np.int32))
+    sc.add("init_neighbor_list")
+    return probes(sc, runs=(100, 200))
+
+
+CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
+
+
+def save(name: str, sc: S.Scene, dumps):
+    blob = {"scene": np.frombuffer(sc.to_bytes(), np.uint8)}
+    for k, (tag, d) in enumerate(dumps):
+        for key, val in d.items():
+            blob[f"d{k:02d}_{tag}_{key}"] = np.asarray(val)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **blob)
+
+
+def main(names=None):
+    if O.build_reference() is None:
+        raise SystemExit("reference checkout not found; golden fixtures are generated where it exists")
+    for name, fn in CASES.items():
+        if names and name not in names:
+            continue
+        sc = fn()
+        dumps = O.run_reference(sc)
+        save(name, sc, dumps)
+        print(f"{name}: {len(dumps)} dumps, {os.path.getsize(os.path.join(OUT, name + '.npz'))} bytes")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
