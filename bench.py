@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 femmd2D timestep (atom-steps/s).
+
+A bench "step" is one System.run(S) call (S leapfrog steps, default 100) on
+the workload's synthetic, seeded system -- the reference's run loop
+(femmd2D/src/integrator.cpp:31-57): forced neighbour rebuild, initial force
+pass, S steps with half-skin rebuilds.  Default workload: the large mixed
+system (4096 hex-ring elastomer disks = 520,192 vertices + 1,000,000 LJ
+solvent, 1,520,192 atoms), the largest single-GPU configuration, on which the
+HBM-roofline target is stated.  Other workloads: suspension (256 disks,
+32,512 atoms), lj_fluid (N = 4096).
+
+  value   atom-steps/s with the state resident in HBM: CUDA events on the
+          library's stream around the timed run() calls.
+  e2e     the same through the C ABI with host buffers: per step the pinned
+          host positions+velocities are copied in (femmd_set_state), run(S),
+          and positions+velocities copied out (femmd_get_state); wall clock.
+  roofline  the step kernel (k_step, the dominant kernel): algorithmic bytes
+          per launch / its mean CUDA-event duration from a direct-launch pass,
+          against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's CPU restatement (C, OpenMP over the pair loop)
+          timed on this host's cores on a bounded sample of the same system.
+
+Multi-GPU (torchrun, one rank per GPU): independent replicas, no collective
+on the data path; value = all ranks' atom-steps / max rank time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload large_mixed|suspension|lj_fluid] [--md-steps S]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from femmd_old_gb300 import scene as S  # noqa: E402
+
+WORKLOADS = {
+    "large_mixed": ("large mixed: 4096 hex-ring disks (127 vertices, 216 triangles, boundary bonds k=100, E=50, "
+                    "nu=0.3) + 1,000,000 LJ solvent (rho=0.8, rc=2.5; vertex pairs WCA), T=1, dt=0.005, skin 0.3",
+                    lambda: S.large_mixed()),
+    "suspension": ("elastomer suspension: 256 hex-ring disks (127 vertices), E=50, nu=0.3, boundary bonds k=100, "
+                   "WCA, phi=0.5, T=0.1, dt=0.002, skin 0.3", lambda: S.suspension()),
+    "lj_fluid": ("plain LJ fluid: N=4096, rho=0.8, rc=2.5, skin 0.3, dt=0.005", lambda: S.lj_fluid()),
+}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS))
+    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------- distributed
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{self.local}")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.p = None
+        self.out = os.path.join("/tmp", f"femmd_clocks_{os.getpid()}.csv")
+        try:
+            self.f = open(self.out, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.out):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------- CPU side
+
+def cpu_baseline(sc, natoms, budget_s, threads):
+    """The oracle's C restatement on this host: a bounded sample of run()."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    o = O.Oracle(image_mode=0, log_mode=0, threads=threads)
+    sc.replay(o)
+    t0 = time.perf_counter()
+    o.run(1)
+    t1 = time.perf_counter() - t0
+    m = max(1, min(1000, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.run(m)
+    dt = time.perf_counter() - t0
+    return {"value": natoms * m / dt, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{m} leapfrog steps (one run({m}) call incl. its initial rebuild and force pass) of the "
+                      f"same {natoms}-atom system, {dt:.2f} s wall, oracle/femmd_oracle.c with OpenMP pair loop"}
+
+
+def reference_arm(args, dist):
+    """--impl reference: the reference's CPU path as restated by the oracle
+    (the reference's own binary is x86-only here), all host threads."""
+    if dist.rank != 0:
+        return None
+    desc, make = WORKLOADS[args.workload]
+    sc = make()
+    natoms = int(sc.meta["N"])
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    o = O.Oracle(image_mode=0, log_mode=0, threads=threads)
+    sc.replay(o)
+    t0 = time.perf_counter()
+    o.run(1)
+    per = time.perf_counter() - t0
+    # each bench step: a run(m) sample sized so the whole K+W run stays ~2 minutes
+    m = max(1, min(args.md_steps, int(120.0 / max(per, 1e-6) / max(args.steps + args.warmup, 1))))
+    for _ in range(args.warmup):
+        o.run(m)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run(m)
+    dt = time.perf_counter() - t0
+    value = natoms * m * args.steps / dt
+    return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "atoms": natoms, "md_steps_per_step": m,
+                       "parallelism": "replicas"},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"run({m}) per step of the {natoms}-atom system; the reference's own binary "
+                                       "(oracle/_ref) is built for x86 and cannot run on this host"},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def load_traffic(workload):
+    """DRAM bytes per k_step launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"k_step_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def step_kernel_bytes(s, sc):
+    """Algorithmic HBM bytes of one k_step launch in the steady state (MID
+    mode): per particle pos in 8 + vel 8 + pos out 8 + vel out 8 + mass 4 +
+    list count 4 (+ type 4 with several types), 4 per list entry, bonded
+    particles: incidence starts 8 + 8 per bond incidence + 12 per triangle
+    incidence (entry + nodal force).  Neighbour/partner position gathers hit
+    in cache (a particle's position is loaded from DRAM once per launch)."""
+    n = s.N
+    st = s.nn_stats()
+    c = s.counts()
+    per = 40 + (4 if sc.meta.get("types", 1) > 1 else 0)
+    nbonded = s._vertex_count()
+    total = per * n + 4 * st["mean_neighbors"] * n + 8 * nbonded + 8 * 2 * c["bonds"] + 12 * 3 * c["triangles"]
+    return total, st
+
+
+def ours(args, dist):
+    import femmd_old_gb300 as F
+    desc, make = WORKLOADS[args.workload]
+    sc = make()
+    sc.meta["types"] = max([a[0] for nm, a in sc.calls if nm == "set_numTypes"] or [1])
+    dev = dist.local
+    s = F.System(dev)
+    sc.replay(s)
+    n = s.N
+    md = args.md_steps
+    s.run(0)
+    for _ in range(args.warmup):
+        s.run(md)
+    flush = None
+    try:
+        import torch
+        torch.cuda.set_device(dev)
+        working = n * (8 * 5 + 4 * 24 + 16 + 8)
+        if working < 2 * L2_BYTES:
+            flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")
+    except Exception:
+        torch = None
+
+    # ---- timed region: state resident in HBM
+    dist.barrier()
+    s.sync()
+    clk = ClockSampler(dev)
+    t_ms = 0.0
+    rebuilds = 0
+    for k in range(args.steps):
+        if flush is not None:
+            flush.zero_()
+            torch.cuda.synchronize()
+        s.event_record(0)
+        s.run(md)
+        s.event_record(1)
+        t_ms += s.event_elapsed_ms(0, 1)
+        rebuilds += s.total_updates() - 1
+    s.sync()
+    clocks = clk.stop()
+    dist.barrier()
+    t_max = dist.max(t_ms)
+    units = n * md * args.steps * dist.world
+    value = units / (t_max / 1e3)
+    nst = s.nn_stats()
+
+    # kernel launches inside the timed region
+    has_tri = 1 if s.counts()["triangles"] else 0
+    launches = args.steps * (1 + 6 + (md + 1) * (1 + has_tri)) + 6 * rebuilds
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if torch is not None:
+        pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True)
+        vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True)
+        s.get_state_ptr(pos.data_ptr(), vel.data_ptr())
+        dist.barrier()
+        s.sync()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            s.set_state_ptr(pos.data_ptr(), vel.data_ptr())
+            s.run(md)
+            s.get_state_ptr(pos.data_ptr(), vel.data_ptr())
+        s.sync()
+        dt = time.perf_counter() - t0
+        dist.barrier()
+        dt = dist.max(dt)
+        e2e = {"value": units / dt, "unit": "atom-steps/s", "h2d_bytes_per_step": 16 * n,
+               "d2h_bytes_per_step": 16 * n}
+
+    # ---- roofline of the step kernel: direct launches with events
+    s.set_profiling(True)
+    for k in range(max(1, min(3, args.steps))):
+        s.run(md)
+    prof = s.profile()
+    s.set_profiling(False)
+    kbytes, st = step_kernel_bytes(s, sc)
+    kms = prof["force_ms"] / max(prof["force_launches"], 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = kbytes / (kms / 1e3) / 1e9
+    traffic = load_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "k_step (fused LJ+bond+triangle gather, leapfrog, FP64 reductions)",
+                "algorithmic_bytes_per_launch": kbytes, "mean_launch_ms": kms,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(make(), n, args.cpu_seconds, os.cpu_count() or 1)
+
+    rb_per_run = rebuilds / max(args.steps, 1)
+    kbar = md / max(rb_per_run, 1e-9) if rebuilds else None
+    line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "atoms": n, "md_steps_per_step": md,
+                       "neighbors_mean": nst["mean_neighbors"], "steps_between_rebuilds": kbar,
+                       "parallelism": "replicas" if dist.world > 1 else "single",
+                       "l2": "L2 flushed between timed steps" if flush is not None else
+                             "inputs larger than L2 (state + lists > 129 MB)",
+                       "image_mode": "exact", "fea_law": "neo-Hookean"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+    return line
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        line = reference_arm(args, dist) if args.impl == "reference" else ours(args, dist)
+        if dist.rank == 0 and line is not None:
+            print(json.dumps(line), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

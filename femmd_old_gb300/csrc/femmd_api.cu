@@ -1,0 +1,1521 @@
+// femmd_api.cu -- host context and C ABI (include/femmd.h) of the GB300
+// femmd2D timestep.
+//
+// Setup calls mirror the reference's System.* surface
+// (femmd2D/src/interface.cpp:229-600) and store their inputs in host arrays,
+// computing derived data with the reference's float operations
+// (Particles::addElastomer particles.cpp:295-385, Bonds::createBond
+// bonds.cpp:14-29, NeighborList::init nn.cpp:200-227).  Compute happens only on
+// the GPU: femmd_run enqueues the kernel sequence of Integrator::run
+// (integrator.cpp:31-57) on the context stream --
+//     run start (forced rebuild) -> first step -> (n-1) x [step -> IF rebuild] -> last step
+// where each "[step -> IF rebuild]" unit is a node pair of a cached CUDA graph
+// and the IF condition is set on the device by the step kernel's last block
+// (the reference's dispHi > skin/2 test), so a run has no host round trip
+// until it ends.  A neighbour-list capacity overflow found at the end rolls
+// the run back to its start checkpoint, grows the list and repeats it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "femmd.h"
+#include "femmd_internal.h"
+#include "launch.h"
+
+using namespace femmd;
+
+namespace {
+
+struct Cluster {
+    int offset, nv, nt, tetOffset;
+    float mass, rho;
+};
+
+template <typename T> struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (cnt == 0) cnt = 1;
+        cudaError_t e = cudaMalloc(&p, cnt * sizeof(T));
+        if (e == cudaSuccess) n = cnt;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct GraphSet {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    void release() {
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+        x = nullptr;
+        g = nullptr;
+    }
+};
+
+constexpr int kGraphUnits = 32;  // [step -> IF rebuild] units per cached graph
+constexpr unsigned kPos = 1, kVel = 2, kAcc = 4, kForce = 8, kEnergy = 16, kAll = 31;
+
+}  // namespace
+
+struct femmd_ctx {
+    int device = 0;
+    std::string err;
+    // MDSystem / Interactions state (host)
+    bool inited = false;
+    float Lx = 0, Ly = 0, dt = 0.005f, density = 0;
+    int pbc = FEMMD_XYPBC, dev_flag = 1, numTypes = 1, steps = 0;
+    std::vector<float> eps, rc, us;
+    float rCutMax = 0;
+    bool bondForces = false, feaForces = false;
+    float kBond = 0, E = 0, nu = 0.3f, lambda = 0, mu = 0, C1 = 0, C2 = 0, C3 = 0, gravity = 0, kArea = 0;
+    int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
+    int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
+    float skin = 0.4f;
+    // Particles
+    std::vector<float2> pos, vel, acc, force, refPos;
+    std::vector<float> mass, sigma, energy;
+    std::vector<int> type, excl, cluster;
+    int nexcl = 0;
+    std::vector<Cluster> clusters;
+    // Bonds and triangles
+    std::vector<int> bond;  // 2 per bond
+    std::vector<float> r0;
+    std::vector<int> tri;   // 3 per triangle
+    std::vector<float> xm, refVol;
+    // NeighborList
+    bool nnInit = false;
+    float nnRadius = 0, nnRadiusSq = 0;
+    int ncx = 0, ncy = 0, ncells = 0;
+    // device
+    cudaStream_t stream = nullptr;
+    bool topoDirty = true, stateDirty = true, forcesValid = false, listBuilt = false;
+    unsigned staleMask = 0;  // host copies older than the device: bits of kPos..kEnergy
+    int cur = 0;
+    int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1;
+    DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF;
+    DBuf<float> dmass, dsigma, denergy, triE, partialsMax;
+    DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, sortedIds, nbr, nbrCount, bStart, tStart,
+        tEnt;
+    DBuf<int2> bEnt;
+    DBuf<int4> triIdx;
+    DBuf<float4> triGeo, cellSorted;
+    DBuf<PairEntry> pair;
+    DBuf<double> partials, triPartials, obs;
+    DBuf<DevScalars> sc;
+    DevScalars *hsc = nullptr;  // pinned mirror
+    int obsCap = 0, obsRows = 0;
+    GraphSet graphs[2][2];      // [parity][0: kGraphUnits units, 1: one unit]
+    // profiling
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> forceEvents;
+    std::vector<cudaEvent_t> eventPool;
+    double profForceMs = 0, profRebuildMs = 0;
+    long long profForceLaunches = 0, profRebuilds = 0, profKernels = 0;
+    long long totalBuilds = 0;
+    cudaEvent_t userEvents[64] = {};
+    double lastMeanNbr = 0;
+    int lastMaxNbr = 0;
+};
+
+// ------------------------------------------------------------------ errors
+
+static femmd_status fail(femmd_ctx *c, femmd_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return st;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return fail(ctx, FEMMD_CUDA_ERROR, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                     \
+    } while (0)
+
+#define NEED(ctx)                                                   \
+    do {                                                            \
+        if (!(ctx)) return FEMMD_INVALID_ARG;                       \
+        (ctx)->err.clear();                                         \
+    } while (0)
+
+// ------------------------------------------------------------- host physics
+
+// Interactions::setElasticConstants (interactions.cpp:43-50)
+static void set_elastic_constants(femmd_ctx *c) {
+    c->lambda = c->E * c->nu / ((1.0f - 2.0f * c->nu) * (1.0f + c->nu));
+    c->mu = c->E / (2.0f * (1.0f + c->nu));
+    c->C1 = c->lambda + 2.0f * c->mu;
+    c->C2 = c->lambda;
+    c->C3 = c->mu;
+}
+
+// pbcCalc (def.h:112)
+static float wrap_coord(float r, float L) { return r - std::floor(r / L) * L; }
+
+// invertMatrix (def.h:154-179)
+static bool invert3(const float *m, float *out) {
+    float inv[9], det;
+    det = -m[2] * m[4] * m[6] + m[1] * m[5] * m[6] + m[2] * m[3] * m[7] - m[0] * m[5] * m[7] - m[1] * m[3] * m[8] +
+          m[0] * m[4] * m[8];
+    if (det == 0) return false;
+    inv[0] = -m[5] * m[7] + m[4] * m[8];
+    inv[1] = m[2] * m[7] - m[1] * m[8];
+    inv[2] = -m[2] * m[4] + m[1] * m[5];
+    inv[3] = m[5] * m[6] - m[3] * m[8];
+    inv[4] = -m[2] * m[6] + m[0] * m[8];
+    inv[5] = m[2] * m[3] - m[0] * m[5];
+    inv[6] = -m[4] * m[6] + m[3] * m[7];
+    inv[7] = m[1] * m[6] - m[0] * m[7];
+    inv[8] = -m[1] * m[3] + m[0] * m[4];
+    det = 1.0f / det;
+    for (int i = 0; i < 9; i++) out[i] = inv[i] * det;
+    return true;
+}
+
+static femmd_status download_state(femmd_ctx *ctx, unsigned what);
+
+// Setup calls that change the system first bring device-newer state home.
+#define HOSTSYNC(ctx)                                                 \
+    do {                                                              \
+        femmd_status hs_;                                             \
+        if ((ctx)->staleMask && (hs_ = download_state((ctx), kAll))) return hs_; \
+    } while (0)
+
+static void mark_topology(femmd_ctx *c) {
+    c->topoDirty = true;
+    c->stateDirty = true;
+    c->forcesValid = false;
+    c->listBuilt = false;
+}
+
+static void release_graphs(femmd_ctx *c) {
+    for (auto &p : c->graphs)
+        for (auto &g : p) g.release();
+}
+
+static void release_device(femmd_ctx *c) {
+    release_graphs(c);
+    c->dpos0.release(); c->dpos1.release(); c->dvel.release(); c->dacc.release(); c->dforce.release();
+    c->dref.release(); c->ckPos.release(); c->ckVel.release(); c->ckAcc.release(); c->triF.release();
+    c->dmass.release(); c->dsigma.release(); c->denergy.release(); c->triE.release(); c->partialsMax.release();
+    c->dtype.release(); c->dexcl.release(); c->cellOf.release(); c->rank.release(); c->cellCount.release();
+    c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->nbr.release();
+    c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
+    c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
+    c->partials.release(); c->triPartials.release(); c->obs.release(); c->sc.release();
+    c->nbrCap = 0;
+    c->obsCap = 0;
+}
+
+static void clear_system(femmd_ctx *c) {
+    c->inited = false;
+    c->Lx = c->Ly = 0;
+    c->dt = 0.005f;
+    c->density = 0;
+    c->pbc = FEMMD_XYPBC;
+    c->numTypes = 1;
+    c->steps = 0;
+    c->eps.clear(); c->rc.clear(); c->us.clear();
+    c->rCutMax = 0;
+    c->bondForces = c->feaForces = false;
+    c->kBond = c->E = 0;
+    c->nu = 0.3f;
+    c->gravity = c->kArea = 0;
+    c->skin = 0.4f;
+    c->pos.clear(); c->vel.clear(); c->acc.clear(); c->force.clear(); c->refPos.clear();
+    c->mass.clear(); c->sigma.clear(); c->energy.clear(); c->type.clear(); c->excl.clear(); c->cluster.clear();
+    c->nexcl = 0;
+    c->clusters.clear();
+    c->bond.clear(); c->r0.clear(); c->tri.clear(); c->xm.clear(); c->refVol.clear();
+    c->nnInit = false;
+    c->nnRadius = c->nnRadiusSq = 0;
+    c->ncx = c->ncy = c->ncells = 0;
+    c->totalBuilds = 0;
+    set_elastic_constants(c);
+    mark_topology(c);
+}
+
+static int add_particle_raw(femmd_ctx *c, float x, float y, float vx, float vy, float m, float sig, int typ) {
+    int pid = (int)c->pos.size();
+    c->pos.push_back(make_float2(x, y));
+    c->vel.push_back(make_float2(vx, vy));
+    c->acc.push_back(make_float2(0.f, 0.f));
+    c->force.push_back(make_float2(0.f, 0.f));
+    c->refPos.push_back(make_float2(0.f, 0.f));
+    c->mass.push_back(m);
+    c->sigma.push_back(sig);
+    c->energy.push_back(0.f);
+    c->type.push_back(typ);
+    c->excl.push_back(-1);
+    c->cluster.push_back(-1);
+    c->density = (float)(int)c->pos.size() / (c->Lx * c->Ly);
+    return pid;
+}
+
+static void create_bond_raw(femmd_ctx *c, int i, int j) {
+    c->bond.push_back(i);
+    c->bond.push_back(j);
+    float dx = c->pos[i].x - c->pos[j].x;
+    float dy = c->pos[i].y - c->pos[j].y;
+    c->r0.push_back(std::sqrt(dx * dx + dy * dy));
+}
+
+// ------------------------------------------------------------- device upload
+
+static DevSys make_sys(femmd_ctx *c) {
+    DevSys s = {};
+    s.N = (int)c->pos.size();
+    s.Ncap = c->Ncap;
+    s.wrapx = (c->pbc == FEMMD_XYPBC || c->pbc == FEMMD_XPBC);
+    s.wrapy = (c->pbc == FEMMD_XYPBC);
+    s.Lx = c->Lx;
+    s.Ly = c->Ly;
+    s.dt = c->dt;
+    s.hdt = 0.5f * c->dt;
+    s.halfSkin = 0.5 * (double)c->skin;
+    s.ncx = c->ncx;
+    s.ncy = c->ncy;
+    s.ncells = c->ncells;
+    s.nnRadiusSq = c->nnRadiusSq;
+    s.imageExact = c->imageMode == FEMMD_IMAGE_EXACT;
+    s.numTypes = c->numTypes;
+    s.sigmaByType = c->sigmaByType;
+    s.pair = c->pair.p;
+    s.pos0 = c->dpos0.p;
+    s.pos1 = c->dpos1.p;
+    s.vel = c->dvel.p;
+    s.acc = c->dacc.p;
+    s.forceOut = c->dforce.p;
+    s.energyOut = c->denergy.p;
+    s.mass = c->dmass.p;
+    s.sigma = c->dsigma.p;
+    s.typeId = c->dtype.p;
+    s.excl = c->dexcl.p;
+    s.cellOf = c->cellOf.p;
+    s.rank = c->rank.p;
+    s.cellCount = c->cellCount.p;
+    s.cellStart = c->cellStart.p;
+    s.blockSums = c->blockSums.p;
+    s.sortedIds = c->sortedIds.p;
+    s.cellSorted = c->cellSorted.p;
+    s.nbr = c->nbr.p;
+    s.nbrCount = c->nbrCount.p;
+    s.nbrCap = c->nbrCap;
+    s.nBonded = c->nBonded;
+    s.bondForces = c->bondForces && !c->r0.empty();
+    s.feaForces = c->feaForces && !c->refVol.empty();
+    s.feaLaw = c->feaLaw;
+    s.bondKMode = c->bondKMode;
+    s.bStart = c->bStart.p;
+    s.bEnt = c->bEnt.p;
+    s.tStart = c->tStart.p;
+    s.tEnt = c->tEnt.p;
+    s.ntri = (int)c->refVol.size();
+    s.triIdx = c->triIdx.p;
+    s.triGeo = c->triGeo.p;
+    s.triF = c->triF.p;
+    s.triE = c->triE.p;
+    s.refPos = c->dref.p;
+    s.kBond = c->kBond;
+    s.E = c->E;
+    s.mu = c->mu;
+    s.lambda = c->lambda;
+    s.C1 = c->C1;
+    s.C2 = c->C2;
+    s.C3 = c->C3;
+    s.partials = c->partials.p;
+    s.partialsMax = c->partialsMax.p;
+    s.triPartials = c->triPartials.p;
+    s.sc = c->sc.p;
+    s.obs = c->obs.p;
+    s.obsCap = c->obsCap;
+    return s;
+}
+
+static femmd_status ensure_stream(femmd_ctx *ctx) {
+    if (ctx->stream) return FEMMD_OK;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&ctx->hsc, sizeof(DevScalars)));
+    memset(ctx->hsc, 0, sizeof(DevScalars));
+    return FEMMD_OK;
+}
+
+static femmd_status validate(femmd_ctx *ctx) {
+    if (!ctx->inited) return fail(ctx, FEMMD_NOT_READY, "init(Lx, Ly) has not been called");
+    if (!ctx->nnInit) return fail(ctx, FEMMD_NOT_READY, "init_neighbor_list() has not been called");
+    int N = (int)ctx->pos.size();
+    if (N > kIdMask) return fail(ctx, FEMMD_INVALID_ARG, "at most %d particles are supported", kIdMask);
+    if (ctx->numTypes < 1 || ctx->numTypes > kMaxTypes)
+        return fail(ctx, FEMMD_INVALID_ARG, "numTypes must be in [1, %d]", kMaxTypes);
+    if ((int)ctx->eps.size() < ctx->numTypes * ctx->numTypes)
+        return fail(ctx, FEMMD_INVALID_ARG, "pair table has %zu entries, numTypes^2 = %d needed", ctx->eps.size(),
+                    ctx->numTypes * ctx->numTypes);
+    for (int i = 0; i < N; i++) {
+        if (ctx->type[i] < 0 || ctx->type[i] >= ctx->numTypes)
+            return fail(ctx, FEMMD_INVALID_ARG, "particle %d has type %d outside [0, %d)", i, ctx->type[i],
+                        ctx->numTypes);
+        if (!(ctx->mass[i] != 0.0f)) return fail(ctx, FEMMD_INVALID_ARG, "particle %d has zero mass", i);
+    }
+    return FEMMD_OK;
+}
+
+static femmd_status upload_topology(femmd_ctx *ctx) {
+    femmd_status st;
+    if ((st = ensure_stream(ctx))) return st;
+    release_graphs(ctx);
+    const int N = (int)ctx->pos.size();
+    ctx->Ncap = std::max(32, (N + 31) / 32 * 32);
+    // sigma as a function of type?
+    {
+        std::vector<float> st_sig(ctx->numTypes, 0.f);
+        std::vector<char> seen(ctx->numTypes, 0);
+        ctx->sigmaByType = 1;
+        for (int i = 0; i < N; i++) {
+            int t = ctx->type[i];
+            if (!seen[t]) { seen[t] = 1; st_sig[t] = ctx->sigma[i]; }
+            else if (st_sig[t] != ctx->sigma[i]) ctx->sigmaByType = 0;
+        }
+        std::vector<PairEntry> tab((size_t)ctx->numTypes * ctx->numTypes);
+        for (int a = 0; a < ctx->numTypes; a++)
+            for (int b = 0; b < ctx->numTypes; b++) {
+                PairEntry &p = tab[a * ctx->numTypes + b];
+                float e = ctx->eps[a * ctx->numTypes + b], r = ctx->rc[a * ctx->numTypes + b];
+                float sij = (st_sig[a] + st_sig[b]) / 2.0f;  // pairForce: (sigma[i]+sigma[j])/2
+                p.rcut2 = r * r * sij * sij;
+                p.sig2 = sij * sij;
+                p.c = 48.0f * e / (sij * sij);
+                p.eps4 = 4.0f * e;
+                p.us = ctx->us[a * ctx->numTypes + b];
+                p.rc = r;
+                p.eps48 = 48.0f * e;
+                p.pad = 0.f;
+            }
+        CK(ctx->pair.ensure(tab.size()));
+        CK(cudaMemcpyAsync(ctx->pair.p, tab.data(), tab.size() * sizeof(PairEntry), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
+    CK(ctx->dpos0.ensure(N)); CK(ctx->dpos1.ensure(N)); CK(ctx->dvel.ensure(N)); CK(ctx->dacc.ensure(N));
+    CK(ctx->dforce.ensure(N)); CK(ctx->denergy.ensure(N)); CK(ctx->dref.ensure(N));
+    CK(ctx->ckPos.ensure(N)); CK(ctx->ckVel.ensure(N)); CK(ctx->ckAcc.ensure(N));
+    CK(ctx->dmass.ensure(N)); CK(ctx->dtype.ensure(N)); CK(ctx->dexcl.ensure(N));
+    CK(ctx->dsigma.ensure(ctx->sigmaByType ? 1 : N));
+    CK(ctx->cellOf.ensure(N)); CK(ctx->rank.ensure(N)); CK(ctx->sortedIds.ensure(N));
+    CK(ctx->cellSorted.ensure(N)); CK(ctx->nbrCount.ensure(N));
+    CK(ctx->cellCount.ensure(ctx->ncells)); CK(ctx->cellStart.ensure(ctx->ncells + 1));
+    CK(ctx->blockSums.ensure(scan_blocks(ctx->ncells)));
+    int fb = force_blocks(N);
+    CK(ctx->partials.ensure(3 * (size_t)std::max(fb, 1))); CK(ctx->partialsMax.ensure(std::max(fb, 1)));
+    CK(ctx->sc.ensure(1));
+    cudaStream_t s = ctx->stream;
+    if (N > 0) {
+        CK(cudaMemcpyAsync(ctx->dmass.p, ctx->mass.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dtype.p, ctx->type.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dexcl.p, ctx->excl.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dref.p, ctx->refPos.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+        if (!ctx->sigmaByType)
+            CK(cudaMemcpyAsync(ctx->dsigma.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemsetAsync(ctx->cellCount.p, 0, sizeof(int) * std::max(ctx->ncells, 1), s));
+    CK(cudaMemsetAsync(ctx->sc.p, 0, sizeof(DevScalars), s));
+    // bonded incidences: bond order / triangle order per particle
+    const int nb = (int)ctx->r0.size(), nt = (int)ctx->refVol.size();
+    int nbd = 0;
+    for (int v : ctx->bond) nbd = std::max(nbd, v + 1);
+    for (int v : ctx->tri) nbd = std::max(nbd, v + 1);
+    ctx->nBonded = nbd;
+    {
+        std::vector<int> bs(nbd + 1, 0), ts(nbd + 1, 0);
+        for (int l = 0; l < nb; l++) { bs[ctx->bond[2 * l] + 1]++; bs[ctx->bond[2 * l + 1] + 1]++; }
+        for (int v : ctx->tri) ts[v + 1]++;
+        for (int v = 0; v < nbd; v++) { bs[v + 1] += bs[v]; ts[v + 1] += ts[v]; }
+        std::vector<int2> be(std::max(bs[nbd], 1));
+        std::vector<int> te(std::max(ts[nbd], 1));
+        std::vector<int> fb2(bs.begin(), bs.end() - 1), ft(ts.begin(), ts.end() - 1);
+        for (int l = 0; l < nb; l++) {
+            int i = ctx->bond[2 * l], j = ctx->bond[2 * l + 1];
+            int r0bits;
+            memcpy(&r0bits, &ctx->r0[l], 4);
+            be[fb2[i]++] = make_int2(j, r0bits);
+            be[fb2[j]++] = make_int2((int)((unsigned)i | 0x80000000u), r0bits);
+        }
+        for (int t = 0; t < nt; t++)
+            for (int k = 0; k < 3; k++) te[ft[ctx->tri[3 * t + k]]++] = t * 4 + k;
+        CK(ctx->bStart.ensure(nbd + 1)); CK(ctx->tStart.ensure(nbd + 1));
+        CK(ctx->bEnt.ensure(be.size())); CK(ctx->tEnt.ensure(te.size()));
+        CK(cudaMemcpyAsync(ctx->bStart.p, bs.data(), bs.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->tStart.p, ts.data(), ts.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->bEnt.p, be.data(), be.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->tEnt.p, te.data(), te.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        // triangle geometry from the reference positions
+        std::vector<int4> ti(std::max(nt, 1));
+        std::vector<float4> tg(2 * (size_t)std::max(nt, 1));
+        for (int t = 0; t < nt; t++) {
+            int p0 = ctx->tri[3 * t], p1 = ctx->tri[3 * t + 1], p2 = ctx->tri[3 * t + 2];
+            ti[t] = make_int4(p0, p1, p2, 0);
+            float X0 = ctx->refPos[p0].x, Y0 = ctx->refPos[p0].y, X1 = ctx->refPos[p1].x, Y1 = ctx->refPos[p1].y;
+            float X2 = ctx->refPos[p2].x, Y2 = ctx->refPos[p2].y;
+            if (ctx->feaLaw == FEMMD_FEA_NEO_HOOKEAN) {
+                // calcFeaForcesCPU2 Dm, Bm, vol0 (interactions.cpp:589-602)
+                float Dm00 = X0 - X2, Dm10 = Y0 - Y2, Dm01 = X1 - X2, Dm11 = Y1 - Y2;
+                float detDm = Dm00 * Dm11 - Dm01 * Dm10;
+                float vol0 = detDm / 2.0f;
+                tg[2 * t] = make_float4(Dm11 / detDm, -Dm10 / detDm, -Dm01 / detDm, Dm00 / detDm);
+                tg[2 * t + 1] = make_float4(vol0, 0.f, 0.f, 0.f);
+            } else {
+                // computeFeaForcesGPU xm and |area| (interactionsCuda.cu:364-383)
+                float aa[9] = {1.0f, X0, Y0, 1.0f, X1, Y1, 1.0f, X2, Y2}, mm[9];
+                if (!invert3(aa, mm)) memset(mm, 0, sizeof mm);
+                float tv = std::fabs(0.5f * ((Y2 - Y0) * (X1 - X0) - (Y1 - Y0) * (X2 - X0)));
+                tg[2 * t] = make_float4(mm[3], mm[4], mm[5], mm[6]);
+                tg[2 * t + 1] = make_float4(mm[7], mm[8], tv, 0.f);
+            }
+        }
+        CK(ctx->triIdx.ensure(ti.size())); CK(ctx->triGeo.ensure(tg.size()));
+        CK(ctx->triF.ensure(3 * ti.size())); CK(ctx->triE.ensure(ti.size()));
+        CK(ctx->triPartials.ensure(std::max(tri_blocks(nt), 1)));
+        CK(cudaMemcpyAsync(ctx->triIdx.p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    }
+    ctx->topoDirty = false;
+    ctx->listBuilt = false;
+    CK(cudaStreamSynchronize(s));
+    return FEMMD_OK;
+}
+
+static femmd_status upload_state(femmd_ctx *ctx) {
+    const int N = (int)ctx->pos.size();
+    cudaStream_t s = ctx->stream;
+    if (N > 0) {
+        CK(cudaMemcpyAsync(ctx->dpos0.p, ctx->pos.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dvel.p, ctx->vel.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dacc.p, ctx->acc.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dforce.p, ctx->force.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+    }
+    ctx->cur = 0;
+    ctx->stateDirty = false;
+    ctx->listBuilt = false;
+    ctx->staleMask = 0;
+    CK(cudaStreamSynchronize(s));
+    return FEMMD_OK;
+}
+
+// Bring the host copies named by 'what' up to date with the device.
+static femmd_status download_state(femmd_ctx *ctx, unsigned what) {
+    what &= ctx->staleMask;
+    if (!what) return FEMMD_OK;
+    const int N = (int)ctx->pos.size();
+    cudaStream_t s = ctx->stream;
+    if (N > 0) {
+        if (what & kPos)
+            CK(cudaMemcpyAsync(ctx->pos.data(), ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, N * sizeof(float2),
+                               cudaMemcpyDeviceToHost, s));
+        if (what & kVel) CK(cudaMemcpyAsync(ctx->vel.data(), ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        if (what & kAcc) CK(cudaMemcpyAsync(ctx->acc.data(), ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        if (what & kForce)
+            CK(cudaMemcpyAsync(ctx->force.data(), ctx->dforce.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        if (what & kEnergy)
+            CK(cudaMemcpyAsync(ctx->energy.data(), ctx->denergy.p, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    ctx->staleMask &= ~what;
+    return FEMMD_OK;
+}
+
+static femmd_status read_scalars(femmd_ctx *ctx) {
+    CK(cudaMemcpyAsync(ctx->hsc, ctx->sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FEMMD_OK;
+}
+
+// Neighbour-list storage for capacity 'cap' per particle.
+static femmd_status alloc_list(femmd_ctx *ctx, int cap) {
+    cap = std::max(1, cap);
+    CK(ctx->nbr.ensure((size_t)cap * ctx->Ncap));
+    ctx->nbrCap = cap;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+// Sizing pass: bin and count with capacity 0, then allocate max count * 1.25 + 8.
+static femmd_status size_list(femmd_ctx *ctx, int min_cap) {
+    DevSys s = make_sys(ctx);
+    s.nbrCap = 0;
+    Launch L;
+    L.stream = ctx->stream;
+    CK(enqueue_rebuild(L, s, ctx->cur, 0));
+    femmd_status st;
+    if ((st = read_scalars(ctx))) return st;
+    int need = ctx->hsc->maxCount + ctx->hsc->maxCount / 4 + 8;
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, sizeof(int), ctx->stream));
+    return alloc_list(ctx, std::max(need, min_cap));
+}
+
+static femmd_status prepare(femmd_ctx *ctx) {
+    femmd_status st;
+    if (!ctx->nnInit) return fail(ctx, FEMMD_NOT_READY, "init_neighbor_list() has not been called");
+    if (ctx->topoDirty && (st = validate(ctx))) return st;
+    if (ctx->topoDirty && (st = upload_topology(ctx))) return st;
+    if (ctx->stateDirty && (st = upload_state(ctx))) return st;
+    if (ctx->nbrCap == 0 && (st = size_list(ctx, 0))) return st;
+    return FEMMD_OK;
+}
+
+static femmd_status ensure_obs(femmd_ctx *ctx, int rows) {
+    rows = std::min(rows, 1 << 20);
+    if (rows <= ctx->obsCap) return FEMMD_OK;
+    int cap = std::max(rows, 1024);
+    CK(ctx->obs.ensure((size_t)cap * kObsCols));
+    ctx->obsCap = cap;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+// Graph of 'units' x [MID step on parity p -> IF(rebuild on 1-p)] starting at parity p.
+static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int units) {
+    gs.release();
+    CK(cudaGraphCreate(&gs.g, 0));
+    DevSys s = make_sys(ctx);
+    Launch L;
+    L.stream = ctx->stream;
+    L.graph = gs.g;
+    int p = parity;
+    for (int u = 0; u < units; u++) {
+        cudaGraphConditionalHandle h;
+        CK(cudaGraphConditionalHandleCreate(&h, gs.g, 0, cudaGraphCondAssignDefault));
+        CK(enqueue_step(L, s, MODE_MID, p, h, 1));
+        Launch body;
+        CK(L.begin_if(h, body));
+        CK(enqueue_rebuild(body, s, 1 - p, 1));
+        p = 1 - p;
+    }
+    CK(cudaGraphInstantiate(&gs.x, gs.g, 0));
+    return FEMMD_OK;
+}
+
+static femmd_status launch_units(femmd_ctx *ctx, int units, bool use_graphs) {
+    if (units <= 0) return FEMMD_OK;
+    if (!use_graphs) {
+        DevSys s = make_sys(ctx);
+        Launch L;
+        L.stream = ctx->stream;
+        if (ctx->profiling) {
+            L.force_events = &ctx->forceEvents;
+            L.event_pool = &ctx->eventPool;
+        }
+        for (int u = 0; u < units; u++) {
+            CK(enqueue_step(L, s, MODE_MID, ctx->cur, 0, 0));
+            CK(enqueue_rebuild(L, s, 1 - ctx->cur, 1));
+            ctx->cur ^= 1;
+        }
+        ctx->profKernels += L.kernels;
+        return FEMMD_OK;
+    }
+    femmd_status st;
+    int big = units / kGraphUnits, rest = units % kGraphUnits;
+    for (int b = 0; b < big; b++) {
+        GraphSet &g = ctx->graphs[ctx->cur][0];
+        if (!g.x && (st = build_graph(ctx, g, ctx->cur, kGraphUnits))) return st;
+        CK(cudaGraphLaunch(g.x, ctx->stream));
+        // kGraphUnits is even: parity unchanged
+    }
+    for (int r = 0; r < rest; r++) {
+        GraphSet &g = ctx->graphs[ctx->cur][1];
+        if (!g.x && (st = build_graph(ctx, g, ctx->cur, 1))) return st;
+        CK(cudaGraphLaunch(g.x, ctx->stream));
+        ctx->cur ^= 1;
+    }
+    return FEMMD_OK;
+}
+
+static femmd_status run_once(femmd_ctx *ctx, int n) {
+    DevSys s = make_sys(ctx);
+    Launch L;
+    L.stream = ctx->stream;
+    if (ctx->profiling) {
+        L.force_events = &ctx->forceEvents;
+        L.event_pool = &ctx->eventPool;
+    }
+    const bool graphs = !ctx->profiling;
+    CK(enqueue_run_start(L, s));
+    CK(enqueue_rebuild(L, s, ctx->cur, 1));
+    if (n == 0) {
+        CK(enqueue_step(L, s, MODE_INIT, ctx->cur, 0, 0));
+        ctx->profKernels += L.kernels;
+        return FEMMD_OK;
+    }
+    CK(enqueue_step(L, s, MODE_FIRST, ctx->cur, 0, 0));
+    ctx->cur ^= 1;
+    ctx->profKernels += L.kernels;
+    femmd_status st;
+    if ((st = launch_units(ctx, n - 1, graphs))) return st;
+    Launch T;
+    T.stream = ctx->stream;
+    if (ctx->profiling) {
+        T.force_events = &ctx->forceEvents;
+        T.event_pool = &ctx->eventPool;
+    }
+    CK(enqueue_step(T, s, MODE_LAST, ctx->cur, 0, 0));
+    ctx->profKernels += T.kernels;
+    return FEMMD_OK;
+}
+
+static femmd_status collect_profile(femmd_ctx *ctx) {
+    if (!ctx->profiling) return FEMMD_OK;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (auto &pr : ctx->forceEvents) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, pr.first, pr.second));
+        ctx->profForceMs += ms;
+        ctx->profForceLaunches++;
+        ctx->eventPool.push_back(pr.first);
+        ctx->eventPool.push_back(pr.second);
+    }
+    ctx->forceEvents.clear();
+    return FEMMD_OK;
+}
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+const char *femmd_version(void) { return "femmd-gb300 0.1 (sm_103a)"; }
+
+femmd_status femmd_create(int device, femmd_ctx **out) {
+    if (!out) return FEMMD_INVALID_ARG;
+    femmd_ctx *c = new (std::nothrow) femmd_ctx();
+    if (!c) return FEMMD_CUDA_ERROR;
+    c->device = device;
+    clear_system(c);
+    *out = c;
+    return FEMMD_OK;
+}
+
+void femmd_destroy(femmd_ctx *ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    release_device(ctx);
+    for (auto &pr : ctx->forceEvents) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto e : ctx->eventPool) cudaEventDestroy(e);
+    for (auto e : ctx->userEvents)
+        if (e) cudaEventDestroy(e);
+    if (ctx->hsc) cudaFreeHost(ctx->hsc);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *femmd_last_error(const femmd_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+femmd_status femmd_init(femmd_ctx *ctx, double Lx, double Ly) {
+    NEED(ctx);
+    if (!(Lx > 0) || !(Ly > 0)) return fail(ctx, FEMMD_INVALID_ARG, "box lengths must be positive");
+    clear_system(ctx);
+    ctx->inited = true;
+    ctx->Lx = (float)Lx;
+    ctx->Ly = (float)Ly;
+    // Interactions::init defaults: WCA, E = 0, nu = 0.3, kBond = 0
+    ctx->eps = {1.0f};
+    ctx->rc = {(float)std::pow(2.0, 1.0 / 6.0)};
+    ctx->us = {1.0f};
+    ctx->rCutMax = ctx->rc[0];
+    return FEMMD_OK;
+}
+
+femmd_status femmd_reset(femmd_ctx *ctx) {
+    NEED(ctx);
+    clear_system(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_box(femmd_ctx *ctx, double Lx, double Ly) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (!(Lx > 0) || !(Ly > 0)) return fail(ctx, FEMMD_INVALID_ARG, "box lengths must be positive");
+    ctx->Lx = (float)Lx;
+    ctx->Ly = (float)Ly;
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_box(const femmd_ctx *ctx, double *Lx, double *Ly) {
+    if (!ctx || !Lx || !Ly) return FEMMD_INVALID_ARG;
+    *Lx = ctx->Lx;
+    *Ly = ctx->Ly;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_pbc(femmd_ctx *ctx, int pbc) {
+    NEED(ctx);
+    ctx->pbc = pbc == 0 ? FEMMD_NOPBC : pbc == 1 ? FEMMD_XPBC : FEMMD_XYPBC;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_dev(femmd_ctx *ctx, int dev) {
+    NEED(ctx);
+    ctx->dev_flag = dev;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_dt(femmd_ctx *ctx, double dt) {
+    NEED(ctx);
+    ctx->dt = (float)dt;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_dt(const femmd_ctx *ctx, double *dt) {
+    if (!ctx || !dt) return FEMMD_INVALID_ARG;
+    *dt = ctx->dt;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_num_types(femmd_ctx *ctx, int n) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (n < 1 || n > kMaxTypes) return fail(ctx, FEMMD_INVALID_ARG, "numTypes must be in [1, %d]", kMaxTypes);
+    ctx->numTypes = n;
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_pair_potential(femmd_ctx *ctx, const double *eps, const double *rc, const double *us, int n2) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    int nt = ctx->numTypes;
+    if (!eps || !rc || !us || n2 < nt * nt)
+        return fail(ctx, FEMMD_INVALID_ARG, "pair tables need numTypes^2 = %d entries", nt * nt);
+    ctx->eps.assign(nt * nt, 0.f);
+    ctx->rc.assign(nt * nt, 0.f);
+    ctx->us.assign(nt * nt, 0.f);
+    ctx->rCutMax = 0;
+    for (int i = 0; i < nt * nt; i++) {
+        ctx->eps[i] = (float)eps[i];
+        ctx->rc[i] = (float)rc[i];
+        if (ctx->rc[i] > ctx->rCutMax) ctx->rCutMax = ctx->rc[i];
+        ctx->us[i] = (float)us[i];
+    }
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_kbond(femmd_ctx *ctx, double k) {
+    NEED(ctx);
+    float kf = (float)k;
+    if (kf > 0) { ctx->kBond = kf; ctx->bondForces = true; } else ctx->bondForces = false;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_youngs_modulus(femmd_ctx *ctx, double E) {
+    NEED(ctx);
+    float Ef = (float)E;
+    if (Ef > 0) { ctx->E = Ef; ctx->feaForces = true; } else ctx->feaForces = false;
+    set_elastic_constants(ctx);
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_poisson_ratio(femmd_ctx *ctx, double nu) {
+    NEED(ctx);
+    ctx->nu = (float)nu;
+    set_elastic_constants(ctx);
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_gravity(femmd_ctx *ctx, double g) {
+    NEED(ctx);
+    ctx->gravity = g > 0 ? (float)g : 0.f;
+    if (g > 0) return fail(ctx, FEMMD_UNSUPPORTED, "gravity forces are outside this build's timestep path");
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_karea(femmd_ctx *ctx, double k) {
+    NEED(ctx);
+    ctx->kArea = k > 0 ? (float)k : 0.f;
+    if (k > 0) return fail(ctx, FEMMD_UNSUPPORTED, "area springs are outside this build's timestep path");
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_skin(femmd_ctx *ctx, double skin) {
+    NEED(ctx);
+    if (!(skin >= 0)) return fail(ctx, FEMMD_INVALID_ARG, "skin must be >= 0");
+    ctx->skin = (float)skin;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_neighbor_capacity(femmd_ctx *ctx, int cap) {
+    NEED(ctx);
+    if (cap < 0) return fail(ctx, FEMMD_INVALID_ARG, "capacity must be >= 0");
+    femmd_status st;
+    if (cap == 0) {
+        ctx->nbrCap = 0;
+        release_graphs(ctx);
+        return FEMMD_OK;
+    }
+    if ((st = prepare(ctx))) return st;
+    return alloc_list(ctx, cap);
+}
+
+femmd_status femmd_get_neighbor_capacity(const femmd_ctx *ctx, int *cap) {
+    if (!ctx || !cap) return FEMMD_INVALID_ARG;
+    *cap = ctx->nbrCap;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_fea_law(femmd_ctx *ctx, int law) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (law != FEMMD_FEA_NEO_HOOKEAN && law != FEMMD_FEA_GREEN_LINEAR)
+        return fail(ctx, FEMMD_INVALID_ARG, "unknown FEA law %d", law);
+    ctx->feaLaw = law;
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_bond_k_mode(femmd_ctx *ctx, int mode) {
+    NEED(ctx);
+    if (mode != FEMMD_BONDK_KBOND && mode != FEMMD_BONDK_E_OVER_R0)
+        return fail(ctx, FEMMD_INVALID_ARG, "unknown bond stiffness mode %d", mode);
+    ctx->bondKMode = mode;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_image_mode(femmd_ctx *ctx, int mode) {
+    NEED(ctx);
+    if (mode != FEMMD_IMAGE_REFERENCE && mode != FEMMD_IMAGE_EXACT)
+        return fail(ctx, FEMMD_INVALID_ARG, "unknown image mode %d", mode);
+    ctx->imageMode = mode;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_elastomer_bonds(femmd_ctx *ctx, int mode) {
+    NEED(ctx);
+    if (mode < 0 || mode > 2) return fail(ctx, FEMMD_INVALID_ARG, "unknown elastomer bond mode %d", mode);
+    ctx->bondMode = mode;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_add_particle(femmd_ctx *ctx, double x, double y, double vx, double vy, double m, double sig,
+                                int typ) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (!ctx->inited) return fail(ctx, FEMMD_NOT_READY, "init(Lx, Ly) has not been called");
+    if ((int)ctx->pos.size() >= kIdMask) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "particle id space exhausted");
+    add_particle_raw(ctx, (float)x, (float)y, (float)vx, (float)vy, (float)m, (float)sig, typ);
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_add_particles(femmd_ctx *ctx, int n, const double *x, const double *y, const double *vx,
+                                 const double *vy, const double *m, const double *sig, const int *typ) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (!ctx->inited) return fail(ctx, FEMMD_NOT_READY, "init(Lx, Ly) has not been called");
+    if (n < 0 || (n > 0 && (!x || !y || !vx || !vy || !m || !sig || !typ)))
+        return fail(ctx, FEMMD_INVALID_ARG, "bad particle arrays");
+    if ((long long)ctx->pos.size() + n > kIdMask) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "too many particles");
+    size_t want = ctx->pos.size() + (size_t)n;
+    ctx->pos.reserve(want); ctx->vel.reserve(want); ctx->acc.reserve(want); ctx->force.reserve(want);
+    ctx->refPos.reserve(want); ctx->mass.reserve(want); ctx->sigma.reserve(want); ctx->energy.reserve(want);
+    ctx->type.reserve(want); ctx->excl.reserve(want); ctx->cluster.reserve(want);
+    for (int k = 0; k < n; k++)
+        add_particle_raw(ctx, (float)x[k], (float)y[k], (float)vx[k], (float)vy[k], (float)m[k], (float)sig[k], typ[k]);
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_add_elastomer(femmd_ctx *ctx, const float *vert, int nv, const int *tet, int nt, double x,
+                                 double y, int typ, int g, double sig, double M, int exclude) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    (void)g;
+    if (!ctx->inited) return fail(ctx, FEMMD_NOT_READY, "init(Lx, Ly) has not been called");
+    if (!vert || !tet || nv <= 0 || nt <= 0) return fail(ctx, FEMMD_INVALID_ARG, "empty mesh");
+    for (int k = 0; k < 3 * nt; k++)
+        if (tet[k] < 1 || tet[k] > nv)
+            return fail(ctx, FEMMD_INVALID_ARG, "triangle index %d outside [1, %d] (indices are 1-based)", tet[k], nv);
+    int offset = (int)ctx->pos.size();
+    if (!ctx->clusters.empty() && (ctx->clusters[0].nv != nv || ctx->clusters[0].nt != nt))
+        return fail(ctx, FEMMD_INVALID_ARG, "all elastomers must share one mesh (particles.cpp:301-325)");
+    if (offset != (int)ctx->clusters.size() * nv)
+        return fail(ctx, FEMMD_INVALID_ARG, "elastomers must be added before free particles (particles.cpp:301-325)");
+    int exclusionGroupId = ctx->nexcl++;
+    int ci = (int)ctx->clusters.size();
+    Cluster cl = {offset, nv, nt, ci * nt, 0.f, 0.f};
+    ctx->clusters.push_back(cl);
+    float fx0 = (float)x, fy0 = (float)y;
+    for (int i = 0; i < nv; i++) {
+        float x1 = vert[2 * i] + fx0;
+        float y1 = vert[2 * i + 1] + fy0;
+        int pid = add_particle_raw(ctx, x1, y1, 0.f, 0.f, 0.f, (float)sig, typ);
+        ctx->refPos[pid] = ctx->pos[pid];
+        if (ctx->pbc == FEMMD_XYPBC) {
+            ctx->pos[pid].x = wrap_coord(ctx->pos[pid].x, ctx->Lx);
+            ctx->pos[pid].y = wrap_coord(ctx->pos[pid].y, ctx->Ly);
+        } else if (ctx->pbc == FEMMD_XPBC) {
+            ctx->pos[pid].x = wrap_coord(ctx->pos[pid].x, ctx->Lx);
+        }
+        if (exclude) ctx->excl[pid] = exclusionGroupId;
+        ctx->cluster[pid] = ci;
+    }
+    float totVol = 0.f;
+    int tetOffset = ci * nt;
+    ctx->tri.resize(3 * (size_t)(tetOffset + nt));
+    ctx->xm.resize(9 * (size_t)(tetOffset + nt));
+    ctx->refVol.resize(tetOffset + nt);
+    for (int i = 0; i < nt; i++) {
+        int i0 = tet[3 * i] + offset - 1, i1 = tet[3 * i + 1] + offset - 1, i2 = tet[3 * i + 2] + offset - 1;
+        int t = i + tetOffset;
+        ctx->tri[3 * t] = i0;
+        ctx->tri[3 * t + 1] = i1;
+        ctx->tri[3 * t + 2] = i2;
+        if (ctx->bondMode == FEMMD_ELASTOMER_BONDS_ALL) {
+            create_bond_raw(ctx, i0, i1);
+            create_bond_raw(ctx, i0, i2);
+            create_bond_raw(ctx, i1, i2);
+        }
+        float aa[9], rx[3], ry[3];
+        for (int j = 0; j < 3; j++) {
+            int ip = ctx->tri[3 * t + j];
+            aa[3 * j] = 1.0f;
+            aa[3 * j + 1] = ctx->refPos[ip].x;
+            aa[3 * j + 2] = ctx->refPos[ip].y;
+            rx[j] = ctx->refPos[ip].x;
+            ry[j] = ctx->refPos[ip].y;
+        }
+        if (!invert3(aa, &ctx->xm[9 * (size_t)t])) memset(&ctx->xm[9 * (size_t)t], 0, 9 * sizeof(float));
+        float vol = (float)(0.5 * (double)((ry[2] - ry[0]) * (rx[1] - rx[0]) - (ry[1] - ry[0]) * (rx[2] - rx[0])));
+        ctx->refVol[t] = vol;
+        totVol += vol;
+    }
+    if (ctx->bondMode == FEMMD_ELASTOMER_BONDS_BOUNDARY) {
+        // one bond per edge of exactly one triangle, triangle order, (0,1) (0,2) (1,2)
+        std::vector<long long> keys(3 * (size_t)nt);
+        for (int i = 0; i < nt; i++) {
+            const int *q = &tet[3 * i];
+            int e[3][2] = {{q[0], q[1]}, {q[0], q[2]}, {q[1], q[2]}};
+            for (int k = 0; k < 3; k++)
+                keys[3 * i + k] = (long long)std::min(e[k][0], e[k][1]) * 4294967296LL + std::max(e[k][0], e[k][1]);
+        }
+        std::vector<long long> sorted(keys);
+        std::sort(sorted.begin(), sorted.end());
+        for (int i = 0; i < nt; i++) {
+            const int *q = &tet[3 * i];
+            int e[3][2] = {{q[0], q[1]}, {q[0], q[2]}, {q[1], q[2]}};
+            for (int k = 0; k < 3; k++) {
+                auto rg = std::equal_range(sorted.begin(), sorted.end(), keys[3 * i + k]);
+                if (rg.second - rg.first == 1) create_bond_raw(ctx, e[k][0] + offset - 1, e[k][1] + offset - 1);
+            }
+        }
+    }
+    Cluster &c = ctx->clusters[ci];
+    c.mass = (float)M;
+    c.rho = c.mass / totVol;
+    for (int it = 0; it < nt; it++)
+        for (int j = 0; j < 3; j++) {
+            int ip = ctx->tri[3 * (size_t)(it + tetOffset) + j];
+            // refVol indexed by the local triangle index, as particles.cpp:364
+            float prod = c.rho * ctx->refVol[it];
+            ctx->mass[ip] = (float)((double)ctx->mass[ip] + (double)prod / 3.0);
+        }
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_create_bond(femmd_ctx *ctx, int i, int j) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    int N = (int)ctx->pos.size();
+    if (i < 0 || j < 0 || i >= N || j >= N || i == j)
+        return fail(ctx, FEMMD_INVALID_ARG, "bond (%d, %d) needs two distinct particles in [0, %d)", i, j, N);
+    create_bond_raw(ctx, i, j);
+    mark_topology(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_velocities(femmd_ctx *ctx, double v0, uint64_t seed) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kAll))) return st;
+    uint64_t z = seed;
+    auto next = [&z]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t r = z;
+        r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ull;
+        r = (r ^ (r >> 27)) * 0x94D049BB133111EBull;
+        return r ^ (r >> 31);
+    };
+    const int N = (int)ctx->pos.size();
+    const double twopi = 8.0 * std::atan(1.0);
+    for (int p = 0; p < N; p++) {
+        double s = (double)(next() >> 11) * (1.0 / 9007199254740992.0) * twopi;
+        ctx->vel[p] = make_float2((float)(std::cos(s) * v0), (float)(std::sin(s) * v0));
+    }
+    // Particles::zeroCM (particles.cpp:246-261)
+    float sx = 0, sy = 0, tm = 0;
+    for (int p = 0; p < N; p++) { sx += ctx->vel[p].x * ctx->mass[p]; sy += ctx->vel[p].y * ctx->mass[p]; tm += ctx->mass[p]; }
+    for (int p = 0; p < N; p++) { ctx->vel[p].x -= sx / tm; ctx->vel[p].y -= sy / tm; }
+    ctx->stateDirty = true;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_allocate_cuda(femmd_ctx *ctx) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = ensure_stream(ctx))) return st;
+    if (ctx->nnInit) return prepare(ctx);
+    return FEMMD_OK;
+}
+
+// NeighborList::init (nn.cpp:192-227): nnRadius = rCutMax + skin, cells of at least nnRadius
+femmd_status femmd_init_neighbor_list(femmd_ctx *ctx) {
+    NEED(ctx);
+    HOSTSYNC(ctx);
+    if (!ctx->inited) return fail(ctx, FEMMD_NOT_READY, "init(Lx, Ly) has not been called");
+    float rc = 1.0f * ctx->rCutMax;
+    ctx->nnRadius = rc + ctx->skin;
+    ctx->nnRadiusSq = ctx->nnRadius * ctx->nnRadius;
+    int nx = (int)std::floor(ctx->Lx / ctx->nnRadius), ny = (int)std::floor(ctx->Ly / ctx->nnRadius);
+    if (nx < 1 || ny < 1)
+        return fail(ctx, FEMMD_INVALID_ARG, "box (%g, %g) is smaller than one list cell (%g)", ctx->Lx, ctx->Ly,
+                    ctx->nnRadius);
+    ctx->ncx = nx;
+    ctx->ncy = ny;
+    ctx->ncells = nx * ny;
+    ctx->nnInit = true;
+    mark_topology(ctx);
+    ctx->nbrCap = 0;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_run(femmd_ctx *ctx, int steps) {
+    NEED(ctx);
+    if (steps < 0) return fail(ctx, FEMMD_INVALID_ARG, "steps must be >= 0");
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    if ((int)ctx->pos.size() == 0) {
+        ctx->steps += steps;
+        return FEMMD_OK;
+    }
+    if ((st = ensure_obs(ctx, steps))) return st;
+    const int N = (int)ctx->pos.size();
+    for (int attempt = 0; attempt < 8; attempt++) {
+        // start checkpoint (positions, velocities, accelerations)
+        const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+        int cur0 = ctx->cur;
+        CK(cudaMemcpyAsync(ctx->ckPos.p, pc, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->ckVel.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->ckAcc.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));  // overflow, nonfinite
+        if ((st = run_once(ctx, steps))) return st;
+        if ((st = collect_profile(ctx))) return st;
+        if ((st = read_scalars(ctx))) return st;
+        if (!ctx->hsc->overflow) {
+            ctx->steps += steps;
+            ctx->staleMask |= kPos | kVel | kAcc | kForce;
+            ctx->forcesValid = true;
+            ctx->listBuilt = true;
+            ctx->obsRows = std::min(ctx->hsc->obsRow, ctx->obsCap);
+            ctx->totalBuilds = (long long)ctx->hsc->builds;
+            if (ctx->hsc->nonfinite)
+                return fail(ctx, FEMMD_NONFINITE, "a force became NaN or infinite during the run");
+            return FEMMD_OK;
+        }
+        // roll back to the checkpoint, grow the list, repeat
+        ctx->cur = cur0;
+        float2 *pd = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+        CK(cudaMemcpyAsync(pd, ctx->ckPos.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->dvel.p, ctx->ckVel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->dacc.p, ctx->ckAcc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        int need = std::max(ctx->hsc->maxCount, ctx->nbrCap + ctx->nbrCap / 2);
+        if ((st = alloc_list(ctx, need + need / 4 + 8))) return st;
+    }
+    return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "neighbour list kept overflowing");
+}
+
+femmd_status femmd_do_step(femmd_ctx *ctx) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    if (!ctx->listBuilt) return fail(ctx, FEMMD_NOT_READY, "do_step needs a previous run or build");
+    if (ctx->pos.empty()) { ctx->steps++; return FEMMD_OK; }
+    DevSys s = make_sys(ctx);
+    Launch L;
+    L.stream = ctx->stream;
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
+    CK(enqueue_drift(L, s, ctx->cur));
+    ctx->cur ^= 1;
+    CK(enqueue_rebuild(L, s, ctx->cur, 1));
+    CK(enqueue_step(L, s, MODE_LAST, ctx->cur, 0, 0));
+    if ((st = read_scalars(ctx))) return st;
+    ctx->steps++;
+    ctx->staleMask |= kPos | kVel | kAcc | kForce;
+    if (ctx->hsc->overflow) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "neighbour list overflow in do_step; run() grows it");
+    if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a force became NaN or infinite");
+    return FEMMD_OK;
+}
+
+femmd_status femmd_build_neighbor_list(femmd_ctx *ctx) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    if (ctx->pos.empty()) return FEMMD_OK;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        DevSys s = make_sys(ctx);
+        Launch L;
+        L.stream = ctx->stream;
+        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, sizeof(int), ctx->stream));
+        CK(enqueue_rebuild(L, s, ctx->cur, 0));
+        if ((st = read_scalars(ctx))) return st;
+        if (!ctx->hsc->overflow) {
+            ctx->listBuilt = true;
+            ctx->totalBuilds = (long long)ctx->hsc->builds;
+            return FEMMD_OK;
+        }
+        int need = ctx->hsc->maxCount;
+        if ((st = alloc_list(ctx, need + need / 4 + 8))) return st;
+    }
+    return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "neighbour list kept overflowing");
+}
+
+femmd_status femmd_calc_forces(femmd_ctx *ctx) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    if (ctx->pos.empty()) return FEMMD_OK;
+    if (!ctx->listBuilt && (st = femmd_build_neighbor_list(ctx))) return st;
+    DevSys s = make_sys(ctx);
+    Launch L;
+    L.stream = ctx->stream;
+    CK(cudaMemsetAsync(&ctx->sc.p->nonfinite, 0, sizeof(int), ctx->stream));
+    CK(enqueue_step(L, s, MODE_FORCES, ctx->cur, 0, 0));
+    if ((st = read_scalars(ctx))) return st;
+    ctx->staleMask |= kForce | kEnergy;
+    ctx->forcesValid = true;
+    if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a force became NaN or infinite");
+    return FEMMD_OK;
+}
+
+femmd_status femmd_zero_stuff(femmd_ctx *ctx) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    size_t N = ctx->pos.size();
+    if (N) {
+        CK(cudaMemsetAsync(ctx->dacc.p, 0, N * sizeof(float2), ctx->stream));
+        CK(cudaMemsetAsync(ctx->dforce.p, 0, N * sizeof(float2), ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->staleMask |= kAcc | kForce;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_sync(femmd_ctx *ctx) {
+    NEED(ctx);
+    if (ctx->stream) CK(cudaStreamSynchronize(ctx->stream));
+    return FEMMD_OK;
+}
+
+int femmd_get_num_particles(const femmd_ctx *ctx) { return ctx ? (int)ctx->pos.size() : 0; }
+int femmd_get_num_bonds(const femmd_ctx *ctx) { return ctx ? (int)ctx->r0.size() : 0; }
+int femmd_get_num_triangles(const femmd_ctx *ctx) { return ctx ? (int)ctx->refVol.size() : 0; }
+int femmd_get_num_elastomers(const femmd_ctx *ctx) { return ctx ? (int)ctx->clusters.size() : 0; }
+int femmd_get_steps(const femmd_ctx *ctx) { return ctx ? ctx->steps : 0; }
+
+static femmd_status copy2(femmd_ctx *ctx, const std::vector<float2> &v, float *out) {
+    if (!out) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    if (!v.empty()) memcpy(out, v.data(), v.size() * sizeof(float2));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_positions(femmd_ctx *ctx, float *out) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kPos))) return st;
+    return copy2(ctx, ctx->pos, out);
+}
+femmd_status femmd_get_velocities(femmd_ctx *ctx, float *out) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kVel))) return st;
+    return copy2(ctx, ctx->vel, out);
+}
+femmd_status femmd_get_accelerations(femmd_ctx *ctx, float *out) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kAcc))) return st;
+    return copy2(ctx, ctx->acc, out);
+}
+femmd_status femmd_get_forces(femmd_ctx *ctx, float *out) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kForce))) return st;
+    return copy2(ctx, ctx->force, out);
+}
+femmd_status femmd_get_particle_energies(femmd_ctx *ctx, float *out) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kEnergy))) return st;
+    if (!out) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    if (!ctx->energy.empty()) memcpy(out, ctx->energy.data(), ctx->energy.size() * sizeof(float));
+    return FEMMD_OK;
+}
+femmd_status femmd_get_masses(const femmd_ctx *ctx, float *out) {
+    if (!ctx || !out) return FEMMD_INVALID_ARG;
+    if (!ctx->mass.empty()) memcpy(out, ctx->mass.data(), ctx->mass.size() * sizeof(float));
+    return FEMMD_OK;
+}
+femmd_status femmd_get_bonds(const femmd_ctx *ctx, int *pairs, float *rl) {
+    if (!ctx) return FEMMD_INVALID_ARG;
+    if (pairs && !ctx->bond.empty()) memcpy(pairs, ctx->bond.data(), ctx->bond.size() * sizeof(int));
+    if (rl && !ctx->r0.empty()) memcpy(rl, ctx->r0.data(), ctx->r0.size() * sizeof(float));
+    return FEMMD_OK;
+}
+femmd_status femmd_get_triangles(const femmd_ctx *ctx, int *tris, float *xm, float *area) {
+    if (!ctx) return FEMMD_INVALID_ARG;
+    if (tris && !ctx->tri.empty()) memcpy(tris, ctx->tri.data(), ctx->tri.size() * sizeof(int));
+    if (xm && !ctx->xm.empty()) memcpy(xm, ctx->xm.data(), ctx->xm.size() * sizeof(float));
+    if (area && !ctx->refVol.empty()) memcpy(area, ctx->refVol.data(), ctx->refVol.size() * sizeof(float));
+    return FEMMD_OK;
+}
+femmd_status femmd_get_exclusion_groups(const femmd_ctx *ctx, int *out) {
+    if (!ctx || !out) return FEMMD_INVALID_ARG;
+    if (!ctx->excl.empty()) memcpy(out, ctx->excl.data(), ctx->excl.size() * sizeof(int));
+    return FEMMD_OK;
+}
+femmd_status femmd_get_reference_positions(const femmd_ctx *ctx, float *out) {
+    if (!ctx || !out) return FEMMD_INVALID_ARG;
+    if (!ctx->refPos.empty()) memcpy(out, ctx->refPos.data(), ctx->refPos.size() * sizeof(float2));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_energies(femmd_ctx *ctx, double *out) {
+    NEED(ctx);
+    if (!out) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    if (!ctx->sc.p) {
+        for (int k = 0; k < 6; k++) out[k] = 0;
+        return FEMMD_OK;
+    }
+    femmd_status st;
+    if ((st = read_scalars(ctx))) return st;
+    const DevScalars &h = *ctx->hsc;
+    out[0] = h.U;
+    out[1] = h.W;
+    out[2] = h.KE;
+    out[3] = h.vvMax;
+    out[4] = h.dispHi;
+    out[5] = h.totalUpdates;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_step_observables(femmd_ctx *ctx, double *out, int max_rows, int *rows) {
+    NEED(ctx);
+    if (!rows) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    int n = std::min(ctx->obsRows, std::max(max_rows, 0));
+    *rows = ctx->obsRows;
+    if (n > 0 && out) {
+        CK(cudaMemcpyAsync(out, ctx->obs.p, (size_t)n * kObsCols * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_grid(const femmd_ctx *ctx, int *ncx, int *ncy) {
+    if (!ctx || !ncx || !ncy) return FEMMD_INVALID_ARG;
+    *ncx = ctx->ncx;
+    *ncy = ctx->ncy;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_cells(femmd_ctx *ctx, int *cell_start, int *cell_ids) {
+    NEED(ctx);
+    if (!ctx->listBuilt) return fail(ctx, FEMMD_NOT_READY, "no neighbour list has been built");
+    const int N = (int)ctx->pos.size();
+    if (cell_start)
+        CK(cudaMemcpyAsync(cell_start, ctx->cellStart.p, (ctx->ncells + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    if (cell_ids && N)
+        CK(cudaMemcpyAsync(cell_ids, ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_neighbor_total(femmd_ctx *ctx, long long *total) {
+    NEED(ctx);
+    if (!total) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    if (!ctx->listBuilt) return fail(ctx, FEMMD_NOT_READY, "no neighbour list has been built");
+    femmd_status st;
+    if ((st = read_scalars(ctx))) return st;
+    *total = (long long)ctx->hsc->nbrSum;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) {
+    NEED(ctx);
+    if (!ctx->listBuilt) return fail(ctx, FEMMD_NOT_READY, "no neighbour list has been built");
+    const int N = (int)ctx->pos.size();
+    std::vector<int> cnt(N);
+    std::vector<int> raw((size_t)ctx->nbrCap * ctx->Ncap);
+    if (N) {
+        CK(cudaMemcpyAsync(cnt.data(), ctx->nbrCount.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(raw.data(), ctx->nbr.p, raw.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    long long k = 0;
+    for (int i = 0; i < N; i++) {
+        if (nbr_start) nbr_start[i] = (int)k;
+        int c = std::min(cnt[i], ctx->nbrCap);
+        for (int q = 0; q < c; q++) {
+            if (nbr_list) nbr_list[k] = raw[(size_t)q * ctx->Ncap + i] & kIdMask;
+            k++;
+        }
+    }
+    if (nbr_start) nbr_start[N] = (int)k;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_nn_stats(femmd_ctx *ctx, double *mean_neighbors, int *max_neighbors, long long *builds) {
+    NEED(ctx);
+    femmd_status st;
+    if (!ctx->sc.p) return fail(ctx, FEMMD_NOT_READY, "nothing has run");
+    if ((st = read_scalars(ctx))) return st;
+    int N = (int)ctx->pos.size();
+    if (mean_neighbors) *mean_neighbors = N ? (double)ctx->hsc->nbrSum / N : 0.0;
+    if (max_neighbors) *max_neighbors = ctx->hsc->maxCount;
+    if (builds) *builds = (long long)ctx->hsc->builds;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_info(const femmd_ctx *ctx, double *o) {
+    if (!ctx || !o) return FEMMD_INVALID_ARG;
+    o[0] = (double)ctx->pos.size();
+    o[1] = (double)ctx->clusters.size();
+    o[2] = (double)ctx->bond.size();  // bondList.size() as the reference reports (2 per bond)
+    o[3] = (double)ctx->refVol.size();
+    o[4] = ctx->dt;
+    o[5] = ctx->kBond;
+    o[6] = ctx->kArea;
+    o[7] = ctx->E;
+    o[8] = ctx->Lx;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_state(femmd_ctx *ctx, const float *p, const float *v) {
+    NEED(ctx);
+    femmd_status st;
+    const size_t N = ctx->pos.size();
+    if (!ctx->topoDirty && !ctx->stateDirty && ctx->stream && N) {
+        // device copy current: copy the caller's arrays straight to the device;
+        // the host copies become stale.  The next run starts with a forced rebuild.
+        float2 *pd = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+        if (p) CK(cudaMemcpyAsync(pd, p, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+        if (v) CK(cudaMemcpyAsync(ctx->dvel.p, v, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->listBuilt = false;
+        if (p) ctx->staleMask |= kPos;
+        if (v) ctx->staleMask |= kVel;
+        return FEMMD_OK;
+    }
+    if ((st = download_state(ctx, kAll))) return st;
+    if (p) memcpy(ctx->pos.data(), p, N * sizeof(float2));
+    if (v) memcpy(ctx->vel.data(), v, N * sizeof(float2));
+    ctx->stateDirty = true;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_state(femmd_ctx *ctx, float *p, float *v, float *a) {
+    NEED(ctx);
+    const size_t N = ctx->pos.size();
+    if (!N) return FEMMD_OK;
+    // device-current arrays go straight into the caller's buffers
+    unsigned dev = ctx->staleMask;
+    cudaStream_t s = ctx->stream;
+    if (p) {
+        if (dev & kPos)
+            CK(cudaMemcpyAsync(p, ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        else
+            memcpy(p, ctx->pos.data(), N * sizeof(float2));
+    }
+    if (v) {
+        if (dev & kVel) CK(cudaMemcpyAsync(v, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        else memcpy(v, ctx->vel.data(), N * sizeof(float2));
+    }
+    if (a) {
+        if (dev & kAcc) CK(cudaMemcpyAsync(a, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        else memcpy(a, ctx->acc.data(), N * sizeof(float2));
+    }
+    if (dev && s) CK(cudaStreamSynchronize(s));
+    return FEMMD_OK;
+}
+
+void *femmd_get_stream(femmd_ctx *ctx) {
+    if (!ctx) return nullptr;
+    if (ensure_stream(ctx) != FEMMD_OK) return nullptr;
+    return (void *)ctx->stream;
+}
+
+femmd_status femmd_event_record(femmd_ctx *ctx, int slot) {
+    NEED(ctx);
+    if (slot < 0 || slot >= 64) return fail(ctx, FEMMD_INVALID_ARG, "event slot outside [0, 64)");
+    femmd_status st;
+    if ((st = ensure_stream(ctx))) return st;
+    if (!ctx->userEvents[slot]) CK(cudaEventCreate(&ctx->userEvents[slot]));
+    CK(cudaEventRecord(ctx->userEvents[slot], ctx->stream));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_event_elapsed(femmd_ctx *ctx, int a, int b, float *ms) {
+    NEED(ctx);
+    if (a < 0 || a >= 64 || b < 0 || b >= 64 || !ms || !ctx->userEvents[a] || !ctx->userEvents[b])
+        return fail(ctx, FEMMD_INVALID_ARG, "unrecorded event slot");
+    CK(cudaEventSynchronize(ctx->userEvents[b]));
+    CK(cudaEventElapsedTime(ms, ctx->userEvents[a], ctx->userEvents[b]));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile) {
+    NEED(ctx);
+    ctx->profiling = profile != 0;
+    ctx->profForceMs = ctx->profRebuildMs = 0;
+    ctx->profForceLaunches = ctx->profRebuilds = ctx->profKernels = 0;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_profile(femmd_ctx *ctx, double *fms, long long *fl, double *rms, long long *rb,
+                               long long *kl) {
+    NEED(ctx);
+    if (fms) *fms = ctx->profForceMs;
+    if (fl) *fl = ctx->profForceLaunches;
+    if (rms) *rms = ctx->profRebuildMs;
+    if (rb) *rb = ctx->profRebuilds;
+    if (kl) *kl = ctx->profKernels;
+    return FEMMD_OK;
+}
+
+}  // extern "C"

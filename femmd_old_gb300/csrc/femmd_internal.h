@@ -1,0 +1,115 @@
+// femmd_internal.h -- device data layout and kernel launch interface of the
+// GB300 femmd2D timestep.  Shared by the kernel translation units and the
+// host context (femmd_api.cu).
+//
+// HBM layout (structure of arrays, one context per system):
+//   pos[2]  float2[N]    ping-pong positions (a step reads one, writes the other)
+//   vel     float2[N]    half-step velocity between fused step kernels
+//   acc     float2[N]    acceleration (written by the last step of a run)
+//   mass    float[N], typeId int[N], sigma float[N] (only when sigma varies inside a type)
+//   excl    int[N]       exclusion group (-1 = none)
+//   cells   cellStart[ncells+1], cellSorted float4[N] = (x, y, id|type<<27, excl)
+//   nbr     int[cap][Ncap] neighbour-major list (entry = id | type<<27), nbrCount[N]
+//   bonds   per-particle incidence CSR (bStart, bEnt = {partner|sign<<31, r0 bits})
+//   tris    triIdx int4[nt], triGeo float4[2nt] (neo-Hookean: Bm, vol0; Green: xm rows 1-2, area),
+//           tStart/tEnt vertex->triangle incidence (t*4+slot), triF float2[3nt] per-step nodal forces
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace femmd {
+
+constexpr int kIdBits = 27;
+constexpr int kIdMask = (1 << kIdBits) - 1;
+constexpr int kMaxTypes = 32;
+constexpr int kBlock = 256;        // threads per block of the per-particle kernels
+constexpr int kScanBlock = 1024;   // cells per block of the cell-start scan
+constexpr int kObsCols = 6;        // per-step observable row: U, W, sum m v^2, max v^2, dispHi, rebuilt
+
+// Per type-pair constants, all formed on the host with the reference's float
+// operations (interactionsCuda.cu:43-55, 79-88) so that the kernel's per-pair
+// arithmetic reproduces the reference bit for bit.
+struct PairEntry {
+    float rcut2;  // (rc*rc)*sigma_ij*sigma_ij      (sigma by type)
+    float sig2;   // sigma_ij*sigma_ij              (sigma by type)
+    float c;      // 48*eps/(sigma_ij*sigma_ij)     (sigma by type)
+    float eps4;   // 4*eps
+    float us;     // uShift
+    float rc;     // rc (units of sigma_ij)
+    float eps48;  // 48*eps
+    float pad;
+};
+
+struct DevScalars {
+    double U, W, KE, Ufea;          // last force evaluation (FP64)
+    float vvMax, dispHi;
+    int rebuild, totalUpdates;
+    unsigned int ticket, triTicket;
+    int overflow, nonfinite, maxCount, obsRow;
+    int maxCand, pad0;
+    unsigned long long nbrSum, builds;
+};
+
+enum StepMode { MODE_FORCES = 0, MODE_FIRST = 1, MODE_MID = 2, MODE_LAST = 3, MODE_INIT = 4 };
+
+struct DevSys {
+    int N, Ncap;
+    int wrapx, wrapy;
+    float Lx, Ly, dt, hdt;
+    double halfSkin;
+    int ncx, ncy, ncells;
+    float nnRadiusSq;
+    int imageExact;
+    int numTypes, sigmaByType;
+    const PairEntry *pair;
+    float2 *pos0, *pos1;
+    float2 *vel, *acc, *forceOut;
+    float *energyOut;
+    const float *mass, *sigma;
+    const int *typeId, *excl;
+    int *cellOf, *rank, *cellCount, *cellStart, *blockSums, *sortedIds;
+    float4 *cellSorted;
+    int *nbr, *nbrCount;
+    int nbrCap;
+    int nBonded, bondForces, feaForces, feaLaw, bondKMode;
+    const int *bStart;
+    const int2 *bEnt;
+    const int *tStart;
+    const int *tEnt;
+    int ntri;
+    const int4 *triIdx;
+    const float4 *triGeo;
+    float2 *triF;
+    float *triE;
+    const float2 *refPos;
+    float kBond, E, mu, lambda, C1, C2, C3;
+    double *partials;      // 3 doubles per force block
+    float *partialsMax;    // 1 float per force block
+    double *triPartials;   // 1 double per triangle block
+    DevScalars *sc;
+    double *obs;
+    int obsCap;
+};
+
+// Kernel launch sink: direct stream launches, or nodes appended to a CUDA
+// graph (optionally inside an IF body).  Implemented in femmd_api.cu.
+struct Launch;
+
+// ---- neighbour list (k_nn.cu)
+// Cell binning + Verlet list on the positions of buffer 'parity'.  With
+// check_flag the kernels return at once unless sc->rebuild is set.
+cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check_flag);
+// Run start (NeighborList::update(1), nn.cpp:114-134): forced rebuild,
+// dispHi = 0, totalUpdates = 1, per-step observable rows restart.
+cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
+
+// ---- forces + integration (k_force.cu)
+cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
+// leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
+cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
+
+int force_blocks(int N);
+int tri_blocks(int ntri);
+int scan_blocks(int ncells);
+
+}  // namespace femmd

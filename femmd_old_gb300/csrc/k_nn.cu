@@ -1,0 +1,248 @@
+// k_nn.cu -- cell binning and Verlet neighbour lists on the GPU.
+//
+// Reference path: updateCellsCPU / updateCellsGPU (femmd2D/src/nn.cpp:8-20,
+// nnCuda.cu:69-82) and buildNNCPUSerial / buildNNGPUKernel (nn.cpp:22-62,
+// nnCuda.cu:84-135), driven by NeighborList::update (nn.cpp:114-134).
+//
+// Binning is an integer counting sort: warp-aggregated atomic histogram
+// (one atomicAdd per distinct cell in a warp, found with __match_any_sync),
+// exclusive scan of the counts into cellStart, scatter to the slots, then a
+// per-cell sort by particle id.  The result is deterministic and is the
+// reference CPU's order (ascending id inside a cell), and it has no per-cell
+// capacity (the reference's cellContent[c*maxPPC+k] has one and never checks
+// it).  Each cell's particles are also copied into cellSorted as
+// (x, y, id|type<<27, excl) so the list build streams contiguous float4s.
+//
+// The list build visits the 3x3 cells in the reference's order (cx outer,
+// cy inner, both axes wrapped as applyCellBC does, nnCuda.cu:26-36), keeps
+// j != i outside i's exclusion group with the reference's float
+// dr2 <= (rc+skin)^2, and writes the neighbour-major layout nbr[k*Ncap + i]
+// (coalesced for the force kernel).  Counts beyond the capacity raise an
+// overflow flag; the host grows the list and repeats the steps.
+#include "femmd_internal.h"
+#include "launch.h"
+#include "device_common.cuh"
+
+namespace femmd {
+
+__global__ void k_run_start(DevSys s) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        DevScalars *c = s.sc;
+        c->rebuild = 1;
+        c->dispHi = 0.0f;
+        c->totalUpdates = 1;
+        c->obsRow = 0;
+        c->ticket = 0;
+        c->triTicket = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_cells_count(DevSys s, int parity, int check) {
+    if (check && !s.sc->rebuild) return;
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = i < s.N;
+    unsigned active = __ballot_sync(0xffffffffu, act);
+    if (!act) return;
+    float2 p = pos[i];
+    int c = cell_of(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
+    s.cellOf[i] = c;
+    unsigned peers = __match_any_sync(active, c);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&s.cellCount[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    s.rank[i] = base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// per-block totals of kScanBlock cell counts
+__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(DevSys s, int check) {
+    if (check && !s.sc->rebuild) return;
+    __shared__ int red[32];
+    int c = blockIdx.x * kScanBlock + threadIdx.x;
+    int v = c < s.ncells ? s.cellCount[c] : 0;
+    v = warp_sum_int(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int w = red[threadIdx.x];
+        w = warp_sum_int(w);
+        if (threadIdx.x == 0) s.blockSums[blockIdx.x] = w;
+    }
+}
+
+// exclusive scan -> cellStart; counts are cleared for the next binning
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(DevSys s, int nblocks, int check) {
+    if (check && !s.sc->rebuild) return;
+    __shared__ int wsum[32];
+    __shared__ int prefix;
+    int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // prefix of earlier blocks (fixed order)
+    int acc = 0;
+    for (int b = t; b < blockIdx.x; b += kScanBlock) acc += s.blockSums[b];
+    acc = warp_sum_int(acc);
+    if (lane == 0) wsum[warp] = acc;
+    __syncthreads();
+    if (t == 0) {
+        int p = 0;
+        for (int w = 0; w < kScanBlock / 32; w++) p += wsum[w];
+        prefix = p;
+    }
+    __syncthreads();
+    int c = blockIdx.x * kScanBlock + t;
+    int v = c < s.ncells ? s.cellCount[c] : 0;
+    // inclusive warp scan
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = wsum[lane];
+        int z = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
+        }
+        wsum[lane] = z - w;  // exclusive warp offsets
+    }
+    __syncthreads();
+    if (c < s.ncells) {
+        s.cellStart[c] = prefix + wsum[warp] + x - v;
+        s.cellCount[c] = 0;
+    }
+    if (blockIdx.x == nblocks - 1 && t == 0) {
+        s.cellStart[s.ncells] = s.N;
+        s.sc->nbrSum = 0ull;
+        s.sc->maxCount = 0;
+        s.sc->maxCand = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter(DevSys s, int check) {
+    if (check && !s.sc->rebuild) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.N) return;
+    s.sortedIds[s.cellStart[s.cellOf[i]] + s.rank[i]] = i;
+}
+
+// ascending id inside each cell + the cell-ordered float4 copy
+__global__ void __launch_bounds__(kBlock) k_cell_sort(DevSys s, int parity, int check) {
+    if (check && !s.sc->rebuild) return;
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int cand = 0;
+    if (c < s.ncells) {
+        int b = s.cellStart[c], e = s.cellStart[c + 1], n = e - b;
+        int *ids = s.sortedIds + b;
+        // insertion sort (cells hold a handful of particles)
+        for (int k = 1; k < n; k++) {
+            int v = ids[k];
+            int m = k - 1;
+            while (m >= 0 && ids[m] > v) {
+                ids[m + 1] = ids[m];
+                m--;
+            }
+            ids[m + 1] = v;
+        }
+        for (int k = 0; k < n; k++) {
+            int id = ids[k];
+            float2 p = pos[id];
+            int tag = id | (s.numTypes > 1 ? (s.typeId[id] << kIdBits) : 0);
+            s.cellSorted[b + k] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[id]));
+        }
+        // candidate count of the 3x3 stencil (capacity sizing)
+        int cy = c / s.ncx, cx = c - cy * s.ncx;
+        for (int dx = -1; dx <= 1; dx++)
+            for (int dy = -1; dy <= 1; dy++) {
+                int nx = cx + dx, ny = cy + dy;
+                if (nx < 0) nx = s.ncx - 1; else if (nx == s.ncx) nx = 0;
+                if (ny < 0) ny = s.ncy - 1; else if (ny == s.ncy) ny = 0;
+                int nc = nx + ny * s.ncx;
+                cand += s.cellStart[nc + 1] - s.cellStart[nc];
+            }
+    }
+    cand = warp_max_int(cand);
+    if ((threadIdx.x & 31) == 0 && cand > 0) atomicMax(&s.sc->maxCand, cand);
+}
+
+__global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int check) {
+    if (check && !s.sc->rebuild) return;
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int k = 0;
+    if (i < s.N) {
+        const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap, Ncap = s.Ncap;
+        const bool wx = s.wrapx, wy = s.wrapy;
+        const float Lx = s.Lx, Ly = s.Ly, R2 = s.nnRadiusSq;
+        int c = s.cellOf[i];
+        int cy0 = c / ncx, cx0 = c - cy0 * ncx;
+        float2 p = pos[i];
+        int gi = s.excl[i];
+        int *out = s.nbr + i;
+        for (int dx = -1; dx <= 1; dx++) {
+            int nx = cx0 + dx;
+            if (nx < 0) nx = ncx - 1; else if (nx == ncx) nx = 0;
+            for (int dy = -1; dy <= 1; dy++) {
+                int ny = cy0 + dy;
+                if (ny < 0) ny = ncy - 1; else if (ny == ncy) ny = 0;
+                int nc = nx + ny * ncx;
+                int qb = __ldg(s.cellStart + nc), qe = __ldg(s.cellStart + nc + 1);
+                for (int q = qb; q < qe; q++) {
+                    float4 e = __ldg(s.cellSorted + q);
+                    int tag = __float_as_int(e.z);
+                    int j = tag & kIdMask;
+                    int gj = __float_as_int(e.w);
+                    if (j != i && (gi == -1 || gj == -1 || gi != gj)) {
+                        float dxr, dxo, dyr, dyo;
+                        image_axis(p.x, e.x, Lx, wx, false, dxr, dxo);
+                        image_axis(p.y, e.y, Ly, wy, false, dyr, dyo);
+                        float dr2 = dxr * dxr + dyr * dyr;
+                        if (dr2 <= R2) {
+                            if (k < cap) out[(size_t)k * Ncap] = tag;
+                            k++;
+                        }
+                    }
+                }
+            }
+        }
+        s.nbrCount[i] = k;
+    }
+    // build statistics and overflow
+    int kmax = warp_max_int(k);
+    int ksum = warp_sum_int(k);
+    if ((threadIdx.x & 31) == 0) {
+        if (ksum) atomicAdd(&s.sc->nbrSum, (unsigned long long)ksum);
+        if (kmax > 0) atomicMax(&s.sc->maxCount, kmax);
+        if (kmax > s.nbrCap) atomicOr(&s.sc->overflow, 1);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
+}
+
+int scan_blocks(int ncells) { return (ncells + kScanBlock - 1) / kScanBlock; }
+
+cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
+    cudaError_t e;
+    int pb = (s.N + kBlock - 1) / kBlock;
+    int nsb = scan_blocks(s.ncells);
+    int cb = (s.ncells + kBlock - 1) / kBlock;
+    if ((e = L.kernel(k_cells_count, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
+    if ((e = L.kernel(k_scan_blocks, dim3(nsb), dim3(kScanBlock), 0, s, check))) return e;
+    if ((e = L.kernel(k_scan_apply, dim3(nsb), dim3(kScanBlock), 0, s, nsb, check))) return e;
+    if ((e = L.kernel(k_scatter, dim3(pb), dim3(kBlock), 0, s, check))) return e;
+    if ((e = L.kernel(k_cell_sort, dim3(cb), dim3(kBlock), 0, s, parity, check))) return e;
+    if ((e = L.kernel(k_build_nn, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_run_start(Launch &L, const DevSys &s) {
+    return L.kernel(k_run_start, dim3(1), dim3(32), 0, s);
+}
+
+}  // namespace femmd

@@ -1,0 +1,208 @@
+/*
+ * femmd.h -- C ABI of the GB300-native femmd2D timestep (libfemmd.so).
+ *
+ * One opaque context per simulated system (the reference keeps one global
+ * MDSystem, femmd2D/src/interface.cpp:19).  Setup calls copy their inputs into
+ * the context's host arrays, exactly as the reference's System.* / c_* calls
+ * copy into its thrust host vectors; femmd_allocate_cuda / femmd_run upload
+ * them and all compute runs on the context's own CUDA stream with
+ * hand-written sm_103a kernels.  There is no CPU compute path: every force,
+ * list and integration call needs a GPU and reports FEMMD_CUDA_ERROR without
+ * one.
+ *
+ * Every call returns a femmd_status (0 = OK).  femmd_last_error() gives the
+ * message of the last failure; nothing calls exit() or traps.
+ *
+ * Index conventions follow the reference: particles are numbered in
+ * insertion order, elastomer triangle files are 1-based (add_elastomer),
+ * create_bond takes 0-based particle ids.  Arrays of 2-vectors are
+ * interleaved x,y float32.
+ */
+#ifndef FEMMD_H
+#define FEMMD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct femmd_ctx femmd_ctx;
+
+typedef enum {
+    FEMMD_OK = 0,
+    FEMMD_INVALID_ARG = 1,        /* bad index, size, order or value */
+    FEMMD_CAPACITY_OVERFLOW = 2,  /* a capacity could not be grown */
+    FEMMD_NONFINITE = 3,          /* a force or energy became NaN/inf */
+    FEMMD_CUDA_ERROR = 4,         /* a CUDA call failed (no GPU, OOM, ...) */
+    FEMMD_TIMEOUT = 5,            /* reserved: bounded device wait expired */
+    FEMMD_NOT_READY = 6,          /* call order: e.g. run before init_neighbor_list */
+    FEMMD_UNSUPPORTED = 7         /* feature of the reference outside this path */
+} femmd_status;
+
+enum { FEMMD_NOPBC = 0, FEMMD_XPBC = 1, FEMMD_XYPBC = 2 };      /* PBCTYPE, femmd2D/src/def.h:41 */
+enum { FEMMD_FEA_NEO_HOOKEAN = 0, FEMMD_FEA_GREEN_LINEAR = 1 }; /* interactions.cpp:532 / interactionsCuda.cu:312 */
+enum { FEMMD_BONDK_KBOND = 0, FEMMD_BONDK_E_OVER_R0 = 1 };      /* interactions.cpp:161 / interactionsCuda.cu:238 */
+enum { FEMMD_IMAGE_REFERENCE = 0, FEMMD_IMAGE_EXACT = 1 };
+enum { FEMMD_ELASTOMER_BONDS_ALL = 0, FEMMD_ELASTOMER_BONDS_BOUNDARY = 1, FEMMD_ELASTOMER_BONDS_NONE = 2 };
+
+/* ----------------------------------------------------------- lifecycle */
+/* MDSystem(0) + setDevice(GPU): femmd2D/src/md3dsystem.h:58-84.  device is the CUDA ordinal. */
+femmd_status femmd_create(int device, femmd_ctx **out);
+void femmd_destroy(femmd_ctx *ctx);
+const char *femmd_last_error(const femmd_ctx *ctx);
+/* Library version string. */
+const char *femmd_version(void);
+
+/* --------------------------------------------------- setup (System.*) */
+/* System.init(Lx, Ly): interface.cpp:229 -> MDSystem::init md3dsystem.cpp:49-80 */
+femmd_status femmd_init(femmd_ctx *ctx, double Lx, double Ly);
+/* System.reset(): interface.cpp:237 -> MDSystem::reset md3dsystem.cpp:82-89 */
+femmd_status femmd_reset(femmd_ctx *ctx);
+/* System.set_box / get_box: interface.cpp:411-427 */
+femmd_status femmd_set_box(femmd_ctx *ctx, double Lx, double Ly);
+femmd_status femmd_get_box(const femmd_ctx *ctx, double *Lx, double *Ly);
+/* System.PBC(0|1|2): interface.cpp:353-363 */
+femmd_status femmd_set_pbc(femmd_ctx *ctx, int pbc);
+/* System.DEV(0|1): interface.cpp:344-351.  Recorded; compute always runs on the GPU. */
+femmd_status femmd_set_dev(femmd_ctx *ctx, int dev);
+/* System.set_dt / get_dt: interface.cpp:400-409 */
+femmd_status femmd_set_dt(femmd_ctx *ctx, double dt);
+femmd_status femmd_get_dt(const femmd_ctx *ctx, double *dt);
+/* System.set_numTypes(n): interface.cpp:436-441 */
+femmd_status femmd_set_num_types(femmd_ctx *ctx, int n);
+/* System.set_pair_potential(eps, rc, ushift), n*n row-major each: interface.cpp:493-531 ->
+ * Interactions::setPairForce interactions.cpp:65-79 (rc in units of sigma_ij). */
+femmd_status femmd_set_pair_potential(femmd_ctx *ctx, const double *eps, const double *rc, const double *ushift,
+                                      int n2);
+/* System.set_kBond(k): interface.cpp:455-465 (k <= 0 disables bonds) */
+femmd_status femmd_set_kbond(femmd_ctx *ctx, double k);
+/* System.set_youngs_modulus(E): interface.cpp:479-490 (E <= 0 disables FEA) */
+femmd_status femmd_set_youngs_modulus(femmd_ctx *ctx, double E);
+/* Interactions::nu (C++ only in the reference, interactions.h:22; default 0.3) */
+femmd_status femmd_set_poisson_ratio(femmd_ctx *ctx, double nu);
+/* System.set_gravity / set_kArea: interface.cpp:443-453, 467-477.  Values > 0
+ * enable forces outside this build's hot path and return FEMMD_UNSUPPORTED. */
+femmd_status femmd_set_gravity(femmd_ctx *ctx, double g);
+femmd_status femmd_set_karea(femmd_ctx *ctx, double k);
+/* NeighborList::setSkin (C++ only, nn.h:64; default 0.4) */
+femmd_status femmd_set_skin(femmd_ctx *ctx, double skin);
+/* Neighbour-list capacity per particle (0 = size from the first build).  A
+ * build that exceeds it makes femmd_run roll back to the run's start, grow the
+ * list and repeat; the reference's fixed maxNeighborsPerParticle
+ * (nn.cpp:223-224) is never checked. */
+femmd_status femmd_set_neighbor_capacity(femmd_ctx *ctx, int cap);
+femmd_status femmd_get_neighbor_capacity(const femmd_ctx *ctx, int *cap);
+/* Law and convention selectors (defaults: neo-Hookean, kBond, exact image).
+ * FEMMD_IMAGE_REFERENCE reproduces the reference's float minimum image
+ * bit for bit; FEMMD_IMAGE_EXACT rounds a cross-boundary difference once. */
+femmd_status femmd_set_fea_law(femmd_ctx *ctx, int law);
+femmd_status femmd_set_bond_k_mode(femmd_ctx *ctx, int mode);
+femmd_status femmd_set_image_mode(femmd_ctx *ctx, int mode);
+/* Which edges of each later add_elastomer become bonds (default: every
+ * triangle edge, interior edges twice, as particles.cpp:335-337). */
+femmd_status femmd_set_elastomer_bonds(femmd_ctx *ctx, int mode);
+
+/* System.add_particle(x, y, vx, vy, m, sig, typ): interface.cpp:243-254 -> particles.cpp:226 */
+femmd_status femmd_add_particle(femmd_ctx *ctx, double x, double y, double vx, double vy, double m, double sig,
+                                int typ);
+/* n calls of femmd_add_particle, one per array element */
+femmd_status femmd_add_particles(femmd_ctx *ctx, int n, const double *x, const double *y, const double *vx,
+                                 const double *vy, const double *m, const double *sig, const int *typ);
+/* System.add_elastomer(verts, tris, x, y, typ, g, sig, mass, exclude): interface.cpp:533-563 ->
+ * Particles::addElastomer particles.cpp:295-385.  verts: nv (x,y) float32; tris: nt 1-based int32 triples.
+ * All elastomers must share one mesh and precede free particles (reference constraint). */
+femmd_status femmd_add_elastomer(femmd_ctx *ctx, const float *verts, int nv, const int *tris, int nt, double x,
+                                 double y, int typ, int g, double sig, double mass, int exclude);
+/* c_createBond(i, j): interface.cpp:67 -> Bonds::createBond bonds.cpp:14-29 */
+femmd_status femmd_create_bond(femmd_ctx *ctx, int i, int j);
+/* System.set_velocities(v0): interface.cpp:337-342 -> particles.cpp:233-261, with a caller seed
+ * instead of rand(): random directions, speed v0, zero net momentum. */
+femmd_status femmd_set_velocities(femmd_ctx *ctx, double v0, uint64_t seed);
+
+/* System.allocate_cuda(): interface.cpp:256 -> MDSystem::allocateCuda md3dsystem.h:86-94 */
+femmd_status femmd_allocate_cuda(femmd_ctx *ctx);
+/* System.init_neighbor_list(): interface.cpp:261 -> NeighborList::init nn.cpp:192-227 */
+femmd_status femmd_init_neighbor_list(femmd_ctx *ctx);
+
+/* --------------------------------------------------------- stepping */
+/* System.run(n): interface.cpp:267 -> Integrator::run integrator.cpp:31-57.  Returns when done. */
+femmd_status femmd_run(femmd_ctx *ctx, int steps);
+/* c_doStep(): interface.cpp:73 -> Integrator::doStep integrator.cpp:8-29 (one step, no
+ * forced rebuild, no initial force pass; needs a prior run or calc_forces). */
+femmd_status femmd_do_step(femmd_ctx *ctx);
+/* c_calcForces() after c_zeroStuff(): interface.cpp:69-71 -> Interactions::calcForces
+ * interactions.cpp:83-109 on the current positions and neighbour list. */
+femmd_status femmd_calc_forces(femmd_ctx *ctx);
+/* c_zeroStuff(): interface.cpp:69 -> Integrator::zeroStuff integrator.cpp:146-162 */
+femmd_status femmd_zero_stuff(femmd_ctx *ctx);
+/* NeighborList::buildNN nn.cpp:137-143 on the current positions (no dispHi change) */
+femmd_status femmd_build_neighbor_list(femmd_ctx *ctx);
+/* Wait for all queued work of the context. */
+femmd_status femmd_sync(femmd_ctx *ctx);
+
+/* ---------------------------------------------------------- getters */
+/* c_getNumberOfParticles / c_getNumberOfBonds: interface.cpp:41-42 */
+int femmd_get_num_particles(const femmd_ctx *ctx);
+int femmd_get_num_bonds(const femmd_ctx *ctx);
+int femmd_get_num_triangles(const femmd_ctx *ctx);
+int femmd_get_num_elastomers(const femmd_ctx *ctx);
+int femmd_get_steps(const femmd_ctx *ctx);
+/* c_getPosPtr / c_getVelPtr (interface.cpp:43-44) as copies: out holds 2N floats */
+femmd_status femmd_get_positions(femmd_ctx *ctx, float *out);
+femmd_status femmd_get_velocities(femmd_ctx *ctx, float *out);
+femmd_status femmd_get_accelerations(femmd_ctx *ctx, float *out);
+/* Forces of the last calc_forces (2N floats). */
+femmd_status femmd_get_forces(femmd_ctx *ctx, float *out);
+/* Per-particle potential energy of the last calc_forces (N floats): bond energy on the
+ * bond's first particle, triangle energy split in thirds, LJ u/2 per ordered pair. */
+femmd_status femmd_get_particle_energies(femmd_ctx *ctx, float *out);
+femmd_status femmd_get_masses(const femmd_ctx *ctx, float *out);
+/* c_getBondsPtr (interface.cpp:45) as a copy: 2*nbonds ints, and nbonds rest lengths */
+femmd_status femmd_get_bonds(const femmd_ctx *ctx, int *pairs, float *rest_lengths);
+/* triangles (3*nt 0-based global ids), their [1 X Y] inverses (9*nt) and signed areas (nt) */
+femmd_status femmd_get_triangles(const femmd_ctx *ctx, int *tris, float *xm, float *ref_area);
+femmd_status femmd_get_exclusion_groups(const femmd_ctx *ctx, int *out);
+femmd_status femmd_get_reference_positions(const femmd_ctx *ctx, float *out);
+/* Scalars of the last force evaluation in FP64: out[0]=U (potEnergy), out[1]=W (pair
+ * virial), out[2]=sum m v^2 (kinEneSum), out[3]=max v^2, out[4]=dispHi, out[5]=totalUpdates. */
+femmd_status femmd_get_energies(femmd_ctx *ctx, double *out);
+/* Per-step observables of the last run: rows of (U, W, sum m v^2, max v^2, dispHi, rebuilt). */
+femmd_status femmd_get_step_observables(femmd_ctx *ctx, double *out, int max_rows, int *rows);
+/* Cell grid and cell lists of the last neighbour build: grid (ncx, ncy); cell_start has
+ * ncx*ncy+1 entries, cell_ids N entries (ascending particle id inside a cell). */
+femmd_status femmd_get_grid(const femmd_ctx *ctx, int *ncx, int *ncy);
+femmd_status femmd_get_cells(femmd_ctx *ctx, int *cell_start, int *cell_ids);
+/* Neighbour lists of the last build in CSR: nbr_start N+1, nbr_list total entries in the
+ * reference's order.  femmd_get_neighbor_total gives the total. */
+femmd_status femmd_get_neighbor_total(femmd_ctx *ctx, long long *total);
+femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list);
+/* Build statistics: mean neighbours per particle at the last build and builds since init. */
+femmd_status femmd_get_nn_stats(femmd_ctx *ctx, double *mean_neighbors, int *max_neighbors, long long *builds);
+/* System.info(): interface.cpp:565-600 -> N, nelastomers, nbonds, ntrigs, dt, kBond, kArea, E, box */
+femmd_status femmd_info(const femmd_ctx *ctx, double *out9);
+
+/* ------------------------------------------------------- state I/O */
+/* Positions/velocities in (2N floats each, NULL = keep).  Marks the device copy stale. */
+femmd_status femmd_set_state(femmd_ctx *ctx, const float *pos, const float *vel);
+/* Copy positions/velocities/accelerations out (NULL = skip). */
+femmd_status femmd_get_state(femmd_ctx *ctx, float *pos, float *vel, float *acc);
+
+/* ------------------------------------------------- device-side access */
+/* The context's CUDA stream (cudaStream_t) for event timing by the caller. */
+void *femmd_get_stream(femmd_ctx *ctx);
+/* CUDA events on the context stream (slots 0..63) for device-side timing. */
+femmd_status femmd_event_record(femmd_ctx *ctx, int slot);
+femmd_status femmd_event_elapsed(femmd_ctx *ctx, int slot_a, int slot_b, float *ms);
+/* Launch each kernel directly (no CUDA graph) with CUDA events around the
+ * force kernel and return its summed time and launch count over the next
+ * femmd_run calls (profile != 0 starts a new tally). */
+femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile);
+femmd_status femmd_get_profile(femmd_ctx *ctx, double *force_kernel_ms, long long *force_kernel_launches,
+                               double *rebuild_ms, long long *rebuilds, long long *kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEMMD_H */
