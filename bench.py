@@ -58,7 +58,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS))
@@ -287,7 +287,8 @@ def ours(args, dist):
 
     # kernel launches inside the timed region
     has_tri = 1 if s.counts()["triangles"] else 0
-    launches = args.steps * (1 + 6 + (md + 1) * (1 + has_tri)) + 6 * rebuilds
+    rebuild_kernels = 7  # k_rebuild_begin, count, scan x2, scatter, cell sort, list build
+    launches = args.steps * (1 + rebuild_kernels + (md + 1) * (1 + has_tri)) + rebuild_kernels * rebuilds
 
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None

@@ -377,6 +377,9 @@ static femmd_status validate(femmd_ctx *ctx) {
             return fail(ctx, FEMMD_INVALID_ARG, "particle %d has type %d outside [0, %d)", i, ctx->type[i],
                         ctx->numTypes);
         if (!(ctx->mass[i] != 0.0f)) return fail(ctx, FEMMD_INVALID_ARG, "particle %d has zero mass", i);
+        if (!std::isfinite(ctx->pos[i].x) || !std::isfinite(ctx->pos[i].y) || !std::isfinite(ctx->vel[i].x) ||
+            !std::isfinite(ctx->vel[i].y))
+            return fail(ctx, FEMMD_INVALID_ARG, "particle %d has a non-finite position or velocity", i);
     }
     return FEMMD_OK;
 }
@@ -564,11 +567,13 @@ static femmd_status size_list(femmd_ctx *ctx, int min_cap) {
     s.nbrCap = 0;
     Launch L;
     L.stream = ctx->stream;
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
     CK(enqueue_rebuild(L, s, ctx->cur, 0));
     femmd_status st;
     if ((st = read_scalars(ctx))) return st;
+    if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a position is NaN or infinite");
     int need = ctx->hsc->maxCount + ctx->hsc->maxCount / 4 + 8;
-    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
     return alloc_list(ctx, std::max(need, min_cap));
 }
 
@@ -1135,6 +1140,7 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         if ((st = run_once(ctx, steps))) return st;
         if ((st = collect_profile(ctx))) return st;
         if ((st = read_scalars(ctx))) return st;
+        if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
         if (!ctx->hsc->overflow) {
             ctx->steps += steps;
             ctx->staleMask |= kPos | kVel | kAcc | kForce;
@@ -1189,9 +1195,11 @@ femmd_status femmd_build_neighbor_list(femmd_ctx *ctx) {
         DevSys s = make_sys(ctx);
         Launch L;
         L.stream = ctx->stream;
-        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, sizeof(int), ctx->stream));
+        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));  // overflow, nonfinite
         CK(enqueue_rebuild(L, s, ctx->cur, 0));
         if ((st = read_scalars(ctx))) return st;
+        if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a position is NaN or infinite");
+        if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
         if (!ctx->hsc->overflow) {
             ctx->listBuilt = true;
             ctx->totalBuilds = (long long)ctx->hsc->builds;

@@ -431,11 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                 o[5] = (double)reb;
             }
             sc->obsRow = row + 1;
-            if (reb) {
-                d = 0.0f;
-                sc->totalUpdates += 1;
-            }
-            sc->dispHi = d;
+            sc->dispHi = d;  // a rebuild (k_rebuild_begin) restarts it and counts the update
         } else {
             reb = (double)sc->dispHi > s.halfSkin;
         }

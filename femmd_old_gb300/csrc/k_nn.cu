@@ -25,15 +25,27 @@
 
 namespace femmd {
 
+// Integrator::run start: NeighborList::update(1) (nn.cpp:114-134) forces a
+// rebuild and leaves totalUpdates = 1, dispHi = 0; k_rebuild_begin of the
+// forced rebuild does the counting.
 __global__ void k_run_start(DevSys s) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         DevScalars *c = s.sc;
         c->rebuild = 1;
         c->dispHi = 0.0f;
-        c->totalUpdates = 1;
+        c->totalUpdates = 0;
         c->obsRow = 0;
         c->ticket = 0;
         c->triTicket = 0;
+    }
+}
+
+// The taken branch of NeighborList::update (nn.cpp:118-124): count the update
+// and restart the displacement accumulator.
+__global__ void k_rebuild_begin(DevSys s) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && s.sc->rebuild) {
+        s.sc->totalUpdates += 1;
+        s.sc->dispHi = 0.0f;
     }
 }
 
@@ -45,6 +57,9 @@ __global__ void __launch_bounds__(kBlock) k_cells_count(DevSys s, int parity, in
     unsigned active = __ballot_sync(0xffffffffu, act);
     if (!act) return;
     float2 p = pos[i];
+    // a non-finite position would land in a clamped edge cell; flag it so the
+    // per-cell sort and the list build (quadratic in a cell's size) are skipped
+    if (!(isfinite(p.x) && isfinite(p.y))) atomicOr(&s.sc->nonfinite, 1);
     int c = cell_of(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
     s.cellOf[i] = c;
     unsigned peers = __match_any_sync(active, c);
@@ -129,27 +144,36 @@ __global__ void __launch_bounds__(kBlock) k_scatter(DevSys s, int check) {
     if (check && !s.sc->rebuild) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.N) return;
-    s.sortedIds[s.cellStart[s.cellOf[i]] + s.rank[i]] = i;
+    int slot = s.cellStart[s.cellOf[i]] + s.rank[i];
+    if (slot >= 0 && slot < s.N)
+        s.sortedIds[slot] = i;
+    else
+        atomicOr(&s.sc->overflow, 2);  // inconsistent counts: never write outside the array
 }
 
 // ascending id inside each cell + the cell-ordered float4 copy
 __global__ void __launch_bounds__(kBlock) k_cell_sort(DevSys s, int parity, int check) {
-    if (check && !s.sc->rebuild) return;
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int cand = 0;
     if (c < s.ncells) {
         int b = s.cellStart[c], e = s.cellStart[c + 1], n = e - b;
         int *ids = s.sortedIds + b;
-        // insertion sort (cells hold a handful of particles)
-        for (int k = 1; k < n; k++) {
-            int v = ids[k];
-            int m = k - 1;
-            while (m >= 0 && ids[m] > v) {
-                ids[m + 1] = ids[m];
-                m--;
+        // Shell sort with gaps 3h+1 ending in insertion sort (a cell holds a
+        // handful of particles; the gaps bound the work of crowded cells)
+        int gap = 1;
+        while (gap < n / 3) gap = 3 * gap + 1;
+        for (; gap > 0; gap /= 3) {
+            for (int k = gap; k < n; k++) {
+                int v = ids[k];
+                int m = k - gap;
+                while (m >= 0 && ids[m] > v) {
+                    ids[m + gap] = ids[m];
+                    m -= gap;
+                }
+                ids[m + gap] = v;
             }
-            ids[m + 1] = v;
         }
         for (int k = 0; k < n; k++) {
             int id = ids[k];
@@ -173,7 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(DevSys s, int parity, int 
 }
 
 __global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int check) {
-    if (check && !s.sc->rebuild) return;
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int k = 0;
@@ -232,6 +256,7 @@ cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
     int pb = (s.N + kBlock - 1) / kBlock;
     int nsb = scan_blocks(s.ncells);
     int cb = (s.ncells + kBlock - 1) / kBlock;
+    if (check && (e = L.kernel(k_rebuild_begin, dim3(1), dim3(32), 0, s))) return e;
     if ((e = L.kernel(k_cells_count, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     if ((e = L.kernel(k_scan_blocks, dim3(nsb), dim3(kScanBlock), 0, s, check))) return e;
     if ((e = L.kernel(k_scan_apply, dim3(nsb), dim3(kScanBlock), 0, s, nsb, check))) return e;

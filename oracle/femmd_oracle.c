@@ -895,7 +895,12 @@ static void image_axis_d(float a, float b, float L, int wraps, double *out) {
     *out = e;
 }
 
-static double tri_neo_hookean_d(const orc *s, int t, double *f) {
+/* Condition scales: for every float expression the sum of the magnitudes of
+ * its operands, propagated through the formula.  |fp32 - fp64| of a correctly
+ * evaluated expression is bounded by a small multiple of eps_f32 times this
+ * scale, whatever cancellation the result suffers. */
+
+static double tri_neo_hookean_d(const orc *s, int t, double *f, double *cf, double *cu) {
     int p0 = s->tri[3 * t], p1 = s->tri[3 * t + 1], p2 = s->tri[3 * t + 2];
     float L = s->Lx, Ly = s->Ly;
     float dx01 = s->px[p0] - s->px[p1], dx02 = s->px[p0] - s->px[p2];
@@ -924,10 +929,24 @@ static double tri_neo_hookean_d(const orc *s, int t, double *f) {
     f[2] = -vol0 * (P00 * B10 + P01 * B11);
     f[3] = -vol0 * (P10 * B10 + P11 * B11);
     f[4] = -f[0] - f[2]; f[5] = -f[1] - f[3];
+    /* condition: |F| entries carry |Ds||Bm| (the entries are differences of
+     * positions, each with magnitude |x|); P carries mu(|F|+|F^-T|)+|lam lnJ||F^-T| */
+    double aF00 = fabs(Ds00) * fabs(B00) + fabs(Ds01) * fabs(B10), aF10 = fabs(Ds10) * fabs(B00) + fabs(Ds11) * fabs(B10);
+    double aF01 = fabs(Ds00) * fabs(B01) + fabs(Ds01) * fabs(B11), aF11 = fabs(Ds10) * fabs(B01) + fabs(Ds11) * fabs(B11);
+    double al = fabs(lam * lJ) + mu;
+    double c00 = mu * aF00 + al * fabs(i00), c10 = mu * aF10 + al * fabs(i01);
+    double c01 = mu * aF01 + al * fabs(i10), c11 = mu * aF11 + al * fabs(i11);
+    double av = fabs(vol0);
+    double h00 = av * (c00 * fabs(B00) + c01 * fabs(B01)), h10 = av * (c10 * fabs(B00) + c11 * fabs(B01));
+    double h01 = av * (c00 * fabs(B10) + c01 * fabs(B11)), h11 = av * (c10 * fabs(B10) + c11 * fabs(B11));
+    cf[0] = sqrt(h00 * h00 + h10 * h10);
+    cf[1] = sqrt(h01 * h01 + h11 * h11);
+    cf[2] = cf[0] + cf[1];
+    *cu = av * (0.5 * mu * (aF00 * aF00 + aF10 * aF10 + aF01 * aF01 + aF11 * aF11 + 2) + mu * fabs(lJ) + 0.5 * fabs(lam) * lJ * lJ);
     return pe * vol0;
 }
 
-static double tri_green_d(const orc *s, int t, double *f) {
+static double tri_green_d(const orc *s, int t, double *f, double *cf, double *cu) {
     int p[3] = {s->tri[3 * t], s->tri[3 * t + 1], s->tri[3 * t + 2]};
     float L = s->Lx, Ly = s->Ly;
     double rx[3], ry[3], X[3], Y[3];
@@ -939,41 +958,51 @@ static double tri_green_d(const orc *s, int t, double *f) {
     if (dy01 > Ly / 2.0f) ry[1] += Ly; if (dy01 < -Ly / 2.0f) ry[1] -= Ly;
     if (dy02 > Ly / 2.0f) ry[2] += Ly; if (dy02 < -Ly / 2.0f) ry[2] -= Ly;
     double vol = fabs(0.5 * ((Y[2] - Y[0]) * (X[1] - X[0]) - (Y[1] - Y[0]) * (X[2] - X[0])));
-    /* gradient rows of inverse([1 X Y]) computed in double */
     double det = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0]);
     double gx[3] = {(Y[1] - Y[2]) / det, (Y[2] - Y[0]) / det, (Y[0] - Y[1]) / det};
     double gy[3] = {(X[2] - X[1]) / det, (X[0] - X[2]) / det, (X[1] - X[0]) / det};
-    double a1 = 0, a2 = 0, b1 = 0, b2 = 0;
+    double a1 = 0, a2 = 0, b1 = 0, b2 = 0, A1 = 0, A2 = 0, B1 = 0, B2 = 0;
     for (int j = 0; j < 3; j++) {
         double ux = rx[j] - X[j], uy = ry[j] - Y[j];
+        double Ux = fabs(rx[j]) + fabs(X[j]), Uy = fabs(ry[j]) + fabs(Y[j]);
         a1 += gx[j] * ux; a2 += gy[j] * ux; b1 += gx[j] * uy; b2 += gy[j] * uy;
+        A1 += fabs(gx[j]) * Ux; A2 += fabs(gy[j]) * Ux; B1 += fabs(gx[j]) * Uy; B2 += fabs(gy[j]) * Uy;
     }
     double e00 = a1 + 0.5 * (a1 * a1 + b1 * b1), e11 = b2 + 0.5 * (a2 * a2 + b2 * b2);
     double e01 = 0.5 * (a2 + b1 + a1 * a2 + b1 * b2);
-    double c1 = s->Cxxxx, c2 = s->Cxxyy, c3 = s->Cxyxy;
+    double E00 = A1 + 0.5 * (A1 * A1 + B1 * B1), E11 = B2 + 0.5 * (A2 * A2 + B2 * B2);
+    double E01 = 0.5 * (A2 + B1 + A1 * A2 + B1 * B2);
+    double c1 = s->Cxxxx, c2 = s->Cxxyy, c3 = s->Cxyxy, k1 = fabs(c1), k2 = fabs(c2), k3 = fabs(c3);
     double pes = c1 * (e00 * e00 + e11 * e11) + 2 * c2 * e00 * e11 + 4 * c3 * e01 * e01;
     for (int i = 0; i < 3; i++) {
-        double m1 = gx[i], m2 = gy[i];
+        double m1 = gx[i], m2 = gy[i], n1 = fabs(m1), n2 = fabs(m2);
         double fxs = -2 * c1 * e00 * m1 * (1 + a1) - 2 * c1 * e11 * m2 * a2 - 2 * c2 * e00 * m2 * a2 - 2 * c2 * e11 * m1 * (1 + a1) -
                      4 * c3 * e01 * m2 * (1 + a1) - 4 * c3 * e01 * m1 * a2;
         double fys = -2 * c1 * e00 * m1 * b1 - 2 * c1 * e11 * m2 * (1 + b2) - 2 * c2 * e00 * m2 * (1 + b2) - 2 * c2 * e11 * m1 * b1 -
                      4 * c3 * e01 * m1 * (1 + b2) - 4 * c3 * e01 * m2 * b1;
+        double cx = 2 * k1 * E00 * n1 * (1 + A1) + 2 * k1 * E11 * n2 * A2 + 2 * k2 * E00 * n2 * A2 + 2 * k2 * E11 * n1 * (1 + A1) +
+                    4 * k3 * E01 * n2 * (1 + A1) + 4 * k3 * E01 * n1 * A2;
+        double cy = 2 * k1 * E00 * n1 * B1 + 2 * k1 * E11 * n2 * (1 + B2) + 2 * k2 * E00 * n2 * (1 + B2) + 2 * k2 * E11 * n1 * B1 +
+                    4 * k3 * E01 * n1 * (1 + B2) + 4 * k3 * E01 * n2 * B1;
         f[2 * i] = fxs * vol;
         f[2 * i + 1] = fys * vol;
+        cf[i] = sqrt(cx * cx + cy * cy) * vol;
     }
+    *cu = vol * (k1 * (E00 * E00 + E11 * E11) + 2 * k2 * E00 * E11 + 4 * k3 * E01 * E01);
     return pes * vol;
 }
 
 /* FP64 forces on the current positions and neighbour list.
- * fx, fy: forces; scale: per-particle sum of |contribution| (the natural
- * floating-point error scale); ui: per-particle potential energy (bond
- * energy split 1/2-1/2, triangle energy 1/3 per vertex, LJ 1/2 per ordered
- * pair); out[0..3] = U, W, sum|u| terms, sum|w| terms. */
-void orc_forces_f64(const orc *s, double *fx, double *fy, double *scale, double *ui, double *out) {
+ * fx, fy: forces; cond: per-particle condition scale of the float force (sum
+ * over contributions of their operand magnitudes); ui: per-particle potential
+ * energy (bond energy on the bond's first particle, triangle energy 1/3 per
+ * vertex, LJ 1/2 per ordered pair); out[0..3] = U, W, condition scales of U
+ * and W. */
+void orc_forces_f64(const orc *s, double *fx, double *fy, double *cond, double *ui, double *out) {
     int N = s->N;
     int wx = (s->pbc == XYPBC || s->pbc == XPBC), wy = (s->pbc == XYPBC);
-    double U = 0, W = 0, Us = 0, Ws = 0;
-    for (int i = 0; i < N; i++) fx[i] = fy[i] = scale[i] = ui[i] = 0;
+    double U = 0, W = 0, Uc = 0, Wc = 0;
+    for (int i = 0; i < N; i++) fx[i] = fy[i] = cond[i] = ui[i] = 0;
     if (s->bondForces) {
         for (int l = 0; l < s->nb; l++) {
             int i = s->bond[2 * l], j = s->bond[2 * l + 1];
@@ -984,23 +1013,23 @@ void orc_forces_f64(const orc *s, double *fx, double *fy, double *scale, double 
             double k = s->bond_k_mode ? (double)s->E / r0 : (double)s->kBond;
             double kdr = -k * dl / r, f1 = kdr * dx, f2 = kdr * dy;
             fx[i] += f1; fy[i] += f2; fx[j] -= f1; fy[j] -= f2;
-            double fm = sqrt(f1 * f1 + f2 * f2);
-            scale[i] += fm; scale[j] += fm;
+            double c = fabs(k) * (r + r0) + fabs(kdr) * r;
+            cond[i] += c; cond[j] += c;
             double u = 0.5 * k * dl * dl;
-            U += u; Us += fabs(u); ui[i] += 0.5 * u; ui[j] += 0.5 * u;
+            U += u; Uc += 0.5 * fabs(k) * (r + r0) * (r + r0); ui[i] += u;
         }
     }
     if (s->feaForces) {
         for (int t = 0; t < s->ntri; t++) {
-            double f[6];
-            double e = s->fea_law ? tri_green_d(s, t, f) : tri_neo_hookean_d(s, t, f);
+            double f[6], cf[3], cu;
+            double e = s->fea_law ? tri_green_d(s, t, f, cf, &cu) : tri_neo_hookean_d(s, t, f, cf, &cu);
             for (int i = 0; i < 3; i++) {
                 int j = s->tri[3 * t + i];
                 fx[j] += f[2 * i]; fy[j] += f[2 * i + 1];
-                scale[j] += sqrt(f[2 * i] * f[2 * i] + f[2 * i + 1] * f[2 * i + 1]);
+                cond[j] += cf[i];
                 ui[j] += e / 3.0;
             }
-            U += e; Us += fabs(e);
+            U += e; Uc += cu;
         }
     }
     for (int pi = 0; pi < N; pi++) {
@@ -1020,13 +1049,15 @@ void orc_forces_f64(const orc *s, double *fx, double *fy, double *scale, double 
             double dr2 = dx * dx + dy * dy, c = 48.0 * eij / (sij * sij), d2i = sij * sij / dr2;
             double d6i = d2i * d2i * d2i, fc = c * d6i * (d6i - 0.5) * d2i;
             fx[pi] += fc * dx; fy[pi] += fc * dy;
-            scale[pi] += fabs(fc) * sqrt(dr2);
+            double fcc = fabs(c) * d6i * (d6i + 0.5) * d2i;
+            cond[pi] += fcc * sqrt(dr2);
             double u = 4.0 * eij * d6i * (d6i - 1.0) + (double)s->us[ti * nt + tj];
-            U += 0.5 * u; Us += fabs(0.5 * u); ui[pi] += 0.5 * u;
-            W += 0.5 * fc * dr2; Ws += fabs(0.5 * fc * dr2);
+            U += 0.5 * u; Uc += 0.5 * (4.0 * fabs(eij) * d6i * (d6i + 1.0) + fabs((double)s->us[ti * nt + tj]));
+            ui[pi] += 0.5 * u;
+            W += 0.5 * fc * dr2; Wc += 0.5 * fcc * dr2;
         }
     }
-    out[0] = U; out[1] = W; out[2] = Us; out[3] = Ws;
+    out[0] = U; out[1] = W; out[2] = Uc; out[3] = Wc;
 }
 
 /* ------------------------------------------------------------- accessors */
