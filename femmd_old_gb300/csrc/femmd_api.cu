@@ -107,7 +107,7 @@ struct femmd_ctx {
     bool topoDirty = true, stateDirty = true, forcesValid = false, listBuilt = false;
     unsigned staleMask = 0;  // host copies older than the device: bits of kPos..kEnergy
     int cur = 0;
-    int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1;
+    int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1, sigmaOne = 0;
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF;
     DBuf<float> dmass, dsigma, denergy, triE, partialsMax;
     DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, sortedIds, nbr, nbrCount, bStart, tStart,
@@ -301,6 +301,7 @@ static DevSys make_sys(femmd_ctx *c) {
     s.imageExact = c->imageMode == FEMMD_IMAGE_EXACT;
     s.numTypes = c->numTypes;
     s.sigmaByType = c->sigmaByType;
+    s.sigmaOne = c->sigmaOne;
     s.pair = c->pair.p;
     s.pos0 = c->dpos0.p;
     s.pos1 = c->dpos1.p;
@@ -415,6 +416,8 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
                 p.eps48 = 48.0f * e;
                 p.pad = 0.f;
             }
+        ctx->sigmaOne = ctx->sigmaByType;
+        for (const PairEntry &p : tab) ctx->sigmaOne = ctx->sigmaOne && p.sig2 == 1.0f;
         CK(ctx->pair.ensure(tab.size()));
         CK(cudaMemcpyAsync(ctx->pair.p, tab.data(), tab.size() * sizeof(PairEntry), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -428,7 +431,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
     CK(ctx->cellSorted.ensure(N)); CK(ctx->nbrCount.ensure(N));
     CK(ctx->cellCount.ensure(ctx->ncells)); CK(ctx->cellStart.ensure(ctx->ncells + 1));
     CK(ctx->blockSums.ensure(scan_blocks(ctx->ncells)));
-    int fb = force_blocks(N);
+    int fb = std::max(force_blocks(N), step_blocks(N));
     CK(ctx->partials.ensure(3 * (size_t)std::max(fb, 1))); CK(ctx->partialsMax.ensure(std::max(fb, 1)));
     CK(ctx->sc.ensure(1));
     cudaStream_t s = ctx->stream;

@@ -23,6 +23,7 @@ constexpr int kIdBits = 27;
 constexpr int kIdMask = (1 << kIdBits) - 1;
 constexpr int kMaxTypes = 32;
 constexpr int kBlock = 256;        // threads per block of the per-particle kernels
+constexpr int kStepBlock = 128;    // threads per block of the step kernel
 constexpr int kScanBlock = 1024;   // cells per block of the cell-start scan
 constexpr int kObsCols = 6;        // per-step observable row: U, W, sum m v^2, max v^2, dispHi, rebuilt
 
@@ -60,7 +61,7 @@ struct DevSys {
     int ncx, ncy, ncells;
     float nnRadiusSq;
     int imageExact;
-    int numTypes, sigmaByType;
+    int numTypes, sigmaByType, sigmaOne;  // sigmaOne: every sigma_ij^2 of the table is exactly 1
     const PairEntry *pair;
     float2 *pos0, *pos1;
     float2 *vel, *acc, *forceOut;
@@ -109,6 +110,7 @@ cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaG
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
 
 int force_blocks(int N);
+int step_blocks(int N);
 int tri_blocks(int ntri);
 int scan_blocks(int ncells);
 

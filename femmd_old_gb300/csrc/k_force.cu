@@ -28,6 +28,7 @@
 namespace femmd {
 
 int force_blocks(int N) { return (N + kBlock - 1) / kBlock; }
+int step_blocks(int N) { return (N + kStepBlock - 1) / kStepBlock; }
 int tri_blocks(int ntri) { return (ntri + kBlock - 1) / kBlock; }
 
 // ------------------------------------------------------------ triangles
@@ -205,11 +206,74 @@ __global__ void __launch_bounds__(kBlock) k_tri_forces(DevSys s, int parity) {
 
 // ------------------------------------------------------------ particles
 
-template <int MODE, bool MT, bool SG>
-__global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraphConditionalHandle h, int use_h) {
+// minImage on one axis with the wrap known at compile time.  Sets *wrapped
+// when the difference crossed the boundary (then the exact-image value can
+// differ from the reference float value).
+template <bool WRAP, bool EX>
+__device__ __forceinline__ float img(float a, float b, float L, float &ref, bool &wrapped) {
+    float d = a - b;
+    ref = d;
+    if (WRAP) {
+        if (d >= 0.5f * L) {
+            ref = d - L;
+            wrapped = true;
+            return EX ? ref + two_sum_err(a, -b, d) : ref;
+        }
+        if (d < -0.5f * L) {
+            ref = d + L;
+            wrapped = true;
+            return EX ? ref + two_sum_err(a, -b, d) : ref;
+        }
+    }
+    return d;
+}
+
+// One Lennard-Jones pair (pairForce/ljforce, interactionsCuda.cu:43-100) added
+// into the running force in list order.  Energy and virial are accumulated
+// doubled (u and fc*dr2 per ordered pair) and halved once per particle.
+template <bool MT, bool SG, bool WX, bool WY, bool EX, bool SIG1>
+__device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, const PairEntry &pe0, int ti, float si,
+                                        float2 pi, int tag, float2 pj, float &fx, float &fy, float &u2, float &w2) {
+    float dxr, dyr;
+    bool wrapped = false;
+    float dx = img<WX, EX>(pi.x, pj.x, s.Lx, dxr, wrapped);
+    float dy = img<WY, EX>(pi.y, pj.y, s.Ly, dyr, wrapped);
+    float dr2r = dxr * dxr + dyr * dyr;
+    const PairEntry &pe = MT ? tab[ti * s.numTypes + ((unsigned)tag >> kIdBits)] : pe0;
+    float rcut2, sig2, c;
+    if (SG) {
+        float sij = (si + __ldg(s.sigma + (tag & kIdMask))) / 2.0f;
+        rcut2 = pe.rc * pe.rc * sij * sij;
+        sig2 = sij * sij;
+        c = pe.eps48 / sig2;
+    } else {
+        rcut2 = pe.rcut2;
+        sig2 = pe.sig2;
+        c = pe.c;
+    }
+    if (dr2r < rcut2) {
+        float dr2 = (EX && wrapped) ? dx * dx + dy * dy : dr2r;
+        // sigma^2/dr2; with sigma_ij = 1 the IEEE quotient 1/dr2 is the
+        // correctly rounded reciprocal
+        float dr2i = SIG1 ? __frcp_rn(dr2) : sig2 / dr2;
+        float dr6i = dr2i * dr2i * dr2i;
+        float fc = c * dr6i * (dr6i - 0.5f) * dr2i;
+        fx += fc * dx;
+        fy += fc * dy;
+        u2 += pe.eps4 * dr6i * (dr6i - 1.0f) + pe.us;
+        w2 += fc * dr2;
+    }
+}
+
+template <bool MT, bool SG, bool WX, bool WY, bool EX, bool SIG1>
+__global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int parity, cudaGraphConditionalHandle h,
+                                                     int use_h) {
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
     extern __shared__ PairEntry tab[];  // numTypes^2 entries (1 without types)
+    __shared__ double red[3][kStepBlock / 32];
+    __shared__ float redm[kStepBlock / 32];
+    __shared__ bool amLast;
     const int nt = s.numTypes;
     if (MT) {
         for (int q = threadIdx.x; q < nt * nt; q += blockDim.x) tab[q] = s.pair[q];
@@ -223,7 +287,6 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
     bool bad = false;
     if (i < s.N) {
         const float2 pi = pin[i];
-        const bool wx = s.wrapx, wy = s.wrapy, ex = s.imageExact;
         const float Lx = s.Lx, Ly = s.Ly;
         float fx = 0.0f, fy = 0.0f;
         if (i < s.nBonded) {
@@ -237,9 +300,10 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                     const float r0 = __int_as_float(en.y);
                     const float2 pj = pin[j];
                     const float2 a = second ? pj : pi, b = second ? pi : pj;
-                    float dxr, dx, dyr, dy;
-                    image_axis(a.x, b.x, Lx, wx, ex, dxr, dx);
-                    image_axis(a.y, b.y, Ly, wy, ex, dyr, dy);
+                    float dxr, dyr;
+                    bool wr = false;
+                    float dx = img<WX, EX>(a.x, b.x, Lx, dxr, wr);
+                    float dy = img<WY, EX>(a.y, b.y, Ly, dyr, wr);
                     float r = sqrtf(dx * dx + dy * dy);
                     float dl = r - r0;
                     float k = s.bondKMode ? s.E / r0 : s.kBond;
@@ -248,7 +312,7 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                     if (!second) {
                         fx += f1;
                         fy += f2;
-                        ue += 0.5f * (k * dl * dl);
+                        ue += k * dl * dl;  // doubled like the pair terms
                     } else {
                         fx -= f1;
                         fy -= f2;
@@ -262,66 +326,41 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                     float2 f = s.triF[3 * (en >> 2) + (en & 3)];
                     fx += f.x;
                     fy += f.y;
-                    if (MODE == MODE_FORCES) utri += s.triE[en >> 2] / 3.0f;
+                    if (mode == MODE_FORCES) utri += s.triE[en >> 2] / 3.0f;
                 }
             }
         }
-        // pairForce over the Verlet list, list order
+        // pairForce over the Verlet list, in list order (next entry prefetched)
         {
             const int cnt = min(s.nbrCount[i], s.nbrCap);
             const int *__restrict__ lst = s.nbr + i;
-            const size_t stride = (size_t)s.Ncap;
+            const int stride = s.Ncap;
             const int ti = MT ? s.typeId[i] : 0;
             const float si = SG ? s.sigma[i] : 0.0f;
-            PairEntry pe0 = tab[0];
-            int k = 0;
+            const PairEntry pe0 = tab[0];
             int tag = cnt > 0 ? __ldg(lst) : 0;
-            for (; k < cnt; k++) {
-                const int tnext = (k + 1 < cnt) ? __ldg(lst + (size_t)(k + 1) * stride) : 0;
-                const int j = tag & kIdMask;
-                const float2 pj = pin[j];
-                float dxr, dx, dyr, dy;
-                image_axis(pi.x, pj.x, Lx, wx, ex, dxr, dx);
-                image_axis(pi.y, pj.y, Ly, wy, ex, dyr, dy);
-                float dr2r = dxr * dxr + dyr * dyr;
-                const PairEntry &pe = MT ? tab[ti * nt + ((unsigned)tag >> kIdBits)] : pe0;
-                float rcut2, sig2, c;
-                if (SG) {
-                    float sij = (si + __ldg(s.sigma + j)) / 2.0f;
-                    rcut2 = pe.rc * pe.rc * sij * sij;
-                    sig2 = sij * sij;
-                    c = pe.eps48 / sig2;
-                } else {
-                    rcut2 = pe.rcut2;
-                    sig2 = pe.sig2;
-                    c = pe.c;
-                }
-                if (dr2r < rcut2) {
-                    float dr2 = ex ? dx * dx + dy * dy : dr2r;
-                    float dr2i = sig2 / dr2;
-                    float dr6i = dr2i * dr2i * dr2i;
-                    float fc = c * dr6i * (dr6i - 0.5f) * dr2i;
-                    fx += fc * dx;
-                    fy += fc * dy;
-                    ue += (pe.eps4 * dr6i * (dr6i - 1.0f) + pe.us) * 0.5f;
-                    we += fc * dr2 * 0.5f;
-                }
+            for (int k = 1; k <= cnt; k++) {
+                lst += stride;
+                const int tnext = k < cnt ? __ldg(lst) : 0;
+                lj_pair<MT, SG, WX, WY, EX, SIG1>(s, tab, pe0, ti, si, pi, tag, pin[tag & kIdMask], fx, fy, ue, we);
                 tag = tnext;
             }
         }
+        ue *= 0.5f;
+        we *= 0.5f;
         bad = !(isfinite(fx) && isfinite(fy));
         const float m = s.mass[i];
         const float ax = fx / m, ay = fy / m;
         const float dt = s.dt, hdt = s.hdt;
-        if (MODE == MODE_FORCES) {
+        if (mode == MODE_FORCES) {
             s.forceOut[i] = make_float2(fx, fy);
             s.energyOut[i] = ue + utri;
-        } else if (MODE == MODE_INIT) {
+        } else if (mode == MODE_INIT) {
             s.acc[i] = make_float2(ax, ay);
             s.forceOut[i] = make_float2(fx, fy);
         } else {
             float2 v = s.vel[i];
-            if (MODE == MODE_MID || MODE == MODE_LAST) {
+            if (mode == MODE_MID || mode == MODE_LAST) {
                 // leapFrogStep2 then evalProps
                 v.x += hdt * ax;
                 v.y += hdt * ay;
@@ -329,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                 vvm = vv;
                 ke = m * vv;
             }
-            if (MODE == MODE_LAST) {
+            if (mode == MODE_LAST) {
                 s.vel[i] = v;
                 s.acc[i] = make_float2(ax, ay);
                 s.forceOut[i] = make_float2(fx, fy);
@@ -338,8 +377,8 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
                 v.x += hdt * ax;
                 v.y += hdt * ay;
                 float2 x = make_float2(pi.x + dt * v.x, pi.y + dt * v.y);
-                if (wx) x.x = wrap_coord(x.x, Lx);
-                if (wy) x.y = wrap_coord(x.y, Ly);
+                if (WX) x.x = wrap_coord(x.x, Lx);
+                if (WY) x.y = wrap_coord(x.y, Ly);
                 pout[i] = x;
                 s.vel[i] = v;
             }
@@ -347,13 +386,10 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
     }
 
     // ---- reductions: FP64 from warp level up, last block finishes in fixed order
-    __shared__ double red[3][kBlock / 32];
-    __shared__ float redm[kBlock / 32];
-    __shared__ bool amLast;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double du = warp_sum((double)ue), dw = warp_sum((double)we), dk = warp_sum((double)ke);
     float mx = warp_max(vvm);
     unsigned anybad = __ballot_sync(0xffffffffu, bad);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
         red[0][warp] = du;
         red[1][warp] = dw;
@@ -365,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
     if (threadIdx.x == 0) {
         double a = 0.0, b = 0.0, c = 0.0;
         float m = 0.0f;
-        for (int w = 0; w < kBlock / 32; w++) {
+        for (int w = 0; w < kStepBlock / 32; w++) {
             a += red[0][w];
             b += red[1][w];
             c += red[2][w];
@@ -376,57 +412,47 @@ __global__ void __launch_bounds__(kBlock) k_step(DevSys s, int parity, cudaGraph
         s.partials[3 * blockIdx.x + 2] = c;
         s.partialsMax[blockIdx.x] = m;
         __threadfence();
-        unsigned tk = atomicAdd(&s.sc->ticket, 1u);
-        amLast = (tk == gridDim.x - 1);
+        amLast = (atomicAdd(&s.sc->ticket, 1u) == gridDim.x - 1);
     }
     __syncthreads();
-    if (!amLast) return;
-    double a = 0.0, b = 0.0, c = 0.0;
-    float m = 0.0f;
-    for (int q = threadIdx.x; q < (int)gridDim.x; q += kBlock) {
-        a += __ldcg(s.partials + 3 * q + 0);
-        b += __ldcg(s.partials + 3 * q + 1);
-        c += __ldcg(s.partials + 3 * q + 2);
-        m = fmaxf(m, __ldcg(s.partialsMax + q));
+    if (!amLast || warp != 0) return;
+    __threadfence();
+    // the grid's last block: its first warp sums the block partials lane-strided,
+    // then the 32 lane sums in fixed order
+    double A = 0.0, B = 0.0, K = 0.0;
+    float vmax = 0.0f;
+    for (int q = lane; q < (int)gridDim.x; q += 32) {
+        A += __ldcg(s.partials + 3 * q + 0);
+        B += __ldcg(s.partials + 3 * q + 1);
+        K += __ldcg(s.partials + 3 * q + 2);
+        vmax = fmaxf(vmax, __ldcg(s.partialsMax + q));
     }
-    a = warp_sum(a);
-    b = warp_sum(b);
-    c = warp_sum(c);
-    m = warp_max(m);
-    __syncthreads();
+    double U = 0.0, W = 0.0, KE = 0.0;
+    float vm2 = 0.0f;
+    for (int w = 0; w < 32; w++) {
+        U += __shfl_sync(0xffffffffu, A, w);
+        W += __shfl_sync(0xffffffffu, B, w);
+        KE += __shfl_sync(0xffffffffu, K, w);
+        vm2 = fmaxf(vm2, __shfl_sync(0xffffffffu, vmax, w));
+    }
     if (lane == 0) {
-        red[0][warp] = a;
-        red[1][warp] = b;
-        red[2][warp] = c;
-        redm[warp] = m;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double U = 0.0, W = 0.0, K = 0.0;
-        float vmax = 0.0f;
-        for (int w = 0; w < kBlock / 32; w++) {
-            U += red[0][w];
-            W += red[1][w];
-            K += red[2][w];
-            vmax = fmaxf(vmax, redm[w]);
-        }
         DevScalars *sc = s.sc;
         if (s.feaForces && s.ntri > 0) U += sc->Ufea;
         sc->U = U;
         sc->W = W;
         int reb;
-        if (MODE == MODE_MID || MODE == MODE_LAST) {
-            sc->KE = K;
-            sc->vvMax = vmax;
-            float d = sc->dispHi + sqrtf(vmax) * s.dt;  // md3dsystem.cpp:177
-            reb = (double)d > s.halfSkin;                // nn.cpp:118
+        if (mode == MODE_MID || mode == MODE_LAST) {
+            sc->KE = KE;
+            sc->vvMax = vm2;
+            float d = sc->dispHi + sqrtf(vm2) * s.dt;  // md3dsystem.cpp:177
+            reb = (double)d > s.halfSkin;               // nn.cpp:118
             int row = sc->obsRow;
             if (s.obs && row < s.obsCap) {
                 double *o = s.obs + (size_t)row * kObsCols;
                 o[0] = U;
                 o[1] = W;
-                o[2] = K;
-                o[3] = (double)vmax;
+                o[2] = KE;
+                o[3] = (double)vm2;
                 o[4] = (double)d;
                 o[5] = (double)reb;
             }
@@ -458,16 +484,31 @@ __global__ void __launch_bounds__(kBlock) k_drift(DevSys s, int parity) {
     s.vel[i] = v;
 }
 
-template <int MODE>
-static cudaError_t launch_mode(Launch &L, const DevSys &s, int parity, cudaGraphConditionalHandle h, int use_h) {
-    dim3 g(force_blocks(s.N)), b(kBlock);
+template <bool MT, bool SG, bool WX, bool WY, bool EX, bool SIG1>
+static cudaError_t launch_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                               int use_h) {
+    dim3 g(step_blocks(s.N)), b(kStepBlock);
     size_t smt = sizeof(PairEntry) * (size_t)(s.numTypes > 1 ? s.numTypes * s.numTypes : 1);
-    if (s.numTypes > 1) {
-        if (s.sigmaByType) return L.kernel(k_step<MODE, true, false>, g, b, smt, s, parity, h, use_h);
-        return L.kernel(k_step<MODE, true, true>, g, b, smt, s, parity, h, use_h);
-    }
-    if (s.sigmaByType) return L.kernel(k_step<MODE, false, false>, g, b, smt, s, parity, h, use_h);
-    return L.kernel(k_step<MODE, false, true>, g, b, smt, s, parity, h, use_h);
+    return L.kernel(k_step<MT, SG, WX, WY, EX, SIG1>, g, b, smt, s, mode, parity, h, use_h);
+}
+
+template <bool MT, bool SG, bool WX, bool WY, bool EX>
+static cudaError_t pick_sig(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h) {
+    if (!SG && s.sigmaOne) return launch_step<MT, SG, WX, WY, EX, true>(L, s, mode, parity, h, use_h);
+    return launch_step<MT, SG, WX, WY, EX, false>(L, s, mode, parity, h, use_h);
+}
+
+template <bool MT, bool SG>
+static cudaError_t pick_image(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                              int use_h) {
+    const bool ex = s.imageExact;
+    if (s.wrapx && s.wrapy)
+        return ex ? pick_sig<MT, SG, true, true, true>(L, s, mode, parity, h, use_h)
+                  : pick_sig<MT, SG, true, true, false>(L, s, mode, parity, h, use_h);
+    if (s.wrapx)
+        return ex ? pick_sig<MT, SG, true, false, true>(L, s, mode, parity, h, use_h)
+                  : pick_sig<MT, SG, true, false, false>(L, s, mode, parity, h, use_h);
+    return pick_sig<MT, SG, false, false, false>(L, s, mode, parity, h, use_h);
 }
 
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h) {
@@ -476,13 +517,12 @@ cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaG
         if ((e = L.kernel(k_tri_forces, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, parity))) return e;
     }
     cudaEvent_t e0 = L.mark();
-    switch (mode) {
-    case MODE_FORCES: e = launch_mode<MODE_FORCES>(L, s, parity, h, use_h); break;
-    case MODE_FIRST: e = launch_mode<MODE_FIRST>(L, s, parity, h, use_h); break;
-    case MODE_MID: e = launch_mode<MODE_MID>(L, s, parity, h, use_h); break;
-    case MODE_LAST: e = launch_mode<MODE_LAST>(L, s, parity, h, use_h); break;
-    default: e = launch_mode<MODE_INIT>(L, s, parity, h, use_h); break;
-    }
+    if (s.numTypes > 1)
+        e = s.sigmaByType ? pick_image<true, false>(L, s, mode, parity, h, use_h)
+                          : pick_image<true, true>(L, s, mode, parity, h, use_h);
+    else
+        e = s.sigmaByType ? pick_image<false, false>(L, s, mode, parity, h, use_h)
+                          : pick_image<false, true>(L, s, mode, parity, h, use_h);
     cudaEvent_t e1 = L.mark();
     if (e0 && e1 && L.force_events) L.force_events->push_back({e0, e1});
     return e;
