@@ -91,6 +91,7 @@ SIGNATURES = {
     "femmd_event_elapsed": (i_, [P, i_, i_, fp]),
     "femmd_set_profiling": (i_, [P, i_]),
     "femmd_get_profile": (i_, [P, dp, llp, dp, llp, llp]),
+    "femmd_bin_cells_noalloc": (i_, [P, i_, d_, d_, i_, i_, P, P, P]),
 }
 
 _lib = None

@@ -202,6 +202,33 @@ femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile);
 femmd_status femmd_get_profile(femmd_ctx *ctx, double *force_kernel_ms, long long *force_kernel_launches,
                                double *rebuild_ms, long long *rebuilds, long long *kernel_launches);
 
+/* ------------------------------------------ cell binning without allocation */
+/* Limits of femmd_bin_cells_noalloc.  Its working memory is one fixed array of
+ * about 9 MB inside the library, which every GPU that loads the library holds
+ * until the process exits. */
+#define FEMMD_NOALLOC_MAX_PARTICLES (1 << 20)
+#define FEMMD_NOALLOC_MAX_CELLS (1 << 18)
+/* Bins n particles into the ncx x ncy cell grid of a (Lx, Ly) box exactly as
+ * the context's neighbour-list build does (the reference's cell ids, ascending
+ * particle id inside a cell), without allocating anything.  It has no
+ * counterpart in the reference.  It is meant for callers that cannot call
+ * cudaMalloc where they need the binning: code being captured into a CUDA
+ * graph (allocation is not permitted during capture) or running under a host
+ * framework that owns all device memory through its own pool (cudaMalloc and
+ * cudaFree would synchronise the device and bypass that pool).
+ * All pointers are device memory owned by the caller: d_pos holds 2n floats,
+ * d_cell_start receives ncx*ncy+1 ints, d_cell_ids receives n ints.  The work
+ * is enqueued on 'stream' (a cudaStream_t; NULL = the default stream) and the
+ * call returns without waiting.  n above FEMMD_NOALLOC_MAX_PARTICLES or
+ * ncx*ncy above FEMMD_NOALLOC_MAX_CELLS returns FEMMD_CAPACITY_OVERFLOW and
+ * does nothing.  The first call on a device looks up the device address of
+ * the working array (once per device, with that device current): make that
+ * first call before any stream capture.  Every call uses the same working
+ * array and leaves its contents behind, so calls that can overlap on the GPU
+ * (different streams without ordering between them) race. */
+femmd_status femmd_bin_cells_noalloc(const float *d_pos, int n, double Lx, double Ly, int ncx, int ncy,
+                                     int *d_cell_start, int *d_cell_ids, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
