@@ -91,6 +91,24 @@ __device__ __forceinline__ float own_logf(float x) {
     return (fk * ln2_lo + lm) + fk * ln2_hi;
 }
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// float -> kFixFrac fixed point; sets *bad when out of range or not finite
+__device__ __forceinline__ unsigned long long to_fixed(float x, bool &bad) {
+    if (!(fabsf(x) < 549755813888.0f)) {  // 2^39
+        bad = true;
+        return 0ull;
+    }
+    return (unsigned long long)__float2ll_rn(x * (float)(1 << kFixFrac));
+}
+__device__ __forceinline__ double from_fixed(unsigned long long v) {
+    return (double)(long long)v * (1.0 / (double)(1 << kFixFrac));
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

@@ -116,7 +116,7 @@ struct femmd_ctx {
     DBuf<int4> triIdx;
     DBuf<float4> triGeo, cellSorted;
     DBuf<PairEntry> pair;
-    DBuf<double> partials, triPartials, obs;
+    DBuf<double> partials, obs;
     DBuf<DevScalars> sc;
     DevScalars *hsc = nullptr;  // pinned mirror
     int obsCap = 0, obsRows = 0;
@@ -223,7 +223,7 @@ static void release_device(femmd_ctx *c) {
     c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->nbr.release();
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
-    c->partials.release(); c->triPartials.release(); c->obs.release(); c->sc.release();
+    c->partials.release(); c->obs.release(); c->sc.release();
     c->nbrCap = 0;
     c->obsCap = 0;
 }
@@ -347,7 +347,6 @@ static DevSys make_sys(femmd_ctx *c) {
     s.C3 = c->C3;
     s.partials = c->partials.p;
     s.partialsMax = c->partialsMax.p;
-    s.triPartials = c->triPartials.p;
     s.sc = c->sc.p;
     s.obs = c->obs.p;
     s.obsCap = c->obsCap;
@@ -500,7 +499,6 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         }
         CK(ctx->triIdx.ensure(ti.size())); CK(ctx->triGeo.ensure(tg.size()));
         CK(ctx->triF.ensure(3 * ti.size())); CK(ctx->triE.ensure(ti.size()));
-        CK(ctx->triPartials.ensure(std::max(tri_blocks(nt), 1)));
         CK(cudaMemcpyAsync(ctx->triIdx.p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     }

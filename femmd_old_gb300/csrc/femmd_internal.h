@@ -41,14 +41,22 @@ struct PairEntry {
     float pad;
 };
 
+// Energy sums are accumulated as 64-bit fixed point with kFixFrac fraction
+// bits: every block adds its partial with one integer atomicAdd, which is
+// exact and order-independent, so the totals are deterministic and no FP64
+// work sits on the per-step path (GB300's FP64 pipe is narrow).
+constexpr int kFixFrac = 24;
+
 struct DevScalars {
-    double U, W, KE, Ufea;          // last force evaluation (FP64)
+    double U, W, KE, Ufea;          // last force evaluation (FP64 from the fixed-point sums)
     float vvMax, dispHi;
     int rebuild, totalUpdates;
     unsigned int ticket, triTicket;
     int overflow, nonfinite, maxCount, obsRow;
     int maxCand, pad0;
     unsigned long long nbrSum, builds;
+    unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
+    unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
 };
 
 enum StepMode { MODE_FORCES = 0, MODE_FIRST = 1, MODE_MID = 2, MODE_LAST = 3, MODE_INIT = 4 };
@@ -84,9 +92,8 @@ struct DevSys {
     float *triE;
     const float2 *refPos;
     float kBond, E, mu, lambda, C1, C2, C3;
-    double *partials;      // 3 doubles per force block
-    float *partialsMax;    // 1 float per force block
-    double *triPartials;   // 1 double per triangle block
+    double *partials;      // 3 doubles per block (kept for diagnostics; the sums use fixed point)
+    float *partialsMax;
     DevScalars *sc;
     double *obs;
     int obsCap;

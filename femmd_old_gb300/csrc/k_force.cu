@@ -160,47 +160,30 @@ __device__ __forceinline__ float tri_green(const DevSys &s, const float2 *pos, i
 __global__ void __launch_bounds__(kBlock) k_tri_forces(DevSys s, int parity) {
     const float2 *pos = parity ? s.pos1 : s.pos0;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
+    float e = 0.0f;
     if (t < s.ntri) {
         float2 f[3];
-        float en;
         if (s.feaLaw == 0)
-            en = tri_neo_hookean(s, pos, t, f[0], f[1], f[2]);
+            e = tri_neo_hookean(s, pos, t, f[0], f[1], f[2]);
         else
-            en = tri_green(s, pos, t, f);
+            e = tri_green(s, pos, t, f);
         s.triF[3 * t + 0] = f[0];
         s.triF[3 * t + 1] = f[1];
         s.triF[3 * t + 2] = f[2];
-        s.triE[t] = en;
-        e = (double)en;
+        s.triE[t] = e;
     }
-    __shared__ double red[kBlock / 32];
-    __shared__ bool amLast;
-    e = warp_sum(e);
+    // triangle energies go straight into the potential-energy accumulator
+    __shared__ float red[kBlock / 32];
+    e = warp_sum_f(e);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double b = 0.0;
+        float b = 0.0f;
         for (int w = 0; w < kBlock / 32; w++) b += red[w];
-        s.triPartials[blockIdx.x] = b;
-        __threadfence();
-        unsigned tk = atomicAdd(&s.sc->triTicket, 1u);
-        amLast = (tk == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (amLast) {
-        double acc = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += kBlock) acc += __ldcg(s.triPartials + b);
-        acc = warp_sum(acc);
-        __syncthreads();
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double u = 0.0;
-            for (int w = 0; w < kBlock / 32; w++) u += red[w];
-            s.sc->Ufea = u;
-            s.sc->triTicket = 0;
-        }
+        bool bad = false;
+        unsigned long long q = to_fixed(b, bad);
+        if (bad) atomicOr(&s.sc->nonfinite, 2);
+        else if (q) atomicAdd(&s.sc->accU, q);
     }
 }
 
@@ -271,9 +254,8 @@ __global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int par
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
     extern __shared__ PairEntry tab[];  // numTypes^2 entries (1 without types)
-    __shared__ double red[3][kStepBlock / 32];
+    __shared__ float red[3][kStepBlock / 32];
     __shared__ float redm[kStepBlock / 32];
-    __shared__ bool amLast;
     const int nt = s.numTypes;
     if (MT) {
         for (int q = threadIdx.x; q < nt * nt; q += blockDim.x) tab[q] = s.pair[q];
@@ -385,85 +367,71 @@ __global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int par
         }
     }
 
-    // ---- reductions: FP64 from warp level up, last block finishes in fixed order
+    // ---- reductions: FP32 within the block, 64-bit fixed-point atomics across
+    // blocks (exact, order-independent); the last block converts and finishes.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double du = warp_sum((double)ue), dw = warp_sum((double)we), dk = warp_sum((double)ke);
+    float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke);
     float mx = warp_max(vvm);
     unsigned anybad = __ballot_sync(0xffffffffu, bad);
     if (lane == 0) {
-        red[0][warp] = du;
-        red[1][warp] = dw;
-        red[2][warp] = dk;
+        red[0][warp] = su;
+        red[1][warp] = sw;
+        red[2][warp] = sk;
         redm[warp] = mx;
         if (anybad) atomicOr(&s.sc->nonfinite, 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0, c = 0.0;
-        float m = 0.0f;
+        float a = 0.0f, b = 0.0f, c = 0.0f, m = 0.0f;
         for (int w = 0; w < kStepBlock / 32; w++) {
             a += red[0][w];
             b += red[1][w];
             c += red[2][w];
             m = fmaxf(m, redm[w]);
         }
-        s.partials[3 * blockIdx.x + 0] = a;
-        s.partials[3 * blockIdx.x + 1] = b;
-        s.partials[3 * blockIdx.x + 2] = c;
-        s.partialsMax[blockIdx.x] = m;
-        __threadfence();
-        amLast = (atomicAdd(&s.sc->ticket, 1u) == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!amLast || warp != 0) return;
-    __threadfence();
-    // the grid's last block: its first warp sums the block partials lane-strided,
-    // then the 32 lane sums in fixed order
-    double A = 0.0, B = 0.0, K = 0.0;
-    float vmax = 0.0f;
-    for (int q = lane; q < (int)gridDim.x; q += 32) {
-        A += __ldcg(s.partials + 3 * q + 0);
-        B += __ldcg(s.partials + 3 * q + 1);
-        K += __ldcg(s.partials + 3 * q + 2);
-        vmax = fmaxf(vmax, __ldcg(s.partialsMax + q));
-    }
-    double U = 0.0, W = 0.0, KE = 0.0;
-    float vm2 = 0.0f;
-    for (int w = 0; w < 32; w++) {
-        U += __shfl_sync(0xffffffffu, A, w);
-        W += __shfl_sync(0xffffffffu, B, w);
-        KE += __shfl_sync(0xffffffffu, K, w);
-        vm2 = fmaxf(vm2, __shfl_sync(0xffffffffu, vmax, w));
-    }
-    if (lane == 0) {
+        bool ob = false;
+        unsigned long long qa = to_fixed(a, ob), qb = to_fixed(b, ob), qc = to_fixed(c, ob);
         DevScalars *sc = s.sc;
-        if (s.feaForces && s.ntri > 0) U += sc->Ufea;
-        sc->U = U;
-        sc->W = W;
-        int reb;
-        if (mode == MODE_MID || mode == MODE_LAST) {
-            sc->KE = KE;
-            sc->vvMax = vm2;
-            float d = sc->dispHi + sqrtf(vm2) * s.dt;  // md3dsystem.cpp:177
-            reb = (double)d > s.halfSkin;               // nn.cpp:118
-            int row = sc->obsRow;
-            if (s.obs && row < s.obsCap) {
-                double *o = s.obs + (size_t)row * kObsCols;
-                o[0] = U;
-                o[1] = W;
-                o[2] = KE;
-                o[3] = (double)vm2;
-                o[4] = (double)d;
-                o[5] = (double)reb;
+        if (ob) atomicOr(&sc->nonfinite, 2);
+        if (qa) atomicAdd(&sc->accU, qa);
+        if (qb) atomicAdd(&sc->accW, qb);
+        if (qc) atomicAdd(&sc->accK, qc);
+        if (m > 0.0f) atomicMax(&sc->vvMaxBits, __float_as_uint(m));
+        __threadfence();
+        if (atomicAdd(&sc->ticket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            // the grid's last block: every block's atomics are visible
+            double U = from_fixed(atomicExch(&sc->accU, 0ull));
+            double W = from_fixed(atomicExch(&sc->accW, 0ull));
+            double KE = from_fixed(atomicExch(&sc->accK, 0ull));
+            float vm2 = __uint_as_float(atomicExch(&sc->vvMaxBits, 0u));
+            sc->U = U;
+            sc->W = W;
+            int reb;
+            if (mode == MODE_MID || mode == MODE_LAST) {
+                sc->KE = KE;
+                sc->vvMax = vm2;
+                float d = sc->dispHi + sqrtf(vm2) * s.dt;  // md3dsystem.cpp:177
+                reb = (double)d > s.halfSkin;               // nn.cpp:118
+                int row = sc->obsRow;
+                if (s.obs && row < s.obsCap) {
+                    double *o = s.obs + (size_t)row * kObsCols;
+                    o[0] = U;
+                    o[1] = W;
+                    o[2] = KE;
+                    o[3] = (double)vm2;
+                    o[4] = (double)d;
+                    o[5] = (double)reb;
+                }
+                sc->obsRow = row + 1;
+                sc->dispHi = d;  // a rebuild (k_rebuild_begin) restarts it and counts the update
+            } else {
+                reb = (double)sc->dispHi > s.halfSkin;
             }
-            sc->obsRow = row + 1;
-            sc->dispHi = d;  // a rebuild (k_rebuild_begin) restarts it and counts the update
-        } else {
-            reb = (double)sc->dispHi > s.halfSkin;
+            sc->rebuild = reb;
+            if (use_h) cudaGraphSetConditional(h, reb ? 1u : 0u);
+            sc->ticket = 0;
         }
-        sc->rebuild = reb;
-        if (use_h) cudaGraphSetConditional(h, reb ? 1u : 0u);
-        sc->ticket = 0;
     }
 }
 

@@ -37,6 +37,8 @@ __global__ void k_run_start(DevSys s) {
         c->obsRow = 0;
         c->ticket = 0;
         c->triTicket = 0;
+        c->accU = c->accW = c->accK = 0ull;
+        c->vvMaxBits = 0u;
     }
 }
 
