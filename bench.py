@@ -52,6 +52,9 @@ WORKLOADS = {
                    "WCA, phi=0.5, T=0.1, dt=0.002, skin 0.3", lambda: S.suspension()),
     "lj_fluid": ("plain LJ fluid: N=4096, rho=0.8, rc=2.5, skin 0.3, dt=0.005", lambda: S.lj_fluid()),
 }
+BATCHED_DESC = ("batched ensemble: 512 independent LJ+elastomer replicas, atom counts log-uniform in [500, 20000] "
+                "(seed 8), density U(0.6, 0.85) and T U(0.1, 1.5) (seed 9), 90 % solvent + hex-ring disks, "
+                "dt=0.005, skin 0.3, one persistent launch per run() under a CUDA graph, autotuned block shape")
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -61,7 +64,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -171,30 +174,46 @@ def cpu_baseline(sc, natoms, budget_s, threads):
 
 def reference_arm(args, dist):
     """--impl reference: the reference's CPU path as restated by the oracle
-    (the reference's own binary is x86-only here), all host threads."""
+    (the reference's own binary is x86-only here), all host threads.  For the
+    batched ensemble the replicas are advanced one after another (the
+    reference has no batched form) on a seeded sample of 8 replicas."""
     if dist.rank != 0:
         return None
-    desc, make = WORKLOADS[args.workload]
-    sc = make()
-    natoms = int(sc.meta["N"])
+    if args.workload == "batched":
+        desc = BATCHED_DESC
+        ens = S.batched_ensemble()
+        pick = np.random.Generator(np.random.PCG64(11)).choice(len(ens), size=8, replace=False)
+        scenes = [ens[int(r)] for r in sorted(pick)]
+    else:
+        desc, make = WORKLOADS[args.workload]
+        scenes = [make()]
+    natoms = sum(int(sc.meta["N"]) for sc in scenes)
     threads = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    o = O.Oracle(image_mode=0, log_mode=0, threads=threads)
-    sc.replay(o)
+    systems = []
+    for sc in scenes:
+        o = O.Oracle(image_mode=0, log_mode=0, threads=threads)
+        sc.replay(o)
+        systems.append(o)
     t0 = time.perf_counter()
-    o.run(1)
+    for o in systems:
+        o.run(1)
     per = time.perf_counter() - t0
     # each bench step: a run(m) sample sized so the whole K+W run stays ~2 minutes
     m = max(1, min(args.md_steps, int(120.0 / max(per, 1e-6) / max(args.steps + args.warmup, 1))))
     for _ in range(args.warmup):
-        o.run(m)
+        for o in systems:
+            o.run(m)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        o.run(m)
+        for o in systems:
+            o.run(m)
     dt = time.perf_counter() - t0
     value = natoms * m * args.steps / dt
+    what = (f"{len(scenes)} replicas ({natoms} atoms) each run({m}) in turn" if len(scenes) > 1 else
+            f"run({m}) of the {natoms}-atom system")
     return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -202,8 +221,8 @@ def reference_arm(args, dist):
             "config": {"workload": args.workload, "description": desc, "atoms": natoms, "md_steps_per_step": m,
                        "parallelism": "replicas"},
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"run({m}) per step of the {natoms}-atom system; the reference's own binary "
-                                       "(oracle/_ref) is built for x86 and cannot run on this host"},
+                             "sample": f"{what} per step; the reference's own binary (oracle/_ref) is built "
+                                       "for x86 and cannot run on this host"},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -327,7 +346,7 @@ def ours(args, dist):
     achieved = kbytes / (kms / 1e3) / 1e9
     traffic = load_traffic(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_step (fused LJ+bond+triangle gather, leapfrog, FP64 reductions)",
+                "traffic": traffic, "kernel": "k_step (fused LJ+bond+triangle gather, leapfrog, fixed-point energy sums)",
                 "algorithmic_bytes_per_launch": kbytes, "mean_launch_ms": kms,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
 
@@ -351,11 +370,104 @@ def ours(args, dist):
     return line
 
 
+def batched(args, dist):
+    """The ensemble advanced by femmd_batch_run (one persistent launch per
+    run() call), next to the same replicas advanced one by one through the
+    plain path (System.run per replica), on the same total atom count."""
+    import femmd_old_gb300 as F
+    import torch
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    scenes = S.batched_ensemble()
+    systems = []
+    b = F.Batch(dev)
+    for sc in scenes:
+        s = F.System(dev)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    natoms = sum(s.N for s in systems)
+    md = args.md_steps
+    b.run(0)
+    tune = b.autotune(20)
+    for _ in range(args.warmup):
+        b.run(md)
+    launch = b.launch()
+
+    dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(dev)
+    t_ms = 0.0
+    for k in range(args.steps):
+        b.event_record(0)
+        b.run(md)
+        b.event_record(1)
+        t_ms += b.event_elapsed_ms(0, 1)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    dist.barrier()
+    t_max = dist.max(t_ms)
+    value = natoms * md * args.steps * dist.world / (t_max / 1e3)
+    rebuilds = sum(s.total_updates() for s in systems)
+
+    # end to end: every replica's positions and velocities in from pinned host
+    # memory and out again around each batched run()
+    host = [(torch.empty((s.N, 2), dtype=torch.float32, pin_memory=True),
+             torch.empty((s.N, 2), dtype=torch.float32, pin_memory=True)) for s in systems]
+    for s, (hp, hv) in zip(systems, host):
+        s.get_state_ptr(hp.data_ptr(), hv.data_ptr())
+    dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        for s, (hp, hv) in zip(systems, host):
+            s.set_state_ptr(hp.data_ptr(), hv.data_ptr())
+        b.run(md)
+        for s, (hp, hv) in zip(systems, host):
+            s.get_state_ptr(hp.data_ptr(), hv.data_ptr())
+    torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = {"value": natoms * md * args.steps * dist.world / e2e_s, "unit": "atom-steps/s",
+           "h2d_bytes_per_step": 16 * natoms, "d2h_bytes_per_step": 16 * natoms}
+
+    # the plain form on the same replicas: one System.run per replica
+    md_plain = max(1, min(md, 100))
+    t0 = time.perf_counter()
+    for s in systems:
+        s.run(md_plain)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_value = natoms * md_plain / plain_s
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        # one mid-sized replica on the host, scaled by atoms
+        mid = sorted(range(len(scenes)), key=lambda r: scenes[r].meta["N"])[len(scenes) // 2]
+        cpu = cpu_baseline(scenes[mid], int(scenes[mid].meta["N"]), args.cpu_seconds, os.cpu_count() or 1)
+        cpu["sample"] = "median-size replica: " + cpu["sample"]
+    launches_per_run = 1
+    return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched", "description": BATCHED_DESC, "replicas": len(systems),
+                       "atoms": natoms, "md_steps_per_step": md, "launch": launch, "autotune": tune,
+                       "rebuilds_last_run": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",
+                       "l2": "inputs larger than L2 (512 replicas' state + lists > 129 MB)"},
+            "plain_same_atoms": {"value": plain_value, "unit": "atom-steps/s", "md_steps": md_plain,
+                                 "how": "System.run on each replica in turn, wall clock"},
+            "batched_over_plain": value / plain_value,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks}
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        line = reference_arm(args, dist) if args.impl == "reference" else ours(args, dist)
+        if args.impl == "reference":
+            line = reference_arm(args, dist)
+        elif args.workload == "batched":
+            line = batched(args, dist)
+        else:
+            line = ours(args, dist)
         if dist.rank == 0 and line is not None:
             print(json.dumps(line), flush=True)
     finally:

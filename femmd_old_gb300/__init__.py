@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from ._lib import FemmdError
 
-__all__ = ["System", "FemmdError", "read_file", "FILECONTENT", "DEV", "PBCTYPE", "lib"]
+__all__ = ["System", "Batch", "FemmdError", "read_file", "FILECONTENT", "DEV", "PBCTYPE", "lib"]
 
 DEV = {"CPU": 0, "GPU": 1}
 PBCTYPE = {"NOPBC": 0, "XPBC": 1, "XYPBC": 2}
@@ -351,6 +351,18 @@ class System:
         v = None if vel is None else np.ascontiguousarray(vel, np.float32).ravel()
         self._call("femmd_set_state", None if p is None else _f(p), None if v is None else _f(v))
 
+    def set_trace(self, on):
+        self._call("femmd_set_trace", int(bool(on)))
+
+    def trace(self):
+        """Per-step device timestamps (ns): tri start/end, step start/end, rebuild start/end."""
+        rows = C.c_int()
+        self._call("femmd_get_trace", None, 0, C.byref(rows))
+        o = np.zeros((rows.value, 6), np.uint64)
+        if rows.value:
+            self._call("femmd_get_trace", o.ctypes.data_as(C.POINTER(C.c_ulonglong)), rows.value, C.byref(rows))
+        return o
+
     def event_record(self, slot):
         self._call("femmd_event_record", int(slot))
 
@@ -385,3 +397,68 @@ class System:
 
     def dump_setup(self):
         self.__dict__.setdefault("dumps", []).append(("setup", self.setup_arrays()))
+
+
+class Batch:
+    """Many Systems advanced together in one persistent launch
+    (femmd_batch_*): run(n) does System.run(n) on every replica, with the same
+    results as running them one by one."""
+
+    def __init__(self, device: int = 0):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        st = self._L.femmd_batch_create(int(device), C.byref(h))
+        if st:
+            raise FemmdError(st, "batch create")
+        self._h = h
+        self.systems = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.femmd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        st = getattr(self._L, name)(self._h, *args)
+        if st != 0:
+            msg = self._L.femmd_batch_last_error(self._h)
+            raise FemmdError(st, msg.decode() if msg else "")
+
+    def add(self, system: "System") -> int:
+        idx = C.c_int()
+        self._call("femmd_batch_add", system._h, C.byref(idx))
+        self.systems.append(system)
+        return idx.value
+
+    def __len__(self):
+        return self._L.femmd_batch_size(self._h)
+
+    def run(self, n):
+        self._call("femmd_batch_run", int(n))
+
+    def set_launch(self, threads, ctas_per_sm):
+        self._call("femmd_batch_set_launch", int(threads), int(ctas_per_sm))
+
+    def launch(self):
+        t, c, k = C.c_int(), C.c_int(), C.c_int()
+        self._call("femmd_batch_get_launch", C.byref(t), C.byref(c), C.byref(k))
+        return dict(threads=t.value, ctas_per_sm=c.value, ctas=k.value)
+
+    def autotune(self, trial_steps=10):
+        t, c, ms = C.c_int(), C.c_int(), C.c_double()
+        self._call("femmd_batch_autotune", int(trial_steps), C.byref(t), C.byref(c), C.byref(ms))
+        return dict(threads=t.value, ctas_per_sm=c.value, trial_ms=ms.value)
+
+    def event_record(self, slot):
+        self._call("femmd_batch_event_record", int(slot))
+
+    def event_elapsed_ms(self, a, b):
+        ms = C.c_float()
+        self._call("femmd_batch_event_elapsed", int(a), int(b), C.byref(ms))
+        return ms.value

@@ -87,11 +87,24 @@ SIGNATURES = {
     "femmd_set_state": (i_, [P, fp, fp]),
     "femmd_get_state": (i_, [P, fp, fp, fp]),
     "femmd_get_stream": (P, [P]),
+    "femmd_set_trace": (i_, [P, i_]),
+    "femmd_get_trace": (i_, [P, C.POINTER(C.c_ulonglong), i_, ip]),
     "femmd_event_record": (i_, [P, i_]),
     "femmd_event_elapsed": (i_, [P, i_, i_, fp]),
     "femmd_set_profiling": (i_, [P, i_]),
     "femmd_get_profile": (i_, [P, dp, llp, dp, llp, llp]),
     "femmd_bin_cells_noalloc": (i_, [P, i_, d_, d_, i_, i_, P, P, P]),
+    "femmd_batch_create": (i_, [i_, C.POINTER(P)]),
+    "femmd_batch_destroy": (None, [P]),
+    "femmd_batch_last_error": (C.c_char_p, [P]),
+    "femmd_batch_add": (i_, [P, P, ip]),
+    "femmd_batch_size": (i_, [P]),
+    "femmd_batch_run": (i_, [P, i_]),
+    "femmd_batch_set_launch": (i_, [P, i_, i_]),
+    "femmd_batch_get_launch": (i_, [P, ip, ip, ip]),
+    "femmd_batch_autotune": (i_, [P, i_, ip, ip, dp]),
+    "femmd_batch_event_record": (i_, [P, i_]),
+    "femmd_batch_event_elapsed": (i_, [P, i_, i_, fp]),
 }
 
 _lib = None

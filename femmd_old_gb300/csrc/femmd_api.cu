@@ -21,6 +21,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -117,6 +118,8 @@ struct femmd_ctx {
     DBuf<float4> triGeo, cellSorted;
     DBuf<PairEntry> pair;
     DBuf<double> partials, obs;
+    DBuf<unsigned long long> trace;
+    bool tracing = false;
     DBuf<DevScalars> sc;
     DevScalars *hsc = nullptr;  // pinned mirror
     int obsCap = 0, obsRows = 0;
@@ -223,7 +226,7 @@ static void release_device(femmd_ctx *c) {
     c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->nbr.release();
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
-    c->partials.release(); c->obs.release(); c->sc.release();
+    c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
     c->nbrCap = 0;
     c->obsCap = 0;
 }
@@ -350,6 +353,7 @@ static DevSys make_sys(femmd_ctx *c) {
     s.sc = c->sc.p;
     s.obs = c->obs.p;
     s.obsCap = c->obsCap;
+    s.trace = c->tracing ? c->trace.p : nullptr;
     return s;
 }
 
@@ -415,8 +419,11 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
                 p.eps48 = 48.0f * e;
                 p.pad = 0.f;
             }
+        // pairs of types that no particle has are never evaluated
         ctx->sigmaOne = ctx->sigmaByType;
-        for (const PairEntry &p : tab) ctx->sigmaOne = ctx->sigmaOne && p.sig2 == 1.0f;
+        for (int a = 0; a < ctx->numTypes; a++)
+            for (int b = 0; b < ctx->numTypes; b++)
+                if (seen[a] && seen[b]) ctx->sigmaOne = ctx->sigmaOne && tab[a * ctx->numTypes + b].sig2 == 1.0f;
         CK(ctx->pair.ensure(tab.size()));
         CK(cudaMemcpyAsync(ctx->pair.p, tab.data(), tab.size() * sizeof(PairEntry), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -593,6 +600,7 @@ static femmd_status ensure_obs(femmd_ctx *ctx, int rows) {
     if (rows <= ctx->obsCap) return FEMMD_OK;
     int cap = std::max(rows, 1024);
     CK(ctx->obs.ensure((size_t)cap * kObsCols));
+    CK(ctx->trace.ensure((size_t)cap * kTraceCols));
     ctx->obsCap = cap;
     release_graphs(ctx);
     return FEMMD_OK;
@@ -1138,6 +1146,9 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(ctx->ckVel.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckAcc.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));  // overflow, nonfinite
+        if (ctx->tracing)
+            CK(cudaMemsetAsync(ctx->trace.p, 0, (size_t)ctx->obsCap * kTraceCols * sizeof(unsigned long long),
+                               ctx->stream));
         if ((st = run_once(ctx, steps))) return st;
         if ((st = collect_profile(ctx))) return st;
         if ((st = read_scalars(ctx))) return st;
@@ -1508,6 +1519,26 @@ femmd_status femmd_event_elapsed(femmd_ctx *ctx, int a, int b, float *ms) {
     return FEMMD_OK;
 }
 
+femmd_status femmd_set_trace(femmd_ctx *ctx, int on) {
+    NEED(ctx);
+    ctx->tracing = on != 0;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_trace(femmd_ctx *ctx, unsigned long long *out, int max_rows, int *rows) {
+    NEED(ctx);
+    if (!rows) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    int n = std::min(ctx->obsRows, std::max(max_rows, 0));
+    *rows = ctx->tracing ? ctx->obsRows : 0;
+    if (ctx->tracing && n > 0 && out) {
+        CK(cudaMemcpyAsync(out, ctx->trace.p, (size_t)n * kTraceCols * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return FEMMD_OK;
+}
+
 femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile) {
     NEED(ctx);
     ctx->profiling = profile != 0;
@@ -1524,6 +1555,380 @@ femmd_status femmd_get_profile(femmd_ctx *ctx, double *fms, long long *fl, doubl
     if (rms) *rms = ctx->profRebuildMs;
     if (rb) *rb = ctx->profRebuilds;
     if (kl) *kl = ctx->profKernels;
+    return FEMMD_OK;
+}
+
+}  // extern "C"
+
+// ================================================================== batches
+//
+// A batch advances many contexts (replicas) in one persistent launch
+// (k_batch.cu).  Each replica keeps its own device state; the batch only
+// holds their descriptors and the CTA assignment.
+
+struct femmd_batch {
+    int device = 0;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    std::vector<femmd_ctx *> reps;
+    int threads = 512, ctasPerSm = 2;
+    DBuf<DevSys> dreps;
+    DBuf<int> order, ctaStart, parity;
+    cudaEvent_t ev[64] = {};
+    GraphSet graph;
+    int graphSteps = -1, graphThreads = 0, graphCtas = 0;
+    const void *graphReps = nullptr;
+    int graphVariant = -1;
+    size_t graphSmem = 0;
+    int ctas = 0;
+};
+
+static femmd_status bfail(femmd_batch *b, femmd_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    return st;
+}
+
+#define BCK(call)                                                                                     \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return bfail(b, FEMMD_CUDA_ERROR, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                         __LINE__);                                                                   \
+    } while (0)
+
+// Upload descriptors, parities and the longest-processing-time assignment.
+static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, std::vector<DevSys> &sys) {
+    const int R = (int)b->reps.size();
+    for (femmd_ctx *c : b->reps) {
+        femmd_status st;
+        if (c->device != b->device) return bfail(b, FEMMD_INVALID_ARG, "replicas must share the batch's device");
+        if ((st = ensure_stream(c)) || (st = prepare(c)) || (st = ensure_obs(c, steps)))
+            return bfail(b, st, "replica: %s", c->err.c_str());
+        // the replica's own uploads must land before the batch stream reads them
+        BCK(cudaStreamSynchronize(c->stream));
+    }
+    sys.resize(R);
+    std::vector<int> par(R);
+    for (int r = 0; r < R; r++) {
+        sys[r] = make_sys(b->reps[r]);
+        par[r] = b->reps[r]->cur;
+    }
+    const DevSys &a = sys[0];
+    for (int r = 1; r < R; r++) {
+        const DevSys &x = sys[r];
+        if ((x.numTypes > 1) != (a.numTypes > 1) || x.sigmaByType != a.sigmaByType || x.wrapx != a.wrapx ||
+            x.wrapy != a.wrapy || x.numTypes != a.numTypes)
+            return bfail(b, FEMMD_INVALID_ARG,
+                         "replica %d differs from replica 0 in type count, sigma mode or periodicity", r);
+    }
+    // 1/dr2 by reciprocal or by division gives the same bits: the reciprocal
+    // form is used only when every replica has unit sigma
+    bool sigmaOne = true;
+    for (int r = 0; r < R; r++) sigmaOne = sigmaOne && sys[r].sigmaOne;
+    int sms = 0;
+    BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    const int ctas = std::max(1, std::min(R, b->ctasPerSm * sms));
+    // LPT: heaviest replica first onto the least loaded CTA
+    std::vector<int> idx(R);
+    std::vector<double> cost(R);
+    for (int r = 0; r < R; r++) {
+        idx[r] = r;
+        cost[r] = (double)sys[r].N + (double)sys[r].ntri;
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    std::vector<double> load(ctas, 0.0);
+    std::vector<std::vector<int>> lists(ctas);
+    for (int r : idx) {
+        if (sys[r].N == 0) continue;  // an empty replica only counts steps
+        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[best] += cost[r];
+        lists[best].push_back(r);
+    }
+    std::vector<int> ord, st(ctas + 1, 0);
+    for (int c = 0; c < ctas; c++) {
+        for (int r : lists[c]) ord.push_back(r);
+        st[c + 1] = (int)ord.size();
+    }
+    BCK(b->dreps.ensure(R));
+    BCK(b->order.ensure(std::max<size_t>(ord.size(), 1)));
+    BCK(b->ctaStart.ensure(ctas + 1));
+    BCK(b->parity.ensure(R));
+    BCK(cudaMemcpyAsync(b->dreps.p, sys.data(), R * sizeof(DevSys), cudaMemcpyHostToDevice, b->stream));
+    if (!ord.empty())
+        BCK(cudaMemcpyAsync(b->order.p, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->ctaStart.p, st.data(), (ctas + 1) * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaMemcpyAsync(b->parity.p, par.data(), R * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    b->ctas = ctas;
+    bl.reps = b->dreps.p;
+    bl.order = b->order.p;
+    bl.ctaStart = b->ctaStart.p;
+    bl.parity = b->parity.p;
+    bl.steps = steps;
+    bl.ctas = ctas;
+    bl.threads = b->threads;
+    bl.smem = sizeof(PairEntry) * (size_t)(a.numTypes > 1 ? a.numTypes * a.numTypes : 1);
+    bl.multiType = a.numTypes > 1;
+    bl.sigmaByType = a.sigmaByType;
+    bl.sigmaOne = sigmaOne;
+    bl.wrapx = a.wrapx;
+    bl.wrapy = a.wrapy;
+    bl.exact = a.imageExact;
+    return FEMMD_OK;
+}
+
+static femmd_status batch_launch(femmd_batch *b, const BatchLaunch &bl) {
+    const int variant = bl.multiType | bl.sigmaByType << 1 | bl.sigmaOne << 2 | bl.wrapx << 3 | bl.wrapy << 4;
+    const bool rebuild = !b->graph.x || b->graphSteps != bl.steps || b->graphThreads != bl.threads ||
+                         b->graphCtas != bl.ctas || b->graphReps != (const void *)bl.reps ||
+                         b->graphVariant != variant || b->graphSmem != bl.smem;
+    if (rebuild) {
+        b->graph.release();
+        BCK(cudaGraphCreate(&b->graph.g, 0));
+        Launch L;
+        L.stream = b->stream;
+        L.graph = b->graph.g;
+        BCK(enqueue_batch(L, bl));
+        BCK(cudaGraphInstantiate(&b->graph.x, b->graph.g, 0));
+        b->graphSteps = bl.steps;
+        b->graphThreads = bl.threads;
+        b->graphCtas = bl.ctas;
+        b->graphReps = bl.reps;
+        b->graphVariant = variant;
+        b->graphSmem = bl.smem;
+    }
+    BCK(cudaGraphLaunch(b->graph.x, b->stream));
+    return FEMMD_OK;
+}
+
+static femmd_status batch_checkpoint(femmd_batch *b, bool restore) {
+    for (femmd_ctx *c : b->reps) {
+        const size_t n = c->pos.size() * sizeof(float2);
+        if (!n) continue;
+        float2 *pd = c->cur ? c->dpos1.p : c->dpos0.p;
+        if (!restore) {
+            BCK(cudaMemcpyAsync(c->ckPos.p, pd, n, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemcpyAsync(c->ckVel.p, c->dvel.p, n, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemcpyAsync(c->ckAcc.p, c->dacc.p, n, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemsetAsync(&c->sc.p->overflow, 0, 2 * sizeof(int), b->stream));
+        } else {
+            BCK(cudaMemcpyAsync(pd, c->ckPos.p, n, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemcpyAsync(c->dvel.p, c->ckVel.p, n, cudaMemcpyDeviceToDevice, b->stream));
+            BCK(cudaMemcpyAsync(c->dacc.p, c->ckAcc.p, n, cudaMemcpyDeviceToDevice, b->stream));
+        }
+    }
+    return FEMMD_OK;
+}
+
+static femmd_status batch_read(femmd_batch *b) {
+    for (femmd_ctx *c : b->reps)
+        if (!c->pos.empty())
+            BCK(cudaMemcpyAsync(c->hsc, c->sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    return FEMMD_OK;
+}
+
+extern "C" {
+
+femmd_status femmd_batch_create(int device, femmd_batch **out) {
+    if (!out) return FEMMD_INVALID_ARG;
+    femmd_batch *b = new (std::nothrow) femmd_batch();
+    if (!b) return FEMMD_CUDA_ERROR;
+    b->device = device;
+    *out = b;
+    return FEMMD_OK;
+}
+
+void femmd_batch_destroy(femmd_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    b->graph.release();
+    b->dreps.release();
+    b->order.release();
+    b->ctaStart.release();
+    b->parity.release();
+    for (auto e : b->ev)
+        if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char *femmd_batch_last_error(const femmd_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+femmd_status femmd_batch_add(femmd_batch *b, femmd_ctx *ctx, int *index) {
+    if (!b || !ctx) return FEMMD_INVALID_ARG;
+    b->err.clear();
+    for (femmd_ctx *c : b->reps)
+        if (c == ctx) return bfail(b, FEMMD_INVALID_ARG, "context already in the batch");
+    if (!ctx->nnInit) return bfail(b, FEMMD_NOT_READY, "add a replica after its init_neighbor_list()");
+    b->reps.push_back(ctx);
+    if (index) *index = (int)b->reps.size() - 1;
+    return FEMMD_OK;
+}
+
+int femmd_batch_size(const femmd_batch *b) { return b ? (int)b->reps.size() : 0; }
+
+femmd_status femmd_batch_set_launch(femmd_batch *b, int threads, int ctas_per_sm) {
+    if (!b) return FEMMD_INVALID_ARG;
+    if (threads < 32 || threads > 1024 || threads % 32 || ctas_per_sm < 1 || ctas_per_sm > 32)
+        return bfail(b, FEMMD_INVALID_ARG, "threads must be a multiple of 32 in [32, 1024], CTAs per SM in [1, 32]");
+    b->threads = threads;
+    b->ctasPerSm = ctas_per_sm;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_batch_get_launch(const femmd_batch *b, int *threads, int *ctas_per_sm, int *ctas) {
+    if (!b) return FEMMD_INVALID_ARG;
+    if (threads) *threads = b->threads;
+    if (ctas_per_sm) *ctas_per_sm = b->ctasPerSm;
+    if (ctas) *ctas = b->ctas;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_batch_run(femmd_batch *b, int steps) {
+    if (!b) return FEMMD_INVALID_ARG;
+    b->err.clear();
+    if (steps < 0) return bfail(b, FEMMD_INVALID_ARG, "steps must be >= 0");
+    if (b->reps.empty()) return FEMMD_OK;
+    if (!b->stream) {
+        BCK(cudaSetDevice(b->device));
+        BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    femmd_status st;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        BatchLaunch bl;
+        std::vector<DevSys> sys;
+        if ((st = batch_prepare(b, steps, bl, sys))) return st;
+        if ((st = batch_checkpoint(b, false))) return st;
+        if ((st = batch_launch(b, bl))) return st;
+        if ((st = batch_read(b))) return st;
+        bool over = false;
+        for (femmd_ctx *c : b->reps) {
+            if (c->pos.empty()) continue;
+            if (c->hsc->overflow & 2) return bfail(b, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
+            over = over || c->hsc->overflow;
+        }
+        if (!over) {
+            int bad = -1;
+            for (size_t r = 0; r < b->reps.size(); r++) {
+                femmd_ctx *c = b->reps[r];
+                c->steps += steps;
+                if (c->pos.empty()) continue;
+                if (steps % 2) c->cur ^= 1;
+                c->staleMask |= kPos | kVel | kAcc | kForce;
+                c->forcesValid = true;
+                c->listBuilt = true;
+                c->obsRows = std::min(c->hsc->obsRow, c->obsCap);
+                c->totalBuilds = (long long)c->hsc->builds;
+                if (c->hsc->nonfinite && bad < 0) bad = (int)r;
+            }
+            if (bad >= 0) return bfail(b, FEMMD_NONFINITE, "replica %d: a force became NaN or infinite", bad);
+            return FEMMD_OK;
+        }
+        // roll every replica back, grow the lists that overflowed, repeat
+        if ((st = batch_checkpoint(b, true))) return st;
+        BCK(cudaStreamSynchronize(b->stream));
+        for (femmd_ctx *c : b->reps)
+            if (!c->pos.empty() && c->hsc->overflow) {
+                int need = std::max(c->hsc->maxCount, c->nbrCap + c->nbrCap / 2);
+                if ((st = alloc_list(c, need + need / 4 + 8))) return bfail(b, st, "%s", c->err.c_str());
+            }
+    }
+    return bfail(b, FEMMD_CAPACITY_OVERFLOW, "neighbour lists kept overflowing");
+}
+
+femmd_status femmd_batch_event_record(femmd_batch *b, int slot) {
+    if (!b || slot < 0 || slot >= 64) return FEMMD_INVALID_ARG;
+    if (!b->stream) {
+        BCK(cudaSetDevice(b->device));
+        BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    if (!b->ev[slot]) BCK(cudaEventCreate(&b->ev[slot]));
+    BCK(cudaEventRecord(b->ev[slot], b->stream));
+    return FEMMD_OK;
+}
+
+femmd_status femmd_batch_event_elapsed(femmd_batch *b, int a, int c, float *ms) {
+    if (!b || !ms || a < 0 || a >= 64 || c < 0 || c >= 64 || !b->ev[a] || !b->ev[c]) return FEMMD_INVALID_ARG;
+    BCK(cudaEventSynchronize(b->ev[c]));
+    BCK(cudaEventElapsedTime(ms, b->ev[a], b->ev[c]));
+    return FEMMD_OK;
+}
+
+// Time each launch shape on the current states (restored after every trial)
+// and keep the fastest.
+femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads_out, int *ctas_per_sm_out,
+                                  double *best_ms) {
+    if (!b) return FEMMD_INVALID_ARG;
+    b->err.clear();
+    if (b->reps.empty()) return bfail(b, FEMMD_NOT_READY, "empty batch");
+    if (trial_steps < 1) trial_steps = 10;
+    if (!b->stream) {
+        BCK(cudaSetDevice(b->device));
+        BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    static const int cand[][2] = {{128, 8}, {256, 4}, {256, 8}, {512, 2}, {512, 4}, {1024, 1}, {1024, 2}};
+    const int t0 = b->threads, c0 = b->ctasPerSm;
+    {
+        BatchLaunch bl;
+        std::vector<DevSys> sys;
+        femmd_status st;
+        if ((st = batch_prepare(b, trial_steps, bl, sys))) return st;
+    }
+    if (femmd_status st = batch_read(b)) return st;
+    std::vector<unsigned long long> builds0;
+    for (femmd_ctx *c : b->reps) builds0.push_back(c->pos.empty() ? 0ull : c->hsc->builds);
+    double best = 1e300;
+    int bt = t0, bc = c0;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    for (const auto &cd : cand) {
+        b->threads = cd[0];
+        b->ctasPerSm = cd[1];
+        BatchLaunch bl;
+        std::vector<DevSys> sys;
+        femmd_status st;
+        if ((st = batch_prepare(b, trial_steps, bl, sys))) return st;
+        if ((st = batch_checkpoint(b, false))) return st;
+        BCK(cudaEventRecord(e0, b->stream));
+        cudaError_t le = cudaSuccess;
+        {
+            Launch L;
+            L.stream = b->stream;
+            le = enqueue_batch(L, bl);
+        }
+        BCK(cudaEventRecord(e1, b->stream));
+        cudaError_t se = cudaStreamSynchronize(b->stream);
+        if (le == cudaSuccess && se == cudaSuccess) {
+            float ms = 0;
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bt = cd[0];
+                bc = cd[1];
+            }
+        } else {
+            cudaGetLastError();  // a shape the device cannot run: skip it
+        }
+        if ((st = batch_checkpoint(b, true))) return st;
+        for (size_t r = 0; r < b->reps.size(); r++)
+            if (!b->reps[r]->pos.empty())
+                BCK(cudaMemcpyAsync(&b->reps[r]->sc.p->builds, &builds0[r], sizeof(unsigned long long),
+                                cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->threads = bt;
+    b->ctasPerSm = bc;
+    if (threads_out) *threads_out = bt;
+    if (ctas_per_sm_out) *ctas_per_sm_out = bc;
+    if (best_ms) *best_ms = best;
     return FEMMD_OK;
 }
 

@@ -26,6 +26,7 @@ constexpr int kBlock = 256;        // threads per block of the per-particle kern
 constexpr int kStepBlock = 128;    // threads per block of the step kernel
 constexpr int kScanBlock = 1024;   // cells per block of the cell-start scan
 constexpr int kObsCols = 6;        // per-step observable row: U, W, sum m v^2, max v^2, dispHi, rebuilt
+constexpr int kTraceCols = 6;      // per-step trace row (ns): tri start/end, step start/end, rebuild start/end
 
 // Per type-pair constants, all formed on the host with the reference's float
 // operations (interactionsCuda.cu:43-55, 79-88) so that the kernel's per-pair
@@ -97,7 +98,14 @@ struct DevSys {
     DevScalars *sc;
     double *obs;
     int obsCap;
+    unsigned long long *trace;  // per-step device timestamps, or null
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Kernel launch sink: direct stream launches, or nodes appended to a CUDA
 // graph (optionally inside an IF body).  Implemented in femmd_api.cu.
@@ -115,6 +123,16 @@ cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
 // leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
+
+// ---- batched replicas (k_batch.cu): one persistent launch over many systems
+struct BatchLaunch {
+    const DevSys *reps;
+    const int *order, *ctaStart, *parity;
+    int steps, ctas, threads;
+    size_t smem;
+    bool multiType, sigmaByType, sigmaOne, wrapx, wrapy, exact;
+};
+cudaError_t enqueue_batch(Launch &L, const BatchLaunch &b);
 
 int force_blocks(int N);
 int step_blocks(int N);

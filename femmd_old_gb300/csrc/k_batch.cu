@@ -1,0 +1,303 @@
+// k_batch.cu -- many independent replicas advanced in one persistent launch.
+//
+// Each replica is a complete femmd2D system (its own box, cell grid, lists,
+// bonds, triangles and run state), described by the same DevSys block as a
+// single context.  One CTA owns a set of replicas (longest-processing-time
+// assignment by the host) and runs the whole run(n) sequence of each -- the
+// reference's Integrator::run (femmd2D/src/integrator.cpp:31-57): forced
+// rebuild, first force pass and drift, n-1 steps with the half-skin rebuild
+// rule, last step -- with block-level rebuilds and steps separated only by
+// __syncthreads.  Replicas never exchange data, so there is no grid-wide
+// synchronisation and no per-step launch: one kernel launch covers all
+// replicas and all steps.
+//
+// The per-particle and per-triangle arithmetic is step_body.cuh /
+// nn_body.cuh, the same code as the single-system kernels, and the list order
+// is the same, so a replica's trajectory is bit-identical to running it alone.
+// Energies are reduced per replica in FP32 inside the block.
+#include <cuda_runtime.h>
+#include "femmd_internal.h"
+#include "launch.h"
+#include "device_common.cuh"
+#include "nn_body.cuh"
+#include "step_body.cuh"
+
+namespace femmd {
+
+namespace {
+
+// block-wide sum / max / or of one value per thread (blockDim a multiple of 32, <= 1024)
+__device__ __forceinline__ float block_sum(float v, float *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum_f(v);
+    __syncthreads();
+    if (lane == 0) scr[warp] = v;
+    __syncthreads();
+    float t = 0.0f;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < nw ? scr[threadIdx.x] : 0.0f;
+        t = warp_sum_f(t);
+    }
+    return t;  // valid in thread 0
+}
+
+__device__ __forceinline__ float block_max(float v, float *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_max(v);
+    __syncthreads();
+    if (lane == 0) scr[warp] = v;
+    __syncthreads();
+    float t = 0.0f;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < nw ? scr[threadIdx.x] : 0.0f;
+        t = warp_max(t);
+    }
+    return t;
+}
+
+__device__ __forceinline__ int block_max_int(int v, int *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_max_int(v);
+    __syncthreads();
+    if (lane == 0) scr[warp] = v;
+    __syncthreads();
+    int t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < nw ? scr[threadIdx.x] : 0;
+        t = warp_max_int(t);
+    }
+    return t;
+}
+
+// NeighborList::update branch + binning + Verlet build for one replica
+__device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *iscr) {
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0 && s.sc->rebuild) {
+        s.sc->totalUpdates += 1;
+        s.sc->dispHi = 0.0f;
+    }
+    // counting sort: warp-aggregated histogram (warp-uniform loop for the match)
+    for (int base = threadIdx.x & ~31; base < s.N; base += blockDim.x) {
+        const int i = base + lane;
+        const bool act = i < s.N;
+        const unsigned active = __ballot_sync(0xffffffffu, act);
+        if (act) {
+            float2 p = pos[i];
+            if (!(isfinite(p.x) && isfinite(p.y))) atomicOr(&s.sc->nonfinite, 1);
+            int c = cell_of(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
+            s.cellOf[i] = c;
+            unsigned peers = __match_any_sync(active, c);
+            int leader = __ffs(peers) - 1;
+            int b = 0;
+            if (lane == leader) b = atomicAdd(&s.cellCount[c], __popc(peers));
+            b = __shfl_sync(peers, b, leader);
+            s.rank[i] = b + __popc(peers & ((1u << lane) - 1u));
+        }
+    }
+    __syncthreads();
+    // exclusive scan of the counts into cellStart, counts cleared
+    {
+        const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        int carry = 0;
+        for (int cb = 0; cb < s.ncells; cb += blockDim.x) {
+            const int c = cb + threadIdx.x;
+            const int v = c < s.ncells ? s.cellCount[c] : 0;
+            int x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) iscr[warp] = x;
+            __syncthreads();
+            if (warp == 0) {
+                int w = lane < nw ? iscr[lane] : 0, z = w;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(0xffffffffu, z, o);
+                    if (lane >= o) z += y;
+                }
+                iscr[lane] = z - w;
+                if (lane == 31) iscr[32] = z;  // chunk total
+            }
+            __syncthreads();
+            if (c < s.ncells) {
+                s.cellStart[c] = carry + iscr[warp] + x - v;
+                s.cellCount[c] = 0;
+            }
+            carry += iscr[32];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            s.cellStart[s.ncells] = s.N;
+            s.sc->nbrSum = 0ull;
+            s.sc->maxCount = 0;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
+        int slot = s.cellStart[s.cellOf[i]] + s.rank[i];
+        if (slot >= 0 && slot < s.N)
+            s.sortedIds[slot] = i;
+        else
+            atomicOr(&s.sc->overflow, 2);
+    }
+    __syncthreads();
+    const bool skip = s.sc->nonfinite != 0;  // crowded cells after a blow-up: skip the quadratic parts
+    int cand = 0;
+    if (!skip)
+        for (int c = threadIdx.x; c < s.ncells; c += blockDim.x) cand = max(cand, sort_cell(s, pos, c));
+    cand = block_max_int(cand, iscr);
+    if (threadIdx.x == 0 && cand > s.sc->maxCand) s.sc->maxCand = cand;
+    __syncthreads();
+    int kmax = 0;
+    unsigned long long ksum = 0;
+    if (!skip)
+        for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
+            int k = build_one<false>(s, pos, i);
+            kmax = max(kmax, k);
+            ksum += (unsigned long long)k;
+        }
+    if (ksum) atomicAdd(&s.sc->nbrSum, ksum);
+    kmax = block_max_int(kmax, iscr);
+    if (threadIdx.x == 0) {
+        s.sc->maxCount = kmax;
+        if (kmax > s.nbrCap) s.sc->overflow |= 1;
+        s.sc->builds += 1ull;
+    }
+    __syncthreads();
+}
+
+// one force evaluation + integration of a replica (k_tri_forces + k_step)
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
+__device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, int mode, int parity, float *fscr) {
+    const float2 *pin = parity ? s.pos1 : s.pos0;
+    float2 *pout = parity ? s.pos0 : s.pos1;
+    float etri = 0.0f;
+    if (s.feaForces && s.ntri > 0) {
+        for (int t = threadIdx.x; t < s.ntri; t += blockDim.x) etri += tri_force(s, pin, t);
+        __syncthreads();  // every nodal force written before the gathers
+    }
+    float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
+    bool bad = false;
+    for (int i = threadIdx.x; i < s.N; i += blockDim.x)
+        particle_step<MT, SG, WX, WY, SIG1, false>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
+    const int anybad = __syncthreads_or(bad);
+    const float te = block_sum(etri, fscr);
+    const float tu = block_sum(ue, fscr);
+    const float tw = block_sum(we, fscr);
+    const float tk = block_sum(ke, fscr);
+    const float tm = block_max(vvm, fscr);
+    if (threadIdx.x == 0) {
+        DevScalars *sc = s.sc;
+        if (anybad) sc->nonfinite |= 1;
+        const double U = (double)te + (double)tu, W = (double)tw, KE = (double)tk;
+        sc->U = U;
+        sc->W = W;
+        int reb;
+        if (mode == MODE_MID || mode == MODE_LAST) {
+            sc->KE = KE;
+            sc->vvMax = tm;
+            float d = sc->dispHi + sqrtf(tm) * s.dt;  // md3dsystem.cpp:177
+            reb = (double)d > s.halfSkin;              // nn.cpp:118
+            int row = sc->obsRow;
+            if (s.obs && row < s.obsCap) {
+                double *o = s.obs + (size_t)row * kObsCols;
+                o[0] = U;
+                o[1] = W;
+                o[2] = KE;
+                o[3] = (double)tm;
+                o[4] = (double)d;
+                o[5] = (double)reb;
+            }
+            sc->obsRow = row + 1;
+            sc->dispHi = d;
+        } else {
+            reb = (double)sc->dispHi > s.halfSkin;
+        }
+        sc->rebuild = reb;
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
+__global__ void __launch_bounds__(1024) k_batch(const DevSys *__restrict__ reps, const int *__restrict__ order,
+                                                const int *__restrict__ ctaStart, const int *__restrict__ parity0,
+                                                int steps) {
+    __shared__ DevSys S;
+    __shared__ float fscr[32];
+    __shared__ int iscr[33];
+    extern __shared__ PairEntry tab[];
+    for (int q = ctaStart[blockIdx.x]; q < ctaStart[blockIdx.x + 1]; q++) {
+        const int r = order[q];
+        // copy the replica's descriptor into shared memory
+        {
+            const int *src = (const int *)(reps + r);
+            int *dst = (int *)&S;
+            for (int w = threadIdx.x; w < (int)(sizeof(DevSys) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+        }
+        __syncthreads();
+        const int nt = S.numTypes > 1 ? S.numTypes * S.numTypes : 1;
+        for (int w = threadIdx.x; w < nt; w += blockDim.x) tab[w] = S.pair[w];
+        if (threadIdx.x == 0) {
+            // run start: NeighborList::update(1)
+            DevScalars *c = S.sc;
+            c->rebuild = 1;
+            c->dispHi = 0.0f;
+            c->totalUpdates = 0;
+            c->obsRow = 0;
+        }
+        __syncthreads();
+        int cur = parity0[r];
+        block_rebuild(S, cur, iscr);
+        if (steps == 0) {
+            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_INIT, cur, fscr);
+        } else {
+            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_FIRST, cur, fscr);
+            cur ^= 1;
+            for (int k = 1; k < steps; k++) {
+                if (S.sc->rebuild) block_rebuild(S, cur, iscr);
+                block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_MID, cur, fscr);
+                cur ^= 1;
+            }
+            if (S.sc->rebuild) block_rebuild(S, cur, iscr);
+            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_LAST, cur, fscr);
+        }
+        __syncthreads();
+    }
+}
+
+namespace {
+
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
+cudaError_t launch_batch(Launch &L, const BatchLaunch &b) {
+    return L.kernel(k_batch<MT, SG, WX, WY, SIG1>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
+                    b.ctaStart, b.parity, b.steps);
+}
+
+template <bool MT, bool SG, bool WX, bool WY>
+cudaError_t pick_sig_b(Launch &L, const BatchLaunch &b) {
+    if constexpr (!SG) {
+        if (b.sigmaOne) return launch_batch<MT, SG, WX, WY, true>(L, b);
+    }
+    return launch_batch<MT, SG, WX, WY, false>(L, b);
+}
+
+template <bool MT, bool SG>
+cudaError_t pick_image_b(Launch &L, const BatchLaunch &b) {
+    if (b.wrapx && b.wrapy) return pick_sig_b<MT, SG, true, true>(L, b);
+    if (b.wrapx) return pick_sig_b<MT, SG, true, false>(L, b);
+    return pick_sig_b<MT, SG, false, false>(L, b);
+}
+
+}  // namespace
+
+cudaError_t enqueue_batch(Launch &L, const BatchLaunch &b) {
+    if (b.multiType) return b.sigmaByType ? pick_image_b<true, false>(L, b) : pick_image_b<true, true>(L, b);
+    return b.sigmaByType ? pick_image_b<false, false>(L, b) : pick_image_b<false, true>(L, b);
+}
+
+}  // namespace femmd

@@ -22,6 +22,7 @@
 #include "femmd_internal.h"
 #include "launch.h"
 #include "device_common.cuh"
+#include "nn_body.cuh"
 
 namespace femmd {
 
@@ -48,6 +49,10 @@ __global__ void k_rebuild_begin(DevSys s) {
     if (threadIdx.x == 0 && blockIdx.x == 0 && s.sc->rebuild) {
         s.sc->totalUpdates += 1;
         s.sc->dispHi = 0.0f;
+        if (s.trace) {
+            int row = s.sc->obsRow - 1;
+            if (row >= 0 && row < s.obsCap) s.trace[(size_t)row * kTraceCols + 4] = global_ns();
+        }
     }
 }
 
@@ -160,39 +165,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(DevSys s, int parity, int 
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int cand = 0;
     if (c < s.ncells) {
-        int b = s.cellStart[c], e = s.cellStart[c + 1], n = e - b;
-        int *ids = s.sortedIds + b;
-        // Shell sort with gaps 3h+1 ending in insertion sort (a cell holds a
-        // handful of particles; the gaps bound the work of crowded cells)
-        int gap = 1;
-        while (gap < n / 3) gap = 3 * gap + 1;
-        for (; gap > 0; gap /= 3) {
-            for (int k = gap; k < n; k++) {
-                int v = ids[k];
-                int m = k - gap;
-                while (m >= 0 && ids[m] > v) {
-                    ids[m + gap] = ids[m];
-                    m -= gap;
-                }
-                ids[m + gap] = v;
-            }
-        }
-        for (int k = 0; k < n; k++) {
-            int id = ids[k];
-            float2 p = pos[id];
-            int tag = id | (s.numTypes > 1 ? (s.typeId[id] << kIdBits) : 0);
-            s.cellSorted[b + k] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[id]));
-        }
-        // candidate count of the 3x3 stencil (capacity sizing)
-        int cy = c / s.ncx, cx = c - cy * s.ncx;
-        for (int dx = -1; dx <= 1; dx++)
-            for (int dy = -1; dy <= 1; dy++) {
-                int nx = cx + dx, ny = cy + dy;
-                if (nx < 0) nx = s.ncx - 1; else if (nx == s.ncx) nx = 0;
-                if (ny < 0) ny = s.ncy - 1; else if (ny == s.ncy) ny = 0;
-                int nc = nx + ny * s.ncx;
-                cand += s.cellStart[nc + 1] - s.cellStart[nc];
-            }
+        cand = sort_cell(s, pos, c);
     }
     cand = warp_max_int(cand);
     if ((threadIdx.x & 31) == 0 && cand > 0) atomicMax(&s.sc->maxCand, cand);
@@ -204,41 +177,7 @@ __global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int c
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int k = 0;
     if (i < s.N) {
-        const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap, Ncap = s.Ncap;
-        const bool wx = s.wrapx, wy = s.wrapy;
-        const float Lx = s.Lx, Ly = s.Ly, R2 = s.nnRadiusSq;
-        int c = s.cellOf[i];
-        int cy0 = c / ncx, cx0 = c - cy0 * ncx;
-        float2 p = pos[i];
-        int gi = s.excl[i];
-        int *out = s.nbr + i;
-        for (int dx = -1; dx <= 1; dx++) {
-            int nx = cx0 + dx;
-            if (nx < 0) nx = ncx - 1; else if (nx == ncx) nx = 0;
-            for (int dy = -1; dy <= 1; dy++) {
-                int ny = cy0 + dy;
-                if (ny < 0) ny = ncy - 1; else if (ny == ncy) ny = 0;
-                int nc = nx + ny * ncx;
-                int qb = __ldg(s.cellStart + nc), qe = __ldg(s.cellStart + nc + 1);
-                for (int q = qb; q < qe; q++) {
-                    float4 e = __ldg(s.cellSorted + q);
-                    int tag = __float_as_int(e.z);
-                    int j = tag & kIdMask;
-                    int gj = __float_as_int(e.w);
-                    if (j != i && (gi == -1 || gj == -1 || gi != gj)) {
-                        float dxr, dxo, dyr, dyo;
-                        image_axis(p.x, e.x, Lx, wx, false, dxr, dxo);
-                        image_axis(p.y, e.y, Ly, wy, false, dyr, dyo);
-                        float dr2 = dxr * dxr + dyr * dyr;
-                        if (dr2 <= R2) {
-                            if (k < cap) out[(size_t)k * Ncap] = tag;
-                            k++;
-                        }
-                    }
-                }
-            }
-        }
-        s.nbrCount[i] = k;
+        k = build_one<true>(s, pos, i);
     }
     // build statistics and overflow
     int kmax = warp_max_int(k);
@@ -249,6 +188,10 @@ __global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int c
         if (kmax > s.nbrCap) atomicOr(&s.sc->overflow, 1);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
+    if (s.trace && (threadIdx.x & 31) == 0) {
+        int row = s.sc->obsRow - 1;
+        if (row >= 0 && row < s.obsCap) atomicMax(&s.trace[(size_t)row * kTraceCols + 5], global_ns());
+    }
 }
 
 int scan_blocks(int ncells) { return (ncells + kScanBlock - 1) / kScanBlock; }

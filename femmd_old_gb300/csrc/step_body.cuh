@@ -1,0 +1,348 @@
+// step_body.cuh -- per-triangle and per-particle work of the femmd2D timestep,
+// shared by the plain kernels (k_force.cu) and the persistent batched kernel
+// (k_batch.cu), so both execute the same arithmetic in the same order.
+//
+// Reference: calcFeaForcesCPU2 (femmd2D/src/interactions.cpp:532-689),
+// computeFeaForcesGPU (interactionsCuda.cu:312-451), calcBondForcesCPU
+// (interactions.cpp:143-173), pairForce/ljforce (interactionsCuda.cu:43-100),
+// leapFrogStep1/2 + updateAcc + evalProps (integrator.cpp:100-135,
+// md3dsystem.cpp:151-179).
+#pragma once
+#include <cuda_runtime.h>
+#include "femmd_internal.h"
+#include "device_common.cuh"
+
+namespace femmd {
+
+// ------------------------------------------------------------ triangles
+
+// calcFeaForcesCPU2 (interactions.cpp:532-689) with Bm and vol0 precomputed
+// from the reference positions by the same float operations.
+__device__ __forceinline__ float tri_neo_hookean(const DevSys &s, const float2 *pos, int t, float2 &f0, float2 &f1,
+                                                 float2 &f2) {
+    int4 q = __ldg(s.triIdx + t);
+    float2 r0 = pos[q.x], r1 = pos[q.y], r2 = pos[q.z];
+    float4 bm = __ldg(s.triGeo + 2 * t);
+    float vol0 = __ldg(s.triGeo + 2 * t + 1).x;
+    const float L = s.Lx, Ly = s.Ly;
+    float dx01 = r0.x - r1.x, dx02 = r0.x - r2.x, dy01 = r0.y - r1.y, dy02 = r0.y - r2.y;
+    int k1x = (dx01 > L / 2.0f) - (dx01 < -L / 2.0f);
+    int k2x = (dx02 > L / 2.0f) - (dx02 < -L / 2.0f);
+    int k1y = (dy01 > Ly / 2.0f) - (dy01 < -Ly / 2.0f);
+    int k2y = (dy02 > Ly / 2.0f) - (dy02 < -Ly / 2.0f);
+    float Ds00, Ds10, Ds01, Ds11;
+    if (s.imageExact) {
+        Ds00 = diff_shift(r0.x, r2.x, -k2x, L);
+        Ds10 = diff_shift(r0.y, r2.y, -k2y, Ly);
+        Ds01 = diff_shift(r1.x, r2.x, k1x - k2x, L);
+        Ds11 = diff_shift(r1.y, r2.y, k1y - k2y, Ly);
+    } else {
+        float r1x = r1.x, r2x = r2.x, r1y = r1.y, r2y = r2.y;
+        if (k1x > 0) r1x += L;
+        if (k1x < 0) r1x -= L;
+        if (k2x > 0) r2x += L;
+        if (k2x < 0) r2x -= L;
+        if (k1y > 0) r1y += Ly;
+        if (k1y < 0) r1y -= Ly;
+        if (k2y > 0) r2y += Ly;
+        if (k2y < 0) r2y -= Ly;
+        Ds00 = r0.x - r2x;
+        Ds10 = r0.y - r2y;
+        Ds01 = r1x - r2x;
+        Ds11 = r1y - r2y;
+    }
+    const float Bm00 = bm.x, Bm10 = bm.y, Bm01 = bm.z, Bm11 = bm.w;
+    float F00 = Ds00 * Bm00 + Ds01 * Bm10;
+    float F10 = Ds10 * Bm00 + Ds11 * Bm10;
+    float F01 = Ds00 * Bm01 + Ds01 * Bm11;
+    float F11 = Ds10 * Bm01 + Ds11 * Bm11;
+    float detF = F00 * F11 - F01 * F10;
+    float logJ = own_logf(detF);
+    float llogJ = s.lambda * logJ;
+    float iF00 = F11 / detF, iF10 = -F10 / detF, iF01 = -F01 / detF, iF11 = F00 / detF;
+    const float mu = s.mu;
+    float P00 = mu * (F00 - iF00) + llogJ * iF00;
+    float P10 = mu * (F10 - iF01) + llogJ * iF01;
+    float P01 = mu * (F01 - iF10) + llogJ * iF10;
+    float P11 = mu * (F11 - iF11) + llogJ * iF11;
+    float nv0 = -vol0;
+    float H00 = nv0 * (P00 * Bm00 + P01 * Bm01);
+    float H10 = nv0 * (P10 * Bm00 + P11 * Bm01);
+    float H01 = nv0 * (P00 * Bm10 + P01 * Bm11);
+    float H11 = nv0 * (P10 * Bm10 + P11 * Bm11);
+    f0 = make_float2(H00, H10);
+    f1 = make_float2(H01, H11);
+    f2 = make_float2(-H00 - H01, -H10 - H11);
+    // energy A0 [mu/2 (I1-2) - mu lnJ + lambda/2 ln^2 J], deviation form:
+    // I1 - 2 - 2 lnJ summed from (F-I) entries to avoid first-order cancellation
+    float d00 = F00 - 1.0f, d11 = F11 - 1.0f;
+    float i1m2 = (2.0f * d00 + d00 * d00) + (2.0f * d11 + d11 * d11) + F01 * F01 + F10 * F10;
+    float pe = 0.5f * mu * (i1m2 - 2.0f * logJ) + 0.5f * s.lambda * logJ * logJ;
+    return pe * vol0;
+}
+
+// computeFeaForcesGPU (interactionsCuda.cu:312-451): Green strain, linear C,
+// float arithmetic of the reference kernel; xm rows 1-2 and |area|
+// precomputed from the reference positions.
+__device__ __forceinline__ float tri_green(const DevSys &s, const float2 *pos, int t, float2 *f) {
+    int4 q = __ldg(s.triIdx + t);
+    int p[3] = {q.x, q.y, q.z};
+    float rx[3], ry[3], X[3], Y[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float2 r = pos[p[i]];
+        float2 R = __ldg(s.refPos + p[i]);
+        rx[i] = r.x;
+        ry[i] = r.y;
+        X[i] = R.x;
+        Y[i] = R.y;
+    }
+    const float L = s.Lx, Ly = s.Ly;
+    float dx01 = rx[0] - rx[1];
+    if (dx01 > L / 2.0f) rx[1] += L;
+    if (dx01 < -L / 2.0f) rx[1] -= L;
+    float dx02 = rx[0] - rx[2];
+    if (dx02 > L / 2.0f) rx[2] += L;
+    if (dx02 < -L / 2.0f) rx[2] -= L;
+    float dy01 = ry[0] - ry[1];
+    if (dy01 > Ly / 2.0f) ry[1] += Ly;
+    if (dy01 < -Ly / 2.0f) ry[1] -= Ly;
+    float dy02 = ry[0] - ry[2];
+    if (dy02 > Ly / 2.0f) ry[2] += Ly;
+    if (dy02 < -Ly / 2.0f) ry[2] -= Ly;
+    float4 g0 = __ldg(s.triGeo + 2 * t), g1 = __ldg(s.triGeo + 2 * t + 1);
+    float m1[3] = {g0.x, g0.y, g0.z};  // xm row 1
+    float m2[3] = {g0.w, g1.x, g1.y};  // xm row 2
+    float tetVol = g1.z;
+    float a1 = 0.0f, a2 = 0.0f, b1 = 0.0f, b2 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        float ux = rx[j] - X[j], uy = ry[j] - Y[j];
+        a1 = a1 + m1[j] * ux;
+        b1 = b1 + m1[j] * uy;
+        a2 = a2 + m2[j] * ux;
+        b2 = b2 + m2[j] * uy;
+    }
+    float e00 = a1 + 0.5f * (a1 * a1 + b1 * b1);
+    float e11 = b2 + 0.5f * (a2 * a2 + b2 * b2);
+    float e01 = 0.5f * (a2 + b1 + a1 * a2 + b1 * b2);
+    const float c1 = s.C1, c2 = s.C2, c3 = s.C3;
+    float pesum = c1 * (e00 * e00 + e11 * e11) + 2.0f * c2 * (e00 * e11) + 4.0f * c3 * (e01 * e01);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float n1 = m1[i], n2 = m2[i];
+        float fxs = -2.0f * c1 * e00 * n1 * (1.0f + a1) - 2.0f * c1 * e11 * n2 * a2 - 2.0f * c2 * e00 * n2 * a2 -
+                    2.0f * c2 * e11 * n1 * (1.0f + a1) - 4.0f * c3 * e01 * n2 * (1.0f + a1) - 4.0f * c3 * e01 * n1 * a2;
+        float fys = -2.0f * c1 * e00 * n1 * b1 - 2.0f * c1 * e11 * n2 * (1.0f + b2) - 2.0f * c2 * e00 * n2 * (1.0f + b2) -
+                    2.0f * c2 * e11 * n1 * b1 - 4.0f * c3 * e01 * n1 * (1.0f + b2) - 4.0f * c3 * e01 * n2 * b1;
+        f[i] = make_float2(fxs * tetVol, fys * tetVol);
+    }
+    return pesum * tetVol;
+}
+
+// Nodal forces of triangle t into triF, energy returned (law of s.feaLaw).
+__device__ __forceinline__ float tri_force(const DevSys &s, const float2 *pos, int t) {
+    float2 f[3];
+    float e;
+    if (s.feaLaw == 0)
+        e = tri_neo_hookean(s, pos, t, f[0], f[1], f[2]);
+    else
+        e = tri_green(s, pos, t, f);
+    s.triF[3 * t + 0] = f[0];
+    s.triF[3 * t + 1] = f[1];
+    s.triF[3 * t + 2] = f[2];
+    s.triE[t] = e;
+    return e;
+}
+
+// ------------------------------------------------------------ particles
+
+// minImage on one axis with the wrap known at compile time.  Sets *wrapped
+// when the difference crossed the boundary (then the exact-image value can
+// differ from the reference float value).
+template <bool WRAP>
+__device__ __forceinline__ float img(float a, float b, float L, bool ex, float &ref, bool &wrapped) {
+    float d = a - b;
+    ref = d;
+    if (WRAP) {
+        if (d >= 0.5f * L) {
+            ref = d - L;
+            wrapped = true;
+            return ex ? ref + two_sum_err(a, -b, d) : ref;
+        }
+        if (d < -0.5f * L) {
+            ref = d + L;
+            wrapped = true;
+            return ex ? ref + two_sum_err(a, -b, d) : ref;
+        }
+    }
+    return d;
+}
+
+// One Lennard-Jones pair (pairForce/ljforce, interactionsCuda.cu:43-100) added
+// into the running force in list order.  Energy and virial are accumulated
+// doubled (u and fc*dr2 per ordered pair) and halved once per particle.
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
+__device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, const PairEntry &pe0, int ti, float si,
+                                        float2 pi, int tag, float2 pj, float &fx, float &fy, float &u2, float &w2) {
+    float dxr, dyr;
+    bool wrapped = false;
+    float dx = img<WX>(pi.x, pj.x, s.Lx, s.imageExact, dxr, wrapped);
+    float dy = img<WY>(pi.y, pj.y, s.Ly, s.imageExact, dyr, wrapped);
+    float dr2r = dxr * dxr + dyr * dyr;
+    const PairEntry &pe = MT ? tab[ti * s.numTypes + ((unsigned)tag >> kIdBits)] : pe0;
+    float rcut2, sig2, c;
+    if (SG) {
+        float sij = (si + __ldg(s.sigma + (tag & kIdMask))) / 2.0f;
+        rcut2 = pe.rc * pe.rc * sij * sij;
+        sig2 = sij * sij;
+        c = pe.eps48 / sig2;
+    } else {
+        rcut2 = pe.rcut2;
+        sig2 = pe.sig2;
+        c = pe.c;
+    }
+    if (dr2r < rcut2) {
+        float dr2 = wrapped ? dx * dx + dy * dy : dr2r;
+        // sigma^2/dr2; with sigma_ij = 1 the IEEE quotient 1/dr2 is the
+        // correctly rounded reciprocal
+        float dr2i = SIG1 ? __frcp_rn(dr2) : sig2 / dr2;
+        float dr6i = dr2i * dr2i * dr2i;
+        float fc = c * dr6i * (dr6i - 0.5f) * dr2i;
+        fx += fc * dx;
+        fy += fc * dy;
+        u2 += pe.eps4 * dr6i * (dr6i - 1.0f) + pe.us;
+        w2 += fc * dr2;
+    }
+}
+
+// One particle's step: bond, triangle and pair forces gathered in the order the
+// reference's CPU path adds them into force[i], then the mode's integration.
+// ue/we (doubled energy and virial), ke and vvm are accumulated by the caller.
+// RO: the list and the neighbours' positions are read through the read-only
+// path (written by an earlier kernel); the batched kernel rewrites both in the
+// same launch and reads them with coherent loads (RO = false).
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true>
+__device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *tab, int i, int mode,
+                                              const float2 *pin, float2 *pout, float &ue_out,
+                                              float &we_out, float &ke, float &vvm, bool &bad) {
+    float ue = 0.0f, we = 0.0f, utri = 0.0f;
+    const float2 pi = pin[i];
+    const float Lx = s.Lx, Ly = s.Ly;
+    float fx = 0.0f, fy = 0.0f;
+    if (i < s.nBonded) {
+        if (s.bondForces) {
+            // calcBondForcesCPU: f on the bond's first particle, -f on the second
+            const int qb = s.bStart[i], qe = s.bStart[i + 1];
+            for (int q = qb; q < qe; q++) {
+                int2 en = __ldg(s.bEnt + q);
+                const bool second = en.x < 0;
+                const int j = en.x & 0x7fffffff;
+                const float r0 = __int_as_float(en.y);
+                const float2 pj = RO ? __ldg(pin + j) : pin[j];
+                const float2 a = second ? pj : pi, b = second ? pi : pj;
+                float dxr, dyr;
+                bool wr = false;
+                float dx = img<WX>(a.x, b.x, Lx, s.imageExact, dxr, wr);
+                float dy = img<WY>(a.y, b.y, Ly, s.imageExact, dyr, wr);
+                float r = sqrtf(dx * dx + dy * dy);
+                float dl = r - r0;
+                float k = s.bondKMode ? s.E / r0 : s.kBond;
+                float kdr = -k * dl / r;
+                float f1 = kdr * dx, f2 = kdr * dy;
+                if (!second) {
+                    fx += f1;
+                    fy += f2;
+                    ue += k * dl * dl;  // doubled like the pair terms
+                } else {
+                    fx -= f1;
+                    fy -= f2;
+                }
+            }
+        }
+        if (s.feaForces) {
+            const int qb = s.tStart[i], qe = s.tStart[i + 1];
+            for (int q = qb; q < qe; q++) {
+                int en = __ldg(s.tEnt + q);
+                float2 f = s.triF[3 * (en >> 2) + (en & 3)];
+                fx += f.x;
+                fy += f.y;
+                if (mode == MODE_FORCES) utri += s.triE[en >> 2] / 3.0f;
+            }
+        }
+    }
+    // pairForce over the Verlet list, in list order.  Entries are taken four
+    // at a time: the four list words and then the four neighbour positions are
+    // loaded before any arithmetic (independent loads in flight together), and
+    // the four pair terms are then added into the running force in order.
+    {
+        const int cnt = min(s.nbrCount[i], s.nbrCap);
+        const int *__restrict__ lst = s.nbr + i;
+        const size_t stride = (size_t)s.Ncap;
+        const int ti = MT ? s.typeId[i] : 0;
+        const float si = SG ? s.sigma[i] : 0.0f;
+        const PairEntry pe0 = tab[0];
+        int k = 0;
+        for (; k + 4 <= cnt; k += 4) {
+            int t[4];
+            float2 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) t[u] = RO ? __ldg(lst + u * stride) : lst[u * stride];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = t[u] & kIdMask;
+                q[u] = RO ? __ldg(pin + j) : pin[j];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, t[u], q[u], fx, fy, ue, we);
+            lst += 4 * stride;
+        }
+        for (; k < cnt; k++) {
+            const int tag = RO ? __ldg(lst) : *lst;
+            const int j = tag & kIdMask;
+            lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tag, RO ? __ldg(pin + j) : pin[j], fx, fy, ue, we);
+            lst += stride;
+        }
+    }
+    ue *= 0.5f;
+    we *= 0.5f;
+    bad = bad || !(isfinite(fx) && isfinite(fy));
+    const float m = s.mass[i];
+    const float ax = fx / m, ay = fy / m;
+    const float dt = s.dt, hdt = s.hdt;
+    if (mode == MODE_FORCES) {
+        s.forceOut[i] = make_float2(fx, fy);
+        s.energyOut[i] = ue + utri;
+    } else if (mode == MODE_INIT) {
+        s.acc[i] = make_float2(ax, ay);
+        s.forceOut[i] = make_float2(fx, fy);
+    } else {
+        float2 v = s.vel[i];
+        if (mode == MODE_MID || mode == MODE_LAST) {
+            // leapFrogStep2 then evalProps
+            v.x += hdt * ax;
+            v.y += hdt * ay;
+            float vv = v.x * v.x + v.y * v.y;
+            vvm = fmaxf(vvm, vv);
+            ke += m * vv;
+        }
+        if (mode == MODE_LAST) {
+            s.vel[i] = v;
+            s.acc[i] = make_float2(ax, ay);
+            s.forceOut[i] = make_float2(fx, fy);
+        } else {
+            // next step's leapFrogStep1 + applyPBC
+            v.x += hdt * ax;
+            v.y += hdt * ay;
+            float2 x = make_float2(pi.x + dt * v.x, pi.y + dt * v.y);
+            if (WX) x.x = wrap_coord(x.x, Lx);
+            if (WY) x.y = wrap_coord(x.y, Ly);
+            pout[i] = x;
+            s.vel[i] = v;
+        }
+    }
+    ue_out += ue;
+    we_out += we;
+}
+
+}  // namespace femmd

@@ -421,3 +421,71 @@ def large_mixed(n_side: int = 64, n_solvent: int = 1_000_000, radius: float = 5.
     sc.add("init_neighbor_list")
     sc.add("set_velocities_array", vel.astype(np.float32))
     return sc
+
+
+def mixed_replica(n_total: int, density: float, T: float, seed: int, radius: float = 5.0, rings: int = 6,
+                  E: float = 50.0, nu: float = 0.3, kbond: float = 100.0, dt: float = 0.005, skin: float = 0.3,
+                  mesh=None) -> Scene:
+    """One replica of the batched ensemble: 90 % LJ solvent by count plus
+    floor(0.1 n_total / 127) hex-ring disks, two types as the large mixed
+    system (solvent-solvent LJ rc = 2.5, pairs with a vertex WCA)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    if mesh is None:
+        verts, tris = hex_disk_mesh(radius, rings, jitter=0.02, seed=3)
+    else:
+        verts, tris = mesh
+    nv = verts.shape[0]
+    nd = int(0.1 * n_total // nv)
+    n_solv = n_total - nd * nv
+    L = math.sqrt(n_solv / density + nd * math.pi * radius ** 2)
+    centers = np.zeros((0, 2))
+    if nd:
+        side = int(math.ceil(math.sqrt(nd)))
+        a = L / side
+        gx, gy = np.meshgrid(np.arange(side), np.arange(side), indexing="xy")
+        lat = (np.stack([gx.ravel(), gy.ravel()], 1) + 0.5) * a
+        centers = lat[rng.permutation(lat.shape[0])[:nd]] + rng.uniform(-0.5, 0.5, size=(nd, 2))
+    excl_r = radius + 1.0
+    avail = L * L - nd * math.pi * excl_r ** 2
+    m = int(math.ceil(L / math.sqrt(max(avail, 1e-9) / (n_solv * 1.05))))
+    while True:
+        sp = L / m
+        sx, sy = np.meshgrid(np.arange(m), np.arange(m), indexing="xy")
+        sites = (np.stack([sx.ravel(), sy.ravel()], 1) + 0.5) * sp + rng.uniform(-0.05 * sp, 0.05 * sp,
+                                                                                 size=(m * m, 2))
+        keep = np.ones(sites.shape[0], bool)
+        for c in centers:
+            d = sites - c
+            d -= L * np.round(d / L)
+            keep &= (d ** 2).sum(1) >= excl_r ** 2
+        if keep.sum() >= n_solv:
+            break
+        m += 1
+    sites = np.mod(sites[keep][:n_solv], L)
+    vel = _mb_velocities(rng, n_total, T)
+    sc = Scene(meta=dict(workload="mixed_replica", N=n_total, L=L, n_disks=nd))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", dt).add("set_numTypes", 2)
+    sc.add("set_pair_potential", [1.0, 1.0, 1.0, 1.0], [2.5, WCA_RC, WCA_RC, WCA_RC], [lj_shift(2.5), 1.0, 1.0, 1.0])
+    sc.add("set_skin", skin)
+    sc.add("set_kBond", kbond).add("set_youngs_modulus", E).add("set_poisson_ratio", nu)
+    sc.add("set_elastomer_bonds", 1)
+    for c in centers:
+        sc.add("add_elastomer", verts, tris, float(c[0]), float(c[1]), 1, 0, 1.0, float(nv), True)
+    sc.add("add_particles", sites[:, 0], sites[:, 1], np.zeros(n_solv), np.zeros(n_solv), np.ones(n_solv),
+           np.ones(n_solv), np.zeros(n_solv, np.int32))
+    sc.add("init_neighbor_list")
+    sc.add("set_velocities_array", vel.astype(np.float32))
+    return sc
+
+
+def batched_ensemble(n_replicas: int = 512, n_min: int = 500, n_max: int = 20000, seeds=(8, 9)):
+    """Benchmark config 4: replica sizes log-uniform in [n_min, n_max] (seed 8),
+    density U(0.6, 0.85) and temperature U(0.1, 1.5) (seed 9)."""
+    rs = np.random.Generator(np.random.PCG64(seeds[0]))
+    rp = np.random.Generator(np.random.PCG64(seeds[1]))
+    sizes = np.rint(np.exp(rs.uniform(math.log(n_min), math.log(n_max), size=n_replicas))).astype(int)
+    dens = rp.uniform(0.6, 0.85, size=n_replicas)
+    temps = rp.uniform(0.1, 1.5, size=n_replicas)
+    mesh = hex_disk_mesh(5.0, 6, jitter=0.02, seed=3)
+    return [mixed_replica(int(sizes[r]), float(dens[r]), float(temps[r]), seed=1000 + r, mesh=mesh)
+            for r in range(n_replicas)]

@@ -192,6 +192,12 @@ femmd_status femmd_get_state(femmd_ctx *ctx, float *pos, float *vel, float *acc)
 /* ------------------------------------------------- device-side access */
 /* The context's CUDA stream (cudaStream_t) for event timing by the caller. */
 void *femmd_get_stream(femmd_ctx *ctx);
+/* Device-side trace of the next runs (on != 0): per step, %globaltimer
+ * nanoseconds at the start and end of the triangle pass, the step kernel and
+ * the neighbour rebuild (0 where a phase did not run), rows as the
+ * observables of femmd_get_step_observables. */
+femmd_status femmd_set_trace(femmd_ctx *ctx, int on);
+femmd_status femmd_get_trace(femmd_ctx *ctx, unsigned long long *out, int max_rows, int *rows);
 /* CUDA events on the context stream (slots 0..63) for device-side timing. */
 femmd_status femmd_event_record(femmd_ctx *ctx, int slot);
 femmd_status femmd_event_elapsed(femmd_ctx *ctx, int slot_a, int slot_b, float *ms);
@@ -201,6 +207,31 @@ femmd_status femmd_event_elapsed(femmd_ctx *ctx, int slot_a, int slot_b, float *
 femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile);
 femmd_status femmd_get_profile(femmd_ctx *ctx, double *force_kernel_ms, long long *force_kernel_launches,
                                double *rebuild_ms, long long *rebuilds, long long *kernel_launches);
+
+/* ------------------------------------------------------- batched replicas */
+/* Many independent systems advanced in one persistent launch: each replica
+ * is a context set up as usual (through init_neighbor_list); femmd_batch_run(n)
+ * performs femmd_run(n) on every replica -- same results, bit for bit, as
+ * running them one by one -- with one CTA per group of replicas
+ * (longest-processing-time assignment) and no per-step launches.  Replicas
+ * must share the number of types, the sigma mode, the periodicity and the
+ * image mode.  A replica's results are read with the usual getters on its
+ * context.  The batch does not own the contexts. */
+typedef struct femmd_batch femmd_batch;
+femmd_status femmd_batch_create(int device, femmd_batch **out);
+void femmd_batch_destroy(femmd_batch *b);
+const char *femmd_batch_last_error(const femmd_batch *b);
+femmd_status femmd_batch_add(femmd_batch *b, femmd_ctx *ctx, int *index);
+int femmd_batch_size(const femmd_batch *b);
+femmd_status femmd_batch_run(femmd_batch *b, int steps);
+/* Launch shape: threads per CTA (multiple of 32, <= 1024) and CTAs per SM. */
+femmd_status femmd_batch_set_launch(femmd_batch *b, int threads, int ctas_per_sm);
+femmd_status femmd_batch_get_launch(const femmd_batch *b, int *threads, int *ctas_per_sm, int *ctas);
+/* Times trial_steps on each candidate launch shape (states restored after each
+ * trial) and keeps the fastest. */
+femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads, int *ctas_per_sm, double *best_ms);
+femmd_status femmd_batch_event_record(femmd_batch *b, int slot);
+femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, float *ms);
 
 /* ------------------------------------------ cell binning without allocation */
 /* Limits of femmd_bin_cells_noalloc.  Its working memory is one fixed array of

@@ -1,0 +1,99 @@
+"""Batched replicas (femmd_batch_*): one persistent launch advancing many
+systems of uneven size.  Every replica must end bit-identical to the same
+system run alone through System.run (positions, velocities, accelerations,
+step and rebuild counters), whatever the launch shape, including when a
+replica's neighbour list overflows and the batch rolls back and repeats."""
+import numpy as np
+import pytest
+
+import golden_io as G
+import femmd_old_gb300 as F
+from femmd_old_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+def replicas(n=7, seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = [300, 700, 1800, 2600, 4100, 900, 1400][:n]
+    return [S.mixed_replica(int(sz), float(rng.uniform(0.6, 0.85)), float(rng.uniform(0.1, 1.5)), seed=100 + k)
+            for k, sz in enumerate(sizes)]
+
+
+def alone(sc, steps_list):
+    s = F.System(0)
+    sc.replay(s)
+    for n in steps_list:
+        s.run(n)
+    return s
+
+
+def same(a, b):
+    pa, va, aa = a.get_state()
+    pb, vb, ab = b.get_state()
+    return (np.array_equal(G.bits(pa), G.bits(pb)) and np.array_equal(G.bits(va), G.bits(vb))
+            and np.array_equal(G.bits(aa), G.bits(ab)) and a.steps() == b.steps()
+            and a.total_updates() == b.total_updates())
+
+
+@pytest.mark.parametrize("launch", [(512, 2), (128, 4), (1024, 1)])
+def test_batch_matches_replicas_run_alone(launch):
+    scs = replicas()
+    b = F.Batch(0)
+    systems = []
+    for sc in scs:
+        s = F.System(0)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    b.set_launch(*launch)
+    b.run(60)
+    b.run(0)
+    b.run(41)
+    for sc, s in zip(scs, systems):
+        assert same(s, alone(sc, [60, 0, 41]))
+
+
+def test_batch_autotune_keeps_results():
+    scs = replicas(5, seed=1)
+    b = F.Batch(0)
+    systems = []
+    for sc in scs:
+        s = F.System(0)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    cfg = b.autotune(5)
+    assert cfg["threads"] in (128, 256, 512, 1024)
+    b.run(50)
+    for sc, s in zip(scs, systems):
+        assert same(s, alone(sc, [50]))
+
+
+def test_batch_overflow_rolls_back_and_repeats():
+    scs = replicas(4, seed=2)
+    b = F.Batch(0)
+    systems = []
+    for k, sc in enumerate(scs):
+        s = F.System(0)
+        sc.replay(s)
+        if k == 2:
+            s.set_neighbor_capacity(2)
+        systems.append(s)
+        b.add(s)
+    b.run(40)
+    assert systems[2].neighbor_capacity() > 2
+    for sc, s in zip(scs, systems):
+        assert same(s, alone(sc, [40]))
+
+
+def test_batch_rejects_mixed_variants():
+    a = F.System(0)
+    S.mixed_replica(500, 0.7, 1.0, seed=7).replay(a)
+    c = F.System(0)
+    S.lj_fluid(n_side=16).replay(c)  # one type: a different kernel variant
+    b = F.Batch(0)
+    b.add(a)
+    b.add(c)
+    with pytest.raises(F.FemmdError):
+        b.run(5)
