@@ -9,7 +9,8 @@ import ctypes as C
 import os
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libfemmd.so")
+# FEMMD_LIBRARY names another build of the same library (same C ABI) to load
+LIB_PATH = os.environ.get("FEMMD_LIBRARY") or os.path.join(PKG, "libfemmd.so")
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CAPACITY_OVERFLOW", 3: "NONFINITE", 4: "CUDA_ERROR", 5: "TIMEOUT",
           6: "NOT_READY", 7: "UNSUPPORTED"}

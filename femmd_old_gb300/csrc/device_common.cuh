@@ -53,14 +53,27 @@ __device__ __forceinline__ float wrap_coord(float r, float L) { return r - floor
 // an index equal to the cell count is moved into the last cell.  Indices
 // outside the grid (only reachable on a non-periodic axis, where the
 // reference reads out of bounds) are clamped.
-__device__ __forceinline__ int cell_of(float x, float y, int ncx, int ncy, float Lx, float Ly) {
-    int ix = (int)(x * (float)ncx / Lx);
+__device__ __forceinline__ void cell_xy(float x, float y, int ncx, int ncy, float Lx, float Ly, int &ix, int &iy) {
+    ix = (int)(x * (float)ncx / Lx);
     if (ix == ncx) ix -= 1;
-    int iy = (int)(y * (float)ncy / Ly);
+    iy = (int)(y * (float)ncy / Ly);
     if (iy == ncy) iy -= 1;
     ix = ix < 0 ? 0 : (ix >= ncx ? ncx - 1 : ix);
     iy = iy < 0 ? 0 : (iy >= ncy ? ncy - 1 : iy);
+}
+
+// the reference's row-major cell index ix + iy*ncx
+__device__ __forceinline__ int cell_of(float x, float y, int ncx, int ncy, float Lx, float Ly) {
+    int ix, iy;
+    cell_xy(x, y, ncx, ncy, Lx, Ly, ix, iy);
     return ix + iy * ncx;
+}
+
+// the column-major index ix*ncy + iy used by the list build
+__device__ __forceinline__ int cell_col(float x, float y, int ncx, int ncy, float Lx, float Ly) {
+    int ix, iy;
+    cell_xy(x, y, ncx, ncy, Lx, Ly, ix, iy);
+    return ix * ncy + iy;
 }
 
 // Natural log by fdlibm-style reduction x = 2^k m, m in [sqrt(1/2), sqrt(2)),

@@ -111,7 +111,7 @@ struct femmd_ctx {
     int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1, sigmaOne = 0;
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF;
     DBuf<float> dmass, dsigma, denergy, triE, partialsMax;
-    DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, sortedIds, nbr, nbrCount, bStart, tStart,
+    DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, unsorted, sortedIds, nbr, nbrCount, bStart, tStart,
         tEnt;
     DBuf<int2> bEnt;
     DBuf<int4> triIdx;
@@ -223,7 +223,7 @@ static void release_device(femmd_ctx *c) {
     c->dref.release(); c->ckPos.release(); c->ckVel.release(); c->ckAcc.release(); c->triF.release();
     c->dmass.release(); c->dsigma.release(); c->denergy.release(); c->triE.release(); c->partialsMax.release();
     c->dtype.release(); c->dexcl.release(); c->cellOf.release(); c->rank.release(); c->cellCount.release();
-    c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->nbr.release();
+    c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->unsorted.release(); c->nbr.release();
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
     c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
@@ -322,6 +322,7 @@ static DevSys make_sys(femmd_ctx *c) {
     s.cellStart = c->cellStart.p;
     s.blockSums = c->blockSums.p;
     s.sortedIds = c->sortedIds.p;
+    s.unsorted = c->unsorted.p;
     s.cellSorted = c->cellSorted.p;
     s.nbr = c->nbr.p;
     s.nbrCount = c->nbrCount.p;
@@ -433,7 +434,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
     CK(ctx->ckPos.ensure(N)); CK(ctx->ckVel.ensure(N)); CK(ctx->ckAcc.ensure(N));
     CK(ctx->dmass.ensure(N)); CK(ctx->dtype.ensure(N)); CK(ctx->dexcl.ensure(N));
     CK(ctx->dsigma.ensure(ctx->sigmaByType ? 1 : N));
-    CK(ctx->cellOf.ensure(N)); CK(ctx->rank.ensure(N)); CK(ctx->sortedIds.ensure(N));
+    CK(ctx->cellOf.ensure(N)); CK(ctx->rank.ensure(N)); CK(ctx->sortedIds.ensure(N)); CK(ctx->unsorted.ensure(N));
     CK(ctx->cellSorted.ensure(N)); CK(ctx->nbrCount.ensure(N));
     CK(ctx->cellCount.ensure(ctx->ncells)); CK(ctx->cellStart.ensure(ctx->ncells + 1));
     CK(ctx->blockSums.ensure(scan_blocks(ctx->ncells)));
@@ -575,13 +576,13 @@ static femmd_status size_list(femmd_ctx *ctx, int min_cap) {
     s.nbrCap = 0;
     Launch L;
     L.stream = ctx->stream;
-    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));
     CK(enqueue_rebuild(L, s, ctx->cur, 0));
     femmd_status st;
     if ((st = read_scalars(ctx))) return st;
     if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a position is NaN or infinite");
     int need = ctx->hsc->maxCount + ctx->hsc->maxCount / 4 + 8;
-    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));
     return alloc_list(ctx, std::max(need, min_cap));
 }
 
@@ -1145,7 +1146,7 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(ctx->ckPos.p, pc, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckVel.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckAcc.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
-        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));  // overflow, nonfinite
+        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));  // overflow, nonfinite, outside
         if (ctx->tracing)
             CK(cudaMemsetAsync(ctx->trace.p, 0, (size_t)ctx->obsCap * kTraceCols * sizeof(unsigned long long),
                                ctx->stream));
@@ -1185,7 +1186,7 @@ femmd_status femmd_do_step(femmd_ctx *ctx) {
     DevSys s = make_sys(ctx);
     Launch L;
     L.stream = ctx->stream;
-    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));
     CK(enqueue_drift(L, s, ctx->cur));
     ctx->cur ^= 1;
     CK(enqueue_rebuild(L, s, ctx->cur, 1));
@@ -1207,7 +1208,7 @@ femmd_status femmd_build_neighbor_list(femmd_ctx *ctx) {
         DevSys s = make_sys(ctx);
         Launch L;
         L.stream = ctx->stream;
-        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 2 * sizeof(int), ctx->stream));  // overflow, nonfinite
+        CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));  // overflow, nonfinite, outside
         CK(enqueue_rebuild(L, s, ctx->cur, 0));
         if ((st = read_scalars(ctx))) return st;
         if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a position is NaN or infinite");
@@ -1377,12 +1378,24 @@ femmd_status femmd_get_cells(femmd_ctx *ctx, int *cell_start, int *cell_ids) {
     NEED(ctx);
     if (!ctx->listBuilt) return fail(ctx, FEMMD_NOT_READY, "no neighbour list has been built");
     const int N = (int)ctx->pos.size();
-    if (cell_start)
-        CK(cudaMemcpyAsync(cell_start, ctx->cellStart.p, (ctx->ncells + 1) * sizeof(int), cudaMemcpyDeviceToHost,
-                           ctx->stream));
-    if (cell_ids && N)
-        CK(cudaMemcpyAsync(cell_ids, ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    // the device numbers cells column-major (ix*ncy + iy); the reference's
+    // numbering is row-major (ix + iy*ncx)
+    std::vector<int> start(ctx->ncells + 1), ids(N);
+    CK(cudaMemcpyAsync(start.data(), ctx->cellStart.p, (ctx->ncells + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    if (N) CK(cudaMemcpyAsync(ids.data(), ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    int at = 0;
+    for (int iy = 0; iy < ctx->ncy; iy++)
+        for (int ix = 0; ix < ctx->ncx; ix++) {
+            const int c = ix * ctx->ncy + iy;
+            if (cell_start) cell_start[ix + iy * ctx->ncx] = at;
+            for (int q = start[c]; q < start[c + 1]; q++) {
+                if (cell_ids && at < N) cell_ids[at] = ids[q];
+                at++;
+            }
+        }
+    if (cell_start) cell_start[ctx->ncells] = at;
     return FEMMD_OK;
 }
 
@@ -1714,7 +1727,7 @@ static femmd_status batch_checkpoint(femmd_batch *b, bool restore) {
             BCK(cudaMemcpyAsync(c->ckPos.p, pd, n, cudaMemcpyDeviceToDevice, b->stream));
             BCK(cudaMemcpyAsync(c->ckVel.p, c->dvel.p, n, cudaMemcpyDeviceToDevice, b->stream));
             BCK(cudaMemcpyAsync(c->ckAcc.p, c->dacc.p, n, cudaMemcpyDeviceToDevice, b->stream));
-            BCK(cudaMemsetAsync(&c->sc.p->overflow, 0, 2 * sizeof(int), b->stream));
+            BCK(cudaMemsetAsync(&c->sc.p->overflow, 0, 3 * sizeof(int), b->stream));
         } else {
             BCK(cudaMemcpyAsync(pd, c->ckPos.p, n, cudaMemcpyDeviceToDevice, b->stream));
             BCK(cudaMemcpyAsync(c->dvel.p, c->ckVel.p, n, cudaMemcpyDeviceToDevice, b->stream));

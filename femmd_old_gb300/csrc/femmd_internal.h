@@ -8,7 +8,9 @@
 //   acc     float2[N]    acceleration (written by the last step of a run)
 //   mass    float[N], typeId int[N], sigma float[N] (only when sigma varies inside a type)
 //   excl    int[N]       exclusion group (-1 = none)
-//   cells   cellStart[ncells+1], cellSorted float4[N] = (x, y, id|type<<27, excl)
+//   cells   column-major cell index c = ix*ncy + iy (so the three cells of one stencil
+//           column are adjacent), cellStart[ncells+1], sortedIds[N] (ascending id
+//           inside a cell), cellSorted float4[N] = (x, y, id|type<<27, excl)
 //   nbr     int[cap][Ncap] neighbour-major list (entry = id | type<<27), nbrCount[N]
 //   bonds   per-particle incidence CSR (bStart, bEnt = {partner|sign<<31, r0 bits})
 //   tris    triIdx int4[nt], triGeo float4[2nt] (neo-Hookean: Bm, vol0; Green: xm rows 1-2, area),
@@ -53,8 +55,8 @@ struct DevScalars {
     float vvMax, dispHi;
     int rebuild, totalUpdates;
     unsigned int ticket, triTicket;
-    int overflow, nonfinite, maxCount, obsRow;
-    int maxCand, pad0;
+    int overflow, nonfinite, outside, maxCount;  // the first three are cleared together by the host
+    int obsRow, pad0;
     unsigned long long nbrSum, builds;
     unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
     unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
@@ -77,7 +79,7 @@ struct DevSys {
     float *energyOut;
     const float *mass, *sigma;
     const int *typeId, *excl;
-    int *cellOf, *rank, *cellCount, *cellStart, *blockSums, *sortedIds;
+    int *cellOf, *rank, *cellCount, *cellStart, *blockSums, *unsorted, *sortedIds;
     float4 *cellSorted;
     int *nbr, *nbrCount;
     int nbrCap;

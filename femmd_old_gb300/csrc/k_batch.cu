@@ -85,7 +85,8 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
         if (act) {
             float2 p = pos[i];
             if (!(isfinite(p.x) && isfinite(p.y))) atomicOr(&s.sc->nonfinite, 1);
-            int c = cell_of(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
+            if (outside_box(s, p)) atomicOr(&s.sc->outside, 1);
+            int c = cell_col(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
             s.cellOf[i] = c;
             unsigned peers = __match_any_sync(active, c);
             int leader = __ffs(peers) - 1;
@@ -139,23 +140,22 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
     for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
         int slot = s.cellStart[s.cellOf[i]] + s.rank[i];
         if (slot >= 0 && slot < s.N)
-            s.sortedIds[slot] = i;
+            s.unsorted[slot] = i;
         else
             atomicOr(&s.sc->overflow, 2);
     }
     __syncthreads();
-    const bool skip = s.sc->nonfinite != 0;  // crowded cells after a blow-up: skip the quadratic parts
-    int cand = 0;
+    // crowded cells after a blow-up or inconsistent counts: skip the quadratic parts
+    const bool skip = s.sc->nonfinite != 0 || (s.sc->overflow & 2);
     if (!skip)
-        for (int c = threadIdx.x; c < s.ncells; c += blockDim.x) cand = max(cand, sort_cell(s, pos, c));
-    cand = block_max_int(cand, iscr);
-    if (threadIdx.x == 0 && cand > s.sc->maxCand) s.sc->maxCand = cand;
+        for (int i = threadIdx.x; i < s.N; i += blockDim.x) place_one<false>(s, pos, i, &s.sc->overflow);
     __syncthreads();
+    const bool fast = fast_walk_ok(s);
     int kmax = 0;
     unsigned long long ksum = 0;
     if (!skip)
         for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
-            int k = build_one<false>(s, pos, i);
+            int k = fast ? build_fast<false>(s, pos, i) : build_general<false>(s, pos, i);
             kmax = max(kmax, k);
             ksum += (unsigned long long)k;
         }

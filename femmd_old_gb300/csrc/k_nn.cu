@@ -65,9 +65,10 @@ __global__ void __launch_bounds__(kBlock) k_cells_count(DevSys s, int parity, in
     if (!act) return;
     float2 p = pos[i];
     // a non-finite position would land in a clamped edge cell; flag it so the
-    // per-cell sort and the list build (quadratic in a cell's size) are skipped
+    // in-cell placement and the list build (quadratic in a cell's size) are skipped
     if (!(isfinite(p.x) && isfinite(p.y))) atomicOr(&s.sc->nonfinite, 1);
-    int c = cell_of(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
+    if (outside_box(s, p)) atomicOr(&s.sc->outside, 1);
+    int c = cell_col(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
     s.cellOf[i] = c;
     unsigned peers = __match_any_sync(active, c);
     int lane = threadIdx.x & 31;
@@ -143,7 +144,6 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(DevSys s, int nblocks
         s.cellStart[s.ncells] = s.N;
         s.sc->nbrSum = 0ull;
         s.sc->maxCount = 0;
-        s.sc->maxCand = 0;
     }
 }
 
@@ -153,32 +153,27 @@ __global__ void __launch_bounds__(kBlock) k_scatter(DevSys s, int check) {
     if (i >= s.N) return;
     int slot = s.cellStart[s.cellOf[i]] + s.rank[i];
     if (slot >= 0 && slot < s.N)
-        s.sortedIds[slot] = i;
+        s.unsorted[slot] = i;
     else
         atomicOr(&s.sc->overflow, 2);  // inconsistent counts: never write outside the array
 }
 
-// ascending id inside each cell + the cell-ordered float4 copy
-__global__ void __launch_bounds__(kBlock) k_cell_sort(DevSys s, int parity, int check) {
-    if ((check && !s.sc->rebuild) || s.sc->nonfinite) return;
+// ascending id inside each cell + the cell-ordered float4 copy, one thread
+// per particle
+__global__ void __launch_bounds__(kBlock) k_cell_place(DevSys s, int parity, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    int cand = 0;
-    if (c < s.ncells) {
-        cand = sort_cell(s, pos, c);
-    }
-    cand = warp_max_int(cand);
-    if ((threadIdx.x & 31) == 0 && cand > 0) atomicMax(&s.sc->maxCand, cand);
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s.N) place_one<true>(s, pos, i, &s.sc->overflow);
 }
 
 __global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int check) {
-    if ((check && !s.sc->rebuild) || s.sc->nonfinite) return;
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool fast = fast_walk_ok(s);
     int k = 0;
-    if (i < s.N) {
-        k = build_one<true>(s, pos, i);
-    }
+    if (i < s.N) k = fast ? build_fast<true>(s, pos, i) : build_general<true>(s, pos, i);
     // build statistics and overflow
     int kmax = warp_max_int(k);
     int ksum = warp_sum_int(k);
@@ -200,13 +195,12 @@ cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
     cudaError_t e;
     int pb = (s.N + kBlock - 1) / kBlock;
     int nsb = scan_blocks(s.ncells);
-    int cb = (s.ncells + kBlock - 1) / kBlock;
     if (check && (e = L.kernel(k_rebuild_begin, dim3(1), dim3(32), 0, s))) return e;
     if ((e = L.kernel(k_cells_count, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     if ((e = L.kernel(k_scan_blocks, dim3(nsb), dim3(kScanBlock), 0, s, check))) return e;
     if ((e = L.kernel(k_scan_apply, dim3(nsb), dim3(kScanBlock), 0, s, nsb, check))) return e;
     if ((e = L.kernel(k_scatter, dim3(pb), dim3(kBlock), 0, s, check))) return e;
-    if ((e = L.kernel(k_cell_sort, dim3(cb), dim3(kBlock), 0, s, parity, check))) return e;
+    if ((e = L.kernel(k_cell_place, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     if ((e = L.kernel(k_build_nn, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     return cudaSuccess;
 }

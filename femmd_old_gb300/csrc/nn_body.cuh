@@ -1,8 +1,16 @@
-// nn_body.cuh -- per-cell and per-particle work of the neighbour-list rebuild,
-// shared by the plain kernels (k_nn.cu) and the persistent batched kernel
-// (k_batch.cu).  Reference: updateCellsCPU (femmd2D/src/nn.cpp:8-20) order
-// inside a cell, buildNNCPUSerial (nn.cpp:22-62) with applyCellBC
-// (nnCuda.cu:26-36).
+// nn_body.cuh -- per-particle work of the neighbour-list rebuild, shared by
+// the plain kernels (k_nn.cu) and the persistent batched kernel (k_batch.cu).
+//
+// Reference: updateCellsCPU (femmd2D/src/nn.cpp:8-20) puts each cell's
+// particles in ascending id order; buildNNCPUSerial (nn.cpp:22-62) walks the
+// 3x3 stencil with dx outer, dy inner, cell indices wrapped as applyCellBC
+// (nnCuda.cu:26-36), and keeps a pair when the minimum-image distance
+// squared is within nnRadius^2 and the two are not in the same exclusion
+// group.  The list order of every particle is that walk's order.
+//
+// Cells are numbered column-major (c = ix*ncy + iy): the dy = -1, 0, +1 cells
+// of one stencil column are then adjacent in cellSorted, so a column is one
+// contiguous range of candidates (two when it wraps in y), in the same order.
 #pragma once
 #include <cuda_runtime.h>
 #include "femmd_internal.h"
@@ -10,81 +18,146 @@
 
 namespace femmd {
 
-// Sort cell c's particle ids ascending, write its cellSorted entries and
-// return the candidate count of its 3x3 stencil.
-__device__ __forceinline__ int sort_cell(const DevSys &s, const float2 *pos, int c) {
-    int cand = 0;
-    int b = s.cellStart[c], e = s.cellStart[c + 1], n = e - b;
-    int *ids = s.sortedIds + b;
-    // Shell sort with gaps 3h+1 ending in insertion sort (a cell holds a
-    // handful of particles; the gaps bound the work of crowded cells)
-    int gap = 1;
-    while (gap < n / 3) gap = 3 * gap + 1;
-    for (; gap > 0; gap /= 3) {
-        for (int k = gap; k < n; k++) {
-            int v = ids[k];
-            int m = k - gap;
-            while (m >= 0 && ids[m] > v) {
-                ids[m + gap] = ids[m];
-                m -= gap;
+// Place particle i at its ascending-id rank inside its cell: count the ids of
+// the cell (scattered in arbitrary order by the counting sort) below i.
+// Writes sortedIds and the cell-ordered float4 copy of the particle.
+template <bool RO>
+__device__ __forceinline__ void place_one(const DevSys &s, const float2 *pos, int i, int *bad) {
+    const int c = s.cellOf[i];
+    const int b = s.cellStart[c], e = s.cellStart[c + 1];
+    int r = 0;
+    for (int q = b; q < e; q++) r += (RO ? __ldg(s.unsorted + q) : s.unsorted[q]) < i;
+    const int slot = b + r;
+    if (slot >= e) {  // inconsistent cell contents: never write outside the cell
+        atomicOr(bad, 2);
+        return;
+    }
+    const float2 p = pos[i];
+    const int tag = i | (s.numTypes > 1 ? (s.typeId[i] << kIdBits) : 0);
+    s.sortedIds[slot] = i;
+    s.cellSorted[slot] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[i]));
+}
+
+// Whether the fast walk below reproduces the reference's minimum image for
+// every candidate: with at least 5 cells along a periodic axis and every
+// position inside [0, L] there, a candidate from a neighbouring cell that did
+// not wrap is closer than L/2 (no image), and one from a wrapped cell is at
+// least L/2 away on the side the wrap says (exactly one shift of L).  Needs
+// 3 distinct stencil cells per axis.
+__device__ __forceinline__ bool fast_walk_ok(const DevSys &s) {
+    return (s.wrapx ? s.ncx >= 5 : s.ncx >= 3) && (s.wrapy ? s.ncy >= 5 : s.ncy >= 3) && !s.sc->outside;
+}
+
+// One contiguous candidate range with a known image shift (sx, sy): the
+// reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
+template <bool RO>
+__device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int i,
+                                           int gi, float R2, int cap, size_t stride, int *&out, int &k) {
+    for (int q = qb; q < qe; q++) {
+        const float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
+        const float dx = (p.x - e.x) - sx;
+        const float dy = (p.y - e.y) - sy;
+        const float dr2 = dx * dx + dy * dy;
+        const int tag = __float_as_int(e.z);
+        const int gj = __float_as_int(e.w);
+        if (dr2 <= R2 && (tag & kIdMask) != i && (gi == -1 || gj == -1 || gi != gj)) {
+            if (k < cap) {
+                *out = tag;
+                out += stride;
             }
-            ids[m + gap] = v;
+            k++;
         }
     }
-    for (int k = 0; k < n; k++) {
-        int id = ids[k];
-        float2 p = pos[id];
-        int tag = id | (s.numTypes > 1 ? (s.typeId[id] << kIdBits) : 0);
-        s.cellSorted[b + k] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[id]));
-    }
-    // candidate count of the 3x3 stencil (capacity sizing)
-    int cy = c / s.ncx, cx = c - cy * s.ncx;
-    for (int dx = -1; dx <= 1; dx++)
-        for (int dy = -1; dy <= 1; dy++) {
-            int nx = cx + dx, ny = cy + dy;
-            if (nx < 0) nx = s.ncx - 1; else if (nx == s.ncx) nx = 0;
-            if (ny < 0) ny = s.ncy - 1; else if (ny == s.ncy) ny = 0;
-            int nc = nx + ny * s.ncx;
-            cand += s.cellStart[nc + 1] - s.cellStart[nc];
-        }
-    return cand;
 }
 
 // Verlet list of particle i in the reference's order; returns its length
 // (entries beyond the capacity are counted, not written).  RO: the cell
-// arrays are read through the read-only path (they were written by an
-// earlier kernel); the batched kernel rewrites them in the same launch and
-// reads them with coherent loads.
+// arrays are read through the read-only path (written by an earlier kernel);
+// the batched kernel rewrites them in the same launch (coherent loads).
 template <bool RO>
-__device__ __forceinline__ int build_one(const DevSys &s, const float2 *pos, int i) {
+__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i) {
+    const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
+    const size_t stride = (size_t)s.Ncap;
+    const float R2 = s.nnRadiusSq;
+    const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
+    const int c = s.cellOf[i];
+    const int ix = c / ncy, iy = c - ix * ncy;
+    const float2 p = pos[i];
+    const int gi = s.excl[i];
+    int *out = s.nbr + i;
+    int k = 0;
+    const int *cs = s.cellStart;
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; dx++) {
+        int nx = ix + dx;
+        float sx = 0.0f;
+        if (nx < 0) {
+            nx = ncx - 1;
+            sx = -Lx;
+        } else if (nx == ncx) {
+            nx = 0;
+            sx = Lx;
+        }
+        const int col = nx * ncy;
+        if (iy > 0 && iy < ncy - 1) {
+            const int qb = RO ? __ldg(cs + col + iy - 1) : cs[col + iy - 1];
+            const int qe = RO ? __ldg(cs + col + iy + 2) : cs[col + iy + 2];
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+        } else if (iy == 0) {
+            // dy = -1 wraps to the top cell, then dy = 0, +1
+            int qb = RO ? __ldg(cs + col + ncy - 1) : cs[col + ncy - 1];
+            int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
+            walk_range<RO>(s, qb, qe, sx, -Ly, p, i, gi, R2, cap, stride, out, k);
+            qb = RO ? __ldg(cs + col) : cs[col];
+            qe = RO ? __ldg(cs + col + 2) : cs[col + 2];
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+        } else {
+            // dy = -1, 0, then dy = +1 wraps to the bottom cell
+            int qb = RO ? __ldg(cs + col + ncy - 2) : cs[col + ncy - 2];
+            int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+            qb = RO ? __ldg(cs + col) : cs[col];
+            qe = RO ? __ldg(cs + col + 1) : cs[col + 1];
+            walk_range<RO>(s, qb, qe, sx, Ly, p, i, gi, R2, cap, stride, out, k);
+        }
+    }
+    s.nbrCount[i] = k;
+    return k;
+}
+
+// The general walk: any grid (1 or 2 cells along an axis visit the same cell
+// more than once, as the reference does), any position, the minimum image
+// decided per pair.
+template <bool RO>
+__device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos, int i) {
     int k = 0;
     const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap, Ncap = s.Ncap;
     const bool wx = s.wrapx, wy = s.wrapy;
     const float Lx = s.Lx, Ly = s.Ly, R2 = s.nnRadiusSq;
-    int c = s.cellOf[i];
-    int cy0 = c / ncx, cx0 = c - cy0 * ncx;
-    float2 p = pos[i];
-    int gi = s.excl[i];
+    const int c = s.cellOf[i];
+    const int ix = c / ncy, iy = c - ix * ncy;
+    const float2 p = pos[i];
+    const int gi = s.excl[i];
     int *out = s.nbr + i;
     for (int dx = -1; dx <= 1; dx++) {
-        int nx = cx0 + dx;
+        int nx = ix + dx;
         if (nx < 0) nx = ncx - 1; else if (nx == ncx) nx = 0;
         for (int dy = -1; dy <= 1; dy++) {
-            int ny = cy0 + dy;
+            int ny = iy + dy;
             if (ny < 0) ny = ncy - 1; else if (ny == ncy) ny = 0;
-            int nc = nx + ny * ncx;
-            int qb = RO ? __ldg(s.cellStart + nc) : s.cellStart[nc];
-            int qe = RO ? __ldg(s.cellStart + nc + 1) : s.cellStart[nc + 1];
+            const int nc = nx * ncy + ny;
+            const int qb = RO ? __ldg(s.cellStart + nc) : s.cellStart[nc];
+            const int qe = RO ? __ldg(s.cellStart + nc + 1) : s.cellStart[nc + 1];
             for (int q = qb; q < qe; q++) {
-                float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
-                int tag = __float_as_int(e.z);
-                int j = tag & kIdMask;
-                int gj = __float_as_int(e.w);
+                const float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
+                const int tag = __float_as_int(e.z);
+                const int j = tag & kIdMask;
+                const int gj = __float_as_int(e.w);
                 if (j != i && (gi == -1 || gj == -1 || gi != gj)) {
                     float dxr, dxo, dyr, dyo;
                     image_axis(p.x, e.x, Lx, wx, false, dxr, dxo);
                     image_axis(p.y, e.y, Ly, wy, false, dyr, dyo);
-                    float dr2 = dxr * dxr + dyr * dyr;
+                    const float dr2 = dxr * dxr + dyr * dyr;
                     if (dr2 <= R2) {
                         if (k < cap) out[(size_t)k * Ncap] = tag;
                         k++;
@@ -95,6 +168,12 @@ __device__ __forceinline__ int build_one(const DevSys &s, const float2 *pos, int
     }
     s.nbrCount[i] = k;
     return k;
+}
+
+// Position of particle i outside [0, L] on a periodic axis (only possible
+// before the first step wraps it): the fast walk is then not used.
+__device__ __forceinline__ bool outside_box(const DevSys &s, float2 p) {
+    return (s.wrapx && !(p.x >= 0.0f && p.x <= s.Lx)) || (s.wrapy && !(p.y >= 0.0f && p.y <= s.Ly));
 }
 
 }  // namespace femmd

@@ -271,39 +271,64 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             }
         }
     }
-    // pairForce over the Verlet list, in list order.  Entries are taken four
-    // at a time: the four list words and then the four neighbour positions are
-    // loaded before any arithmetic (independent loads in flight together), and
-    // the four pair terms are then added into the running force in order.
+#ifndef FEMMD_PIPE
+#define FEMMD_PIPE 0
+#endif
+#if FEMMD_PIPE > 0
+    // pairForce over the Verlet list, in list order, software-pipelined: the
+    // list words of the next chunk of D entries are in flight while the D
+    // neighbour positions of the current chunk are gathered and its pair
+    // terms added in order.
     {
+        constexpr int D = FEMMD_PIPE;
         const int cnt = min(s.nbrCount[i], s.nbrCap);
         const int *__restrict__ lst = s.nbr + i;
         const size_t stride = (size_t)s.Ncap;
         const int ti = MT ? s.typeId[i] : 0;
         const float si = SG ? s.sigma[i] : 0.0f;
         const PairEntry pe0 = tab[0];
-        int k = 0;
-        for (; k + 4 <= cnt; k += 4) {
-            int t[4];
-            float2 q[4];
+        int cur[D];
 #pragma unroll
-            for (int u = 0; u < 4; u++) t[u] = RO ? __ldg(lst + u * stride) : lst[u * stride];
+        for (int u = 0; u < D; u++) cur[u] = u < cnt ? (RO ? __ldg(lst + u * stride) : lst[u * stride]) : 0;
+        for (int base = 0; base < cnt; base += D) {
+            int nxt[D];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int j = t[u] & kIdMask;
-                q[u] = RO ? __ldg(pin + j) : pin[j];
+            for (int u = 0; u < D; u++) {
+                const int k = base + D + u;
+                nxt[u] = k < cnt ? (RO ? __ldg(lst + k * stride) : lst[k * stride]) : 0;
+            }
+            float2 q[D];
+#pragma unroll
+            for (int u = 0; u < D; u++) {
+                const int j = cur[u] & kIdMask;
+                q[u] = base + u < cnt ? (RO ? __ldg(pin + j) : pin[j]) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, t[u], q[u], fx, fy, ue, we);
-            lst += 4 * stride;
-        }
-        for (; k < cnt; k++) {
-            const int tag = RO ? __ldg(lst) : *lst;
-            const int j = tag & kIdMask;
-            lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tag, RO ? __ldg(pin + j) : pin[j], fx, fy, ue, we);
-            lst += stride;
+            for (int u = 0; u < D; u++)
+                if (base + u < cnt) lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, cur[u], q[u], fx, fy, ue, we);
+#pragma unroll
+            for (int u = 0; u < D; u++) cur[u] = nxt[u];
         }
     }
+#else
+    // pairForce over the Verlet list, in list order (next entry prefetched)
+    {
+        const int cnt = min(s.nbrCount[i], s.nbrCap);
+        const int *__restrict__ lst = s.nbr + i;
+        const int stride = s.Ncap;
+        const int ti = MT ? s.typeId[i] : 0;
+        const float si = SG ? s.sigma[i] : 0.0f;
+        const PairEntry pe0 = tab[0];
+        int tag = cnt > 0 ? (RO ? __ldg(lst) : *lst) : 0;
+        for (int k = 1; k <= cnt; k++) {
+            lst += stride;
+            const int tnext = k < cnt ? (RO ? __ldg(lst) : *lst) : 0;
+            const int j = tag & kIdMask;
+            lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tag, RO ? __ldg(pin + j) : pin[j], fx, fy, ue, we);
+            tag = tnext;
+        }
+    }
+#endif
     ue *= 0.5f;
     we *= 0.5f;
     bad = bad || !(isfinite(fx) && isfinite(fy));
