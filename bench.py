@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -68,6 +69,8 @@ def parse():
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched and adjoint measurements added to the default line")
     return ap.parse_args()
 
 
@@ -101,6 +104,17 @@ class Dist:
     def close(self):
         if self.pg:
             self.pg.destroy_process_group()
+
+
+class _Solo:
+    """Single-process stand-in for Dist (the extra measurements run on rank 0)."""
+    world, rank, local = 1, 0, 0
+
+    def barrier(self):
+        pass
+
+    def max(self, x):
+        return x
 
 
 # ------------------------------------------------------------------ clocks
@@ -438,6 +452,22 @@ def batched(args, dist):
     plain_s = time.perf_counter() - t0
     plain_value = natoms * md_plain / plain_s
 
+    # the plain form on one system of the same total atom count (LJ fluid,
+    # rho = 0.8, rc = 2.5, the plain-LJ composition scaled up)
+    side = int(round(math.sqrt(natoms)))
+    big = F.System(dev)
+    S.lj_fluid(n_side=side).replay(big)
+    big.run(0)
+    big.run(md)
+    big_ms = []
+    for k in range(max(1, min(args.steps, 3))):
+        big.event_record(0)
+        big.run(md)
+        big.event_record(1)
+        big_ms.append(big.event_elapsed_ms(0, 1))
+    single_value = side * side * md / (statistics.median(big_ms) / 1e3)
+    del big
+
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         # one mid-sized replica on the host, scaled by atoms
@@ -454,8 +484,50 @@ def batched(args, dist):
                        "l2": "inputs larger than L2 (512 replicas' state + lists > 129 MB)"},
             "plain_same_atoms": {"value": plain_value, "unit": "atom-steps/s", "md_steps": md_plain,
                                  "how": "System.run on each replica in turn, wall clock"},
+            "plain_single_system": {"value": single_value, "unit": "atom-steps/s", "atoms": side * side,
+                                    "how": f"one LJ fluid of {side}x{side} atoms (rho 0.8, rc 2.5), run({md}), "
+                                           "CUDA events"},
             "batched_over_plain": value / plain_value,
+            "batched_over_single_system": value / single_value,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks}
+
+
+def adjoint_ratio(dev, reps=3, steps=200, every=20):
+    """Config 5: wall time of femmd_adjoint_backward (recompute of every
+    checkpoint segment + reverse steps) over femmd_adjoint_forward (the same
+    200 steps as run(20) segments with checkpoints), each call synchronous;
+    a fresh system per repetition."""
+    import femmd_old_gb300 as F
+    sc = S.compression(steps=steps)
+    fw, bw, plain = [], [], []
+    for r in range(reps + 1):
+        s = F.System(dev)
+        sc.replay(s)
+        s.run(0)
+        t0 = time.perf_counter()
+        s.adjoint_forward(steps, every)
+        t1 = time.perf_counter()
+        s.adjoint_backward()
+        t2 = time.perf_counter()
+        p = F.System(dev)
+        sc.replay(p)
+        p.run(0)
+        p.sync()
+        t3 = time.perf_counter()
+        p.run(steps)
+        p.sync()
+        t4 = time.perf_counter()
+        if r:  # the first repetition builds graphs and buffers
+            fw.append(t1 - t0)
+            bw.append(t2 - t1)
+            plain.append(t4 - t3)
+    f, b, pl = statistics.median(fw), statistics.median(bw), statistics.median(plain)
+    return {"workload": "compression: 64 hex-ring disks (8128 vertices), XPBC, harmonic top wall k=100 moving "
+                        "2% of L in 200 steps, per-disk E~U(20,80), nu~U(0.2,0.45), dt=0.002",
+            "steps": steps, "checkpoint_every": every, "forward_ms": 1e3 * f, "backward_ms": 1e3 * b,
+            "plain_run_ms": 1e3 * pl, "adjoint_over_forward": b / f, "adjoint_over_plain_run": b / pl,
+            "observable": "mean wall stress + FEA energy at the final step",
+            "gradients": "initial positions and velocities, per-disk E and nu, log eps, log sigma"}
 
 
 def main():
@@ -468,6 +540,17 @@ def main():
             line = batched(args, dist)
         else:
             line = ours(args, dist)
+            if dist.rank == 0 and args.workload == "large_mixed" and not args.no_extras:
+                dev = dist.local
+                line["adjoint"] = adjoint_ratio(dev)
+                sub = argparse.Namespace(**vars(args))
+                sub.steps, sub.warmup, sub.md_steps, sub.no_cpu_baseline = 3, 3, 100, True
+                b = batched(sub, _Solo())
+                line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "plain_same_atoms",
+                                                     "plain_single_system", "batched_over_plain",
+                                                     "batched_over_single_system", "e2e", "clocks")}
+                line["batched"]["config"] = {k: b["config"][k] for k in ("description", "replicas", "atoms",
+                                                                         "md_steps_per_step", "launch")}
         if dist.rank == 0 and line is not None:
             print(json.dumps(line), flush=True)
     finally:

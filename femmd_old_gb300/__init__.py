@@ -163,6 +163,53 @@ class System:
     def set_poisson_ratio(self, nu):
         self._call("femmd_set_poisson_ratio", float(nu))
 
+    def set_elastomer_material(self, e, E, nu):
+        self._call("femmd_set_elastomer_material", int(e), float(E), float(nu))
+
+    def set_moving_wall(self, k, y0, v):
+        self._call("femmd_set_moving_wall", float(k), float(y0), float(v))
+
+    def wall_forces(self):
+        t, b = C.c_double(), C.c_double()
+        self._call("femmd_get_wall_forces", C.byref(t), C.byref(b))
+        return t.value, b.value
+
+    def adjoint_forward(self, steps, every=20):
+        self._call("femmd_adjoint_forward", int(steps), int(every))
+
+    def adjoint_observable(self):
+        ws, fe = C.c_double(), C.c_double()
+        self._call("femmd_adjoint_observable", C.byref(ws), C.byref(fe))
+        return ws.value, fe.value
+
+    def adjoint_backward(self, c_wall=1.0, c_fea=1.0, xbar_final=None, vbar_final=None):
+        """Gradients of c_wall * wall stress + c_fea * FEA energy (+ <xbar_final,
+        x_N> + <vbar_final, v_N>) after adjoint_forward: dict with x0, v0
+        (N x 2 float32), E, nu (per elastomer), log_eps, log_sigma."""
+        n = self.N
+        ne = self._L.femmd_get_num_elastomers(self._h)
+        fp = C.POINTER(C.c_float)
+        dp = C.POINTER(C.c_double)
+
+        def seed(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, np.float32).reshape(n, 2)
+            return a
+
+        xs, vs = seed(xbar_final), seed(vbar_final)
+        gx = np.zeros((n, 2), np.float32)
+        gv = np.zeros((n, 2), np.float32)
+        gE = np.zeros(max(ne, 1), np.float64)
+        gnu = np.zeros(max(ne, 1), np.float64)
+        ge, gs = C.c_double(), C.c_double()
+        self._call("femmd_adjoint_backward", float(c_wall), float(c_fea),
+                   xs.ctypes.data_as(fp) if xs is not None else None,
+                   vs.ctypes.data_as(fp) if vs is not None else None,
+                   gx.ctypes.data_as(fp), gv.ctypes.data_as(fp), gE.ctypes.data_as(dp), gnu.ctypes.data_as(dp),
+                   C.byref(ge), C.byref(gs))
+        return dict(x0=gx, v0=gv, E=gE[:ne], nu=gnu[:ne], log_eps=ge.value, log_sigma=gs.value)
+
     def set_skin(self, s):
         self._call("femmd_set_skin", float(s))
 

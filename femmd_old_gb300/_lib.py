@@ -43,6 +43,12 @@ SIGNATURES = {
     "femmd_set_gravity": (i_, [P, d_]),
     "femmd_set_karea": (i_, [P, d_]),
     "femmd_set_skin": (i_, [P, d_]),
+    "femmd_set_elastomer_material": (i_, [P, i_, d_, d_]),
+    "femmd_set_moving_wall": (i_, [P, d_, d_, d_]),
+    "femmd_get_wall_forces": (i_, [P, dp, dp]),
+    "femmd_adjoint_forward": (i_, [P, i_, i_]),
+    "femmd_adjoint_backward": (i_, [P, d_, d_, fp, fp, fp, fp, dp, dp, dp, dp]),
+    "femmd_adjoint_observable": (i_, [P, dp, dp]),
     "femmd_set_neighbor_capacity": (i_, [P, i_]),
     "femmd_get_neighbor_capacity": (i_, [P, ip]),
     "femmd_set_fea_law": (i_, [P, i_]),

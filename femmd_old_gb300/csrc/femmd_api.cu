@@ -88,6 +88,11 @@ struct femmd_ctx {
     int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
     int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
     float skin = 0.4f;
+    // per-elastomer material (E, nu) where set; walls
+    std::vector<float> elE, elNu;
+    std::vector<char> elOwn;
+    bool wallOn = false;
+    float wallK = 0, wallY0 = 0, wallV = 0;
     // Particles
     std::vector<float2> pos, vel, acc, force, refPos;
     std::vector<float> mass, sigma, energy;
@@ -109,8 +114,9 @@ struct femmd_ctx {
     unsigned staleMask = 0;  // host copies older than the device: bits of kPos..kEnergy
     int cur = 0;
     int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1, sigmaOne = 0;
-    DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF;
-    DBuf<float> dmass, dsigma, denergy, triE, partialsMax;
+    DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF, triLame;
+    DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta;
+    bool ownMaterial = false, materialDirty = false;
     DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, unsorted, sortedIds, nbr, nbrCount, bStart, tStart,
         tEnt;
     DBuf<int2> bEnt;
@@ -132,6 +138,15 @@ struct femmd_ctx {
     long long profForceLaunches = 0, profRebuilds = 0, profKernels = 0;
     long long totalBuilds = 0;
     cudaEvent_t userEvents[64] = {};
+    // adjoint: segment checkpoints of the last femmd_adjoint_forward and the
+    // backward sweep's buffers
+    struct {
+        bool ready = false;
+        int every = 0, endStep = 0, maxLen = 0;
+        std::vector<int> segStart, segLen;
+        DBuf<float2> ckX, ckV, slots, finalX, finalV, finalA, xbar, vbar, w0, w1, triD;
+        DBuf<double> gMu, gLam, epsAcc, sigAcc;
+    } adj;
     double lastMeanNbr = 0;
     int lastMaxNbr = 0;
 };
@@ -165,13 +180,21 @@ static femmd_status fail(femmd_ctx *c, femmd_status st, const char *fmt, ...) {
 // ------------------------------------------------------------- host physics
 
 // Interactions::setElasticConstants (interactions.cpp:43-50)
+static void lame(float E, float nu, float &mu, float &lambda) {
+    lambda = E * nu / ((1.0f - 2.0f * nu) * (1.0f + nu));
+    mu = E / (2.0f * (1.0f + nu));
+}
+
 static void set_elastic_constants(femmd_ctx *c) {
-    c->lambda = c->E * c->nu / ((1.0f - 2.0f * c->nu) * (1.0f + c->nu));
-    c->mu = c->E / (2.0f * (1.0f + c->nu));
+    lame(c->E, c->nu, c->mu, c->lambda);
     c->C1 = c->lambda + 2.0f * c->mu;
     c->C2 = c->lambda;
     c->C3 = c->mu;
 }
+
+// contact range of a wall in units of sigma: 2^(1/6) as the reference's
+// wall routines form it (interactions.cpp:187), rounded to float
+static float wall_range() { return (float)std::pow(2.0, 1.0 / 6.0); }
 
 // pbcCalc (def.h:112)
 static float wrap_coord(float r, float L) { return r - std::floor(r / L) * L; }
@@ -227,6 +250,12 @@ static void release_device(femmd_ctx *c) {
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
     c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
+    c->triLame.release(); c->wallDelta.release();
+    auto &a = c->adj;
+    a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
+    a.xbar.release(); a.vbar.release(); a.w0.release(); a.w1.release(); a.triD.release();
+    a.gMu.release(); a.gLam.release(); a.epsAcc.release(); a.sigAcc.release();
+    a.ready = false;
     c->nbrCap = 0;
     c->obsCap = 0;
 }
@@ -246,6 +275,9 @@ static void clear_system(femmd_ctx *c) {
     c->nu = 0.3f;
     c->gravity = c->kArea = 0;
     c->skin = 0.4f;
+    c->elE.clear(); c->elNu.clear(); c->elOwn.clear();
+    c->wallOn = false;
+    c->wallK = c->wallY0 = c->wallV = 0;
     c->pos.clear(); c->vel.clear(); c->acc.clear(); c->force.clear(); c->refPos.clear();
     c->mass.clear(); c->sigma.clear(); c->energy.clear(); c->type.clear(); c->excl.clear(); c->cluster.clear();
     c->nexcl = 0;
@@ -355,6 +387,13 @@ static DevSys make_sys(femmd_ctx *c) {
     s.obs = c->obs.p;
     s.obsCap = c->obsCap;
     s.trace = c->tracing ? c->trace.p : nullptr;
+    s.triLame = c->ownMaterial ? c->triLame.p : nullptr;
+    s.wallOn = c->wallOn;
+    s.wallK = c->wallK;
+    s.wallY0 = c->wallY0;
+    s.wallV = c->wallV;
+    s.wallDelta = c->wallOn ? c->wallDelta.p : nullptr;
+    s.stepBase = c->steps;
     return s;
 }
 
@@ -386,6 +425,44 @@ static femmd_status validate(femmd_ctx *ctx) {
             !std::isfinite(ctx->vel[i].y))
             return fail(ctx, FEMMD_INVALID_ARG, "particle %d has a non-finite position or velocity", i);
     }
+    if (ctx->wallOn && ctx->pbc == FEMMD_XYPBC)
+        return fail(ctx, FEMMD_INVALID_ARG, "walls need a box that is not periodic in y (PBC 0 or 1)");
+    bool own = false;
+    for (char o : ctx->elOwn) own = own || o;
+    if (own && ctx->feaLaw != FEMMD_FEA_NEO_HOOKEAN)
+        return fail(ctx, FEMMD_UNSUPPORTED, "per-elastomer materials are implemented for the neo-Hookean law");
+    return FEMMD_OK;
+}
+
+// Per-triangle Lame constants (the elastomer's own (E, nu) through the same
+// float operations as the global constants, or the global ones) and the
+// per-particle wall contact ranges.
+static femmd_status upload_material(femmd_ctx *ctx) {
+    const int N = (int)ctx->pos.size(), nt = (int)ctx->refVol.size();
+    cudaStream_t s = ctx->stream;
+    ctx->ownMaterial = false;
+    for (char o : ctx->elOwn) ctx->ownMaterial = ctx->ownMaterial || o;
+    if (ctx->ownMaterial) {
+        std::vector<float2> lm(std::max(nt, 1), make_float2(ctx->mu, ctx->lambda));
+        for (size_t e = 0; e < ctx->clusters.size() && e < ctx->elOwn.size(); e++) {
+            if (!ctx->elOwn[e]) continue;
+            float mu, lambda;
+            lame(ctx->elE[e], ctx->elNu[e], mu, lambda);
+            const Cluster &cl = ctx->clusters[e];
+            for (int t = cl.tetOffset; t < cl.tetOffset + cl.nt && t < nt; t++) lm[t] = make_float2(mu, lambda);
+        }
+        CK(ctx->triLame.ensure(lm.size()));
+        CK(cudaMemcpyAsync(ctx->triLame.p, lm.data(), lm.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
+    }
+    if (ctx->wallOn && N > 0) {
+        std::vector<float> dl(N);
+        const float range = wall_range();
+        for (int i = 0; i < N; i++) dl[i] = range * ctx->sigma[i];
+        CK(ctx->wallDelta.ensure(N));
+        CK(cudaMemcpyAsync(ctx->wallDelta.p, dl.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    ctx->materialDirty = false;
     return FEMMD_OK;
 }
 
@@ -510,6 +587,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->triIdx.p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     }
+    if ((st = upload_material(ctx))) return st;
     ctx->topoDirty = false;
     ctx->listBuilt = false;
     CK(cudaStreamSynchronize(s));
@@ -589,9 +667,10 @@ static femmd_status size_list(femmd_ctx *ctx, int min_cap) {
 static femmd_status prepare(femmd_ctx *ctx) {
     femmd_status st;
     if (!ctx->nnInit) return fail(ctx, FEMMD_NOT_READY, "init_neighbor_list() has not been called");
-    if (ctx->topoDirty && (st = validate(ctx))) return st;
+    if ((ctx->topoDirty || ctx->materialDirty) && (st = validate(ctx))) return st;
     if (ctx->topoDirty && (st = upload_topology(ctx))) return st;
     if (ctx->stateDirty && (st = upload_state(ctx))) return st;
+    if (ctx->materialDirty && (st = upload_material(ctx))) return st;
     if (ctx->nbrCap == 0 && (st = size_list(ctx, 0))) return st;
     return FEMMD_OK;
 }
@@ -857,6 +936,64 @@ femmd_status femmd_set_poisson_ratio(femmd_ctx *ctx, double nu) {
     ctx->nu = (float)nu;
     set_elastic_constants(ctx);
     release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_elastomer_material(femmd_ctx *ctx, int elastomer, double E, double nu) {
+    NEED(ctx);
+    if (elastomer < 0 || elastomer >= (int)ctx->clusters.size())
+        return fail(ctx, FEMMD_INVALID_ARG, "elastomer %d does not exist (%zu added)", elastomer, ctx->clusters.size());
+    if (!(E > 0) || !(nu > -1.0 && nu < 0.5))
+        return fail(ctx, FEMMD_INVALID_ARG, "need E > 0 and -1 < nu < 0.5 (got %g, %g)", E, nu);
+    const size_t n = ctx->clusters.size();
+    ctx->elE.resize(n, 0.0f);
+    ctx->elNu.resize(n, 0.0f);
+    ctx->elOwn.resize(n, 0);
+    ctx->elE[elastomer] = (float)E;
+    ctx->elNu[elastomer] = (float)nu;
+    ctx->elOwn[elastomer] = 1;
+    ctx->materialDirty = true;
+    ctx->forcesValid = false;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_set_moving_wall(femmd_ctx *ctx, double k, double y0, double v) {
+    NEED(ctx);
+    if (!std::isfinite(k) || !std::isfinite(y0) || !std::isfinite(v))
+        return fail(ctx, FEMMD_INVALID_ARG, "wall parameters must be finite");
+    ctx->wallOn = k > 0;
+    ctx->wallK = ctx->wallOn ? (float)k : 0.0f;
+    ctx->wallY0 = (float)y0;
+    ctx->wallV = (float)v;
+    ctx->materialDirty = true;
+    ctx->forcesValid = false;
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+// Force of the particles on the two walls at the current positions x_n
+// (n = the context's step count): sum of k_w * overlap, float terms summed
+// in double.
+femmd_status femmd_get_wall_forces(femmd_ctx *ctx, double *top, double *bottom) {
+    NEED(ctx);
+    if (!top || !bottom) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    *top = *bottom = 0.0;
+    if (!ctx->wallOn) return FEMMD_OK;
+    HOSTSYNC(ctx);
+    femmd_status st;
+    if ((st = download_state(ctx, kPos))) return st;
+    const float range = wall_range();
+    const float yw = ctx->wallY0 - ctx->wallV * ((float)ctx->steps * ctx->dt);
+    double ft = 0.0, fb = 0.0;
+    for (size_t i = 0; i < ctx->pos.size(); i++) {
+        const float dl = range * ctx->sigma[i], y = ctx->pos[i].y;
+        const float ht = (y + dl) - yw, hb = dl - y;
+        if (ht > 0.0f) ft += (double)(ctx->wallK * ht);
+        if (hb > 0.0f) fb += (double)(ctx->wallK * hb);
+    }
+    *top = ft;
+    *bottom = fb;
     return FEMMD_OK;
 }
 
@@ -1234,6 +1371,8 @@ femmd_status femmd_calc_forces(femmd_ctx *ctx) {
     Launch L;
     L.stream = ctx->stream;
     CK(cudaMemsetAsync(&ctx->sc.p->nonfinite, 0, sizeof(int), ctx->stream));
+    ctx->hsc->stepNow = ctx->steps;
+    CK(cudaMemcpyAsync(&ctx->sc.p->stepNow, &ctx->hsc->stepNow, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(enqueue_step(L, s, MODE_FORCES, ctx->cur, 0, 0));
     if ((st = read_scalars(ctx))) return st;
     ctx->staleMask |= kForce | kEnergy;
@@ -1568,6 +1707,243 @@ femmd_status femmd_get_profile(femmd_ctx *ctx, double *fms, long long *fl, doubl
     if (rms) *rms = ctx->profRebuildMs;
     if (rb) *rb = ctx->profRebuilds;
     if (kl) *kl = ctx->profKernels;
+    return FEMMD_OK;
+}
+
+
+// ================================================================== adjoint
+
+static float wall_y_host(const femmd_ctx *ctx, int n) { return ctx->wallY0 - ctx->wallV * ((float)n * ctx->dt); }
+
+static femmd_status adj_supported(femmd_ctx *ctx) {
+    if (ctx->feaForces && !ctx->refVol.empty() && ctx->feaLaw != FEMMD_FEA_NEO_HOOKEAN)
+        return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint implements the neo-Hookean triangle law");
+    if (ctx->bondForces && !ctx->r0.empty() && ctx->bondKMode != FEMMD_BONDK_KBOND)
+        return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint implements bonds with the constant kBond");
+    return FEMMD_OK;
+}
+
+femmd_status femmd_adjoint_forward(femmd_ctx *ctx, int steps, int every) {
+    NEED(ctx);
+    femmd_status st;
+    if (steps < 1 || every < 1) return fail(ctx, FEMMD_INVALID_ARG, "steps and every must be >= 1");
+    if ((st = prepare(ctx))) return st;
+    if ((st = adj_supported(ctx))) return st;
+    const int N = (int)ctx->pos.size();
+    if (N == 0) return fail(ctx, FEMMD_NOT_READY, "no particles");
+    auto &a = ctx->adj;
+    a.ready = false;
+    const int nseg = (steps + every - 1) / every;
+    a.every = every;
+    a.segStart.assign(nseg, 0);
+    a.segLen.assign(nseg, 0);
+    CK(a.ckX.ensure((size_t)nseg * N));
+    CK(a.ckV.ensure((size_t)nseg * N));
+    for (int g = 0; g < nseg; g++) {
+        const int len = std::min(every, steps - g * every);
+        const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+        CK(cudaMemcpyAsync(a.ckX.p + (size_t)g * N, pc, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(a.ckV.p + (size_t)g * N, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+        a.segStart[g] = ctx->steps;
+        a.segLen[g] = len;
+        if ((st = femmd_run(ctx, len))) return st;
+    }
+    a.maxLen = std::min(every, steps);
+    a.endStep = ctx->steps;
+    a.ready = true;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_adjoint_observable(femmd_ctx *ctx, double *wall_stress, double *fea_energy) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = femmd_calc_forces(ctx))) return st;
+    double ws = 0.0, fe = 0.0;
+    if (ctx->wallOn) {
+        double top, bottom;
+        if ((st = femmd_get_wall_forces(ctx, &top, &bottom))) return st;
+        ws = (top + bottom) / (2.0 * (double)ctx->Lx);
+    }
+    const int nt = (int)ctx->refVol.size();
+    if (ctx->feaForces && nt > 0) {
+        std::vector<float> e(nt);
+        CK(cudaMemcpyAsync(e.data(), ctx->triE.p, nt * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (float v : e) fe += (double)v;
+    }
+    if (wall_stress) *wall_stress = ws;
+    if (fea_energy) *fea_energy = fe;
+    return FEMMD_OK;
+}
+
+// Recompute segment g from its checkpoint (the forward's kernels in the
+// forward's order, launched directly) and record its positions in slots
+// 0..K; returns the rebuild points (slot indices whose positions a list was
+// built from).
+static femmd_status adj_recompute(femmd_ctx *ctx, int g, std::vector<int> &rebuilt) {
+    auto &a = ctx->adj;
+    const int N = (int)ctx->pos.size(), K = a.segLen[g];
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->dpos0.p, a.ckX.p + (size_t)g * N, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(ctx->dvel.p, a.ckV.p + (size_t)g * N, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(a.slots.p, ctx->dpos0.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    ctx->cur = 0;
+    ctx->steps = a.segStart[g];
+    DevSys s = make_sys(ctx);
+    Launch L;
+    L.stream = st;
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), st));
+    CK(enqueue_run_start(L, s));
+    CK(enqueue_rebuild(L, s, 0, 1));
+    CK(enqueue_step(L, s, MODE_FIRST, 0, 0, 0));
+    int cur = 1;
+    CK(cudaMemcpyAsync(a.slots.p + N, ctx->dpos1.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    for (int u = 1; u < K; u++) {
+        CK(enqueue_step(L, s, MODE_MID, cur, 0, 0));
+        float2 *pout = cur ? ctx->dpos0.p : ctx->dpos1.p;
+        CK(cudaMemcpyAsync(a.slots.p + (size_t)(u + 1) * N, pout, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+        CK(enqueue_rebuild(L, s, 1 - cur, 1));
+        cur ^= 1;
+    }
+    femmd_status e;
+    if ((e = read_scalars(ctx))) return e;
+    if (ctx->hsc->overflow || ctx->hsc->nonfinite)
+        return fail(ctx, ctx->hsc->overflow ? FEMMD_CAPACITY_OVERFLOW : FEMMD_NONFINITE,
+                    "the recomputed segment differs from the forward pass (overflow or non-finite force)");
+    // MID step u (forces at slot u) writes observable row u-1; its rebuild
+    // flag means a list was built from slot u+1
+    rebuilt.assign(1, 0);
+    const int rows = std::max(K - 1, 0);
+    if (rows > 0) {
+        std::vector<double> o((size_t)rows * kObsCols);
+        CK(cudaMemcpyAsync(o.data(), ctx->obs.p, o.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int u = 1; u < K; u++)
+            if (o[(size_t)(u - 1) * kObsCols + 5] != 0.0) rebuilt.push_back(u + 1);
+    }
+    return FEMMD_OK;
+}
+
+femmd_status femmd_adjoint_backward(femmd_ctx *ctx, double c_wall, double c_fea, const float *xbar_final,
+                                    const float *vbar_final, float *xbar_init, float *vbar_init, double *dJ_dE,
+                                    double *dJ_dnu, double *dJ_dlog_eps, double *dJ_dlog_sigma) {
+    NEED(ctx);
+    auto &a = ctx->adj;
+    if (!a.ready) return fail(ctx, FEMMD_NOT_READY, "femmd_adjoint_forward has not been run");
+    if (ctx->steps != a.endStep || ctx->topoDirty || ctx->stateDirty || ctx->materialDirty)
+        return fail(ctx, FEMMD_NOT_READY, "the system changed after femmd_adjoint_forward");
+    femmd_status st;
+    if ((st = adj_supported(ctx))) return st;
+    const int N = (int)ctx->pos.size(), nt = (int)ctx->refVol.size();
+    const int nseg = (int)a.segLen.size();
+    cudaStream_t sm = ctx->stream;
+    // keep the final state; the sweep overwrites the context's buffers
+    CK(a.finalX.ensure(N)); CK(a.finalV.ensure(N)); CK(a.finalA.ensure(N));
+    CK(a.slots.ensure((size_t)(a.maxLen + 1) * N));
+    CK(a.xbar.ensure(N)); CK(a.vbar.ensure(N)); CK(a.w0.ensure(N)); CK(a.w1.ensure(N));
+    CK(a.triD.ensure(3 * (size_t)std::max(nt, 1)));
+    CK(a.gMu.ensure(std::max(nt, 1))); CK(a.gLam.ensure(std::max(nt, 1)));
+    CK(a.epsAcc.ensure(N)); CK(a.sigAcc.ensure(N));
+    if ((st = ensure_obs(ctx, a.maxLen))) return st;
+    // FEA nodal forces and energies at x_N for the seed
+    if ((st = femmd_calc_forces(ctx))) return st;
+    const float2 *pN = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+    CK(cudaMemcpyAsync(a.finalX.p, pN, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaMemcpyAsync(a.finalV.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaMemcpyAsync(a.finalA.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaMemsetAsync(a.gMu.p, 0, sizeof(double) * std::max(nt, 1), sm));
+    CK(cudaMemsetAsync(a.gLam.p, 0, sizeof(double) * std::max(nt, 1), sm));
+    CK(cudaMemsetAsync(a.epsAcc.p, 0, sizeof(double) * N, sm));
+    CK(cudaMemsetAsync(a.sigAcc.p, 0, sizeof(double) * N, sm));
+    if (xbar_final)
+        CK(cudaMemcpyAsync(a.xbar.p, xbar_final, N * sizeof(float2), cudaMemcpyHostToDevice, sm));
+    else
+        CK(cudaMemsetAsync(a.xbar.p, 0, N * sizeof(float2), sm));
+    if (vbar_final)
+        CK(cudaMemcpyAsync(a.vbar.p, vbar_final, N * sizeof(float2), cudaMemcpyHostToDevice, sm));
+    else
+        CK(cudaMemsetAsync(a.vbar.p, 0, N * sizeof(float2), sm));
+    float2 *wc = a.w0.p, *wn = a.w1.p;
+    {
+        DevSys s = make_sys(ctx);
+        Launch L;
+        L.stream = sm;
+        CK(enqueue_adj_seed(L, s, a.finalX.p, a.xbar.p, a.vbar.p, wc, (float)c_wall, (float)c_fea,
+                            wall_y_host(ctx, a.endStep), a.sigAcc.p, a.gMu.p, a.gLam.p));
+    }
+    const float dt = ctx->dt, h = 0.5f * ctx->dt;
+    std::vector<int> rebuilt;
+    for (int g = nseg - 1; g >= 0; g--) {
+        if ((st = adj_recompute(ctx, g, rebuilt))) return st;
+        const int K = a.segLen[g], s0 = a.segStart[g];
+        DevSys s = make_sys(ctx);
+        Launch L;
+        L.stream = sm;
+        int listFrom = -1;
+        for (int k = K; k >= (g == 0 ? 0 : 1); k--) {
+            int r = 0;
+            for (int v : rebuilt)
+                if (v <= k) r = std::max(r, v);
+            const float2 *pk = a.slots.p + (size_t)k * N;
+            if (r != listFrom) {
+                DevSys sb = s;
+                sb.pos0 = const_cast<float2 *>(a.slots.p + (size_t)r * N);
+                CK(enqueue_rebuild(L, sb, 0, 0));
+                listFrom = r;
+            }
+            const int n = s0 + k;
+            const int update = k >= 1;
+            const float cNext = (n - 1 == a.segStart[0]) ? h : dt;
+            CK(enqueue_adj_step(L, s, pk, wc, a.triD.p, a.gMu.p, a.gLam.p, a.xbar.p, a.vbar.p, wn, cNext, update,
+                                wall_y_host(ctx, n), a.epsAcc.p, a.sigAcc.p));
+            if (update) std::swap(wc, wn);
+        }
+    }
+    // outputs
+    if (xbar_init) CK(cudaMemcpyAsync(xbar_init, a.xbar.p, N * sizeof(float2), cudaMemcpyDeviceToHost, sm));
+    if (vbar_init) CK(cudaMemcpyAsync(vbar_init, a.vbar.p, N * sizeof(float2), cudaMemcpyDeviceToHost, sm));
+    std::vector<double> gm(std::max(nt, 1)), gl(std::max(nt, 1)), ea(N), sa(N);
+    CK(cudaMemcpyAsync(gm.data(), a.gMu.p, gm.size() * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(gl.data(), a.gLam.p, gl.size() * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(ea.data(), a.epsAcc.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(sa.data(), a.sigAcc.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    // restore the final state
+    CK(cudaMemcpyAsync(ctx->dpos0.p, a.finalX.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->dvel.p, a.finalV.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->dacc.p, a.finalA.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, sm));
+    CK(cudaStreamSynchronize(sm));
+    ctx->cur = 0;
+    ctx->steps = a.endStep;
+    ctx->listBuilt = false;
+    ctx->forcesValid = false;
+    ctx->staleMask |= kPos | kVel | kAcc | kForce;
+    if (dJ_dlog_eps) {
+        double t = 0.0;
+        for (double v : ea) t += v;
+        *dJ_dlog_eps = t;
+    }
+    if (dJ_dlog_sigma) {
+        double t = 0.0;
+        for (double v : sa) t += v;
+        *dJ_dlog_sigma = t;
+    }
+    // per elastomer: chain mu = E / (2 (1 + nu)), lambda = E nu / ((1 + nu)(1 - 2 nu))
+    for (size_t e = 0; e < ctx->clusters.size(); e++) {
+        const bool own = e < ctx->elOwn.size() && ctx->elOwn[e];
+        const double E = own ? ctx->elE[e] : ctx->E, nu = own ? ctx->elNu[e] : ctx->nu;
+        const double dmu_dE = 1.0 / (2.0 * (1.0 + nu)), dmu_dnu = -E / (2.0 * (1.0 + nu) * (1.0 + nu));
+        const double D = (1.0 + nu) * (1.0 - 2.0 * nu);
+        const double dla_dE = nu / D, dla_dnu = E * (1.0 + 2.0 * nu * nu) / (D * D);
+        double sm_ = 0.0, sl = 0.0;
+        const Cluster &cl = ctx->clusters[e];
+        for (int t = cl.tetOffset; t < cl.tetOffset + cl.nt && t < nt; t++) {
+            sm_ += gm[t];
+            sl += gl[t];
+        }
+        if (dJ_dE) dJ_dE[e] = sm_ * dmu_dE + sl * dla_dE;
+        if (dJ_dnu) dJ_dnu[e] = sm_ * dmu_dnu + sl * dla_dnu;
+    }
     return FEMMD_OK;
 }
 

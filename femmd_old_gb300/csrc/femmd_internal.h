@@ -56,7 +56,7 @@ struct DevScalars {
     int rebuild, totalUpdates;
     unsigned int ticket, triTicket;
     int overflow, nonfinite, outside, maxCount;  // the first three are cleared together by the host
-    int obsRow, pad0;
+    int obsRow, stepNow;  // stepNow: index n of the positions x_n the next force evaluation sees
     unsigned long long nbrSum, builds;
     unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
     unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
@@ -101,6 +101,15 @@ struct DevSys {
     double *obs;
     int obsCap;
     unsigned long long *trace;  // per-step device timestamps, or null
+    // per-triangle (mu, lambda) when elastomers have their own material, else null
+    const float2 *triLame;
+    // moving harmonic walls (XPBC / NOPBC): bottom at y = 0, top at
+    // y_w(n) = wallY0 - wallV * (n dt); particle i touches a wall closer than
+    // wallDelta[i] = 2^(1/6) sigma_i and is pushed back with k_w * overlap
+    int wallOn;
+    float wallK, wallY0, wallV;
+    const float *wallDelta;
+    int stepBase;  // the context's step count when the run started
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -125,6 +134,18 @@ cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
 // leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
+
+// ---- adjoint (k_adjoint.cu)
+// Seed at the final positions: xbar += dJ/dx of cWall * wall stress + cFea *
+// FEA energy, direct parameter terms, and wOut = h vbar / m.
+cudaError_t enqueue_adj_seed(Launch &L, const DevSys &s, const float2 *pos, float2 *xbar, const float2 *vbar,
+                             float2 *wOut, float cWall, float cFea, float yw, double *sigAcc, double *gMu,
+                             double *gLam);
+// One reverse step at positions pos with weights w: xbar += (df/dx)^T w,
+// parameter terms; with update, vbar += dt xbar and wOut = cNext vbar / m.
+cudaError_t enqueue_adj_step(Launch &L, const DevSys &s, const float2 *pos, const float2 *w, float2 *triD,
+                             double *gMu, double *gLam, float2 *xbar, float2 *vbar, float2 *wOut, float cNext,
+                             int update, float yw, double *epsAcc, double *sigAcc);
 
 // ---- batched replicas (k_batch.cu): one persistent launch over many systems
 struct BatchLaunch {

@@ -217,6 +217,7 @@ __device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, i
             reb = (double)sc->dispHi > s.halfSkin;
         }
         sc->rebuild = reb;
+        if (mode == MODE_FIRST || mode == MODE_MID) sc->stepNow += 1;
     }
     __syncthreads();
 }
@@ -249,6 +250,7 @@ __global__ void __launch_bounds__(1024) k_batch(const DevSys *__restrict__ reps,
             c->dispHi = 0.0f;
             c->totalUpdates = 0;
             c->obsRow = 0;
+            c->stepNow = S.stepBase;
         }
         __syncthreads();
         int cur = parity0[r];

@@ -83,7 +83,10 @@ __global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int par
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
     bool bad = false;
-    if (i < s.N) particle_step<MT, SG, WX, WY, SIG1>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
+    // one type: the pair loop is pipelined four entries deep (measured faster
+    // on a 1M-atom LJ fluid); several types: the plain loop keeps registers low
+    // enough for the type-pair lookups (measured faster on the mixed system)
+    if (i < s.N) particle_step<MT, SG, WX, WY, SIG1, true, MT ? 0 : 4>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
 
     // ---- reductions: FP32 within the block, 64-bit fixed-point atomics across
     // blocks (exact, order-independent); the last block converts and finishes.
@@ -147,6 +150,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int par
                 reb = (double)sc->dispHi > s.halfSkin;
             }
             sc->rebuild = reb;
+            if (mode == MODE_FIRST || mode == MODE_MID) sc->stepNow += 1;  // the drift made x_{n+1}
             if (use_h) cudaGraphSetConditional(h, reb ? 1u : 0u);
             sc->ticket = 0;
             if (s.trace) {
@@ -162,6 +166,7 @@ __global__ void __launch_bounds__(kBlock) k_drift(DevSys s, int parity) {
     const float2 *pin = parity ? s.pos1 : s.pos0;
     float2 *pout = parity ? s.pos0 : s.pos1;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) s.sc->stepNow = s.stepBase + 1;
     if (i >= s.N) return;
     float2 v = s.vel[i], a = s.acc[i], p = pin[i];
     v.x += s.hdt * a.x;

@@ -40,6 +40,7 @@ __global__ void k_run_start(DevSys s) {
         c->triTicket = 0;
         c->accU = c->accW = c->accK = 0ull;
         c->vvMaxBits = 0u;
+        c->stepNow = s.stepBase;
     }
 }
 

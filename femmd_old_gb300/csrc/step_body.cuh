@@ -58,9 +58,14 @@ __device__ __forceinline__ float tri_neo_hookean(const DevSys &s, const float2 *
     float F11 = Ds10 * Bm01 + Ds11 * Bm11;
     float detF = F00 * F11 - F01 * F10;
     float logJ = own_logf(detF);
-    float llogJ = s.lambda * logJ;
+    float mu = s.mu, lambda = s.lambda;
+    if (s.triLame) {
+        const float2 ml = __ldg(s.triLame + t);
+        mu = ml.x;
+        lambda = ml.y;
+    }
+    float llogJ = lambda * logJ;
     float iF00 = F11 / detF, iF10 = -F10 / detF, iF01 = -F01 / detF, iF11 = F00 / detF;
-    const float mu = s.mu;
     float P00 = mu * (F00 - iF00) + llogJ * iF00;
     float P10 = mu * (F10 - iF01) + llogJ * iF01;
     float P01 = mu * (F01 - iF10) + llogJ * iF10;
@@ -77,7 +82,7 @@ __device__ __forceinline__ float tri_neo_hookean(const DevSys &s, const float2 *
     // I1 - 2 - 2 lnJ summed from (F-I) entries to avoid first-order cancellation
     float d00 = F00 - 1.0f, d11 = F11 - 1.0f;
     float i1m2 = (2.0f * d00 + d00 * d00) + (2.0f * d11 + d11 * d11) + F01 * F01 + F10 * F10;
-    float pe = 0.5f * mu * (i1m2 - 2.0f * logJ) + 0.5f * s.lambda * logJ * logJ;
+    float pe = 0.5f * mu * (i1m2 - 2.0f * logJ) + 0.5f * lambda * logJ * logJ;
     return pe * vol0;
 }
 
@@ -157,6 +162,9 @@ __device__ __forceinline__ float tri_force(const DevSys &s, const float2 *pos, i
 
 // ------------------------------------------------------------ particles
 
+// top wall position when the positions are x_n: y0 - v (n dt), in float
+__device__ __forceinline__ float wall_y(const DevSys &s, int n) { return s.wallY0 - s.wallV * ((float)n * s.dt); }
+
 // minImage on one axis with the wrap known at compile time.  Sets *wrapped
 // when the difference crossed the boundary (then the exact-image value can
 // differ from the reference float value).
@@ -222,7 +230,7 @@ __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, c
 // RO: the list and the neighbours' positions are read through the read-only
 // path (written by an earlier kernel); the batched kernel rewrites both in the
 // same launch and reads them with coherent loads (RO = false).
-template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true>
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true, int PIPE = 0>
 __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *tab, int i, int mode,
                                               const float2 *pin, float2 *pout, float &ue_out,
                                               float &we_out, float &ke, float &vvm, bool &bad) {
@@ -271,16 +279,12 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             }
         }
     }
-#ifndef FEMMD_PIPE
-#define FEMMD_PIPE 0
-#endif
-#if FEMMD_PIPE > 0
-    // pairForce over the Verlet list, in list order, software-pipelined: the
-    // list words of the next chunk of D entries are in flight while the D
-    // neighbour positions of the current chunk are gathered and its pair
-    // terms added in order.
-    {
-        constexpr int D = FEMMD_PIPE;
+    if constexpr (PIPE > 0) {
+        // pairForce over the Verlet list, in list order, software-pipelined:
+        // the list words of the next chunk of PIPE entries are in flight while
+        // the neighbour positions of the current chunk are gathered and its
+        // pair terms added in order.
+        constexpr int D = PIPE;
         const int cnt = min(s.nbrCount[i], s.nbrCap);
         const int *__restrict__ lst = s.nbr + i;
         const size_t stride = (size_t)s.Ncap;
@@ -309,10 +313,8 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
 #pragma unroll
             for (int u = 0; u < D; u++) cur[u] = nxt[u];
         }
-    }
-#else
-    // pairForce over the Verlet list, in list order (next entry prefetched)
-    {
+    } else {
+        // pairForce over the Verlet list, in list order (next entry prefetched)
         const int cnt = min(s.nbrCount[i], s.nbrCap);
         const int *__restrict__ lst = s.nbr + i;
         const int stride = s.Ncap;
@@ -328,9 +330,23 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             tag = tnext;
         }
     }
-#endif
     ue *= 0.5f;
     we *= 0.5f;
+    if (s.wallOn) {
+        // harmonic walls after the pair forces: top wall at y_w(n), bottom at 0
+        const float yw = wall_y(s, s.sc->stepNow);
+        const float dl = s.wallDelta[i];
+        const float ht = (pi.y + dl) - yw;
+        if (ht > 0.0f) {
+            fy -= s.wallK * ht;
+            ue += 0.5f * s.wallK * ht * ht;
+        }
+        const float hb = dl - pi.y;
+        if (hb > 0.0f) {
+            fy += s.wallK * hb;
+            ue += 0.5f * s.wallK * hb * hb;
+        }
+    }
     bad = bad || !(isfinite(fx) && isfinite(fy));
     const float m = s.mass[i];
     const float ax = fx / m, ay = fy / m;

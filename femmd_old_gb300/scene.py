@@ -363,6 +363,52 @@ def suspension(n_side: int = 16, radius: float = 5.0, rings: int = 6, phi: float
     return sc
 
 
+def compression(n_side: int = 8, radius: float = 5.0, rings: int = 6, phi: float = 0.5, kbond: float = 100.0,
+                T: float = 0.01, dt: float = 0.002, skin: float = 0.3, wall_k: float = 100.0, strain: float = 0.02,
+                steps: int = 200, E_range=(20.0, 80.0), nu_range=(0.2, 0.45), mesh=None, center_jitter: float = 0.5,
+                seeds=(3, 4, 5, 10)) -> Scene:
+    """Differentiable compression (benchmark config 5 at n_side=8): 64 hex-ring
+    disks as the suspension, periodic in x, a fixed harmonic wall at y = 0 and
+    a harmonic top wall (k_w = 100) that starts at y = L and moves down by
+    strain * L over 'steps' steps; per-disk E ~ U(20, 80), nu ~ U(0.2, 0.45)
+    (seed 10); dt = 0.002.  The default strain, 2 % of L in 200 steps, moves
+    the wall at 5 sigma/tau, about the disks' elastic wave speed; at 10 % in
+    200 steps (25 sigma/tau) the top row of disks inverts (det F <= 0) within
+    about 100 steps in float and in double alike."""
+    nd = n_side * n_side
+    L = math.sqrt(nd * math.pi * radius ** 2 / phi)
+    if mesh is None:
+        verts, tris = hex_disk_mesh(radius, rings, jitter=0.02, seed=seeds[0])
+    else:
+        verts, tris = mesh
+    nv = verts.shape[0]
+    rp = np.random.Generator(np.random.PCG64(seeds[1]))
+    rv = np.random.Generator(np.random.PCG64(seeds[2]))
+    rm = np.random.Generator(np.random.PCG64(seeds[3]))
+    a = L / n_side
+    v_wall = strain * L / (steps * dt)
+    Es = rm.uniform(*E_range, size=nd)
+    nus = rm.uniform(*nu_range, size=nd)
+    sc = Scene(meta=dict(workload="compression", N=nd * nv, L=L, n_disks=nd, steps=steps, wall_k=wall_k,
+                         wall_v=v_wall, E=Es, nu=nus))
+    sc.add("init", L, L).add("PBC", 1).add("set_dt", dt).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [WCA_RC], [1.0])
+    sc.add("set_skin", skin)
+    sc.add("set_kBond", kbond).add("set_youngs_modulus", float(np.mean(E_range))).add("set_poisson_ratio", 0.3)
+    sc.add("set_elastomer_bonds", 1)
+    for iy in range(n_side):
+        for ix in range(n_side):
+            c = (np.array([ix, iy]) + 0.5) * a + rp.uniform(-center_jitter, center_jitter, size=2)
+            sc.add("add_elastomer", verts, tris, float(c[0]), float(c[1]), 0, 0, 1.0, float(nv), True)
+    for e in range(nd):
+        sc.add("set_elastomer_material", e, float(Es[e]), float(nus[e]))
+    sc.add("set_moving_wall", wall_k, L, v_wall)
+    sc.add("init_neighbor_list")
+    vel = _mb_velocities(rv, nd * nv, T)
+    sc.add("set_velocities_array", vel.astype(np.float32))
+    return sc
+
+
 def large_mixed(n_side: int = 64, n_solvent: int = 1_000_000, radius: float = 5.0, rings: int = 6,
                 E: float = 50.0, nu: float = 0.3, kbond: float = 100.0, T: float = 1.0, dt: float = 0.005,
                 skin: float = 0.3, density: float = 0.8, center_jitter: float = 2.0,

@@ -86,6 +86,19 @@ femmd_status femmd_set_poisson_ratio(femmd_ctx *ctx, double nu);
  * enable forces outside this build's hot path and return FEMMD_UNSUPPORTED. */
 femmd_status femmd_set_gravity(femmd_ctx *ctx, double g);
 femmd_status femmd_set_karea(femmd_ctx *ctx, double k);
+/* Per-elastomer material: elastomer e (in add order) gets its own Young's
+ * modulus and Poisson ratio instead of the global ones (neo-Hookean law only).
+ * The reference has one global E (Interactions::E, interactions.h:20). */
+femmd_status femmd_set_elastomer_material(femmd_ctx *ctx, int elastomer, double E, double nu);
+/* Moving harmonic walls for boxes not periodic in y: a bottom wall at y = 0
+ * and a top wall at y_w(n) = y0 - v * n * dt, n the step index of the
+ * positions.  A particle closer than 2^(1/6) sigma_i to a wall (the contact
+ * range of calcTopBottomWallForces, interactions.cpp:242-270) gets the force
+ * k * overlap away from it and the energy k/2 overlap^2.  k <= 0 removes them. */
+femmd_status femmd_set_moving_wall(femmd_ctx *ctx, double k, double y0, double v);
+/* Forces the particles exert on the top and bottom walls at the current
+ * positions (sum of k * overlap). */
+femmd_status femmd_get_wall_forces(femmd_ctx *ctx, double *top, double *bottom);
 /* NeighborList::setSkin (C++ only, nn.h:64; default 0.4) */
 femmd_status femmd_set_skin(femmd_ctx *ctx, double skin);
 /* Neighbour-list capacity per particle (0 = size from the first build).  A
@@ -232,6 +245,33 @@ femmd_status femmd_batch_get_launch(const femmd_batch *b, int *threads, int *cta
 femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads, int *ctas_per_sm, double *best_ms);
 femmd_status femmd_batch_event_record(femmd_batch *b, int slot);
 femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, float *ms);
+
+/* ------------------------------------------------------------ adjoint */
+/* Gradients of an observable of the final state through the whole run, by the
+ * discrete adjoint of the leapfrog step (no counterpart in the reference).
+ *
+ * femmd_adjoint_forward runs 'steps' steps as run(every) segments (the same
+ * kernels as femmd_run) and keeps positions and velocities at the start of
+ * every segment.  femmd_adjoint_backward then sweeps the segments backwards:
+ * each segment is recomputed from its checkpoint, its positions recorded, and
+ * the reverse steps applied with the forward's own neighbour lists.  The
+ * observable is
+ *   J = c_wall * (F_top + F_bottom) / (2 Lx) + c_fea * U_fea
+ *       + <xbar_final, x_N> + <vbar_final, v_N>
+ * (wall stress and FEA energy at the final positions; the two seed arrays,
+ * 2N floats each, may be null).  Outputs (host arrays, each may be null):
+ * dJ/dx_0 and dJ/dv_0 (2N floats), dJ/dE and dJ/dnu per elastomer (neo-Hookean
+ * law; the elastomer's own values or the global ones), and dJ/d(log eps),
+ * dJ/d(log sigma) for one common scale on every pair epsilon and every
+ * particle sigma (the wall contact ranges scale with sigma).  The context's
+ * final state is restored afterwards.  Bond stiffness is taken as the
+ * constant kBond. */
+femmd_status femmd_adjoint_forward(femmd_ctx *ctx, int steps, int every);
+femmd_status femmd_adjoint_backward(femmd_ctx *ctx, double c_wall, double c_fea, const float *xbar_final,
+                                    const float *vbar_final, float *xbar_init, float *vbar_init, double *dJ_dE,
+                                    double *dJ_dnu, double *dJ_dlog_eps, double *dJ_dlog_sigma);
+/* Wall stress (F_top + F_bottom) / (2 Lx) and FEA energy at the current positions. */
+femmd_status femmd_adjoint_observable(femmd_ctx *ctx, double *wall_stress, double *fea_energy);
 
 /* ------------------------------------------ cell binning without allocation */
 /* Limits of femmd_bin_cells_noalloc.  Its working memory is one fixed array of

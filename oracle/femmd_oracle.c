@@ -87,6 +87,11 @@ typedef struct orc {
     float potEnergy, virial, feaVirial, kinEneSum, vvMax;
     /* scratch for threaded pair loop */
     float *ui, *wi;
+    /* per-elastomer material (own E, nu) and moving harmonic walls */
+    float *clE, *clNu;
+    int *clOwn, clMatCap;
+    int wallOn;
+    float wallK, wallY0, wallV;
 } orc;
 
 /* ---------------------------------------------------------------- helpers */
@@ -196,6 +201,7 @@ static void free_all(orc *s) {
     free(s->bond); free(s->r0); free(s->eps); free(s->rc); free(s->us);
     free(s->cellStart); free(s->cellIds); free(s->cellOf); free(s->nbrStart); free(s->nbrList);
     free(s->ui); free(s->wi);
+    free(s->clE); free(s->clNu); free(s->clOwn);
 }
 
 void orc_destroy(orc *s) {
@@ -205,9 +211,13 @@ void orc_destroy(orc *s) {
 }
 
 /* Interactions::setElasticConstants (src/interactions.cpp:43-50) */
+static void lame(float E, float nu, float *mu, float *lambda) {
+    *lambda = E * nu / ((1.0f - 2.0f * nu) * (1.0f + nu));
+    *mu = E / (2.0f * (1.0f + nu));
+}
+
 static void set_elastic_constants(orc *s) {
-    s->lambda = s->E * s->nu / ((1.0f - 2.0f * s->nu) * (1.0f + s->nu));
-    s->mu = s->E / (2.0f * (1.0f + s->nu));
+    lame(s->E, s->nu, &s->mu, &s->lambda);
     s->Cxxxx = s->lambda + 2.0f * s->mu;
     s->Cxxyy = s->lambda;
     s->Cxyxy = s->mu;
@@ -271,6 +281,68 @@ void orc_set_youngs_modulus(orc *s, double E) {
     set_elastic_constants(s);
 }
 void orc_set_nu(orc *s, double nu) { s->nu = (float)nu; set_elastic_constants(s); }
+
+/* Own (E, nu) of elastomer e (neo-Hookean law); no counterpart in the
+ * reference, which has one global E. */
+int orc_set_elastomer_material(orc *s, int e, double E, double nu) {
+    if (e < 0 || e >= s->ncl) return 1;
+    if (s->clMatCap < s->ncl) {
+        s->clE = (float *)xrealloc(s->clE, sizeof(float) * (size_t)s->ncl);
+        s->clNu = (float *)xrealloc(s->clNu, sizeof(float) * (size_t)s->ncl);
+        s->clOwn = (int *)xrealloc(s->clOwn, sizeof(int) * (size_t)s->ncl);
+        for (int k = s->clMatCap; k < s->ncl; k++) { s->clE[k] = 0; s->clNu[k] = 0; s->clOwn[k] = 0; }
+        s->clMatCap = s->ncl;
+    }
+    s->clE[e] = (float)E; s->clNu[e] = (float)nu; s->clOwn[e] = 1;
+    return 0;
+}
+
+/* Moving harmonic walls: bottom at y = 0, top at y0 - v (n dt) for the
+ * positions of step n; contact range 2^(1/6) sigma_i (the range of
+ * calcTopBottomWallForces, src/interactions.cpp:242-270); force k * overlap. */
+void orc_set_moving_wall(orc *s, double k, double y0, double v) {
+    s->wallOn = k > 0;
+    s->wallK = s->wallOn ? (float)k : 0.0f;
+    s->wallY0 = (float)y0;
+    s->wallV = (float)v;
+}
+
+static float wall_range(void) { return (float)pow(2.0, 1.0 / 6.0); }
+static float wall_y(const orc *s) { return s->wallY0 - s->wallV * ((float)s->steps * s->dt); }
+
+/* Lame constants of triangle t: its elastomer's own, or the global ones. */
+static void tri_lame(const orc *s, int t, float *mu, float *lambda) {
+    *mu = s->mu; *lambda = s->lambda;
+    if (!s->clOwn) return;
+    int e = s->cluster[s->tri[3 * t]];
+    if (e >= 0 && e < s->clMatCap && s->clOwn[e]) lame(s->clE[e], s->clNu[e], mu, lambda);
+}
+
+/* wall forces of every particle, after the pair forces */
+static void wall_forces(orc *s) {
+    if (!s->wallOn) return;
+    float yw = wall_y(s), range = wall_range();
+    for (int i = 0; i < s->N; i++) {
+        float dl = range * s->sigma[i];
+        float ht = (s->py[i] + dl) - yw;
+        if (ht > 0.0f) { s->fy[i] -= s->wallK * ht; s->potEnergy += 0.5f * s->wallK * ht * ht; }
+        float hb = dl - s->py[i];
+        if (hb > 0.0f) { s->fy[i] += s->wallK * hb; s->potEnergy += 0.5f * s->wallK * hb * hb; }
+    }
+}
+
+/* forces of the particles on the top and bottom walls at the current positions */
+void orc_wall_forces(const orc *s, double *top, double *bottom) {
+    *top = *bottom = 0;
+    if (!s->wallOn) return;
+    float yw = wall_y(s), range = wall_range();
+    for (int i = 0; i < s->N; i++) {
+        float dl = range * s->sigma[i];
+        float ht = (s->py[i] + dl) - yw, hb = dl - s->py[i];
+        if (ht > 0.0f) *top += (double)(s->wallK * ht);
+        if (hb > 0.0f) *bottom += (double)(s->wallK * hb);
+    }
+}
 
 /* Particles::addParticle (src/particles.cpp:201-231) */
 int orc_add_particle(orc *s, double x, double y, double vx, double vy, double m, double sig, int typ) {
@@ -668,16 +740,17 @@ static float tri_neo_hookean(const orc *s, int t, float *f) {
     float F11 = Ds10 * Bm01 + Ds11 * Bm11;
     float detF = F00 * F11 - F01 * F10;
     float logJ = fea_log(s, detF);
-    float llogJ = s->lambda * logJ;
+    float mu, lambda;
+    tri_lame(s, t, &mu, &lambda);
+    float llogJ = lambda * logJ;
     float iF00 = F11 / detF, iF10 = -F10 / detF, iF01 = -F01 / detF, iF11 = F00 / detF;
-    float mu = s->mu;
     float P00 = mu * (F00 - iF00) + llogJ * iF00;
     float P10 = mu * (F10 - iF01) + llogJ * iF01;
     float P01 = mu * (F01 - iF10) + llogJ * iF10;
     float P11 = mu * (F11 - iF11) + llogJ * iF11;
     float I1 = F00 * F00 + F10 * F10 + F01 * F01 + F11 * F11;
     float pe = (float)(0.5 * (double)mu * (double)(I1 - 2.0f) - (double)(mu * logJ) +
-                       0.5 * (double)s->lambda * (double)logJ * (double)logJ);
+                       0.5 * (double)lambda * (double)logJ * (double)logJ);
     float nv0 = -vol0;
     float H00 = nv0 * (P00 * Bm00 + P01 * Bm01);
     float H10 = nv0 * (P10 * Bm00 + P11 * Bm01);
@@ -819,6 +892,7 @@ void orc_calc_forces(orc *s) {
     if (s->bondForces) bond_forces(s);
     if (s->feaForces) fea_forces(s);
     lj_forces(s);
+    wall_forces(s);
 }
 
 /* ------------------------------------------------------------ integrator */
@@ -918,7 +992,9 @@ static double tri_neo_hookean_d(const orc *s, int t, double *f, double *cf, doub
     double F00 = Ds00 * B00 + Ds01 * B10, F10 = Ds10 * B00 + Ds11 * B10;
     double F01 = Ds00 * B01 + Ds01 * B11, F11 = Ds10 * B01 + Ds11 * B11;
     double J = F00 * F11 - F01 * F10, lJ = log(J);
-    double lam = s->lambda, mu = s->mu;
+    float muf, lamf;
+    tri_lame(s, t, &muf, &lamf);
+    double lam = lamf, mu = muf;
     double i00 = F11 / J, i10 = -F10 / J, i01 = -F01 / J, i11 = F00 / J;
     double P00 = mu * (F00 - i00) + lam * lJ * i00, P10 = mu * (F10 - i01) + lam * lJ * i01;
     double P01 = mu * (F01 - i10) + lam * lJ * i10, P11 = mu * (F11 - i11) + lam * lJ * i11;
@@ -1057,6 +1133,17 @@ void orc_forces_f64(const orc *s, double *fx, double *fy, double *cond, double *
             W += 0.5 * fc * dr2; Wc += 0.5 * fcc * dr2;
         }
     }
+    if (s->wallOn) {
+        double yw = wall_y(s), range = wall_range();
+        for (int i = 0; i < N; i++) {
+            double dl = range * (double)s->sigma[i], y = s->py[i], k = s->wallK;
+            double ht = (y + dl) - yw, hb = dl - y;
+            if (ht > 0) { fy[i] -= k * ht; ui[i] += 0.5 * k * ht * ht; U += 0.5 * k * ht * ht;
+                          cond[i] += k * (fabs(y) + dl + fabs(yw)); Uc += 0.5 * k * ht * ht; }
+            if (hb > 0) { fy[i] += k * hb; ui[i] += 0.5 * k * hb * hb; U += 0.5 * k * hb * hb;
+                          cond[i] += k * (fabs(y) + dl); Uc += 0.5 * k * hb * hb; }
+        }
+    }
     out[0] = U; out[1] = W; out[2] = Uc; out[3] = Wc;
 }
 
@@ -1065,6 +1152,7 @@ void orc_forces_f64(const orc *s, double *fx, double *fy, double *cond, double *
 int orc_n(const orc *s) { return s->N; }
 int orc_nbonds(const orc *s) { return s->nb; }
 int orc_ntri(const orc *s) { return s->ntri; }
+int orc_ncl(const orc *s) { return s->ncl; }
 int orc_nref(const orc *s) { return s->ncl > 0 ? s->ncl * s->cl[0].nv : 0; }
 int orc_steps(const orc *s) { return s->steps; }
 int orc_total_updates(const orc *s) { return s->totalUpdates; }
@@ -1114,3 +1202,414 @@ void orc_set_vel(orc *s, const float *v) {
     for (int i = 0; i < s->N; i++) { s->vx[i] = v[2 * i]; s->vy[i] = v[2 * i + 1]; }
 }
 float orc_logf_own(float x) { return own_logf(x); }
+
+/* ================================================ FP64 trajectory and adjoint
+ *
+ * An independent double-precision engine for checking gradients: the same
+ * physics (harmonic bonds with constant kBond, neo-Hookean triangles with
+ * per-elastomer E and nu, Lennard-Jones pairs between particles of different
+ * exclusion groups, harmonic walls, kick-drift-kick leapfrog) on double
+ * state, with pairs found by a fresh cell search at every force evaluation
+ * (no Verlet list, so no list decisions are shared with the float path).
+ * Parameters are doubles: per-elastomer (E, nu), one scale on every pair
+ * epsilon and one on every particle sigma.  orc_d_backward is the discrete
+ * adjoint of orc_d_forward written out by hand; central differences of
+ * orc_d_forward check it. */
+
+typedef struct {
+    int N, ntri, nb, ncl, steps;
+    double dt, Lx, Ly;
+    int wx, wy;
+    double *x, *v, *m, *sig;     /* 2N, 2N, N, N */
+    int *type, *excl;
+    double *E, *nu;              /* per elastomer */
+    int *triCl;                  /* elastomer of each triangle */
+    double *B, *vol0;            /* 4 per triangle (Bm00, Bm10, Bm01, Bm11), 1 per triangle */
+    double epsScale, sigScale;
+    double *traj;                /* (steps+1) x 2N positions */
+    double *f, *a, *w, *g;       /* scratch 2N */
+    int *cstart, *cids, *ccell;  /* cell search scratch */
+    int ncx, ncy;
+} orc_d;
+
+static orc_d D_;  /* one engine per process (test infrastructure) */
+
+static double d_img(double d, double L, int wrap) {
+    if (wrap) {
+        if (d >= 0.5 * L) d -= L;
+        else if (d < -0.5 * L) d += L;
+    }
+    return d;
+}
+
+void orc_d_init(const orc *s) {
+    orc_d *d = &D_;
+    free(d->x); free(d->v); free(d->m); free(d->sig); free(d->type); free(d->excl); free(d->E); free(d->nu);
+    free(d->triCl); free(d->B); free(d->vol0); free(d->traj); free(d->f); free(d->a); free(d->w); free(d->g);
+    free(d->cstart); free(d->cids); free(d->ccell);
+    memset(d, 0, sizeof *d);
+    int N = s->N;
+    d->N = N; d->ntri = s->ntri; d->nb = s->nb; d->ncl = s->ncl;
+    d->dt = s->dt; d->Lx = s->Lx; d->Ly = s->Ly;
+    d->wx = (s->pbc == XYPBC || s->pbc == XPBC); d->wy = (s->pbc == XYPBC);
+    d->x = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->v = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->m = (double *)calloc((size_t)N + 1, sizeof(double));
+    d->sig = (double *)calloc((size_t)N + 1, sizeof(double));
+    d->type = (int *)calloc((size_t)N + 1, sizeof(int));
+    d->excl = (int *)calloc((size_t)N + 1, sizeof(int));
+    for (int i = 0; i < N; i++) {
+        d->x[2 * i] = s->px[i]; d->x[2 * i + 1] = s->py[i];
+        d->v[2 * i] = s->vx[i]; d->v[2 * i + 1] = s->vy[i];
+        d->m[i] = s->mass[i]; d->sig[i] = s->sigma[i]; d->type[i] = s->type[i]; d->excl[i] = s->excl[i];
+    }
+    d->E = (double *)calloc((size_t)d->ncl + 1, sizeof(double));
+    d->nu = (double *)calloc((size_t)d->ncl + 1, sizeof(double));
+    for (int e = 0; e < d->ncl; e++) {
+        int own = s->clOwn && e < s->clMatCap && s->clOwn[e];
+        d->E[e] = own ? s->clE[e] : s->E;
+        d->nu[e] = own ? s->clNu[e] : s->nu;
+    }
+    d->triCl = (int *)calloc((size_t)d->ntri + 1, sizeof(int));
+    d->B = (double *)calloc(4 * (size_t)d->ntri + 4, sizeof(double));
+    d->vol0 = (double *)calloc((size_t)d->ntri + 1, sizeof(double));
+    for (int t = 0; t < d->ntri; t++) {
+        int p0 = s->tri[3 * t], p1 = s->tri[3 * t + 1], p2 = s->tri[3 * t + 2];
+        d->triCl[t] = s->cluster[p0];
+        double Dm00 = (double)s->refx[p0] - s->refx[p2], Dm10 = (double)s->refy[p0] - s->refy[p2];
+        double Dm01 = (double)s->refx[p1] - s->refx[p2], Dm11 = (double)s->refy[p1] - s->refy[p2];
+        double det = Dm00 * Dm11 - Dm01 * Dm10;
+        d->B[4 * t] = Dm11 / det; d->B[4 * t + 1] = -Dm10 / det; d->B[4 * t + 2] = -Dm01 / det; d->B[4 * t + 3] = Dm00 / det;
+        d->vol0[t] = det / 2;
+    }
+    d->epsScale = 1; d->sigScale = 1;
+    d->f = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->a = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->w = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->g = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    d->ccell = (int *)calloc((size_t)N + 1, sizeof(int));
+    d->cids = (int *)calloc((size_t)N + 1, sizeof(int));
+}
+
+void orc_d_set_material(int e, double E, double nu) { if (e >= 0 && e < D_.ncl) { D_.E[e] = E; D_.nu[e] = nu; } }
+void orc_d_set_scales(double eps_scale, double sig_scale) { D_.epsScale = eps_scale; D_.sigScale = sig_scale; }
+void orc_d_set_state(const double *x, const double *v) {
+    memcpy(D_.x, x, sizeof(double) * 2 * (size_t)D_.N);
+    memcpy(D_.v, v, sizeof(double) * 2 * (size_t)D_.N);
+}
+void orc_d_get_state(double *x, double *v) {
+    memcpy(x, D_.x, sizeof(double) * 2 * (size_t)D_.N);
+    memcpy(v, D_.v, sizeof(double) * 2 * (size_t)D_.N);
+}
+
+static void d_lame(double E, double nu, double *mu, double *la) {
+    *la = E * nu / ((1 - 2 * nu) * (1 + nu));
+    *mu = E / (2 * (1 + nu));
+}
+
+/* cell search over the positions x (cells of at least the largest cutoff) */
+static void d_cells(const orc *s, const double *x) {
+    orc_d *d = &D_;
+    double rmax = 0;
+    for (int k = 0; k < s->numTypes * s->numTypes; k++) if (s->rc[k] > rmax) rmax = s->rc[k];
+    double smax = 0;
+    for (int i = 0; i < d->N; i++) if (d->sig[i] > smax) smax = d->sig[i];
+    double cut = rmax * smax * d->sigScale;
+    d->ncx = (int)floor(d->Lx / cut); d->ncy = (int)floor(d->Ly / cut);
+    if (d->ncx < 1) d->ncx = 1;
+    if (d->ncy < 1) d->ncy = 1;
+    int nc = d->ncx * d->ncy;
+    free(d->cstart);
+    d->cstart = (int *)calloc((size_t)nc + 1, sizeof(int));
+    for (int i = 0; i < d->N; i++) {
+        int ix = (int)floor(x[2 * i] / d->Lx * d->ncx), iy = (int)floor(x[2 * i + 1] / d->Ly * d->ncy);
+        ix = ix < 0 ? 0 : ix >= d->ncx ? d->ncx - 1 : ix;
+        iy = iy < 0 ? 0 : iy >= d->ncy ? d->ncy - 1 : iy;
+        d->ccell[i] = ix + iy * d->ncx;
+        d->cstart[d->ccell[i] + 1]++;
+    }
+    for (int c = 0; c < nc; c++) d->cstart[c + 1] += d->cstart[c];
+    int *fill = (int *)calloc((size_t)nc, sizeof(int));
+    for (int i = 0; i < d->N; i++) d->cids[d->cstart[d->ccell[i]] + fill[d->ccell[i]]++] = i;
+    free(fill);
+}
+
+/* Forces at x (into f, 2N); with w != NULL instead the directional
+ * derivative of the forces along w (into f) and the parameter terms
+ * w . df/dtheta accumulated into gMu/gLam (per elastomer), ge, gs. */
+static void d_forces(const orc *s, const double *x, double *f, const double *w, int step, double *gMu, double *gLam,
+                     double *ge, double *gs) {
+    orc_d *d = &D_;
+    int N = d->N;
+    for (int k = 0; k < 2 * N; k++) f[k] = 0;
+    /* bonds */
+    if (s->bondForces) {
+        for (int l = 0; l < d->nb; l++) {
+            int i = s->bond[2 * l], j = s->bond[2 * l + 1];
+            double dx = d_img(x[2 * i] - x[2 * j], d->Lx, d->wx), dy = d_img(x[2 * i + 1] - x[2 * j + 1], d->Ly, d->wy);
+            double r = sqrt(dx * dx + dy * dy), r0 = s->r0[l], k = s->kBond;
+            double kdr = -k * (r - r0) / r;
+            double f1, f2;
+            if (!w) { f1 = kdr * dx; f2 = kdr * dy; }
+            else {
+                double ddx = w[2 * i] - w[2 * j], ddy = w[2 * i + 1] - w[2 * j + 1];
+                double dr = (dx * ddx + dy * ddy) / r, dk = -k * r0 * dr / (r * r);
+                f1 = dk * dx + kdr * ddx; f2 = dk * dy + kdr * ddy;
+            }
+            f[2 * i] += f1; f[2 * i + 1] += f2; f[2 * j] -= f1; f[2 * j + 1] -= f2;
+        }
+    }
+    /* neo-Hookean triangles */
+    if (s->feaForces) {
+        for (int t = 0; t < d->ntri; t++) {
+            int p[3] = {s->tri[3 * t], s->tri[3 * t + 1], s->tri[3 * t + 2]};
+            double mu, la;
+            d_lame(d->E[d->triCl[t]], d->nu[d->triCl[t]], &mu, &la);
+            double Ds00 = d_img(x[2 * p[0]] - x[2 * p[2]], d->Lx, d->wx), Ds10 = d_img(x[2 * p[0] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            double Ds01 = d_img(x[2 * p[1]] - x[2 * p[2]], d->Lx, d->wx), Ds11 = d_img(x[2 * p[1] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            const double *B = d->B + 4 * t;
+            double F00 = Ds00 * B[0] + Ds01 * B[1], F10 = Ds10 * B[0] + Ds11 * B[1];
+            double F01 = Ds00 * B[2] + Ds01 * B[3], F11 = Ds10 * B[2] + Ds11 * B[3];
+            double J = F00 * F11 - F01 * F10, lJ = log(J);
+            double i00 = F11 / J, i10 = -F10 / J, i01 = -F01 / J, i11 = F00 / J;
+            double nv = -d->vol0[t];
+            double P00, P10, P01, P11;
+            if (!w) {
+                P00 = mu * (F00 - i00) + la * lJ * i00; P10 = mu * (F10 - i01) + la * lJ * i01;
+                P01 = mu * (F01 - i10) + la * lJ * i10; P11 = mu * (F11 - i11) + la * lJ * i11;
+            } else {
+                double e00 = w[2 * p[0]] - w[2 * p[2]], e10 = w[2 * p[0] + 1] - w[2 * p[2] + 1];
+                double e01 = w[2 * p[1]] - w[2 * p[2]], e11 = w[2 * p[1] + 1] - w[2 * p[2] + 1];
+                double dF00 = e00 * B[0] + e01 * B[1], dF10 = e10 * B[0] + e11 * B[1];
+                double dF01 = e00 * B[2] + e01 * B[3], dF11 = e10 * B[2] + e11 * B[3];
+                double dJ = dF00 * F11 + F00 * dF11 - dF01 * F10 - F01 * dF10, dlJ = dJ / J;
+                /* d(F^-1) = -F^-1 dF F^-1 */
+                double t00 = i00 * dF00 + i01 * dF10, t01 = i00 * dF01 + i01 * dF11;
+                double t10 = i10 * dF00 + i11 * dF10, t11 = i10 * dF01 + i11 * dF11;
+                double di00 = -(t00 * i00 + t01 * i10), di01 = -(t00 * i01 + t01 * i11);
+                double di10 = -(t10 * i00 + t11 * i10), di11 = -(t10 * i01 + t11 * i11);
+                P00 = mu * (dF00 - di00) + la * dlJ * i00 + la * lJ * di00;
+                P10 = mu * (dF10 - di01) + la * dlJ * i01 + la * lJ * di01;
+                P01 = mu * (dF01 - di10) + la * dlJ * i10 + la * lJ * di10;
+                P11 = mu * (dF11 - di11) + la * dlJ * i11 + la * lJ * di11;
+                /* w . f_mu, w . f_lambda */
+                double Hm00 = nv * ((F00 - i00) * B[0] + (F01 - i10) * B[2]), Hm10 = nv * ((F10 - i01) * B[0] + (F11 - i11) * B[2]);
+                double Hm01 = nv * ((F00 - i00) * B[1] + (F01 - i10) * B[3]), Hm11 = nv * ((F10 - i01) * B[1] + (F11 - i11) * B[3]);
+                double Hl00 = nv * lJ * (i00 * B[0] + i10 * B[2]), Hl10 = nv * lJ * (i01 * B[0] + i11 * B[2]);
+                double Hl01 = nv * lJ * (i00 * B[1] + i10 * B[3]), Hl11 = nv * lJ * (i01 * B[1] + i11 * B[3]);
+                int e = d->triCl[t];
+                gMu[e] += e00 * Hm00 + e10 * Hm10 + e01 * Hm01 + e11 * Hm11;
+                gLam[e] += e00 * Hl00 + e10 * Hl10 + e01 * Hl01 + e11 * Hl11;
+            }
+            double H00 = nv * (P00 * B[0] + P01 * B[2]), H10 = nv * (P10 * B[0] + P11 * B[2]);
+            double H01 = nv * (P00 * B[1] + P01 * B[3]), H11 = nv * (P10 * B[1] + P11 * B[3]);
+            f[2 * p[0]] += H00; f[2 * p[0] + 1] += H10;
+            f[2 * p[1]] += H01; f[2 * p[1] + 1] += H11;
+            f[2 * p[2]] -= H00 + H01; f[2 * p[2] + 1] -= H10 + H11;
+        }
+    }
+    /* Lennard-Jones pairs by cell search */
+    d_cells(s, x);
+    int nt = s->numTypes;
+    for (int i = 0; i < N; i++) {
+        int c = d->ccell[i], cx = c % d->ncx, cy = c / d->ncx;
+        int seen[9], ns = 0;
+        for (int ox = -1; ox <= 1; ox++)
+            for (int oy = -1; oy <= 1; oy++) {
+                int nx = (cx + ox + d->ncx) % d->ncx, ny = (cy + oy + d->ncy) % d->ncy, nc = nx + ny * d->ncx, dup = 0;
+                for (int q = 0; q < ns; q++) dup |= seen[q] == nc;
+                if (dup) continue;
+                seen[ns++] = nc;
+                for (int q = d->cstart[nc]; q < d->cstart[nc + 1]; q++) {
+                    int j = d->cids[q];
+                    if (j == i) continue;
+                    if (d->excl[i] != -1 && d->excl[i] == d->excl[j]) continue;
+                    double dx = d_img(x[2 * i] - x[2 * j], d->Lx, d->wx), dy = d_img(x[2 * i + 1] - x[2 * j + 1], d->Ly, d->wy);
+                    int tt = d->type[i] * nt + d->type[j];
+                    double sij = 0.5 * (d->sig[i] + d->sig[j]) * d->sigScale, rc = s->rc[tt], eps = s->eps[tt] * d->epsScale;
+                    double dr2 = dx * dx + dy * dy;
+                    if (!(dr2 < rc * rc * sij * sij)) continue;
+                    double s2 = sij * sij / dr2, s6 = s2 * s2 * s2, c48 = 48.0 * eps / (sij * sij);
+                    double fc = c48 * s6 * (s6 - 0.5) * s2;
+                    if (!w) { f[2 * i] += fc * dx; f[2 * i + 1] += fc * dy; }
+                    else {
+                        double cs2 = c48 * s2, dfc = -(cs2 / dr2) * (7 * s6 * s6 - 2 * s6);
+                        double ddx = w[2 * i] - w[2 * j], ddy = w[2 * i + 1] - w[2 * j + 1], dot = dx * ddx + dy * ddy;
+                        f[2 * i] += fc * ddx + 2 * dfc * dot * dx;
+                        f[2 * i + 1] += fc * ddy + 2 * dfc * dot * dy;
+                        *ge += w[2 * i] * fc * dx + w[2 * i + 1] * fc * dy;
+                        double fs = cs2 * (12 * s6 * s6 - 3 * s6);
+                        *gs += w[2 * i] * fs * dx + w[2 * i + 1] * fs * dy;
+                    }
+                }
+            }
+    }
+    /* walls */
+    if (s->wallOn) {
+        double yw = (double)s->wallY0 - (double)s->wallV * (step * d->dt), k = s->wallK;
+        double range = pow(2.0, 1.0 / 6.0);
+        for (int i = 0; i < N; i++) {
+            double dl = range * d->sig[i] * d->sigScale, y = x[2 * i + 1];
+            double ht = (y + dl) - yw, hb = dl - y;
+            if (!w) {
+                if (ht > 0) f[2 * i + 1] -= k * ht;
+                if (hb > 0) f[2 * i + 1] += k * hb;
+            } else {
+                if (ht > 0) { f[2 * i + 1] -= k * w[2 * i + 1]; *gs += w[2 * i + 1] * (-k * dl); }
+                if (hb > 0) { f[2 * i + 1] -= k * w[2 * i + 1]; *gs += w[2 * i + 1] * (k * dl); }
+            }
+        }
+    }
+}
+
+/* observable J = cWall (F_top + F_bottom) / (2 Lx) + cFea U_fea at x (step n) */
+static double d_observable(const orc *s, const double *x, int n, double cWall, double cFea) {
+    orc_d *d = &D_;
+    double J = 0;
+    if (s->wallOn && cWall != 0) {
+        double yw = (double)s->wallY0 - (double)s->wallV * (n * d->dt), k = s->wallK, range = pow(2.0, 1.0 / 6.0), F = 0;
+        for (int i = 0; i < d->N; i++) {
+            double dl = range * d->sig[i] * d->sigScale, y = x[2 * i + 1];
+            if ((y + dl) - yw > 0) F += k * ((y + dl) - yw);
+            if (dl - y > 0) F += k * (dl - y);
+        }
+        J += cWall * F / (2 * d->Lx);
+    }
+    if (s->feaForces && cFea != 0) {
+        for (int t = 0; t < d->ntri; t++) {
+            int p[3] = {s->tri[3 * t], s->tri[3 * t + 1], s->tri[3 * t + 2]};
+            double mu, la;
+            d_lame(d->E[d->triCl[t]], d->nu[d->triCl[t]], &mu, &la);
+            double Ds00 = d_img(x[2 * p[0]] - x[2 * p[2]], d->Lx, d->wx), Ds10 = d_img(x[2 * p[0] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            double Ds01 = d_img(x[2 * p[1]] - x[2 * p[2]], d->Lx, d->wx), Ds11 = d_img(x[2 * p[1] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            const double *B = d->B + 4 * t;
+            double F00 = Ds00 * B[0] + Ds01 * B[1], F10 = Ds10 * B[0] + Ds11 * B[1];
+            double F01 = Ds00 * B[2] + Ds01 * B[3], F11 = Ds10 * B[2] + Ds11 * B[3];
+            double lJ = log(F00 * F11 - F01 * F10), I1 = F00 * F00 + F10 * F10 + F01 * F01 + F11 * F11;
+            J += cFea * d->vol0[t] * (0.5 * mu * (I1 - 2) - mu * lJ + 0.5 * la * lJ * lJ);
+        }
+    }
+    return J;
+}
+
+/* FP64 run of 'steps' kick-drift-kick steps from the engine state, starting
+ * at step index n0 (the wall clock); keeps every position set.  Returns J at
+ * the final positions. */
+double orc_d_forward(const orc *s, int n0, int steps, double cWall, double cFea) {
+    orc_d *d = &D_;
+    int N = d->N;
+    d->steps = steps;
+    free(d->traj);
+    d->traj = (double *)malloc(sizeof(double) * 2 * (size_t)N * (size_t)(steps + 1));
+    double h = 0.5 * d->dt;
+    memcpy(d->traj, d->x, sizeof(double) * 2 * (size_t)N);
+    d_forces(s, d->x, d->f, NULL, n0, NULL, NULL, NULL, NULL);
+    for (int i = 0; i < N; i++) { d->a[2 * i] = d->f[2 * i] / d->m[i]; d->a[2 * i + 1] = d->f[2 * i + 1] / d->m[i]; }
+    for (int n = 0; n < steps; n++) {
+        for (int k = 0; k < 2 * N; k++) { d->v[k] += h * d->a[k]; d->x[k] += d->dt * d->v[k]; }
+        for (int i = 0; i < N; i++) {
+            if (d->wx) d->x[2 * i] -= floor(d->x[2 * i] / d->Lx) * d->Lx;
+            if (d->wy) d->x[2 * i + 1] -= floor(d->x[2 * i + 1] / d->Ly) * d->Ly;
+        }
+        memcpy(d->traj + 2 * (size_t)N * (n + 1), d->x, sizeof(double) * 2 * (size_t)N);
+        d_forces(s, d->x, d->f, NULL, n0 + n + 1, NULL, NULL, NULL, NULL);
+        for (int i = 0; i < N; i++) { d->a[2 * i] = d->f[2 * i] / d->m[i]; d->a[2 * i + 1] = d->f[2 * i + 1] / d->m[i]; }
+        for (int k = 0; k < 2 * N; k++) d->v[k] += h * d->a[k];
+    }
+    return d_observable(s, d->x, n0 + steps, cWall, cFea);
+}
+
+/* Replace the stored trajectory by (steps + 1) given position sets, e.g. a
+ * float run's, so that orc_d_backward differentiates along it in double. */
+void orc_d_set_traj(const double *traj, int steps) {
+    orc_d *d = &D_;
+    free(d->traj);
+    size_t n = 2 * (size_t)d->N * (size_t)(steps + 1);
+    d->traj = (double *)malloc(sizeof(double) * n);
+    memcpy(d->traj, traj, sizeof(double) * n);
+    d->steps = steps;
+}
+
+/* dJ/dx at x by central differences would be slow; the observable's
+ * gradient is formed analytically: walls and -f_fea. */
+static void d_obs_grad(const orc *s, const double *x, int n, double cWall, double cFea, double *gx, double *gMu,
+                       double *gLam, double *gs) {
+    orc_d *d = &D_;
+    int N = d->N;
+    for (int k = 0; k < 2 * N; k++) gx[k] = 0;
+    if (s->wallOn && cWall != 0) {
+        double yw = (double)s->wallY0 - (double)s->wallV * (n * d->dt), k = s->wallK, range = pow(2.0, 1.0 / 6.0);
+        double a = cWall * k / (2 * d->Lx);
+        for (int i = 0; i < N; i++) {
+            double dl = range * d->sig[i] * d->sigScale, y = x[2 * i + 1];
+            if ((y + dl) - yw > 0) { gx[2 * i + 1] += a; *gs += a * dl; }
+            if (dl - y > 0) { gx[2 * i + 1] -= a; *gs += a * dl; }
+        }
+    }
+    if (s->feaForces && cFea != 0) {
+        for (int t = 0; t < d->ntri; t++) {
+            int p[3] = {s->tri[3 * t], s->tri[3 * t + 1], s->tri[3 * t + 2]};
+            double mu, la;
+            d_lame(d->E[d->triCl[t]], d->nu[d->triCl[t]], &mu, &la);
+            double Ds00 = d_img(x[2 * p[0]] - x[2 * p[2]], d->Lx, d->wx), Ds10 = d_img(x[2 * p[0] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            double Ds01 = d_img(x[2 * p[1]] - x[2 * p[2]], d->Lx, d->wx), Ds11 = d_img(x[2 * p[1] + 1] - x[2 * p[2] + 1], d->Ly, d->wy);
+            const double *B = d->B + 4 * t;
+            double F00 = Ds00 * B[0] + Ds01 * B[1], F10 = Ds10 * B[0] + Ds11 * B[1];
+            double F01 = Ds00 * B[2] + Ds01 * B[3], F11 = Ds10 * B[2] + Ds11 * B[3];
+            double J = F00 * F11 - F01 * F10, lJ = log(J);
+            double i00 = F11 / J, i10 = -F10 / J, i01 = -F01 / J, i11 = F00 / J;
+            double P00 = mu * (F00 - i00) + la * lJ * i00, P10 = mu * (F10 - i01) + la * lJ * i01;
+            double P01 = mu * (F01 - i10) + la * lJ * i10, P11 = mu * (F11 - i11) + la * lJ * i11;
+            double v0 = d->vol0[t];
+            /* dU/dx = -f = vol0 P Bm^T on vertices 0, 1; vertex 2 minus their sum */
+            double H00 = v0 * (P00 * B[0] + P01 * B[2]), H10 = v0 * (P10 * B[0] + P11 * B[2]);
+            double H01 = v0 * (P00 * B[1] + P01 * B[3]), H11 = v0 * (P10 * B[1] + P11 * B[3]);
+            gx[2 * p[0]] += cFea * H00; gx[2 * p[0] + 1] += cFea * H10;
+            gx[2 * p[1]] += cFea * H01; gx[2 * p[1] + 1] += cFea * H11;
+            gx[2 * p[2]] -= cFea * (H00 + H01); gx[2 * p[2] + 1] -= cFea * (H10 + H11);
+            double I1 = F00 * F00 + F10 * F10 + F01 * F01 + F11 * F11;
+            int e = d->triCl[t];
+            gMu[e] += cFea * v0 * (0.5 * (I1 - 2) - lJ);
+            gLam[e] += cFea * v0 * 0.5 * lJ * lJ;
+        }
+    }
+}
+
+/* Adjoint of orc_d_forward: gradients of J (+ <xseed, x_N> + <vseed, v_N>
+ * for non-null seeds) w.r.t. the initial positions and velocities (2N each),
+ * per-elastomer E and nu, log eps_scale, log sig_scale. */
+void orc_d_backward(const orc *s, int n0, double cWall, double cFea, const double *xseed, const double *vseed,
+                    double *gx0, double *gv0, double *gE, double *gnu, double *glogeps, double *glogsig) {
+    orc_d *d = &D_;
+    int N = d->N, ne = d->ncl, steps = d->steps;
+    double h = 0.5 * d->dt, dt = d->dt;
+    double *xb = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    double *vb = (double *)calloc(2 * (size_t)N + 2, sizeof(double));
+    double *gMu = (double *)calloc((size_t)ne + 1, sizeof(double));
+    double *gLam = (double *)calloc((size_t)ne + 1, sizeof(double));
+    double ge = 0, gs = 0;
+    d_obs_grad(s, d->traj + 2 * (size_t)N * steps, n0 + steps, cWall, cFea, xb, gMu, gLam, &gs);
+    if (xseed) for (int k = 0; k < 2 * N; k++) xb[k] += xseed[k];
+    if (vseed) for (int k = 0; k < 2 * N; k++) vb[k] = vseed[k];
+    double c = h;
+    for (int n = steps; n >= 0; n--) {
+        for (int i = 0; i < N; i++) { d->w[2 * i] = c * vb[2 * i] / d->m[i]; d->w[2 * i + 1] = c * vb[2 * i + 1] / d->m[i]; }
+        d_forces(s, d->traj + 2 * (size_t)N * n, d->g, d->w, n0 + n, gMu, gLam, &ge, &gs);
+        for (int k = 0; k < 2 * N; k++) xb[k] += d->g[k];
+        if (n == 0) break;
+        for (int k = 0; k < 2 * N; k++) vb[k] += dt * xb[k];
+        c = (n - 1 == 0) ? h : dt;
+    }
+    memcpy(gx0, xb, sizeof(double) * 2 * (size_t)N);
+    memcpy(gv0, vb, sizeof(double) * 2 * (size_t)N);
+    for (int e = 0; e < ne; e++) {
+        double E = d->E[e], nu = d->nu[e];
+        double dmu_dE = 1.0 / (2 * (1 + nu)), dmu_dnu = -E / (2 * (1 + nu) * (1 + nu));
+        double Dd = (1 + nu) * (1 - 2 * nu), dla_dE = nu / Dd, dla_dnu = E * (1 + 2 * nu * nu) / (Dd * Dd);
+        gE[e] = gMu[e] * dmu_dE + gLam[e] * dla_dE;
+        gnu[e] = gMu[e] * dmu_dnu + gLam[e] * dla_dnu;
+    }
+    *glogeps = ge;
+    *glogsig = gs;
+    free(xb); free(vb); free(gMu); free(gLam);
+}

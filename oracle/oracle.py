@@ -83,6 +83,14 @@ def lib():
             "orc_get_tris": (None, [P, ip, fp, fp]), "orc_get_cells": (None, [P, ip, ip]),
             "orc_get_nbrs": (None, [P, ip, ip]), "orc_set_pos": (None, [P, fp]), "orc_set_vel": (None, [P, fp]),
             "orc_logf_own": (C.c_float, [C.c_float]),
+            "orc_set_elastomer_material": (C.c_int, [P, C.c_int, C.c_double, C.c_double]),
+            "orc_set_moving_wall": (None, [P, C.c_double, C.c_double, C.c_double]),
+            "orc_wall_forces": (None, [P, dp, dp]),
+            "orc_ncl": (C.c_int, [P]), "orc_d_init": (None, [P]), "orc_d_set_material": (None, [C.c_int, C.c_double, C.c_double]),
+            "orc_d_set_scales": (None, [C.c_double, C.c_double]), "orc_d_set_state": (None, [dp, dp]),
+            "orc_d_get_state": (None, [dp, dp]), "orc_d_set_traj": (None, [dp, C.c_int]),
+            "orc_d_forward": (C.c_double, [P, C.c_int, C.c_int, C.c_double, C.c_double]),
+            "orc_d_backward": (None, [P, C.c_int, C.c_double, C.c_double, dp, dp, dp, dp, dp, dp, dp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -153,6 +161,78 @@ class Oracle:
 
     def set_skin(self, s):
         self.L.orc_set_skin(self.h, s)
+
+    def set_elastomer_material(self, e, E, nu):
+        if self.L.orc_set_elastomer_material(self.h, int(e), float(E), float(nu)):
+            raise ValueError(f"no elastomer {e}")
+
+    def set_moving_wall(self, k, y0, v):
+        self.L.orc_set_moving_wall(self.h, float(k), float(y0), float(v))
+
+    def n_elastomers(self):
+        return self.L.orc_ncl(self.h)
+
+    # ---- FP64 trajectory and adjoint (one engine per process)
+    def d_init(self):
+        self.L.orc_d_init(self.h)
+
+    def d_set_material(self, e, E, nu):
+        self.L.orc_d_set_material(int(e), float(E), float(nu))
+
+    def d_set_scales(self, eps_scale, sig_scale):
+        self.L.orc_d_set_scales(float(eps_scale), float(sig_scale))
+
+    def d_set_state(self, x, v):
+        x = np.ascontiguousarray(x, np.float64).ravel()
+        v = np.ascontiguousarray(v, np.float64).ravel()
+        self.L.orc_d_set_state(_ptr(x, C.c_double), _ptr(v, C.c_double))
+
+    def d_get_state(self):
+        n = self.N
+        x = np.zeros(2 * n)
+        v = np.zeros(2 * n)
+        self.L.orc_d_get_state(_ptr(x, C.c_double), _ptr(v, C.c_double))
+        return x.reshape(n, 2), v.reshape(n, 2)
+
+    def d_set_traj(self, traj):
+        t = np.ascontiguousarray(traj, np.float64)
+        self.L.orc_d_set_traj(_ptr(t, C.c_double), t.shape[0] - 1)
+
+    def float_trajectory(self, steps, every):
+        """Positions of every step of a float run done as run(every) segments
+        (run(0) then do_step, which is what run(k) does)."""
+        traj = [self.positions().astype(np.float64)]
+        done = 0
+        while done < steps:
+            k = min(every, steps - done)
+            self.run(0)
+            for _ in range(k):
+                self.do_step()
+                traj.append(self.positions().astype(np.float64))
+            done += k
+        return np.stack(traj)
+
+    def d_forward(self, n0, steps, c_wall=1.0, c_fea=1.0):
+        return self.L.orc_d_forward(self.h, int(n0), int(steps), float(c_wall), float(c_fea))
+
+    def d_backward(self, n0, c_wall=1.0, c_fea=1.0, xseed=None, vseed=None):
+        n = self.N
+        ne = max(1, self.n_elastomers())
+        gx, gv = np.zeros(2 * n), np.zeros(2 * n)
+        gE, gnu = np.zeros(ne), np.zeros(ne)
+        ge, gs = np.zeros(1), np.zeros(1)
+        sx = None if xseed is None else np.ascontiguousarray(xseed, np.float64).ravel()
+        sv = None if vseed is None else np.ascontiguousarray(vseed, np.float64).ravel()
+        self.L.orc_d_backward(self.h, int(n0), float(c_wall), float(c_fea),
+                              None if sx is None else _ptr(sx, C.c_double), None if sv is None else _ptr(sv, C.c_double),
+                              *[_ptr(a, C.c_double) for a in (gx, gv, gE, gnu, ge, gs)])
+        return dict(x0=gx.reshape(n, 2), v0=gv.reshape(n, 2), E=gE, nu=gnu, log_eps=float(ge[0]),
+                    log_sigma=float(gs[0]))
+
+    def wall_forces(self):
+        t, b = C.c_double(), C.c_double()
+        self.L.orc_wall_forces(self.h, C.byref(t), C.byref(b))
+        return t.value, b.value
 
     def set_elastomer_bonds(self, mode):
         self.L.orc_set_elastomer_bonds(self.h, int(mode))
