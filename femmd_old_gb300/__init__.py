@@ -174,6 +174,15 @@ class System:
         self._call("femmd_get_wall_forces", C.byref(t), C.byref(b))
         return t.value, b.value
 
+    PROPERTY_NAMES = ("uKinetic", "uPotential", "uTotal", "temperature", "virial", "feaVirial", "pressure",
+                      "clusterUKinetic", "clusterVirial", "molPressure")
+
+    def properties(self):
+        """Properties::evaluate at the current state (dict by the reference's names)."""
+        out = (C.c_double * 10)()
+        self._call("femmd_get_properties", out)
+        return dict(zip(self.PROPERTY_NAMES, list(out)))
+
     def adjoint_forward(self, steps, every=20):
         self._call("femmd_adjoint_forward", int(steps), int(every))
 

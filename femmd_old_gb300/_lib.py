@@ -46,6 +46,7 @@ SIGNATURES = {
     "femmd_set_elastomer_material": (i_, [P, i_, d_, d_]),
     "femmd_set_moving_wall": (i_, [P, d_, d_, d_]),
     "femmd_get_wall_forces": (i_, [P, dp, dp]),
+    "femmd_get_properties": (i_, [P, dp]),
     "femmd_adjoint_forward": (i_, [P, i_, i_]),
     "femmd_adjoint_backward": (i_, [P, d_, d_, fp, fp, fp, fp, dp, dp, dp, dp]),
     "femmd_adjoint_observable": (i_, [P, dp, dp]),

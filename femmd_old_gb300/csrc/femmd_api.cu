@@ -117,6 +117,12 @@ struct femmd_ctx {
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF, triLame;
     DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta;
     bool ownMaterial = false, materialDirty = false;
+    // observables: cluster ranges and masses, cluster of each particle, FP64 terms
+    DBuf<int2> clRange;
+    DBuf<float> clMass;
+    DBuf<int> clusterOf;
+    DBuf<double2> unf, cmPos, cmVel;
+    DBuf<double> clKin, feaVir, kinTerm, clVir;
     DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, unsorted, sortedIds, nbr, nbrCount, bStart, tStart,
         tEnt;
     DBuf<int2> bEnt;
@@ -251,6 +257,8 @@ static void release_device(femmd_ctx *c) {
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
     c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
     c->triLame.release(); c->wallDelta.release();
+    c->clRange.release(); c->clMass.release(); c->clusterOf.release(); c->unf.release(); c->cmPos.release();
+    c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
     auto &a = c->adj;
     a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
     a.xbar.release(); a.vbar.release(); a.w0.release(); a.w1.release(); a.triD.release();
@@ -1710,6 +1718,72 @@ femmd_status femmd_get_profile(femmd_ctx *ctx, double *fms, long long *fl, doubl
     return FEMMD_OK;
 }
 
+
+// ============================================================== observables
+
+// Properties::evaluate (properties.cpp:15-36) at the current state:
+// out[0..9] = uKinetic, uPotential, uTotal, temperature, virial, feaVirial,
+// pressure, clusterUKinetic, clusterVirial, molPressure.
+femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
+    NEED(ctx);
+    if (!out) return fail(ctx, FEMMD_INVALID_ARG, "null output");
+    femmd_status st;
+    if ((st = femmd_calc_forces(ctx))) return st;
+    const int N = (int)ctx->pos.size(), nt = (int)ctx->refVol.size(), ncl = (int)ctx->clusters.size();
+    for (int k = 0; k < 10; k++) out[k] = 0.0;
+    if (N == 0) return FEMMD_OK;
+    cudaStream_t sm = ctx->stream;
+    if (ncl > 0) {
+        std::vector<int2> rg(ncl);
+        std::vector<float> ms(ncl);
+        for (int c = 0; c < ncl; c++) {
+            rg[c] = make_int2(ctx->clusters[c].offset, ctx->clusters[c].nv);
+            ms[c] = ctx->clusters[c].mass;
+        }
+        CK(ctx->clRange.ensure(ncl)); CK(ctx->clMass.ensure(ncl)); CK(ctx->clusterOf.ensure(N));
+        CK(ctx->cmPos.ensure(ncl)); CK(ctx->cmVel.ensure(ncl)); CK(ctx->clKin.ensure(ncl));
+        CK(ctx->feaVir.ensure(std::max(nt, 1)));
+        CK(cudaMemcpyAsync(ctx->clRange.p, rg.data(), ncl * sizeof(int2), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(ctx->clMass.p, ms.data(), ncl * sizeof(float), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(ctx->clusterOf.p, ctx->cluster.data(), N * sizeof(int), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemsetAsync(ctx->feaVir.p, 0, sizeof(double) * std::max(nt, 1), sm));
+    }
+    CK(ctx->unf.ensure(N)); CK(ctx->kinTerm.ensure(N)); CK(ctx->clVir.ensure(N));
+    DevSys s = make_sys(ctx);
+    const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+    Launch L;
+    L.stream = sm;
+    CK(enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p, ctx->cmPos.p,
+                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p));
+    std::vector<double> kin(N), cv(N), fv(std::max(nt, 1), 0.0), ck(std::max(ncl, 1), 0.0);
+    CK(cudaMemcpyAsync(kin.data(), ctx->kinTerm.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(cv.data(), ctx->clVir.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    if (ncl > 0) {
+        CK(cudaMemcpyAsync(ck.data(), ctx->clKin.p, ncl * sizeof(double), cudaMemcpyDeviceToHost, sm));
+        if (nt > 0) CK(cudaMemcpyAsync(fv.data(), ctx->feaVir.p, nt * sizeof(double), cudaMemcpyDeviceToHost, sm));
+    }
+    if ((st = read_scalars(ctx))) return st;
+    double kinEneSum = 0, clusterVirial = 0, feaVirial = 0, clusterKin = 0;
+    for (double v : kin) kinEneSum += v;
+    for (double v : cv) clusterVirial += v;
+    if (ncl > 0) {
+        for (int t = 0; t < nt; t++) feaVirial += fv[t];
+        for (int c = 0; c < ncl; c++) clusterKin += ck[c];
+    }
+    const double V = (double)ctx->Lx * (double)ctx->Ly;
+    const double U = ctx->hsc->U, W = ctx->hsc->W;
+    out[0] = 0.5 * kinEneSum / N;
+    out[1] = U / N;
+    out[2] = out[0] + out[1];
+    out[3] = out[0];
+    out[4] = W;
+    out[5] = feaVirial;
+    out[6] = 0.5 * kinEneSum / V + 0.5 * (W + feaVirial) / V;
+    out[7] = ncl > 0 ? 0.5 * clusterKin / ncl : 0.0;
+    out[8] = clusterVirial;
+    out[9] = 0.5 * clusterKin / V - 0.5 * clusterVirial / V;
+    return FEMMD_OK;
+}
 
 // ================================================================== adjoint
 

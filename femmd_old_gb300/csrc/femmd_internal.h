@@ -26,6 +26,10 @@ constexpr int kIdMask = (1 << kIdBits) - 1;
 constexpr int kMaxTypes = 32;
 constexpr int kBlock = 256;        // threads per block of the per-particle kernels
 constexpr int kStepBlock = 128;    // threads per block of the step kernel
+#ifndef FEMMD_NN_BLOCK
+#define FEMMD_NN_BLOCK 256
+#endif
+constexpr int kNnBlock = FEMMD_NN_BLOCK;  // threads per block of the list build
 constexpr int kScanBlock = 1024;   // cells per block of the cell-start scan
 constexpr int kObsCols = 6;        // per-step observable row: U, W, sum m v^2, max v^2, dispHi, rebuilt
 constexpr int kTraceCols = 6;      // per-step trace row (ns): tri start/end, step start/end, rebuild start/end
@@ -146,6 +150,12 @@ cudaError_t enqueue_adj_seed(Launch &L, const DevSys &s, const float2 *pos, floa
 cudaError_t enqueue_adj_step(Launch &L, const DevSys &s, const float2 *pos, const float2 *w, float2 *triD,
                              double *gMu, double *gLam, float2 *xbar, float2 *vbar, float2 *wOut, float cNext,
                              int update, float yw, double *epsAcc, double *sigAcc);
+
+// ---- observables (k_props.cu): cluster unfolding, centre of mass and
+// velocity, feaVirial and cluster-virial terms, m v^2 per particle
+cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
+                          const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
+                          double *clKin, double *feaVir, double *kin, double *clVir);
 
 // ---- batched replicas (k_batch.cu): one persistent launch over many systems
 struct BatchLaunch {

@@ -26,35 +26,7 @@ namespace femmd {
 
 namespace {
 
-// block-wide sum / max / or of one value per thread (blockDim a multiple of 32, <= 1024)
-__device__ __forceinline__ float block_sum(float v, float *scr) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum_f(v);
-    __syncthreads();
-    if (lane == 0) scr[warp] = v;
-    __syncthreads();
-    float t = 0.0f;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < nw ? scr[threadIdx.x] : 0.0f;
-        t = warp_sum_f(t);
-    }
-    return t;  // valid in thread 0
-}
-
-__device__ __forceinline__ float block_max(float v, float *scr) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_max(v);
-    __syncthreads();
-    if (lane == 0) scr[warp] = v;
-    __syncthreads();
-    float t = 0.0f;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < nw ? scr[threadIdx.x] : 0.0f;
-        t = warp_max(t);
-    }
-    return t;
-}
-
+// block-wide max of one value per thread (blockDim a multiple of 32, <= 1024)
 __device__ __forceinline__ int block_max_int(int v, int *scr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_max_int(v);
@@ -67,6 +39,41 @@ __device__ __forceinline__ int block_max_int(int v, int *scr) {
         t = warp_max_int(t);
     }
     return t;
+}
+
+// One pass over the block for the step's four sums, the max and the any-bad
+// flag (two barriers instead of ten).  scr holds 6 values per warp.  The
+// results are valid in thread 0.
+__device__ __forceinline__ void block_reduce_step(float &a, float &b, float &c, float &d, float &m, int &bad,
+                                                  float *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    a = warp_sum_f(a);
+    b = warp_sum_f(b);
+    c = warp_sum_f(c);
+    d = warp_sum_f(d);
+    m = warp_max(m);
+    bad = __any_sync(0xffffffffu, bad);
+    __syncthreads();  // scr may still be read by the previous reduction
+    if (lane == 0) {
+        float *w = scr + 6 * warp;
+        w[0] = a;
+        w[1] = b;
+        w[2] = c;
+        w[3] = d;
+        w[4] = m;
+        w[5] = bad ? 1.0f : 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const bool in = lane < nw;
+        const float *w = scr + 6 * lane;
+        a = warp_sum_f(in ? w[0] : 0.0f);
+        b = warp_sum_f(in ? w[1] : 0.0f);
+        c = warp_sum_f(in ? w[2] : 0.0f);
+        d = warp_sum_f(in ? w[3] : 0.0f);
+        m = warp_max(in ? w[4] : 0.0f);
+        bad = __any_sync(0xffffffffu, in && w[5] != 0.0f);
+    }
 }
 
 // NeighborList::update branch + binning + Verlet build for one replica
@@ -155,7 +162,9 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
     unsigned long long ksum = 0;
     if (!skip)
         for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
-            int k = fast ? build_fast<false>(s, pos, i) : build_general<false>(s, pos, i);
+            int k = fast ? build_fast<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
+                         : build_general<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+            s.nbrCount[i] = k;
             kmax = max(kmax, k);
             ksum += (unsigned long long)k;
         }
@@ -183,12 +192,9 @@ __device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, i
     bool bad = false;
     for (int i = threadIdx.x; i < s.N; i += blockDim.x)
         particle_step<MT, SG, WX, WY, SIG1, false>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
-    const int anybad = __syncthreads_or(bad);
-    const float te = block_sum(etri, fscr);
-    const float tu = block_sum(ue, fscr);
-    const float tw = block_sum(we, fscr);
-    const float tk = block_sum(ke, fscr);
-    const float tm = block_max(vvm, fscr);
+    int anybad = bad;
+    block_reduce_step(etri, ue, we, ke, vvm, anybad, fscr);
+    const float te = etri, tu = ue, tw = we, tk = ke, tm = vvm;
     if (threadIdx.x == 0) {
         DevScalars *sc = s.sc;
         if (anybad) sc->nonfinite |= 1;
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(1024) k_batch(const DevSys *__restrict__ reps,
                                                 const int *__restrict__ ctaStart, const int *__restrict__ parity0,
                                                 int steps) {
     __shared__ DevSys S;
-    __shared__ float fscr[32];
+    __shared__ float fscr[6 * 32];
     __shared__ int iscr[33];
     extern __shared__ PairEntry tab[];
     for (int q = ctaStart[blockIdx.x]; q < ctaStart[blockIdx.x + 1]; q++) {

@@ -60,8 +60,13 @@ __global__ void __launch_bounds__(kBlock) k_tri_forces(DevSys s, int parity) {
     }
 }
 
+// Resident blocks per SM the register allocation must allow: 16 (64 warps,
+// 32 registers) with several types, 12 (48 warps, 40 registers) for the
+// pipelined one-type loop; both measured faster than the unconstrained
+// allocation (44-54 registers) on the 1.5M-atom mixed system and a 1M-atom
+// LJ fluid, the small spills notwithstanding.
 template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
-__global__ void __launch_bounds__(kStepBlock) k_step(DevSys s, int mode, int parity, cudaGraphConditionalHandle h,
+__global__ void __launch_bounds__(kStepBlock, MT ? 16 : 12) k_step(DevSys s, int mode, int parity, cudaGraphConditionalHandle h,
                                                      int use_h) {
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;

@@ -168,13 +168,19 @@ __global__ void __launch_bounds__(kBlock) k_cell_place(DevSys s, int parity, int
     if (i < s.N) place_one<true>(s, pos, i, &s.sc->overflow);
 }
 
-__global__ void __launch_bounds__(kBlock) k_build_nn(DevSys s, int parity, int check) {
+// One thread per particle, writing its list straight to HBM (staging the
+// lists in shared memory for coalesced stores measured slower).
+__global__ void __launch_bounds__(kNnBlock) k_build_nn(DevSys s, int parity, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool fast = fast_walk_ok(s);
     int k = 0;
-    if (i < s.N) k = fast ? build_fast<true>(s, pos, i) : build_general<true>(s, pos, i);
+    if (i < s.N) {
+        k = fast ? build_fast<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
+                 : build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+        s.nbrCount[i] = k;
+    }
     // build statistics and overflow
     int kmax = warp_max_int(k);
     int ksum = warp_sum_int(k);
@@ -202,7 +208,8 @@ cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
     if ((e = L.kernel(k_scan_apply, dim3(nsb), dim3(kScanBlock), 0, s, nsb, check))) return e;
     if ((e = L.kernel(k_scatter, dim3(pb), dim3(kBlock), 0, s, check))) return e;
     if ((e = L.kernel(k_cell_place, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
-    if ((e = L.kernel(k_build_nn, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
+    const int nb = (s.N + kNnBlock - 1) / kNnBlock;
+    if ((e = L.kernel(k_build_nn, dim3(nb), dim3(kNnBlock), 0, s, parity, check))) return e;
     return cudaSuccess;
 }
 

@@ -1,0 +1,217 @@
+// k_props.cu -- the observables of Properties::evaluate
+// (femmd2D/src/properties.cpp:15-36) at the current state, with the cluster
+// quantities of FeaElements::unfoldPos (feaElements.cpp:86-150) and the
+// cluster virial of calcPairForcesNN (interactions.cpp:347-389).  Per-cluster,
+// per-triangle and per-particle terms are formed in FP64 and written to
+// arrays that the host sums in a fixed order.
+#include <cuda_runtime.h>
+#include "femmd_internal.h"
+#include "launch.h"
+#include "device_common.cuh"
+#include "step_body.cuh"
+
+namespace femmd {
+
+namespace {
+
+__device__ __forceinline__ double block_sum_d(double v, double *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) scr[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) t = warp_sum(lane < nw ? scr[lane] : 0.0);
+    __syncthreads();
+    if (threadIdx.x == 0) scr[0] = t;
+    __syncthreads();
+    return scr[0];
+}
+
+__device__ __forceinline__ float block_min_f(float v, float *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) scr[warp] = v;
+    __syncthreads();
+    float t = 3.0e38f;
+    if (threadIdx.x < 32) {
+        t = lane < nw ? scr[lane] : 3.0e38f;
+        for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) scr[0] = t;
+    __syncthreads();
+    return scr[0];
+}
+
+}  // namespace
+
+// One block per cluster (elastomer): unfold across the periodic boundary the
+// reference's way (a cluster wider than half the box has its vertices beyond
+// L/2 moved down by L, and all moved up by L again when their mean is
+// negative), then the mass-weighted centre of mass and velocity and the
+// cluster kinetic term M |v_cm|^2.
+__global__ void k_props_cluster(DevSys s, const float2 *pos, const int2 *clRange, const float *clMass, double2 *unf,
+                                double2 *cmPos, double2 *cmVel, double *clKin) {
+    __shared__ double dscr[32];
+    __shared__ float fscr[32];
+    const int c = blockIdx.x;
+    const int off = clRange[c].x, n = clRange[c].y;
+    float xmin = 3.0e38f, ymin = 3.0e38f, nxmax = 3.0e38f, nymax = 3.0e38f;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        float2 p = pos[off + k];
+        xmin = fminf(xmin, p.x);
+        ymin = fminf(ymin, p.y);
+        nxmax = fminf(nxmax, -p.x);
+        nymax = fminf(nymax, -p.y);
+    }
+    xmin = block_min_f(xmin, fscr);
+    ymin = block_min_f(ymin, fscr);
+    const float xmax = -block_min_f(nxmax, fscr), ymax = -block_min_f(nymax, fscr);
+    const bool ux = xmax - xmin > s.Lx / 2.0f;  // whatever the periodicity, as the reference
+    const bool uy = ymax - ymin > s.Ly / 2.0f;
+    double sx = 0.0, sy = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        float2 p = pos[off + k];
+        double x = p.x, y = p.y;
+        if (ux && p.x > s.Lx / 2.0f) x -= s.Lx;
+        if (uy && p.y > s.Ly / 2.0f) y -= s.Ly;
+        sx += x;
+        sy += y;
+    }
+    sx = block_sum_d(sx, dscr);
+    sy = block_sum_d(sy, dscr);
+    const bool upx = ux && sx / n < 0.0, upy = uy && sy / n < 0.0;
+    double mx = 0.0, my = 0.0, mvx = 0.0, mvy = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int i = off + k;
+        float2 p = pos[i], v = s.vel[i];
+        double x = p.x, y = p.y;
+        if (ux && p.x > s.Lx / 2.0f) x -= s.Lx;
+        if (uy && p.y > s.Ly / 2.0f) y -= s.Ly;
+        if (upx) x += s.Lx;
+        if (upy) y += s.Ly;
+        unf[i] = make_double2(x, y);
+        const double m = s.mass[i];
+        mx += m * x;
+        my += m * y;
+        mvx += m * v.x;
+        mvy += m * v.y;
+    }
+    mx = block_sum_d(mx, dscr);
+    my = block_sum_d(my, dscr);
+    mvx = block_sum_d(mvx, dscr);
+    mvy = block_sum_d(mvy, dscr);
+    if (threadIdx.x == 0) {
+        const double M = clMass[c];
+        cmPos[c] = make_double2(mx / M, my / M);
+        const double vx = mvx / M, vy = mvy / M;
+        cmVel[c] = make_double2(vx, vy);
+        clKin[c] = M * (vx * vx + vy * vy);
+    }
+}
+
+// feaVirial terms: per triangle sum over its vertices of f . unfolded position
+// (interactions.cpp:681), with the nodal forces of the last force evaluation.
+__global__ void __launch_bounds__(kBlock) k_props_tri(DevSys s, const double2 *unf, double *feaVir) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= s.ntri) return;
+    const int4 q = __ldg(s.triIdx + t);
+    const int v[3] = {q.x, q.y, q.z};
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float2 f = s.triF[3 * t + k];
+        const double2 u = unf[v[k]];
+        acc += (double)f.x * u.x + (double)f.y * u.y;
+    }
+    feaVir[t] = acc;
+}
+
+// Per particle: m v^2 and the cluster virial 1/2 f_ij . (R_ci - R_cj)
+// (nearest image) over its Verlet list, for pairs of two cluster particles.
+template <bool WX, bool WY>
+__global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const float2 *pos, const int *clusterOf,
+                                                              const double2 *cmPos, double *kin, double *clVir) {
+    extern __shared__ PairEntry tab[];
+    const int nt2 = s.numTypes > 1 ? s.numTypes * s.numTypes : 1;
+    for (int k = threadIdx.x; k < nt2; k += blockDim.x) tab[k] = s.pair[k];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.N) return;
+    const float2 vi = s.vel[i];
+    kin[i] = (double)s.mass[i] * ((double)vi.x * vi.x + (double)vi.y * vi.y);
+    double cv = 0.0;
+    const int ci = clusterOf ? clusterOf[i] : -1;
+    if (ci >= 0) {
+        const float2 pi = pos[i];
+        const int cnt = min(s.nbrCount[i], s.nbrCap);
+        const int ti = s.numTypes > 1 ? s.typeId[i] : 0;
+        const float si = s.sigmaByType ? 0.0f : s.sigma[i];
+        const double2 Ri = cmPos[ci];
+        for (int k = 0; k < cnt; k++) {
+            const int tag = s.nbr[(size_t)k * s.Ncap + i];
+            const int j = tag & kIdMask;
+            const int cj = clusterOf[j];
+            if (cj < 0) continue;
+            const float2 pj = pos[j];
+            float dxr, dyr;
+            bool wrapped = false;
+            float dx = img<WX>(pi.x, pj.x, s.Lx, s.imageExact, dxr, wrapped);
+            float dy = img<WY>(pi.y, pj.y, s.Ly, s.imageExact, dyr, wrapped);
+            float dr2r = dxr * dxr + dyr * dyr;
+            const PairEntry &pe = tab[s.numTypes > 1 ? ti * s.numTypes + ((unsigned)tag >> kIdBits) : 0];
+            float rcut2, sig2, c;
+            if (!s.sigmaByType) {
+                float sij = (si + s.sigma[j]) / 2.0f;
+                rcut2 = pe.rc * pe.rc * sij * sij;
+                sig2 = sij * sij;
+                c = pe.eps48 / sig2;
+            } else {
+                rcut2 = pe.rcut2;
+                sig2 = pe.sig2;
+                c = pe.c;
+            }
+            if (!(dr2r < rcut2)) continue;
+            float dr2 = wrapped ? dx * dx + dy * dy : dr2r;
+            float s2 = sig2 / dr2, s6 = s2 * s2 * s2;
+            float fc = c * s6 * (s6 - 0.5f) * s2;
+            const double2 Rj = cmPos[cj];
+            double rx = Ri.x - Rj.x, ry = Ri.y - Rj.y;
+            if (s.wrapx) {
+                if (rx >= 0.5 * s.Lx) rx -= s.Lx;
+                else if (rx < -0.5 * s.Lx) rx += s.Lx;
+            }
+            if (s.wrapy) {
+                if (ry >= 0.5 * s.Ly) ry -= s.Ly;
+                else if (ry < -0.5 * s.Ly) ry += s.Ly;
+            }
+            cv += 0.5 * ((double)(fc * dx) * rx + (double)(fc * dy) * ry);
+        }
+    }
+    clVir[i] = cv;
+}
+
+cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
+                          const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
+                          double *clKin, double *feaVir, double *kin, double *clVir) {
+    cudaError_t e;
+    if (ncl > 0) {
+        if ((e = L.kernel(k_props_cluster, dim3(ncl), dim3(128), 0, s, pos, clRange, clMass, unf, cmPos, cmVel, clKin)))
+            return e;
+        if (s.ntri > 0 && s.feaForces) {
+            if ((e = L.kernel(k_props_tri, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, (const double2 *)unf, feaVir)))
+                return e;
+        }
+    }
+    dim3 g(step_blocks(s.N)), b(kStepBlock);
+    size_t smt = sizeof(PairEntry) * (size_t)(s.numTypes > 1 ? s.numTypes * s.numTypes : 1);
+    const int *co = ncl > 0 ? clusterOf : nullptr;
+    if (s.wrapx && s.wrapy)
+        return L.kernel(k_props_particle<true, true>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
+    if (s.wrapx) return L.kernel(k_props_particle<true, false>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
+    return L.kernel(k_props_particle<false, false>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
+}
+
+}  // namespace femmd

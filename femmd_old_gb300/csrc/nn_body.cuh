@@ -70,21 +70,20 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
     }
 }
 
-// Verlet list of particle i in the reference's order; returns its length
-// (entries beyond the capacity are counted, not written).  RO: the cell
-// arrays are read through the read-only path (written by an earlier kernel);
-// the batched kernel rewrites them in the same launch (coherent loads).
+// Verlet list of particle i in the reference's order, written to out[k *
+// stride]; returns its length (entries beyond the capacity are counted, not
+// written).  RO: the cell arrays are read through the read-only path
+// (written by an earlier kernel); the batched kernel rewrites them in the
+// same launch (coherent loads).
 template <bool RO>
-__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i) {
+__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
     const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
-    const size_t stride = (size_t)s.Ncap;
     const float R2 = s.nnRadiusSq;
     const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
     const int c = s.cellOf[i];
     const int ix = c / ncy, iy = c - ix * ncy;
     const float2 p = pos[i];
     const int gi = s.excl[i];
-    int *out = s.nbr + i;
     int k = 0;
     const int *cs = s.cellStart;
 #pragma unroll 1
@@ -121,7 +120,6 @@ __device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, in
             walk_range<RO>(s, qb, qe, sx, Ly, p, i, gi, R2, cap, stride, out, k);
         }
     }
-    s.nbrCount[i] = k;
     return k;
 }
 
@@ -129,16 +127,15 @@ __device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, in
 // more than once, as the reference does), any position, the minimum image
 // decided per pair.
 template <bool RO>
-__device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos, int i) {
+__device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
     int k = 0;
-    const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap, Ncap = s.Ncap;
+    const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
     const bool wx = s.wrapx, wy = s.wrapy;
     const float Lx = s.Lx, Ly = s.Ly, R2 = s.nnRadiusSq;
     const int c = s.cellOf[i];
     const int ix = c / ncy, iy = c - ix * ncy;
     const float2 p = pos[i];
     const int gi = s.excl[i];
-    int *out = s.nbr + i;
     for (int dx = -1; dx <= 1; dx++) {
         int nx = ix + dx;
         if (nx < 0) nx = ncx - 1; else if (nx == ncx) nx = 0;
@@ -159,14 +156,13 @@ __device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos,
                     image_axis(p.y, e.y, Ly, wy, false, dyr, dyo);
                     const float dr2 = dxr * dxr + dyr * dyr;
                     if (dr2 <= R2) {
-                        if (k < cap) out[(size_t)k * Ncap] = tag;
+                        if (k < cap) out[(size_t)k * stride] = tag;
                         k++;
                     }
                 }
             }
         }
     }
-    s.nbrCount[i] = k;
     return k;
 }
 

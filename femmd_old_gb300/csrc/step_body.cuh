@@ -190,14 +190,36 @@ __device__ __forceinline__ float img(float a, float b, float L, bool ex, float &
 // One Lennard-Jones pair (pairForce/ljforce, interactionsCuda.cu:43-100) added
 // into the running force in list order.  Energy and virial are accumulated
 // doubled (u and fc*dr2 per ordered pair) and halved once per particle.
+// The minimum image is the reference's float one (d - L / d + L); in exact
+// image mode a pair inside the cutoff whose difference crossed the boundary
+// takes the once-rounded value instead (ref + TwoSum error), a branch that
+// only boundary pairs enter.
 template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
 __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, const PairEntry &pe0, int ti, float si,
                                         float2 pi, int tag, float2 pj, float &fx, float &fy, float &u2, float &w2) {
-    float dxr, dyr;
-    bool wrapped = false;
-    float dx = img<WX>(pi.x, pj.x, s.Lx, s.imageExact, dxr, wrapped);
-    float dy = img<WY>(pi.y, pj.y, s.Ly, s.imageExact, dyr, wrapped);
-    float dr2r = dxr * dxr + dyr * dyr;
+    float dx = pi.x - pj.x, dy = pi.y - pj.y;
+    bool wrx = false, wry = false;
+    if (WX) {
+        const float h = 0.5f * s.Lx;
+        if (dx >= h) {
+            dx = dx - s.Lx;
+            wrx = true;
+        } else if (dx < -h) {
+            dx = dx + s.Lx;
+            wrx = true;
+        }
+    }
+    if (WY) {
+        const float h = 0.5f * s.Ly;
+        if (dy >= h) {
+            dy = dy - s.Ly;
+            wry = true;
+        } else if (dy < -h) {
+            dy = dy + s.Ly;
+            wry = true;
+        }
+    }
+    float dr2 = dx * dx + dy * dy;
     const PairEntry &pe = MT ? tab[ti * s.numTypes + ((unsigned)tag >> kIdBits)] : pe0;
     float rcut2, sig2, c;
     if (SG) {
@@ -210,8 +232,13 @@ __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, c
         sig2 = pe.sig2;
         c = pe.c;
     }
-    if (dr2r < rcut2) {
-        float dr2 = wrapped ? dx * dx + dy * dy : dr2r;
+    if (dr2 < rcut2) {
+        if (__builtin_expect((wrx || wry) && s.imageExact, 0)) {
+            const float ex = pi.x - pj.x, ey = pi.y - pj.y;
+            if (wrx) dx = dx + two_sum_err(pi.x, -pj.x, ex);
+            if (wry) dy = dy + two_sum_err(pi.y, -pj.y, ey);
+            dr2 = dx * dx + dy * dy;
+        }
         // sigma^2/dr2; with sigma_ij = 1 the IEEE quotient 1/dr2 is the
         // correctly rounded reciprocal
         float dr2i = SIG1 ? __frcp_rn(dr2) : sig2 / dr2;

@@ -246,6 +246,16 @@ femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads,
 femmd_status femmd_batch_event_record(femmd_batch *b, int slot);
 femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, float *ms);
 
+/* -------------------------------------------------------- observables */
+/* Properties::evaluate (properties.cpp:15-36) at the current state, FP64
+ * sums on the device: out[0..9] = uKinetic, uPotential, uTotal, temperature,
+ * virial, feaVirial, pressure, clusterUKinetic, clusterVirial, molPressure.
+ * Clusters are unfolded across the periodic boundary as
+ * FeaElements::unfoldPos (feaElements.cpp:86-150) does; the cluster virial
+ * sums pairs of two cluster particles (the reference indexes clusters[-1] for
+ * free particles). */
+femmd_status femmd_get_properties(femmd_ctx *ctx, double *out);
+
 /* ------------------------------------------------------------ adjoint */
 /* Gradients of an observable of the final state through the whole run, by the
  * discrete adjoint of the leapfrog step (no counterpart in the reference).

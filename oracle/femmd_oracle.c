@@ -1613,3 +1613,98 @@ void orc_d_backward(const orc *s, int n0, double cWall, double cFea, const doubl
     *glogsig = gs;
     free(xb); free(vb); free(gMu); free(gLam);
 }
+
+/* ------------------------------------------------------------ observables
+ * Properties::evaluate (src/properties.cpp:15-36) in double on the current
+ * float state: clusters unfolded as FeaElements::unfoldPos
+ * (src/feaElements.cpp:86-150), feaVirial as src/interactions.cpp:681 with
+ * FP64 nodal forces, cluster virial of calcPairForcesNN
+ * (src/interactions.cpp:347-389) over pairs of two cluster particles, U and W
+ * from orc_forces_f64.  out[0..9] = uKinetic, uPotential, uTotal,
+ * temperature, virial, feaVirial, pressure, clusterUKinetic, clusterVirial,
+ * molPressure. */
+void orc_properties(const orc *s, double *out) {
+    int N = s->N, ncl = s->ncl;
+    int wx = (s->pbc == XYPBC || s->pbc == XPBC), wy = (s->pbc == XYPBC);
+    double *fx = (double *)calloc((size_t)N + 1, sizeof(double)), *fy = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *cond = (double *)calloc((size_t)N + 1, sizeof(double)), *ui = (double *)calloc((size_t)N + 1, sizeof(double));
+    double tot[4];
+    orc_forces_f64(s, fx, fy, cond, ui, tot);
+    double *ux = (double *)calloc((size_t)N + 1, sizeof(double)), *uy = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *cmx = (double *)calloc((size_t)ncl + 1, sizeof(double)), *cmy = (double *)calloc((size_t)ncl + 1, sizeof(double));
+    double clusterKin = 0;
+    for (int c = 0; c < ncl; c++) {
+        int off = s->cl[c].offset, n = s->cl[c].nv;
+        float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+        for (int k = 0; k < n; k++) {
+            float x = s->px[off + k], y = s->py[off + k];
+            if (x < xmin) xmin = x; if (x > xmax) xmax = x;
+            if (y < ymin) ymin = y; if (y > ymax) ymax = y;
+        }
+        int fxu = xmax - xmin > s->Lx / 2.0f, fyu = ymax - ymin > s->Ly / 2.0f;
+        double sx = 0, sy = 0;
+        for (int k = 0; k < n; k++) {
+            int i = off + k;
+            ux[i] = s->px[i]; uy[i] = s->py[i];
+            if (fxu && s->px[i] > s->Lx / 2.0f) ux[i] -= s->Lx;
+            if (fyu && s->py[i] > s->Ly / 2.0f) uy[i] -= s->Ly;
+            sx += ux[i]; sy += uy[i];
+        }
+        int upx = fxu && sx / n < 0, upy = fyu && sy / n < 0;
+        double mx = 0, my = 0, mvx = 0, mvy = 0, M = s->cl[c].mass;
+        for (int k = 0; k < n; k++) {
+            int i = off + k;
+            if (upx) ux[i] += s->Lx;
+            if (upy) uy[i] += s->Ly;
+            mx += s->mass[i] * ux[i]; my += s->mass[i] * uy[i];
+            mvx += (double)s->mass[i] * s->vx[i]; mvy += (double)s->mass[i] * s->vy[i];
+        }
+        cmx[c] = mx / M; cmy[c] = my / M;
+        double vx = mvx / M, vy = mvy / M;
+        clusterKin += M * (vx * vx + vy * vy);
+    }
+    double feaVir = 0;
+    if (s->feaForces && ncl > 0) {
+        for (int t = 0; t < s->ntri; t++) {
+            double f[6], cf[3], cu;
+            if (s->fea_law) tri_green_d(s, t, f, cf, &cu); else tri_neo_hookean_d(s, t, f, cf, &cu);
+            for (int k = 0; k < 3; k++) {
+                int j = s->tri[3 * t + k];
+                feaVir += f[2 * k] * ux[j] + f[2 * k + 1] * uy[j];
+            }
+        }
+    }
+    double clVir = 0, kin = 0;
+    for (int i = 0; i < N; i++) kin += (double)s->mass[i] * ((double)s->vx[i] * s->vx[i] + (double)s->vy[i] * s->vy[i]);
+    if (ncl > 0 && s->nn_ready) {
+        for (int pi = 0; pi < N; pi++) {
+            int ci = s->cluster[pi];
+            if (ci < 0) continue;
+            for (int q = s->nbrStart[pi]; q < s->nbrStart[pi + 1]; q++) {
+                int pj = s->nbrList[q], cj = s->cluster[pj];
+                if (cj < 0) continue;
+                int ti = s->type[pi], tj = s->type[pj], nt = s->numTypes;
+                float sijf = (s->sigma[pi] + s->sigma[pj]) / 2.0f, rcij = s->rc[ti * nt + tj];
+                float dxr, dyr, dxo, dyo;
+                image_axis(s->px[pi], s->px[pj], s->Lx, wx, 0, &dxr, &dxo);
+                image_axis(s->py[pi], s->py[pj], s->Ly, wy, 0, &dyr, &dyo);
+                if (!(dxr * dxr + dyr * dyr < rcij * rcij * sijf * sijf)) continue;
+                double dx, dy;
+                image_axis_d(s->px[pi], s->px[pj], s->Lx, wx, &dx);
+                image_axis_d(s->py[pi], s->py[pj], s->Ly, wy, &dy);
+                double eij = s->eps[ti * nt + tj], sij = 0.5 * ((double)s->sigma[pi] + (double)s->sigma[pj]);
+                double dr2 = dx * dx + dy * dy, c48 = 48.0 * eij / (sij * sij), d2i = sij * sij / dr2;
+                double d6i = d2i * d2i * d2i, fc = c48 * d6i * (d6i - 0.5) * d2i;
+                double rx = cmx[ci] - cmx[cj], ry = cmy[ci] - cmy[cj];
+                if (wx) { if (rx >= 0.5 * s->Lx) rx -= s->Lx; else if (rx < -0.5 * s->Lx) rx += s->Lx; }
+                if (wy) { if (ry >= 0.5 * s->Ly) ry -= s->Ly; else if (ry < -0.5 * s->Ly) ry += s->Ly; }
+                clVir += 0.5 * (fc * dx * rx + fc * dy * ry);
+            }
+        }
+    }
+    double V = (double)s->Lx * (double)s->Ly;
+    out[0] = 0.5 * kin / N; out[1] = tot[0] / N; out[2] = out[0] + out[1]; out[3] = out[0];
+    out[4] = tot[1]; out[5] = feaVir; out[6] = 0.5 * kin / V + 0.5 * (tot[1] + feaVir) / V;
+    out[7] = ncl > 0 ? 0.5 * clusterKin / ncl : 0; out[8] = clVir; out[9] = 0.5 * clusterKin / V - 0.5 * clVir / V;
+    free(fx); free(fy); free(cond); free(ui); free(ux); free(uy); free(cmx); free(cmy);
+}
