@@ -50,19 +50,41 @@ __device__ __forceinline__ bool fast_walk_ok(const DevSys &s) {
 
 // One contiguous candidate range with a known image shift (sx, sy): the
 // reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
+// Candidates are taken four at a time: the four loads are issued before any
+// test, then the hits are appended in candidate order.
+__device__ __forceinline__ bool walk_hit(float4 e, float sx, float sy, float2 p, int i, int gi, float R2) {
+    const float dx = (p.x - e.x) - sx;
+    const float dy = (p.y - e.y) - sy;
+    const float dr2 = dx * dx + dy * dy;
+    const int tag = __float_as_int(e.z);
+    const int gj = __float_as_int(e.w);
+    return dr2 <= R2 && (tag & kIdMask) != i && (gi == -1 || gj == -1 || gi != gj);
+}
+
 template <bool RO>
 __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int i,
                                            int gi, float R2, int cap, size_t stride, int *&out, int &k) {
-    for (int q = qb; q < qe; q++) {
+    int q = qb;
+    for (; q + 4 <= qe; q += 4) {
+        float4 e[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) e[u] = RO ? __ldg(s.cellSorted + q + u) : s.cellSorted[q + u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
+                if (k < cap) {
+                    *out = __float_as_int(e[u].z);
+                    out += stride;
+                }
+                k++;
+            }
+        }
+    }
+    for (; q < qe; q++) {
         const float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
-        const float dx = (p.x - e.x) - sx;
-        const float dy = (p.y - e.y) - sy;
-        const float dr2 = dx * dx + dy * dy;
-        const int tag = __float_as_int(e.z);
-        const int gj = __float_as_int(e.w);
-        if (dr2 <= R2 && (tag & kIdMask) != i && (gi == -1 || gj == -1 || gi != gj)) {
+        if (walk_hit(e, sx, sy, p, i, gi, R2)) {
             if (k < cap) {
-                *out = tag;
+                *out = __float_as_int(e.z);
                 out += stride;
             }
             k++;
