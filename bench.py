@@ -467,6 +467,22 @@ def batched(args, dist):
         big_ms.append(big.event_elapsed_ms(0, 1))
     single_value = side * side * md / (statistics.median(big_ms) / 1e3)
     del big
+    # and one system of the ensemble's composition (2025 hex-ring disks, about
+    # 10 % of the atoms, in LJ solvent at rho 0.8) with the same atom count
+    mix = F.System(dev)
+    mixed_scene = S.large_mixed(n_side=45, n_solvent=natoms - 45 * 45 * 127)
+    mixed_scene.replay(mix)
+    mix.run(0)
+    mix.run(md)
+    mix_ms = []
+    for k in range(max(1, min(args.steps, 3))):
+        mix.event_record(0)
+        mix.run(md)
+        mix.event_record(1)
+        mix_ms.append(mix.event_elapsed_ms(0, 1))
+    mixed_value = mix.N * md / (statistics.median(mix_ms) / 1e3)
+    mixed_atoms = mix.N
+    del mix
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -487,8 +503,12 @@ def batched(args, dist):
             "plain_single_system": {"value": single_value, "unit": "atom-steps/s", "atoms": side * side,
                                     "how": f"one LJ fluid of {side}x{side} atoms (rho 0.8, rc 2.5), run({md}), "
                                            "CUDA events"},
+            "plain_single_system_same_mix": {"value": mixed_value, "unit": "atom-steps/s", "atoms": mixed_atoms,
+                                             "how": "one system of 2025 hex-ring disks in LJ solvent (rho 0.8), "
+                                                    f"run({md}), CUDA events"},
             "batched_over_plain": value / plain_value,
             "batched_over_single_system": value / single_value,
+            "batched_over_single_system_same_mix": value / mixed_value,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_run * args.steps, "clocks": clocks}
 
 
@@ -547,8 +567,9 @@ def main():
                 sub.steps, sub.warmup, sub.md_steps, sub.no_cpu_baseline = 3, 3, 100, True
                 b = batched(sub, _Solo())
                 line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "plain_same_atoms",
-                                                     "plain_single_system", "batched_over_plain",
-                                                     "batched_over_single_system", "e2e", "clocks")}
+                                                     "plain_single_system", "plain_single_system_same_mix",
+                                                     "batched_over_plain", "batched_over_single_system",
+                                                     "batched_over_single_system_same_mix", "e2e", "clocks")}
                 line["batched"]["config"] = {k: b["config"][k] for k in ("description", "replicas", "atoms",
                                                                          "md_steps_per_step", "launch")}
         if dist.rank == 0 and line is not None:

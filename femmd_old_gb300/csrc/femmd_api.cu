@@ -85,6 +85,8 @@ struct femmd_ctx {
     float rCutMax = 0;
     bool bondForces = false, feaForces = false;
     float kBond = 0, E = 0, nu = 0.3f, lambda = 0, mu = 0, C1 = 0, C2 = 0, C3 = 0, gravity = 0, kArea = 0;
+    float kWall = 10.0f;  // Interactions::init (interactions.cpp:22)
+    bool gravityForce = false;
     int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
     int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
     float skin = 0.4f;
@@ -115,7 +117,7 @@ struct femmd_ctx {
     int cur = 0;
     int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1, sigmaOne = 0;
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF, triLame;
-    DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta;
+    DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta, wallSig;
     bool ownMaterial = false, materialDirty = false;
     // observables: cluster ranges and masses, cluster of each particle, FP64 terms
     DBuf<int2> clRange;
@@ -256,7 +258,7 @@ static void release_device(femmd_ctx *c) {
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
     c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
-    c->triLame.release(); c->wallDelta.release();
+    c->triLame.release(); c->wallDelta.release(); c->wallSig.release();
     c->clRange.release(); c->clMass.release(); c->clusterOf.release(); c->unf.release(); c->cmPos.release();
     c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
     auto &a = c->adj;
@@ -282,6 +284,8 @@ static void clear_system(femmd_ctx *c) {
     c->kBond = c->E = 0;
     c->nu = 0.3f;
     c->gravity = c->kArea = 0;
+    c->gravityForce = false;
+    c->kWall = 10.0f;
     c->skin = 0.4f;
     c->elE.clear(); c->elNu.clear(); c->elOwn.clear();
     c->wallOn = false;
@@ -402,6 +406,11 @@ static DevSys make_sys(femmd_ctx *c) {
     s.wallV = c->wallV;
     s.wallDelta = c->wallOn ? c->wallDelta.p : nullptr;
     s.stepBase = c->steps;
+    s.refWalls = (!c->wallOn && c->pbc != FEMMD_XYPBC) ? (c->pbc == FEMMD_NOPBC ? 1 : 2) : 0;
+    s.kWall = c->kWall;
+    s.wallRc = wall_range();
+    s.gravity = c->gravityForce ? c->gravity : 0.0f;
+    s.wallSig = (c->wallOn || c->pbc != FEMMD_XYPBC) ? c->wallSig.p : nullptr;
     return s;
 }
 
@@ -462,12 +471,14 @@ static femmd_status upload_material(femmd_ctx *ctx) {
         CK(ctx->triLame.ensure(lm.size()));
         CK(cudaMemcpyAsync(ctx->triLame.p, lm.data(), lm.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
     }
-    if (ctx->wallOn && N > 0) {
+    if ((ctx->wallOn || ctx->pbc != FEMMD_XYPBC) && N > 0) {
         std::vector<float> dl(N);
         const float range = wall_range();
         for (int i = 0; i < N; i++) dl[i] = range * ctx->sigma[i];
         CK(ctx->wallDelta.ensure(N));
+        CK(ctx->wallSig.ensure(N));
         CK(cudaMemcpyAsync(ctx->wallDelta.p, dl.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->wallSig.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
     }
     CK(cudaStreamSynchronize(s));
     ctx->materialDirty = false;
@@ -870,6 +881,7 @@ femmd_status femmd_get_box(const femmd_ctx *ctx, double *Lx, double *Ly) {
 femmd_status femmd_set_pbc(femmd_ctx *ctx, int pbc) {
     NEED(ctx);
     ctx->pbc = pbc == 0 ? FEMMD_NOPBC : pbc == 1 ? FEMMD_XPBC : FEMMD_XYPBC;
+    ctx->materialDirty = true;  // the fixed walls need the per-particle sigma
     release_graphs(ctx);
     return FEMMD_OK;
 }
@@ -1005,10 +1017,18 @@ femmd_status femmd_get_wall_forces(femmd_ctx *ctx, double *top, double *bottom) 
     return FEMMD_OK;
 }
 
+// DukSystemSetGravity (interface.cpp:443-453): g > 0 sets and enables it,
+// otherwise gravity is disabled (the stored value is kept)
 femmd_status femmd_set_gravity(femmd_ctx *ctx, double g) {
     NEED(ctx);
-    ctx->gravity = g > 0 ? (float)g : 0.f;
-    if (g > 0) return fail(ctx, FEMMD_UNSUPPORTED, "gravity forces are outside this build's timestep path");
+    if (g > 0) {
+        ctx->gravity = (float)g;
+        ctx->gravityForce = true;
+    } else {
+        ctx->gravityForce = false;
+    }
+    ctx->forcesValid = false;
+    release_graphs(ctx);
     return FEMMD_OK;
 }
 
@@ -1790,6 +1810,8 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
 static float wall_y_host(const femmd_ctx *ctx, int n) { return ctx->wallY0 - ctx->wallV * ((float)n * ctx->dt); }
 
 static femmd_status adj_supported(femmd_ctx *ctx) {
+    if (!ctx->wallOn && ctx->pbc != FEMMD_XYPBC)
+        return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint implements the moving walls, not the reference's fixed walls");
     if (ctx->feaForces && !ctx->refVol.empty() && ctx->feaLaw != FEMMD_FEA_NEO_HOOKEAN)
         return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint implements the neo-Hookean triangle law");
     if (ctx->bondForces && !ctx->r0.empty() && ctx->bondKMode != FEMMD_BONDK_KBOND)
@@ -2036,7 +2058,7 @@ struct femmd_batch {
     std::vector<femmd_ctx *> reps;
     int threads = 512, ctasPerSm = 2;
     DBuf<DevSys> dreps;
-    DBuf<int> order, ctaStart, parity;
+    DBuf<int> order, queue, parity;
     cudaEvent_t ev[64] = {};
     GraphSet graph;
     int graphSteps = -1, graphThreads = 0, graphCtas = 0;
@@ -2096,7 +2118,8 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
     int sms = 0;
     BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
     const int ctas = std::max(1, std::min(R, b->ctasPerSm * sms));
-    // LPT: heaviest replica first onto the least loaded CTA
+    // heaviest replica first: the kernel hands them out in this order to
+    // whichever CTA is free (greedy list scheduling)
     std::vector<int> idx(R);
     std::vector<double> cost(R);
     for (int r = 0; r < R; r++) {
@@ -2104,32 +2127,27 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
         cost[r] = (double)sys[r].N + (double)sys[r].ntri;
     }
     std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return cost[x] > cost[y]; });
-    std::vector<double> load(ctas, 0.0);
-    std::vector<std::vector<int>> lists(ctas);
-    for (int r : idx) {
-        if (sys[r].N == 0) continue;  // an empty replica only counts steps
-        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[best] += cost[r];
-        lists[best].push_back(r);
-    }
-    std::vector<int> ord, st(ctas + 1, 0);
-    for (int c = 0; c < ctas; c++) {
-        for (int r : lists[c]) ord.push_back(r);
-        st[c + 1] = (int)ord.size();
-    }
+    // heaviest first; empty replicas only count steps
+    std::vector<int> ord;
+    for (int r : idx)
+        if (sys[r].N > 0) ord.push_back(r);
     BCK(b->dreps.ensure(R));
     BCK(b->order.ensure(std::max<size_t>(ord.size(), 1)));
-    BCK(b->ctaStart.ensure(ctas + 1));
+    if (!b->queue.p) {
+        BCK(b->queue.ensure(2));
+        BCK(cudaMemsetAsync(b->queue.p, 0, 2 * sizeof(int), b->stream));
+    }
     BCK(b->parity.ensure(R));
     BCK(cudaMemcpyAsync(b->dreps.p, sys.data(), R * sizeof(DevSys), cudaMemcpyHostToDevice, b->stream));
     if (!ord.empty())
         BCK(cudaMemcpyAsync(b->order.p, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMemcpyAsync(b->ctaStart.p, st.data(), (ctas + 1) * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->parity.p, par.data(), R * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     b->ctas = ctas;
     bl.reps = b->dreps.p;
     bl.order = b->order.p;
-    bl.ctaStart = b->ctaStart.p;
+    bl.queue = b->queue.p;
+    bl.nwork = (int)ord.size();
+    bl.minBlocks = b->ctasPerSm >= 2 && b->threads > 512 ? 2 : 1;
     bl.parity = b->parity.p;
     bl.steps = steps;
     bl.ctas = ctas;
@@ -2164,6 +2182,7 @@ static femmd_status batch_launch(femmd_batch *b, const BatchLaunch &bl) {
         b->graphVariant = variant;
         b->graphSmem = bl.smem;
     }
+    BCK(cudaMemsetAsync(bl.queue, 0, 2 * sizeof(int), b->stream));
     BCK(cudaGraphLaunch(b->graph.x, b->stream));
     return FEMMD_OK;
 }
@@ -2212,7 +2231,7 @@ void femmd_batch_destroy(femmd_batch *b) {
     b->graph.release();
     b->dreps.release();
     b->order.release();
-    b->ctaStart.release();
+    b->queue.release();
     b->parity.release();
     for (auto e : b->ev)
         if (e) cudaEventDestroy(e);
@@ -2358,6 +2377,7 @@ femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads_
         femmd_status st;
         if ((st = batch_prepare(b, trial_steps, bl, sys))) return st;
         if ((st = batch_checkpoint(b, false))) return st;
+        BCK(cudaMemsetAsync(bl.queue, 0, 2 * sizeof(int), b->stream));
         BCK(cudaEventRecord(e0, b->stream));
         cudaError_t le = cudaSuccess;
         {

@@ -114,6 +114,12 @@ struct DevSys {
     float wallK, wallY0, wallV;
     const float *wallDelta;
     int stepBase;  // the context's step count when the run started
+    // the reference's fixed walls, first in calcForces (interactions.cpp:83-93):
+    // 1 = LJ walls on every side (NOPBC), 2 = harmonic top/bottom (XPBC); and
+    // gravity f_y -= m g (interactions.cpp:111-126)
+    int refWalls;
+    float kWall, wallRc, gravity;
+    const float *wallSig;  // sigma_i, with walls of either kind
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -160,7 +166,9 @@ cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl
 // ---- batched replicas (k_batch.cu): one persistent launch over many systems
 struct BatchLaunch {
     const DevSys *reps;
-    const int *order, *ctaStart, *parity;
+    const int *order, *parity;
+    int *queue;  // {next work index, finished CTAs}, zero before a launch
+    int nwork, minBlocks;
     int steps, ctas, threads;
     size_t smem;
     bool multiType, sigmaByType, sigmaOne, wrapx, wrapy, exact;

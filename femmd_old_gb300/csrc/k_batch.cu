@@ -230,15 +230,26 @@ __device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, i
 
 }  // namespace
 
-template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
-__global__ void __launch_bounds__(1024) k_batch(const DevSys *__restrict__ reps, const int *__restrict__ order,
-                                                const int *__restrict__ ctaStart, const int *__restrict__ parity0,
-                                                int steps) {
+// Replicas are handed out from a queue: 'order' lists them heaviest first,
+// and each CTA takes the next one when it is free (greedy list scheduling,
+// which also balances CTAs that share an SM).  queue[0] is the next index,
+// queue[1] counts finished CTAs; the last CTA to finish resets both.
+// MINB: resident CTAs per SM the register allocation must allow.
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, int MINB>
+__global__ void __launch_bounds__(1024, MINB) k_batch(const DevSys *__restrict__ reps, const int *__restrict__ order,
+                                                      int nwork, int *queue, const int *__restrict__ parity0,
+                                                      int steps) {
     __shared__ DevSys S;
     __shared__ float fscr[6 * 32];
     __shared__ int iscr[33];
+    __shared__ int next;
     extern __shared__ PairEntry tab[];
-    for (int q = ctaStart[blockIdx.x]; q < ctaStart[blockIdx.x + 1]; q++) {
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= nwork) break;
         const int r = order[q];
         // copy the replica's descriptor into shared memory
         {
@@ -276,14 +287,24 @@ __global__ void __launch_bounds__(1024) k_batch(const DevSys *__restrict__ reps,
         }
         __syncthreads();
     }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+        }
+    }
 }
 
 namespace {
 
 template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
 cudaError_t launch_batch(Launch &L, const BatchLaunch &b) {
-    return L.kernel(k_batch<MT, SG, WX, WY, SIG1>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
-                    b.ctaStart, b.parity, b.steps);
+    if (b.minBlocks >= 2)
+        return L.kernel(k_batch<MT, SG, WX, WY, SIG1, 2>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
+                        b.nwork, b.queue, b.parity, b.steps);
+    return L.kernel(k_batch<MT, SG, WX, WY, SIG1, 1>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
+                    b.nwork, b.queue, b.parity, b.steps);
 }
 
 template <bool MT, bool SG, bool WX, bool WY>

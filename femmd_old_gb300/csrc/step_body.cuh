@@ -162,6 +162,55 @@ __device__ __forceinline__ float tri_force(const DevSys &s, const float2 *pos, i
 
 // ------------------------------------------------------------ particles
 
+// ljwallforce (femmd2D/src/interactionsCuda.cu:31-40), float operations as
+// written there (its "zi6" is zi^9)
+__device__ __forceinline__ float ljwallforce(float zi, float sigma, float &fz) {
+    zi = sigma / zi;
+    const float zi3 = zi * zi * zi;
+    const float zi6 = zi3 * zi3 * zi3;
+    const float u = 4.0f * zi6 * (zi6 - 1.0f) + 1.0f;
+    const float fc = 48.0f * zi6 * (zi6 - 0.5f) / zi;
+    fz = fabsf(fc);
+    return u;
+}
+
+// The reference's fixed walls for particle i, added before every other
+// force: calcWallForces (NOPBC, interactions.cpp:176-236) and
+// calcTopBottomWallForces (XPBC, :238-286).
+__device__ __forceinline__ void ref_walls(const DevSys &s, int i, float2 p, float &fx, float &fy, float &u) {
+    const float s0 = s.wallSig[i];
+    const float r = s0 * s.wallRc;
+    float f;
+    if (s.refWalls == 1) {
+        if ((s.Ly - p.y) < r) {
+            u += ljwallforce(s.Ly - p.y, s0, f);
+            fy += -f;
+        } else if (p.y < r) {
+            u += ljwallforce(p.y, s0, f);
+            fy += f;
+        }
+        if ((s.Lx - p.x) < r) {
+            u += ljwallforce(s.Lx - p.x, s0, f);
+            fx += -f;
+        } else if (p.x < r) {
+            u += ljwallforce(p.x, s0, f);
+            fx += f;
+        }
+    } else {
+        if ((s.Ly - p.y) < r) {
+            const float yi = s.Ly - p.y;
+            f = s.kWall * yi;
+            u += (float)(0.5 * (double)s.kWall * (double)yi * (double)yi);
+            fy += -f;
+        } else if (p.y < r) {
+            const float yi = p.y;
+            f = s.kWall * yi;
+            u += (float)(0.5 * (double)s.kWall * (double)yi * (double)yi);
+            fy += f;
+        }
+    }
+}
+
 // top wall position when the positions are x_n: y0 - v (n dt), in float
 __device__ __forceinline__ float wall_y(const DevSys &s, int n) { return s.wallY0 - s.wallV * ((float)n * s.dt); }
 
@@ -261,10 +310,12 @@ template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true, int PIP
 __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *tab, int i, int mode,
                                               const float2 *pin, float2 *pout, float &ue_out,
                                               float &we_out, float &ke, float &vvm, bool &bad) {
-    float ue = 0.0f, we = 0.0f, utri = 0.0f;
+    float ue = 0.0f, we = 0.0f, utri = 0.0f, uwall = 0.0f;
     const float2 pi = pin[i];
     const float Lx = s.Lx, Ly = s.Ly;
     float fx = 0.0f, fy = 0.0f;
+    if (s.refWalls) ref_walls(s, i, pi, fx, fy, uwall);
+    if (s.gravity > 0.0f) fy -= s.mass[i] * s.gravity;
     if (i < s.nBonded) {
         if (s.bondForces) {
             // calcBondForcesCPU: f on the bond's first particle, -f on the second
@@ -359,6 +410,7 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
     }
     ue *= 0.5f;
     we *= 0.5f;
+    ue += uwall;
     if (s.wallOn) {
         // harmonic walls after the pair forces: top wall at y_w(n), bottom at 0
         const float yw = wall_y(s, s.sc->stepNow);

@@ -92,6 +92,9 @@ typedef struct orc {
     int *clOwn, clMatCap;
     int wallOn;
     float wallK, wallY0, wallV;
+    /* Interactions::kWall, gravity (src/interactions.h:14-18) */
+    float kWall, gravity;
+    int gravityForce;
 } orc;
 
 /* ---------------------------------------------------------------- helpers */
@@ -255,6 +258,7 @@ void orc_init(orc *s, double Lx, double Ly) {
     s->skin = 0.4f; /* NeighborList() default, src/nn.h:63 */
     s->initialUpdate = 1;
     s->nu = 0.3f;
+    s->kWall = 10.0f; /* Interactions::init, src/interactions.cpp:22 */
     set_elastic_constants(s);
     double eps = 1.0, rc = pow(2.0, 1.0 / 6.0), us = 1.0;
     orc_set_pair_potential(s, &eps, &rc, &us, 1);
@@ -316,6 +320,79 @@ static void tri_lame(const orc *s, int t, float *mu, float *lambda) {
     if (!s->clOwn) return;
     int e = s->cluster[s->tri[3 * t]];
     if (e >= 0 && e < s->clMatCap && s->clOwn[e]) lame(s->clE[e], s->clNu[e], mu, lambda);
+}
+
+/* DukSystemSetGravity (src/interface.cpp:443-453) */
+void orc_set_gravity(orc *s, double g) {
+    if (g > 0) { s->gravity = (float)g; s->gravityForce = 1; } else s->gravityForce = 0;
+}
+
+/* ljwallforce (src/interactionsCuda.cu:31-40), float operations as written
+ * (zi6 is zi^9 there) */
+static float ljwallforce(float zi, float sigma, float *fz) {
+    zi = sigma / zi;
+    float zi3 = zi * zi * zi;
+    float zi6 = zi3 * zi3 * zi3;
+    float u = 4.0f * zi6 * (zi6 - 1.0f) + 1.0f;
+    float fcVal = 48.0f * zi6 * (zi6 - 0.5f) / zi;
+    *fz = fabsf(fcVal);
+    return u;
+}
+
+/* The reference's fixed walls, first in calcForces (src/interactions.cpp:
+ * 83-93): calcWallForces (NOPBC, :176-236: LJ wall on each side) and
+ * calcTopBottomWallForces (XPBC, :238-286: f = kWall * distance within the
+ * contact range).  The moving walls replace them when set. */
+static void ref_wall_forces(orc *s) {
+    if (s->wallOn || s->pbc == XYPBC) return;
+    float rc = (float)pow(2.0, 1.0 / 6.0);
+    for (int i = 0; i < s->N; i++) {
+        float s0 = s->sigma[i], f;
+        if (s->pbc == NOPBC) {
+            if ((s->Ly - s->py[i]) < s0 * rc) {
+                float yi = s->Ly - s->py[i];
+                float u = ljwallforce(yi, s0, &f);
+                s->fy[i] += -f;
+                s->potEnergy += u;
+            } else if (s->py[i] < s0 * rc) {
+                float yi = s->py[i];
+                float u = ljwallforce(yi, s0, &f);
+                s->fy[i] += f;
+                s->potEnergy += u;
+            }
+            if ((s->Lx - s->px[i]) < s0 * rc) {
+                float xi = s->Lx - s->px[i];
+                float u = ljwallforce(xi, s0, &f);
+                s->fx[i] += -f;
+                s->potEnergy += u;
+            } else if (s->px[i] < s0 * rc) {
+                float xi = s->px[i];
+                float u = ljwallforce(xi, s0, &f);
+                s->fx[i] += f;
+                s->potEnergy += u;
+            }
+        } else {
+            if ((s->Ly - s->py[i]) < s0 * rc) {
+                float yi = s->Ly - s->py[i];
+                f = s->kWall * yi;
+                float u = (float)(0.5 * s->kWall * yi * yi);
+                s->fy[i] += -f;
+                s->potEnergy += u;
+            } else if (s->py[i] < s0 * rc) {
+                float yi = s->py[i];
+                f = s->kWall * yi;
+                float u = (float)(0.5 * s->kWall * yi * yi);
+                s->fy[i] += f;
+                s->potEnergy += u;
+            }
+        }
+    }
+}
+
+/* calcGravityForces (src/interactions.cpp:111-126) */
+static void gravity_forces(orc *s) {
+    if (!s->gravityForce || !(s->gravity > 0)) return;
+    for (int i = 0; i < s->N; i++) s->fy[i] -= s->mass[i] * s->gravity;
 }
 
 /* wall forces of every particle, after the pair forces */
@@ -886,9 +963,13 @@ static void lj_forces(orc *s) {
     for (int pi = 0; pi < s->N; pi++) { s->potEnergy += s->ui[pi]; s->virial += s->wi[pi]; }
 }
 
-/* Interactions::calcForces (src/interactions.cpp:83-109), XYPBC/XPBC/NOPBC
- * without walls, gravity or area springs. */
+/* Interactions::calcForces (src/interactions.cpp:83-109): the fixed walls
+ * of NOPBC / XPBC boxes, gravity, bonds, FEA, pairs (area springs, which
+ * displace positions inside the force loop, are not restated), then the
+ * moving walls of this build. */
 void orc_calc_forces(orc *s) {
+    ref_wall_forces(s);
+    gravity_forces(s);
     if (s->bondForces) bond_forces(s);
     if (s->feaForces) fea_forces(s);
     lj_forces(s);
@@ -1079,6 +1160,42 @@ void orc_forces_f64(const orc *s, double *fx, double *fy, double *cond, double *
     int wx = (s->pbc == XYPBC || s->pbc == XPBC), wy = (s->pbc == XYPBC);
     double U = 0, W = 0, Uc = 0, Wc = 0;
     for (int i = 0; i < N; i++) fx[i] = fy[i] = cond[i] = ui[i] = 0;
+    if (!s->wallOn && s->pbc != XYPBC) {
+        /* the reference's fixed walls; contact decisions from the float path.
+         * Condition: the LJ wall force varies like d^-19 with the float
+         * distance d = L - y, so its scale carries 20 (L + |y|) / d. */
+        float rc = (float)pow(2.0, 1.0 / 6.0);
+        for (int i = 0; i < N; i++) {
+            float s0 = s->sigma[i];
+            double sd = s0;
+            for (int ax = 0; ax < (s->pbc == NOPBC ? 2 : 1); ax++) {
+                float p = ax == 0 ? s->py[i] : s->px[i], L = ax == 0 ? s->Ly : s->Lx;
+                double *fa = ax == 0 ? fy : fx;
+                double d = 0, sign = 0;
+                if ((L - p) < s0 * rc) { d = (double)L - p; sign = -1; }
+                else if (p < s0 * rc) { d = p; sign = 1; }
+                if (sign == 0) continue;
+                double f, u;
+                if (s->pbc == NOPBC) {
+                    double z = sd / d, z3 = z * z * z, z6 = z3 * z3 * z3;
+                    u = 4 * z6 * (z6 - 1) + 1;
+                    f = fabs(48 * z6 * (z6 - 0.5) / z);
+                    cond[i] += f * (1 + 20 * ((double)L + fabs((double)p)) / d);
+                    Uc += fabs(u) * (1 + 20 * ((double)L + fabs((double)p)) / d);
+                } else {
+                    f = (double)s->kWall * d;
+                    u = 0.5 * s->kWall * d * d;
+                    cond[i] += fabs((double)s->kWall) * ((double)L + fabs((double)p));
+                    Uc += u;
+                }
+                fa[i] += sign * f;
+                ui[i] += u;
+                U += u;
+            }
+        }
+    }
+    if (s->gravityForce && s->gravity > 0)
+        for (int i = 0; i < N; i++) { fy[i] -= (double)s->mass[i] * s->gravity; cond[i] += fabs((double)s->mass[i] * s->gravity); }
     if (s->bondForces) {
         for (int l = 0; l < s->nb; l++) {
             int i = s->bond[2 * l], j = s->bond[2 * l + 1];
@@ -1622,7 +1739,8 @@ void orc_d_backward(const orc *s, int n0, double cWall, double cFea, const doubl
  * (src/interactions.cpp:347-389) over pairs of two cluster particles, U and W
  * from orc_forces_f64.  out[0..9] = uKinetic, uPotential, uTotal,
  * temperature, virial, feaVirial, pressure, clusterUKinetic, clusterVirial,
- * molPressure. */
+ * molPressure; out[10..12] = condition scales (sums of term magnitudes) of
+ * virial, feaVirial and clusterVirial. */
 void orc_properties(const orc *s, double *out) {
     int N = s->N, ncl = s->ncl;
     int wx = (s->pbc == XYPBC || s->pbc == XPBC), wy = (s->pbc == XYPBC);
@@ -1663,7 +1781,7 @@ void orc_properties(const orc *s, double *out) {
         double vx = mvx / M, vy = mvy / M;
         clusterKin += M * (vx * vx + vy * vy);
     }
-    double feaVir = 0;
+    double feaVir = 0, feaScale = 0, clScale = 0;
     if (s->feaForces && ncl > 0) {
         for (int t = 0; t < s->ntri; t++) {
             double f[6], cf[3], cu;
@@ -1671,6 +1789,7 @@ void orc_properties(const orc *s, double *out) {
             for (int k = 0; k < 3; k++) {
                 int j = s->tri[3 * t + k];
                 feaVir += f[2 * k] * ux[j] + f[2 * k + 1] * uy[j];
+                feaScale += (cf[k] + fabs(f[2 * k]) + fabs(f[2 * k + 1])) * (fabs(ux[j]) + fabs(uy[j]));
             }
         }
     }
@@ -1699,6 +1818,7 @@ void orc_properties(const orc *s, double *out) {
                 if (wx) { if (rx >= 0.5 * s->Lx) rx -= s->Lx; else if (rx < -0.5 * s->Lx) rx += s->Lx; }
                 if (wy) { if (ry >= 0.5 * s->Ly) ry -= s->Ly; else if (ry < -0.5 * s->Ly) ry += s->Ly; }
                 clVir += 0.5 * (fc * dx * rx + fc * dy * ry);
+                clScale += 0.5 * fabs(c48) * d6i * (d6i + 0.5) * d2i * (fabs(dx) + fabs(dy)) * (fabs(rx) + fabs(ry));
             }
         }
     }
@@ -1706,5 +1826,6 @@ void orc_properties(const orc *s, double *out) {
     out[0] = 0.5 * kin / N; out[1] = tot[0] / N; out[2] = out[0] + out[1]; out[3] = out[0];
     out[4] = tot[1]; out[5] = feaVir; out[6] = 0.5 * kin / V + 0.5 * (tot[1] + feaVir) / V;
     out[7] = ncl > 0 ? 0.5 * clusterKin / ncl : 0; out[8] = clVir; out[9] = 0.5 * clusterKin / V - 0.5 * clVir / V;
+    out[10] = tot[3]; out[11] = feaScale; out[12] = clScale;
     free(fx); free(fy); free(cond); free(ui); free(ux); free(uy); free(cmx); free(cmy);
 }

@@ -86,7 +86,7 @@ def lib():
             "orc_set_elastomer_material": (C.c_int, [P, C.c_int, C.c_double, C.c_double]),
             "orc_set_moving_wall": (None, [P, C.c_double, C.c_double, C.c_double]),
             "orc_wall_forces": (None, [P, dp, dp]),
-            "orc_ncl": (C.c_int, [P]), "orc_d_init": (None, [P]), "orc_properties": (None, [P, dp]), "orc_d_set_material": (None, [C.c_int, C.c_double, C.c_double]),
+            "orc_set_gravity": (None, [P, C.c_double]), "orc_ncl": (C.c_int, [P]), "orc_d_init": (None, [P]), "orc_properties": (None, [P, dp]), "orc_d_set_material": (None, [C.c_int, C.c_double, C.c_double]),
             "orc_d_set_scales": (None, [C.c_double, C.c_double]), "orc_d_set_state": (None, [dp, dp]),
             "orc_d_get_state": (None, [dp, dp]), "orc_d_set_traj": (None, [dp, C.c_int]),
             "orc_d_forward": (C.c_double, [P, C.c_int, C.c_int, C.c_double, C.c_double]),
@@ -162,6 +162,9 @@ class Oracle:
     def set_skin(self, s):
         self.L.orc_set_skin(self.h, s)
 
+    def set_gravity(self, g):
+        self.L.orc_set_gravity(self.h, float(g))
+
     def set_elastomer_material(self, e, E, nu):
         if self.L.orc_set_elastomer_material(self.h, int(e), float(E), float(nu)):
             raise ValueError(f"no elastomer {e}")
@@ -172,10 +175,13 @@ class Oracle:
     PROPERTY_NAMES = ("uKinetic", "uPotential", "uTotal", "temperature", "virial", "feaVirial", "pressure",
                       "clusterUKinetic", "clusterVirial", "molPressure")
 
-    def properties(self):
-        out = np.zeros(10)
+    def properties(self, scales=False):
+        out = np.zeros(13)
         self.L.orc_properties(self.h, _ptr(out, C.c_double))
-        return dict(zip(self.PROPERTY_NAMES, out.tolist()))
+        d = dict(zip(self.PROPERTY_NAMES, out[:10].tolist()))
+        if scales:
+            d.update(virialScale=out[10], feaVirialScale=out[11], clusterVirialScale=out[12])
+        return d
 
     def n_elastomers(self):
         return self.L.orc_ncl(self.h)

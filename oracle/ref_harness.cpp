@@ -21,7 +21,8 @@ enum Op {
     OP_END = 0, OP_INIT = 1, OP_PBC = 2, OP_DT = 3, OP_NUMTYPES = 4, OP_PAIR = 5, OP_KBOND = 6,
     OP_YOUNG = 7, OP_NU = 8, OP_SKIN = 9, OP_ELASTOMER = 10, OP_PARTICLE = 11, OP_BOND = 12,
     OP_INITNN = 13, OP_CAPACITY = 14, OP_RUN = 15, OP_STEP = 16, OP_BUILDNN = 17, OP_FORCES = 18,
-    OP_ELASTOMER_BONDS = 19, OP_DUMP_STATE = 20, OP_DUMP_NN = 21, OP_DUMP_SETUP = 22, OP_SETVEL = 23
+    OP_ELASTOMER_BONDS = 19, OP_DUMP_STATE = 20, OP_DUMP_NN = 21, OP_DUMP_SETUP = 22, OP_SETVEL = 23,
+    OP_GRAVITY = 24
 };
 
 // Bond set of an elastomer: 0 keeps the reference's bonds on every triangle
@@ -183,6 +184,15 @@ int main(int argc, char **argv) {
             std::vector<float> v;
             rdv(v, 2 * (size_t)s.N);
             for (int i = 0; i < s.N; i++) { s.particles.vel[i].x = v[2 * i]; s.particles.vel[i].y = v[2 * i + 1]; }
+            break;
+        }
+        case OP_GRAVITY: {  // DukSystemSetGravity (interface.cpp:443-453)
+            real g = rd<double>();
+            if (g > 0) {
+                s.interactions.gravity = g;
+                s.interactions.gravityForce = true;
+            } else
+                s.interactions.gravityForce = false;
             break;
         }
         case OP_PARTICLE: {

@@ -89,6 +89,48 @@ def case_lj_nopbc():
     return _slab(0, 32)
 
 
+def case_lj_nopbc_walls():
+    """NOPBC box filled to the edges, velocities pointing outward: particles
+    enter the contact range of the reference's LJ walls on every side."""
+    n_side = 12
+    L = 14.0
+    rng = np.random.Generator(np.random.PCG64(33))
+    ij = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy"), -1).reshape(-1, 2)
+    pos = 0.9 + ij * ((L - 1.8) / (n_side - 1)) + rng.uniform(-0.05, 0.05, size=(n_side * n_side, 2))
+    vel = (pos - L / 2) * 0.4 + rng.normal(0, 0.2, size=pos.shape)
+    sc = S.Scene(meta=dict(workload="nopbc_walls"))
+    sc.add("init", L, L).add("PBC", 0).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [2.5], [S.lj_shift(2.5)])
+    sc.add("set_skin", 0.3)
+    n = pos.shape[0]
+    sc.add("add_particles", pos[:, 0], pos[:, 1], vel[:, 0], vel[:, 1], np.ones(n), np.ones(n),
+           np.zeros(n, np.int32))
+    sc.add("init_neighbor_list")
+    return probes(sc, runs=(60, 120))
+
+
+def case_susp_xpbc_gravity():
+    """XPBC suspension under gravity: disks settle onto the reference's
+    harmonic bottom wall (kWall = 10); one starts at the top wall."""
+    verts, tris = S.hex_disk_mesh(2.5, 3, jitter=0.02, seed=71)
+    nv = verts.shape[0]
+    L = 22.0
+    sc = S.Scene(meta=dict(workload="susp_xpbc_gravity"))
+    sc.add("init", L, L).add("PBC", 1).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [S.WCA_RC], [1.0]).add("set_skin", 0.3)
+    sc.add("set_kBond", 80.0).add("set_youngs_modulus", 40.0).add("set_poisson_ratio", 0.3)
+    sc.add("set_elastomer_bonds", 1).add("set_gravity", 2.0)
+    for c in [(5.0, 3.2), (12.0, 3.4), (18.5, 9.0), (8.0, 18.9)]:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 0, 0, 1.0, float(nv), True)
+    sc.add("init_neighbor_list")
+    # the reference's per-cell capacity heuristic (nn.cpp:214-220) is too
+    # small once the disks settle onto the wall; raise it as its C++ allows
+    sc.add("set_capacity", 64, 256)
+    rng = np.random.Generator(np.random.PCG64(72))
+    sc.add("set_velocities_array", rng.normal(0, 0.2, size=(4 * nv, 2)).astype(np.float32))
+    return probes(sc, runs=(150, 300))
+
+
 def case_tiny_box():
     """Box of two cells per axis: the 3x3 stencil visits cells twice and the
     reference's list holds duplicates (applyCellBC always wraps)."""

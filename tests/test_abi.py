@@ -44,8 +44,10 @@ def test_version_and_errors_without_gpu():
         s.create_bond(0, 1)  # no particles
     with pytest.raises(F.FemmdError):
         s.run(5)  # no init_neighbor_list
+    s.set_gravity(1.0)  # calcGravityForces is on the path
+    s.set_gravity(0.0)
     with pytest.raises(F.FemmdError) as e:
-        s.set_gravity(1.0)
+        s.set_kArea(1.0)
     assert "UNSUPPORTED" in str(e.value)
 
 

@@ -22,7 +22,7 @@ def test_oracle_matches_reference_bitwise(name):
 def test_golden_cases_cover_edge_cases():
     names = set(G.names())
     for required in ("lj_xy", "lj_multitype", "lj_xpbc", "lj_nopbc", "tiny_box", "susp_all", "susp_boundary",
-                     "susp_refdisk", "susp_crossing", "susp_mixed"):
+                     "susp_refdisk", "susp_crossing", "susp_mixed", "lj_nopbc_walls", "susp_xpbc_gravity"):
         assert required in names
 
 
