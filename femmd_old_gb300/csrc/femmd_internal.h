@@ -26,10 +26,7 @@ constexpr int kIdMask = (1 << kIdBits) - 1;
 constexpr int kMaxTypes = 32;
 constexpr int kBlock = 256;        // threads per block of the per-particle kernels
 constexpr int kStepBlock = 128;    // threads per block of the step kernel
-#ifndef FEMMD_NN_BLOCK
-#define FEMMD_NN_BLOCK 256
-#endif
-constexpr int kNnBlock = FEMMD_NN_BLOCK;  // threads per block of the list build
+constexpr int kNnBlock = 256;      // threads per block of the list build
 constexpr int kScanBlock = 1024;   // cells per block of the cell-start scan
 constexpr int kObsCols = 6;        // per-step observable row: U, W, sum m v^2, max v^2, dispHi, rebuilt
 constexpr int kTraceCols = 6;      // per-step trace row (ns): tri start/end, step start/end, rebuild start/end

@@ -169,17 +169,29 @@ __global__ void __launch_bounds__(kBlock) k_cell_place(DevSys s, int parity, int
 }
 
 // One thread per particle, writing its list straight to HBM (staging the
-// lists in shared memory for coalesced stores measured slower).
+// lists in shared memory for coalesced stores measured slower).  Threads
+// take the particles in cell order (slot t of cellSorted), so the lanes of a
+// warp sit in the same or adjacent cells of one column and walk nearly the
+// same candidate ranges; each particle's list is still its own column.
 __global__ void __launch_bounds__(kNnBlock) k_build_nn(DevSys s, int parity, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const float2 *pos = parity ? s.pos1 : s.pos0;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool fast = fast_walk_ok(s);
     int k = 0;
-    if (i < s.N) {
-        k = fast ? build_fast<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
-                 : build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
-        s.nbrCount[i] = k;
+    if (t < s.N) {
+        if (fast) {
+            const float4 me = __ldg(s.cellSorted + t);  // position, tag and group of the slot's particle
+            const int i = __float_as_int(me.z) & kIdMask;
+            k = build_fast_at<true>(s, i, s.cellOf[i], make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
+                                    (size_t)s.Ncap);
+            s.nbrCount[i] = k;
+        } else {
+            const int i = t;
+            k = fast ? build_fast<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
+                     : build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+            s.nbrCount[i] = k;
+        }
     }
     // build statistics and overflow
     int kmax = warp_max_int(k);

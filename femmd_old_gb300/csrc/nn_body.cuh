@@ -98,14 +98,12 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
 // (written by an earlier kernel); the batched kernel rewrites them in the
 // same launch (coherent loads).
 template <bool RO>
-__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
+__device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, float2 p, int gi, int *out,
+                                             size_t stride) {
     const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
     const float R2 = s.nnRadiusSq;
     const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
-    const int c = s.cellOf[i];
     const int ix = c / ncy, iy = c - ix * ncy;
-    const float2 p = pos[i];
-    const int gi = s.excl[i];
     int k = 0;
     const int *cs = s.cellStart;
 #pragma unroll 1
@@ -143,6 +141,11 @@ __device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, in
         }
     }
     return k;
+}
+
+template <bool RO>
+__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
+    return build_fast_at<RO>(s, i, s.cellOf[i], pos[i], s.excl[i], out, stride);
 }
 
 // The general walk: any grid (1 or 2 cells along an axis visit the same cell

@@ -248,7 +248,8 @@ __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, c
                                         float2 pi, int tag, float2 pj, float &fx, float &fy, float &u2, float &w2) {
     float dx = pi.x - pj.x, dy = pi.y - pj.y;
     bool wrx = false, wry = false;
-    if (WX) {
+    // |d| >= L/2 is rare (boundary pairs): one compare on the common path
+    if (WX && __builtin_expect(fabsf(dx) >= 0.5f * s.Lx, 0)) {
         const float h = 0.5f * s.Lx;
         if (dx >= h) {
             dx = dx - s.Lx;
@@ -258,7 +259,7 @@ __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, c
             wrx = true;
         }
     }
-    if (WY) {
+    if (WY && __builtin_expect(fabsf(dy) >= 0.5f * s.Ly, 0)) {
         const float h = 0.5f * s.Ly;
         if (dy >= h) {
             dy = dy - s.Ly;
