@@ -174,6 +174,15 @@ class System:
         self._call("femmd_get_wall_forces", C.byref(t), C.byref(b))
         return t.value, b.value
 
+    def set_trajectory(self, path, every, fmt=0):
+        """Frames every 'every' steps of run(): fmt 0 dump, 1 xyz, 2 vtk."""
+        self._call("femmd_set_trajectory", None if path is None else str(path).encode(), int(every), int(fmt))
+
+    def flush_trajectory(self):
+        n = C.c_longlong()
+        self._call("femmd_flush_trajectory", C.byref(n))
+        return n.value
+
     PROPERTY_NAMES = ("uKinetic", "uPotential", "uTotal", "temperature", "virial", "feaVirial", "pressure",
                       "clusterUKinetic", "clusterVirial", "molPressure")
 
@@ -235,8 +244,8 @@ class System:
         self._call("femmd_set_elastomer_bonds", int(m))
 
     def set_capacity(self, ppc, nbr):
-        """The reference sizes its fixed cell/list arrays here; this build's
-        cells are CSR and its lists grow on overflow, so nothing is needed."""
+        """The reference sizes its fixed cell/list arrays here; here cells are
+        CSR and lists grow on overflow, so nothing is needed."""
 
     def add_particles(self, x, y, vx, vy, m, sig, typ):
         cols = [np.ascontiguousarray(c, np.float64) for c in (x, y, vx, vy, m, sig)]

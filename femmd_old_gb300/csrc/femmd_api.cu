@@ -21,8 +21,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <climits>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "femmd.h"
@@ -73,6 +78,40 @@ constexpr int kGraphUnits = 32;  // [step -> IF rebuild] units per cached graph
 constexpr unsigned kPos = 1, kVel = 2, kAcc = 4, kForce = 8, kEnergy = 16, kAll = 31;
 
 }  // namespace
+
+// Trajectory frames (Integrator::doStep, integrator.cpp:20-26): positions and
+// velocities copied device-to-host into pinned slots during a run and
+// formatted by a writer thread.  Frames of a run are committed to the writer
+// once the run (or the part of it before a slot had to be reused) is known
+// to be free of list overflow, so a repeated run never writes a frame twice.
+struct TrajFrame {
+    int step, slot;
+};
+
+struct Trajectory {
+    bool on = false;
+    std::string path;
+    int every = 0, format = 0;
+    long long lastCommitted = LLONG_MIN;
+    int N = 0;
+    std::vector<float2 *> pos, vel;  // pinned slots
+    std::vector<char> busy;
+    std::vector<TrajFrame> pending;
+    // writer
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<TrajFrame> queue;
+    bool stop = false;
+    std::string error;
+    long long written = 0;
+    // metadata the writer formats with (copied when the topology is uploaded)
+    std::vector<int> type, tri;
+    std::vector<float> mass;
+    std::vector<int2> clusters;  // (offset, vertices)
+    std::vector<float> clusterMass;
+    float Lx = 0, Ly = 0;
+};
 
 struct femmd_ctx {
     int device = 0;
@@ -146,6 +185,7 @@ struct femmd_ctx {
     long long profForceLaunches = 0, profRebuilds = 0, profKernels = 0;
     long long totalBuilds = 0;
     cudaEvent_t userEvents[64] = {};
+    Trajectory traj;
     // adjoint: segment checkpoints of the last femmd_adjoint_forward and the
     // backward sweep's buffers
     struct {
@@ -270,7 +310,12 @@ static void release_device(femmd_ctx *c) {
     c->obsCap = 0;
 }
 
+static void traj_stop(Trajectory &T);
+static void traj_refresh_meta(femmd_ctx *ctx);
+
 static void clear_system(femmd_ctx *c) {
+    traj_stop(c->traj);  // MDSystem::init clears saveTrajectory (md3dsystem.cpp:65)
+    c->traj.on = false;
     c->inited = false;
     c->Lx = c->Ly = 0;
     c->dt = 0.005f;
@@ -687,7 +732,10 @@ static femmd_status prepare(femmd_ctx *ctx) {
     femmd_status st;
     if (!ctx->nnInit) return fail(ctx, FEMMD_NOT_READY, "init_neighbor_list() has not been called");
     if ((ctx->topoDirty || ctx->materialDirty) && (st = validate(ctx))) return st;
-    if (ctx->topoDirty && (st = upload_topology(ctx))) return st;
+    if (ctx->topoDirty) {
+        if ((st = upload_topology(ctx))) return st;
+        traj_refresh_meta(ctx);
+    }
     if (ctx->stateDirty && (st = upload_state(ctx))) return st;
     if (ctx->materialDirty && (st = upload_material(ctx))) return st;
     if (ctx->nbrCap == 0 && (st = size_list(ctx, 0))) return st;
@@ -762,7 +810,251 @@ static femmd_status launch_units(femmd_ctx *ctx, int units, bool use_graphs) {
     return FEMMD_OK;
 }
 
-static femmd_status run_once(femmd_ctx *ctx, int n) {
+// ------------------------------------------------------------ trajectory
+
+// FeaElements::unfoldPos (feaElements.cpp:86-150) on the host, float
+// arithmetic as the reference, for one cluster of a frame.
+static void unfold_cluster(const float2 *p, float *ux, float *uy, int off, int n, float Lx, float Ly) {
+    float xmin = 100000, xmax = -100000, ymin = 100000, ymax = -100000;
+    for (int k = 0; k < n; k++) {
+        ux[k] = p[off + k].x;
+        uy[k] = p[off + k].y;
+        xmin = std::min(xmin, ux[k]);
+        xmax = std::max(xmax, ux[k]);
+        ymin = std::min(ymin, uy[k]);
+        ymax = std::max(ymax, uy[k]);
+    }
+    if (xmax - xmin > Lx / 2) {
+        float xc = 0;
+        for (int k = 0; k < n; k++) {
+            if (ux[k] > Lx / 2) ux[k] -= Lx;
+            xc += ux[k];
+        }
+        if (xc / n < 0)
+            for (int k = 0; k < n; k++) ux[k] += Lx;
+    }
+    if (ymax - ymin > Ly / 2) {
+        float yc = 0;
+        for (int k = 0; k < n; k++) {
+            if (uy[k] > Ly / 2) uy[k] -= Ly;
+            yc += uy[k];
+        }
+        if (yc / n < 0)
+            for (int k = 0; k < n; k++) uy[k] += Ly;
+    }
+}
+
+// One frame in the reference's layouts: 0 = saveClusterXYZ's dump
+// (md3dsystem.cpp:248-273, every particle), 1 = saveXYZ (:232-246),
+// 2 = saveVtk (:275-328, one file per frame, clusters unfolded).
+static bool write_frame(Trajectory &T, int step, const float2 *p, const float2 *v, std::string &err) {
+    const int N = T.N;
+    if (T.format == 2) {
+        if (T.clusters.empty()) return true;  // saveVtk writes nothing without elastomers
+        char name[1024];
+        snprintf(name, sizeof name, "%s%.9d.vtk", T.path.c_str(), step);
+        FILE *f = fopen(name, "w");
+        if (!f) {
+            err = std::string("cannot open ") + name;
+            return false;
+        }
+        std::vector<float> ux(N), uy(N);
+        for (int i = 0; i < N; i++) {
+            ux[i] = p[i].x;
+            uy[i] = p[i].y;
+        }
+        for (const int2 &c : T.clusters) unfold_cluster(p, ux.data() + c.x, uy.data() + c.x, c.x, c.y, T.Lx, T.Ly);
+        fprintf(f, "# vtk DataFile Version 3.1\nReally cool data\nASCII\nDATASET UNSTRUCTURED_GRID\n\n");
+        fprintf(f, "POINTS %d FLOAT\n", N);
+        for (int i = 0; i < N; i++) fprintf(f, "%f %f %f\n", ux[i], uy[i], 0.0f);
+        fprintf(f, "\n");
+        const int nt = (int)T.tri.size() / 3;
+        if (nt > 0) {
+            fprintf(f, "CELLS %d %d\n", nt, 4 * nt);
+            for (int t = 0; t < nt; t++) fprintf(f, "%d %d %d %d\n", 3, T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2]);
+            fprintf(f, "\nCELL_TYPES %d\n", nt);
+            for (int t = 0; t < nt; t++) fprintf(f, "%d ", 5);
+            fprintf(f, "\n\n");
+        }
+        fprintf(f, "POINT_DATA %d\nSCALARS VelocitySquare FLOAT\nLOOKUP_TABLE default\n", N);
+        for (int i = 0; i < N; i++) fprintf(f, "%f\n", v[i].x * v[i].x + v[i].y * v[i].y);
+        fprintf(f, "\n\nVECTORS Velocity FLOAT\n");
+        for (int i = 0; i < N; i++) fprintf(f, "%f %f %f\n", v[i].x, v[i].y, 0.0f);
+        fclose(f);
+        return true;
+    }
+    FILE *f = fopen(T.path.c_str(), "a");
+    if (!f) {
+        err = "cannot open " + T.path;
+        return false;
+    }
+    if (T.format == 1) {
+        fprintf(f, "%d\n\n", N);
+        for (int i = 0; i < N; i++) fprintf(f, "A\t%f\t%f\t%f\n", p[i].x, p[i].y, 0.0f);
+    } else {
+        fprintf(f, "ITEM: TIMESTEP\n%d\nITEM: NUMBER OF ATOMS\n%d\n", step, N);
+        fprintf(f, "ITEM: BOX BOUNDS pp pp pp\n%f %f\n%f %f\n%f %f\n", 0.0, (double)T.Lx, 0.0, (double)T.Ly, 0.0, 0.0);
+        fprintf(f, "ITEM: ATOMS id type x y z vx vy vz\n");
+        for (int i = 0; i < N; i++)
+            fprintf(f, "%d %d %f %f %f %f %f %f\n", i, T.type[i], p[i].x, p[i].y, 0.0f, v[i].x, v[i].y, 0.0f);
+    }
+    fclose(f);
+    return true;
+}
+
+static void traj_writer(Trajectory *T) {
+    for (;;) {
+        TrajFrame fr;
+        {
+            std::unique_lock<std::mutex> lk(T->mu);
+            T->cv.wait(lk, [&] { return T->stop || !T->queue.empty(); });
+            if (T->queue.empty()) return;  // stop requested and drained
+            fr = T->queue.front();
+        }
+        std::string err;
+        const bool ok = write_frame(*T, fr.step, T->pos[fr.slot], T->vel[fr.slot], err);
+        {
+            std::lock_guard<std::mutex> lk(T->mu);
+            T->queue.pop_front();
+            T->busy[fr.slot] = 0;
+            if (!ok && T->error.empty()) T->error = err;
+            T->written++;
+        }
+        T->cv.notify_all();
+    }
+}
+
+// Wait until every committed frame is written.
+static void traj_drain(Trajectory &T) {
+    std::unique_lock<std::mutex> lk(T.mu);
+    T.cv.wait(lk, [&] { return T.queue.empty(); });
+}
+
+static void traj_stop(Trajectory &T) {
+    if (T.th.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(T.mu);
+            T.stop = true;
+        }
+        T.cv.notify_all();
+        T.th.join();
+    }
+    for (auto p : T.pos) cudaFreeHost(p);
+    for (auto p : T.vel) cudaFreeHost(p);
+    T.pos.clear();
+    T.vel.clear();
+    T.busy.clear();
+    T.pending.clear();
+    T.queue.clear();
+    T.stop = false;
+}
+
+static void traj_commit(Trajectory &T) {
+    if (T.pending.empty()) return;
+    {
+        std::lock_guard<std::mutex> lk(T.mu);
+        for (const TrajFrame &f : T.pending) {
+            T.queue.push_back(f);
+            T.lastCommitted = std::max<long long>(T.lastCommitted, f.step);
+        }
+    }
+    T.pending.clear();
+    T.cv.notify_all();
+}
+
+static void traj_discard(Trajectory &T) {
+    std::lock_guard<std::mutex> lk(T.mu);
+    for (const TrajFrame &f : T.pending) T.busy[f.slot] = 0;
+    T.pending.clear();
+}
+
+static femmd_status read_scalars(femmd_ctx *ctx);
+
+// Capture the frame of step m from the current buffers.  When no pinned slot
+// is free, the frames so far are committed if the run has not overflowed up
+// to here (then 'aborted' stays false and the writer frees slots), else the
+// run is abandoned for femmd_run to repeat.
+static femmd_status traj_snapshot(femmd_ctx *ctx, int m, bool &aborted) {
+    Trajectory &T = ctx->traj;
+    const int N = (int)ctx->pos.size();
+    constexpr int kSlots = 8;
+    if (T.N != N) {
+        traj_drain(T);
+        for (auto p : T.pos) cudaFreeHost(p);
+        for (auto p : T.vel) cudaFreeHost(p);
+        T.pos.clear();
+        T.vel.clear();
+        T.busy.clear();
+        T.N = N;
+    }
+    int slot = -1;
+    {
+        std::lock_guard<std::mutex> lk(T.mu);
+        for (size_t k = 0; k < T.busy.size(); k++)
+            if (!T.busy[k]) {
+                slot = (int)k;
+                break;
+            }
+    }
+    if (slot < 0 && (int)T.busy.size() < kSlots) {
+        float2 *p = nullptr, *v = nullptr;
+        CK(cudaMallocHost(&p, std::max(N, 1) * sizeof(float2)));
+        CK(cudaMallocHost(&v, std::max(N, 1) * sizeof(float2)));
+        std::lock_guard<std::mutex> lk(T.mu);
+        T.pos.push_back(p);
+        T.vel.push_back(v);
+        T.busy.push_back(0);
+        slot = (int)T.busy.size() - 1;
+    }
+    if (slot < 0) {
+        femmd_status st;
+        if ((st = read_scalars(ctx))) return st;  // synchronises: the pending frames are in host memory
+        if (ctx->hsc->overflow) {
+            aborted = true;
+            return FEMMD_OK;
+        }
+        traj_commit(T);
+        std::unique_lock<std::mutex> lk(T.mu);
+        T.cv.wait(lk, [&] {
+            for (char b : T.busy)
+                if (!b) return true;
+            return false;
+        });
+        for (size_t k = 0; k < T.busy.size(); k++)
+            if (!T.busy[k]) {
+                slot = (int)k;
+                break;
+            }
+    }
+    {
+        std::lock_guard<std::mutex> lk(T.mu);
+        T.busy[slot] = 1;
+    }
+    const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+    CK(cudaMemcpyAsync(T.pos[slot], pc, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(T.vel[slot], ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+    T.pending.push_back({m, slot});
+    return FEMMD_OK;
+}
+
+static void traj_refresh_meta(femmd_ctx *ctx) {
+    Trajectory &T = ctx->traj;
+    if (!T.on) return;
+    traj_drain(T);
+    T.type = ctx->type;
+    T.tri = ctx->tri;
+    T.mass = ctx->mass;
+    T.clusters.clear();
+    T.clusterMass.clear();
+    for (const Cluster &c : ctx->clusters) {
+        T.clusters.push_back(make_int2(c.offset, c.nv));
+        T.clusterMass.push_back(c.mass);
+    }
+    T.Lx = ctx->Lx;
+    T.Ly = ctx->Ly;
+}
+
+static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
     DevSys s = make_sys(ctx);
     Launch L;
     L.stream = ctx->stream;
@@ -780,17 +1072,42 @@ static femmd_status run_once(femmd_ctx *ctx, int n) {
     }
     CK(enqueue_step(L, s, MODE_FIRST, ctx->cur, 0, 0));
     ctx->cur ^= 1;
-    ctx->profKernels += L.kernels;
     femmd_status st;
-    if ((st = launch_units(ctx, n - 1, graphs))) return st;
-    Launch T;
-    T.stream = ctx->stream;
-    if (ctx->profiling) {
-        T.force_events = &ctx->forceEvents;
-        T.event_pool = &ctx->eventPool;
+    // trajectory frames at the steps m in (s0, s0 + n] that are multiples of
+    // 'every' (the reference's steps % trajectorySteps == 0).  Unit u of the
+    // run computes the forces at x_{s0+u}; a frame inside the run replaces
+    // its unit by LAST (completes v_m), the copy, and FIRST (the same forces
+    // again, first half kick and drift) followed by the rebuild check, which
+    // is the unit's work bit for bit.
+    const int s0 = ctx->steps;
+    std::vector<int> frames;
+    Trajectory &T = ctx->traj;
+    if (T.on && T.every > 0)
+        for (long long m = ((long long)s0 / T.every + 1) * T.every; m <= (long long)s0 + n; m += T.every)
+            if (m > T.lastCommitted) frames.push_back((int)m);
+    int u = 1;
+    for (int m : frames) {
+        const int upto = m - s0;
+        if (upto >= n) break;
+        if ((st = launch_units(ctx, upto - u, graphs))) return st;
+        Launch D = L;
+        D.kernels = 0;
+        CK(enqueue_step(D, s, MODE_LAST, ctx->cur, 0, 0));
+        if ((st = traj_snapshot(ctx, m, aborted))) return st;
+        if (aborted) return FEMMD_OK;
+        CK(enqueue_step(D, s, MODE_FIRST, ctx->cur, 0, 0));
+        ctx->cur ^= 1;
+        CK(enqueue_rebuild(D, s, ctx->cur, 1));
+        ctx->profKernels += D.kernels;
+        u = upto + 1;
     }
-    CK(enqueue_step(T, s, MODE_LAST, ctx->cur, 0, 0));
-    ctx->profKernels += T.kernels;
+    ctx->profKernels += L.kernels;
+    if ((st = launch_units(ctx, n - u, graphs))) return st;
+    Launch T2 = L;
+    T2.kernels = 0;
+    CK(enqueue_step(T2, s, MODE_LAST, ctx->cur, 0, 0));
+    ctx->profKernels += T2.kernels;
+    if (!frames.empty() && frames.back() == s0 + n && (st = traj_snapshot(ctx, s0 + n, aborted))) return st;
     return FEMMD_OK;
 }
 
@@ -828,6 +1145,7 @@ femmd_status femmd_create(int device, femmd_ctx **out) {
 void femmd_destroy(femmd_ctx *ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    traj_stop(ctx->traj);
     release_device(ctx);
     for (auto &pr : ctx->forceEvents) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto e : ctx->eventPool) cudaEventDestroy(e);
@@ -1035,7 +1353,7 @@ femmd_status femmd_set_gravity(femmd_ctx *ctx, double g) {
 femmd_status femmd_set_karea(femmd_ctx *ctx, double k) {
     NEED(ctx);
     ctx->kArea = k > 0 ? (float)k : 0.f;
-    if (k > 0) return fail(ctx, FEMMD_UNSUPPORTED, "area springs are outside this build's timestep path");
+    if (k > 0) return fail(ctx, FEMMD_UNSUPPORTED, "area springs (positions moved inside the force loop) are not supported");
     return FEMMD_OK;
 }
 
@@ -1315,11 +1633,13 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         if (ctx->tracing)
             CK(cudaMemsetAsync(ctx->trace.p, 0, (size_t)ctx->obsCap * kTraceCols * sizeof(unsigned long long),
                                ctx->stream));
-        if ((st = run_once(ctx, steps))) return st;
+        bool aborted = false;
+        if ((st = run_once(ctx, steps, aborted))) return st;
         if ((st = collect_profile(ctx))) return st;
         if ((st = read_scalars(ctx))) return st;
         if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
-        if (!ctx->hsc->overflow) {
+        if (!ctx->hsc->overflow && !aborted) {
+            traj_commit(ctx->traj);
             ctx->steps += steps;
             ctx->staleMask |= kPos | kVel | kAcc | kForce;
             ctx->forcesValid = true;
@@ -1331,6 +1651,7 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
             return FEMMD_OK;
         }
         // roll back to the checkpoint, grow the list, repeat
+        traj_discard(ctx->traj);
         ctx->cur = cur0;
         float2 *pd = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
         CK(cudaMemcpyAsync(pd, ctx->ckPos.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1738,6 +2059,45 @@ femmd_status femmd_get_profile(femmd_ctx *ctx, double *fms, long long *fl, doubl
     return FEMMD_OK;
 }
 
+
+// ============================================================= trajectory
+
+femmd_status femmd_set_trajectory(femmd_ctx *ctx, const char *path, int every, int format) {
+    NEED(ctx);
+    Trajectory &T = ctx->traj;
+    traj_stop(T);
+    T.on = false;
+    if (!path || every <= 0) return FEMMD_OK;
+    if (format < 0 || format > 2) return fail(ctx, FEMMD_INVALID_ARG, "format must be 0 (dump), 1 (xyz) or 2 (vtk)");
+    T.path = path;
+    T.every = every;
+    T.format = format;
+    T.error.clear();
+    T.written = 0;
+    T.N = 0;
+    T.lastCommitted = (long long)ctx->steps;  // frames from the next step on
+    if (format != 2) {
+        FILE *f = fopen(path, "w");  // a new trajectory starts a new file
+        if (!f) return fail(ctx, FEMMD_INVALID_ARG, "cannot create %s", path);
+        fclose(f);
+    }
+    T.on = true;
+    traj_refresh_meta(ctx);
+    T.th = std::thread(traj_writer, &T);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_flush_trajectory(femmd_ctx *ctx, long long *frames_written) {
+    NEED(ctx);
+    Trajectory &T = ctx->traj;
+    traj_drain(T);
+    if (frames_written) {
+        std::lock_guard<std::mutex> lk(T.mu);
+        *frames_written = T.written;
+    }
+    if (!T.error.empty()) return fail(ctx, FEMMD_INVALID_ARG, "trajectory: %s", T.error.c_str());
+    return FEMMD_OK;
+}
 
 // ============================================================== observables
 

@@ -251,6 +251,21 @@ femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads,
 femmd_status femmd_batch_event_record(femmd_batch *b, int slot);
 femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, float *ms);
 
+/* --------------------------------------------------------- trajectory */
+/* System.save_trajectory / set_trajectory_steps (interface.cpp:289-299):
+ * during femmd_run, every 'every' steps (at step counts that are multiples of
+ * it, as Integrator::doStep, integrator.cpp:20-26) the positions and
+ * velocities are copied to pinned host memory and written by a host thread
+ * while the run goes on.  format 0: the layout of saveClusterXYZ
+ * (md3dsystem.cpp:248-273; that routine lists only the first NC particles,
+ * every particle is listed here), appended to 'path'; 1: saveXYZ
+ * (:232-246); 2: saveVtk (:275-328), one file '<path><step, 9 digits>.vtk'
+ * per frame with the clusters unfolded.  The run's results are bit for bit
+ * those without frames.  path NULL or every <= 0 stops writing. */
+femmd_status femmd_set_trajectory(femmd_ctx *ctx, const char *path, int every, int format);
+/* Wait until every captured frame is on disk; the count written so far. */
+femmd_status femmd_flush_trajectory(femmd_ctx *ctx, long long *frames_written);
+
 /* -------------------------------------------------------- observables */
 /* Properties::evaluate (properties.cpp:15-36) at the current state, FP64
  * sums on the device: out[0..9] = uKinetic, uPotential, uTotal, temperature,

@@ -7,7 +7,7 @@
  * triangle elasticity (both material laws of the reference) and the
  * kick-drift-kick leapfrog with the reference's half-skin rebuild rule.
  * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may
- * load it, and only as the checker (or the timed CPU baseline); the CUDA
+ * load it, and only to check results (or as the timed CPU baseline); the CUDA
  * product never links or calls it.
  *
  * Arithmetic families
@@ -966,7 +966,7 @@ static void lj_forces(orc *s) {
 /* Interactions::calcForces (src/interactions.cpp:83-109): the fixed walls
  * of NOPBC / XPBC boxes, gravity, bonds, FEA, pairs (area springs, which
  * displace positions inside the force loop, are not restated), then the
- * moving walls of this build. */
+ * moving harmonic walls (no counterpart in the reference). */
 void orc_calc_forces(orc *s) {
     ref_wall_forces(s);
     gravity_forces(s);
