@@ -484,6 +484,19 @@ def batched(args, dist):
     mixed_atoms = mix.N
     del mix
 
+    # opt-in tuning of the rebuild cadence and cell size (changes rounding,
+    # not physics), reported beside the reference-exact figure
+    tuned = b.autotune_lists(20, skins=(0.3, 0.45, 0.6), factors=(1.0,))
+    for _ in range(2):
+        b.run(md)
+    tms = []
+    for k in range(max(1, min(args.steps, 3))):
+        b.event_record(0)
+        b.run(md)
+        b.event_record(1)
+        tms.append(b.event_elapsed_ms(0, 1))
+    tuned_value = natoms * md / (statistics.median(tms) / 1e3)
+
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         # one mid-sized replica on the host, scaled by atoms
@@ -506,6 +519,9 @@ def batched(args, dist):
             "plain_single_system_same_mix": {"value": mixed_value, "unit": "atom-steps/s", "atoms": mixed_atoms,
                                              "how": "one system of 2025 hex-ring disks in LJ solvent (rho 0.8), "
                                                     f"run({md}), CUDA events"},
+            "batched_tuned_lists": {"value": tuned_value, "unit": "atom-steps/s", "skin": tuned["skin"],
+                                    "cell_factor": tuned["cell_factor"],
+                                    "note": "opt-in skin/cell-size tuning: same physics, other rounding"},
             "batched_over_plain": value / plain_value,
             "batched_over_single_system": value / single_value,
             "batched_over_single_system_same_mix": value / mixed_value,
@@ -568,6 +584,7 @@ def main():
                 b = batched(sub, _Solo())
                 line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "plain_same_atoms",
                                                      "plain_single_system", "plain_single_system_same_mix",
+                                                     "batched_tuned_lists",
                                                      "batched_over_plain", "batched_over_single_system",
                                                      "batched_over_single_system_same_mix", "e2e", "clocks")}
                 line["batched"]["config"] = {k: b["config"][k] for k in ("description", "replicas", "atoms",

@@ -228,6 +228,9 @@ class System:
                    C.byref(ge), C.byref(gs))
         return dict(x0=gx, v0=gv, E=gE[:ne], nu=gnu[:ne], log_eps=ge.value, log_sigma=gs.value)
 
+    def set_cell_factor(self, f):
+        self._call("femmd_set_cell_factor", float(f))
+
     def set_skin(self, s):
         self._call("femmd_set_skin", float(s))
 
@@ -519,6 +522,15 @@ class Batch:
         t, c, ms = C.c_int(), C.c_int(), C.c_double()
         self._call("femmd_batch_autotune", int(trial_steps), C.byref(t), C.byref(c), C.byref(ms))
         return dict(threads=t.value, ctas_per_sm=c.value, trial_ms=ms.value)
+
+    def autotune_lists(self, trial_steps=20, skins=(0.3, 0.45, 0.6), factors=(1.0,)):
+        """Opt-in: pick the skin (rebuild cadence) and cell factor by timing."""
+        sk = (C.c_double * len(skins))(*skins)
+        fa = (C.c_double * len(factors))(*factors)
+        bs, bf, ms = C.c_double(), C.c_double(), C.c_double()
+        self._call("femmd_batch_autotune_lists", int(trial_steps), sk, len(skins), fa, len(factors),
+                   C.byref(bs), C.byref(bf), C.byref(ms))
+        return dict(skin=bs.value, cell_factor=bf.value, trial_ms=ms.value)
 
     def event_record(self, slot):
         self._call("femmd_batch_event_record", int(slot))

@@ -113,6 +113,8 @@ SIGNATURES = {
     "femmd_batch_set_launch": (i_, [P, i_, i_]),
     "femmd_batch_get_launch": (i_, [P, ip, ip, ip]),
     "femmd_batch_autotune": (i_, [P, i_, ip, ip, dp]),
+    "femmd_batch_autotune_lists": (i_, [P, i_, dp, i_, dp, i_, dp, dp, dp]),
+    "femmd_set_cell_factor": (i_, [P, d_]),
     "femmd_batch_event_record": (i_, [P, i_]),
     "femmd_batch_event_elapsed": (i_, [P, i_, i_, fp]),
 }

@@ -129,6 +129,7 @@ struct femmd_ctx {
     int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
     int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
     float skin = 0.4f;
+    float cellFactor = 1.0f;  // list cells of cellFactor * nnRadius (1: the reference's)
     // per-elastomer material (E, nu) where set; walls
     std::vector<float> elE, elNu;
     std::vector<char> elOwn;
@@ -332,6 +333,7 @@ static void clear_system(femmd_ctx *c) {
     c->gravityForce = false;
     c->kWall = 10.0f;
     c->skin = 0.4f;
+    c->cellFactor = 1.0f;
     c->elE.clear(); c->elNu.clear(); c->elOwn.clear();
     c->wallOn = false;
     c->wallK = c->wallY0 = c->wallV = 0;
@@ -1364,6 +1366,17 @@ femmd_status femmd_set_skin(femmd_ctx *ctx, double skin) {
     return FEMMD_OK;
 }
 
+// List cells of factor * (rc + skin) instead of the reference's (factor 1):
+// fewer, larger cells.  Takes effect at the next femmd_init_neighbor_list.
+// Any factor other than 1 changes the list order, so the pair sums round
+// differently from the reference's.
+femmd_status femmd_set_cell_factor(femmd_ctx *ctx, double factor) {
+    NEED(ctx);
+    if (!(factor >= 1.0) || !(factor <= 8.0)) return fail(ctx, FEMMD_INVALID_ARG, "cell factor must be in [1, 8]");
+    ctx->cellFactor = (float)factor;
+    return FEMMD_OK;
+}
+
 femmd_status femmd_set_neighbor_capacity(femmd_ctx *ctx, int cap) {
     NEED(ctx);
     if (cap < 0) return fail(ctx, FEMMD_INVALID_ARG, "capacity must be >= 0");
@@ -1598,7 +1611,8 @@ femmd_status femmd_init_neighbor_list(femmd_ctx *ctx) {
     float rc = 1.0f * ctx->rCutMax;
     ctx->nnRadius = rc + ctx->skin;
     ctx->nnRadiusSq = ctx->nnRadius * ctx->nnRadius;
-    int nx = (int)std::floor(ctx->Lx / ctx->nnRadius), ny = (int)std::floor(ctx->Ly / ctx->nnRadius);
+    const float cell = ctx->nnRadius * ctx->cellFactor;
+    int nx = (int)std::floor(ctx->Lx / cell), ny = (int)std::floor(ctx->Ly / cell);
     if (nx < 1 || ny < 1)
         return fail(ctx, FEMMD_INVALID_ARG, "box (%g, %g) is smaller than one list cell (%g)", ctx->Lx, ctx->Ly,
                     ctx->nnRadius);
@@ -2771,6 +2785,80 @@ femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads_
     b->ctasPerSm = bc;
     if (threads_out) *threads_out = bt;
     if (ctas_per_sm_out) *ctas_per_sm_out = bc;
+    if (best_ms) *best_ms = best;
+    return FEMMD_OK;
+}
+
+
+// Rebuild cadence and cell size: time run(trial_steps) of the whole batch for
+// every (skin, cell factor) pair on the current states (restored after each
+// trial), then keep the fastest pair on every replica.  Opt-in: both change
+// the lists' order and rebuild steps, so the trajectories no longer round as
+// the reference's do.
+femmd_status femmd_batch_autotune_lists(femmd_batch *b, int trial_steps, const double *skins, int nskins,
+                                        const double *factors, int nfactors, double *best_skin,
+                                        double *best_factor, double *best_ms) {
+    if (!b || !skins || nskins < 1 || !factors || nfactors < 1) return FEMMD_INVALID_ARG;
+    b->err.clear();
+    if (b->reps.empty()) return bfail(b, FEMMD_NOT_READY, "empty batch");
+    if (trial_steps < 1) trial_steps = 20;
+    if (!b->stream) {
+        BCK(cudaSetDevice(b->device));
+        BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    auto apply = [&](double skin, double f) -> femmd_status {
+        for (femmd_ctx *c : b->reps) {
+            femmd_status st;
+            if ((st = femmd_set_skin(c, skin)) || (st = femmd_set_cell_factor(c, f)) ||
+                (st = femmd_init_neighbor_list(c)))
+                return bfail(b, st, "replica: %s", c->err.c_str());
+        }
+        return FEMMD_OK;
+    };
+    std::vector<float> skin0, fac0;
+    for (femmd_ctx *c : b->reps) {
+        skin0.push_back(c->skin);
+        fac0.push_back(c->cellFactor);
+    }
+    double best = 1e300, bs = skin0[0], bf = fac0[0];
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    for (int i = 0; i < nskins; i++)
+        for (int j = 0; j < nfactors; j++) {
+            femmd_status st;
+            if ((st = apply(skins[i], factors[j]))) return st;
+            BatchLaunch bl;
+            std::vector<DevSys> sys;
+            if ((st = batch_prepare(b, trial_steps, bl, sys))) return st;
+            if ((st = batch_checkpoint(b, false))) return st;
+            BCK(cudaMemsetAsync(bl.queue, 0, 2 * sizeof(int), b->stream));
+            BCK(cudaEventRecord(e0, b->stream));
+            {
+                Launch L;
+                L.stream = b->stream;
+                BCK(enqueue_batch(L, bl));
+            }
+            BCK(cudaEventRecord(e1, b->stream));
+            BCK(cudaStreamSynchronize(b->stream));
+            float ms = 0;
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            if ((st = batch_read(b))) return st;
+            bool over = false;
+            for (femmd_ctx *c : b->reps) over = over || (!c->pos.empty() && c->hsc->overflow);
+            if (!over && ms < best) {  // a trial whose lists overflowed is not a fair time
+                best = ms;
+                bs = skins[i];
+                bf = factors[j];
+            }
+            if ((st = batch_checkpoint(b, true))) return st;
+            BCK(cudaStreamSynchronize(b->stream));
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (femmd_status st = apply(bs, bf)) return st;
+    if (best_skin) *best_skin = bs;
+    if (best_factor) *best_factor = bf;
     if (best_ms) *best_ms = best;
     return FEMMD_OK;
 }

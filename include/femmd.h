@@ -104,6 +104,10 @@ femmd_status femmd_set_moving_wall(femmd_ctx *ctx, double k, double y0, double v
 /* Forces the particles exert on the top and bottom walls at the current
  * positions (sum of k * overlap). */
 femmd_status femmd_get_wall_forces(femmd_ctx *ctx, double *top, double *bottom);
+/* List cells of factor * (rc + skin), factor in [1, 8] (1: the reference's
+ * cell size); applied by the next femmd_init_neighbor_list.  A factor other
+ * than 1 changes the list order and therefore the rounding of the sums. */
+femmd_status femmd_set_cell_factor(femmd_ctx *ctx, double factor);
 /* NeighborList::setSkin (C++ only, nn.h:64; default 0.4) */
 femmd_status femmd_set_skin(femmd_ctx *ctx, double skin);
 /* Neighbour-list capacity per particle (0 = size from the first build).  A
@@ -248,6 +252,15 @@ femmd_status femmd_batch_get_launch(const femmd_batch *b, int *threads, int *cta
 /* Times trial_steps on each candidate launch shape (states restored after each
  * trial) and keeps the fastest. */
 femmd_status femmd_batch_autotune(femmd_batch *b, int trial_steps, int *threads, int *ctas_per_sm, double *best_ms);
+/* Opt-in tuning of the rebuild cadence and cell size: every (skin, cell
+ * factor) pair is timed on run(trial_steps) of the whole batch from the
+ * current states (restored after each trial) and the fastest pair is applied
+ * to every replica (femmd_set_skin, femmd_set_cell_factor,
+ * femmd_init_neighbor_list).  Trajectories then no longer round as the
+ * reference's do; the physics is unchanged. */
+femmd_status femmd_batch_autotune_lists(femmd_batch *b, int trial_steps, const double *skins, int nskins,
+                                        const double *factors, int nfactors, double *best_skin,
+                                        double *best_factor, double *best_ms);
 femmd_status femmd_batch_event_record(femmd_batch *b, int slot);
 femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, float *ms);
 

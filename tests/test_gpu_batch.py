@@ -97,3 +97,58 @@ def test_batch_rejects_mixed_variants():
     b.add(c)
     with pytest.raises(F.FemmdError):
         b.run(5)
+
+
+def test_batch_walls_gravity_and_moving_walls():
+    """XPBC replicas: the reference's harmonic walls under gravity and the
+    moving compression wall, each bit-identical to running alone."""
+    import golden_io as G
+    base, _ = G.load("susp_xpbc_gravity")
+    calls = []
+    for name, args in base.calls:
+        if name == "dump_setup":
+            break
+        calls.append((name, args))
+    scs = []
+    for g in (0.5, 2.0, 3.5):
+        sc = S.Scene(calls=[(n, (g,) if n == "set_gravity" else a) for n, a in calls])
+        scs.append(sc)
+    scs.append(S.compression(n_side=3, steps=60))
+    scs.append(S.compression(n_side=2, steps=60, seeds=(3, 14, 15, 11)))
+    b = F.Batch(0)
+    systems = []
+    for sc in scs:
+        s = F.System(0)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    b.run(60)
+    b.run(37)
+    for sc, s in zip(scs, systems):
+        assert same(s, alone(sc, [60, 37]))
+
+
+def test_batch_autotune_lists_applies_the_choice():
+    """Opt-in cadence/cell tuning: afterwards every replica runs exactly like
+    the same system set up alone with the chosen skin and cell factor."""
+    scs = replicas(4, seed=4)
+    b = F.Batch(0)
+    systems = []
+    for sc in scs:
+        s = F.System(0)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    b.run(10)
+    r = b.autotune_lists(15, skins=(0.3, 0.5), factors=(1.0, 1.25))
+    assert r["skin"] in (0.3, 0.5) and r["cell_factor"] in (1.0, 1.25)
+    b.run(40)
+    for sc, s in zip(scs, systems):
+        a = F.System(0)
+        sc.replay(a)
+        a.run(10)
+        a.set_skin(r["skin"])
+        a.set_cell_factor(r["cell_factor"])
+        a.init_neighbor_list()
+        a.run(40)
+        assert same(s, a)
