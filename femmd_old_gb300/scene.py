@@ -26,7 +26,7 @@ import numpy as np
 OP = dict(END=0, INIT=1, PBC=2, DT=3, NUMTYPES=4, PAIR=5, KBOND=6, YOUNG=7, NU=8, SKIN=9,
           ELASTOMER=10, PARTICLE=11, BOND=12, INITNN=13, CAPACITY=14, RUN=15, STEP=16,
           BUILDNN=17, FORCES=18, ELASTOMER_BONDS=19, DUMP_STATE=20, DUMP_NN=21, DUMP_SETUP=22,
-          SETVEL=23, GRAVITY=24)
+          SETVEL=23, GRAVITY=24, KAREA=25)
 
 WCA_RC = 2.0 ** (1.0 / 6.0)
 
@@ -73,6 +73,8 @@ class Scene:
                 w(struct.pack("<id", OP["KBOND"], a[0]))
             elif name == "set_gravity":
                 w(struct.pack("<id", OP["GRAVITY"], a[0]))
+            elif name == "set_kArea":
+                w(struct.pack("<id", OP["KAREA"], a[0]))
             elif name == "set_youngs_modulus":
                 w(struct.pack("<id", OP["YOUNG"], a[0]))
             elif name == "set_poisson_ratio":
@@ -176,6 +178,8 @@ class Scene:
                 sc.add("set_kBond", *take("d"))
             elif name == "GRAVITY":
                 sc.add("set_gravity", *take("d"))
+            elif name == "KAREA":
+                sc.add("set_kArea", *take("d"))
             elif name == "YOUNG":
                 sc.add("set_youngs_modulus", *take("d"))
             elif name == "NU":

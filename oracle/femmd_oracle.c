@@ -95,6 +95,9 @@ typedef struct orc {
     /* Interactions::kWall, gravity (src/interactions.h:14-18) */
     float kWall, gravity;
     int gravityForce;
+    /* Interactions::kArea, areaForces (src/interactions.h:14,20) */
+    float kArea;
+    int areaForces;
 } orc;
 
 /* ---------------------------------------------------------------- helpers */
@@ -325,6 +328,11 @@ static void tri_lame(const orc *s, int t, float *mu, float *lambda) {
 /* DukSystemSetGravity (src/interface.cpp:443-453) */
 void orc_set_gravity(orc *s, double g) {
     if (g > 0) { s->gravity = (float)g; s->gravityForce = 1; } else s->gravityForce = 0;
+}
+
+/* DukSystemSetKArea (src/interface.cpp:466-476) */
+void orc_set_karea(orc *s, double k) {
+    if (k > 0) { s->kArea = (float)k; s->areaForces = 1; } else s->areaForces = 0;
 }
 
 /* ljwallforce (src/interactionsCuda.cu:31-40), float operations as written
@@ -963,15 +971,61 @@ static void lj_forces(orc *s) {
     for (int pi = 0; pi < s->N; pi++) { s->potEnergy += s->ui[pi]; s->virial += s->wi[pi]; }
 }
 
+/* calcAreaForcesCPU (src/interactions.cpp:696-750).  Triangle by triangle
+ * in list order, each reading the positions the earlier ones left: r1 and r2
+ * moved to r0's side by the half-box rule on both axes (whatever the
+ * periodicity), the reference area A0 and the current area A (float products,
+ * halved in double), c = -kArea (A - A0) / (2 A0) formed in double and
+ * rounded to float, and the vertices displaced -- positions, not forces -- by
+ * f1 = c (y2 - y0, -(x2 - x0)), f2 = c (-(y1 - y0), x1 - x0), f0 = -f1 - f2.
+ * The energy 1/2 kArea (A - A0)^2 is added in double to the float sum. */
+static void area_springs(orc *s) {
+    const float Lx = s->Lx, Ly = s->Ly;
+    for (int t = 0; t < s->ntri; t++) {
+        const int *v = s->tri + 3 * t;
+        float rx[3], ry[3], qx[3], qy[3];
+        for (int k = 0; k < 3; k++) {
+            rx[k] = s->px[v[k]]; ry[k] = s->py[v[k]];
+            qx[k] = s->refx[v[k]]; qy[k] = s->refy[v[k]];
+        }
+        float dx01 = rx[0] - rx[1], dx02 = rx[0] - rx[2];
+        if (dx01 > Lx / 2.0) rx[1] += Lx;
+        if (dx01 < -Lx / 2.0) rx[1] -= Lx;
+        if (dx02 > Lx / 2.0) rx[2] += Lx;
+        if (dx02 < -Lx / 2.0) rx[2] -= Lx;
+        float dy01 = ry[0] - ry[1], dy02 = ry[0] - ry[2];
+        if (dy01 > Ly / 2.0) ry[1] += Ly;
+        if (dy01 < -Ly / 2.0) ry[1] -= Ly;
+        if (dy02 > Ly / 2.0) ry[2] += Ly;
+        if (dy02 < -Ly / 2.0) ry[2] -= Ly;
+        float pa = (qy[2] - qy[0]) * (qx[1] - qx[0]), pb = (qy[1] - qy[0]) * (qx[2] - qx[0]);
+        float A0 = (float)(0.5 * (float)(pa - pb));
+        pa = (ry[2] - ry[0]) * (rx[1] - rx[0]);
+        pb = (ry[1] - ry[0]) * (rx[2] - rx[0]);
+        float A = (float)(0.5 * (float)(pa - pb));
+        float dA = A - A0;
+        float c = (float)(-0.5 * (double)s->kArea * (double)dA / (double)A0);
+        s->potEnergy = (float)((double)s->potEnergy + 0.5 * (double)s->kArea * (double)dA * (double)dA);
+        float f1x = c * (ry[2] - ry[0]), f1y = -c * (rx[2] - rx[0]);
+        float f2x = -c * (ry[1] - ry[0]), f2y = c * (rx[1] - rx[0]);
+        float fxs[3] = {-f1x - f2x, f1x, f2x}, fys[3] = {-f1y - f2y, f1y, f2y};
+        for (int k = 0; k < 3; k++) {
+            s->px[v[k]] += fxs[k];
+            s->py[v[k]] += fys[k];
+        }
+    }
+}
+
 /* Interactions::calcForces (src/interactions.cpp:83-109): the fixed walls
- * of NOPBC / XPBC boxes, gravity, bonds, FEA, pairs (area springs, which
- * displace positions inside the force loop, are not restated), then the
- * moving harmonic walls (no counterpart in the reference). */
+ * of NOPBC / XPBC boxes, gravity, bonds, FEA, area springs (which move the
+ * positions the pair forces then see), pairs, then the moving harmonic walls
+ * (no counterpart in the reference). */
 void orc_calc_forces(orc *s) {
     ref_wall_forces(s);
     gravity_forces(s);
     if (s->bondForces) bond_forces(s);
     if (s->feaForces) fea_forces(s);
+    if (s->areaForces) area_springs(s);
     lj_forces(s);
     wall_forces(s);
 }

@@ -86,7 +86,7 @@ def lib():
             "orc_set_elastomer_material": (C.c_int, [P, C.c_int, C.c_double, C.c_double]),
             "orc_set_moving_wall": (None, [P, C.c_double, C.c_double, C.c_double]),
             "orc_wall_forces": (None, [P, dp, dp]),
-            "orc_set_gravity": (None, [P, C.c_double]), "orc_ncl": (C.c_int, [P]), "orc_d_init": (None, [P]), "orc_properties": (None, [P, dp]), "orc_d_set_material": (None, [C.c_int, C.c_double, C.c_double]),
+            "orc_set_gravity": (None, [P, C.c_double]), "orc_set_karea": (None, [P, C.c_double]), "orc_ncl": (C.c_int, [P]), "orc_d_init": (None, [P]), "orc_properties": (None, [P, dp]), "orc_d_set_material": (None, [C.c_int, C.c_double, C.c_double]),
             "orc_d_set_scales": (None, [C.c_double, C.c_double]), "orc_d_set_state": (None, [dp, dp]),
             "orc_d_get_state": (None, [dp, dp]), "orc_d_set_traj": (None, [dp, C.c_int]),
             "orc_d_forward": (C.c_double, [P, C.c_int, C.c_int, C.c_double, C.c_double]),
@@ -164,6 +164,9 @@ class Oracle:
 
     def set_gravity(self, g):
         self.L.orc_set_gravity(self.h, float(g))
+
+    def set_kArea(self, k):
+        self.L.orc_set_karea(self.h, float(k))
 
     def set_elastomer_material(self, e, E, nu):
         if self.L.orc_set_elastomer_material(self.h, int(e), float(E), float(nu)):

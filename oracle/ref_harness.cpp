@@ -22,7 +22,7 @@ enum Op {
     OP_YOUNG = 7, OP_NU = 8, OP_SKIN = 9, OP_ELASTOMER = 10, OP_PARTICLE = 11, OP_BOND = 12,
     OP_INITNN = 13, OP_CAPACITY = 14, OP_RUN = 15, OP_STEP = 16, OP_BUILDNN = 17, OP_FORCES = 18,
     OP_ELASTOMER_BONDS = 19, OP_DUMP_STATE = 20, OP_DUMP_NN = 21, OP_DUMP_SETUP = 22, OP_SETVEL = 23,
-    OP_GRAVITY = 24
+    OP_GRAVITY = 24, OP_KAREA = 25
 };
 
 // Bond set of an elastomer: 0 keeps the reference's bonds on every triangle
@@ -193,6 +193,15 @@ int main(int argc, char **argv) {
                 s.interactions.gravityForce = true;
             } else
                 s.interactions.gravityForce = false;
+            break;
+        }
+        case OP_KAREA: {  // DukSystemSetKArea (interface.cpp:466-476)
+            real k = rd<double>();
+            if (k > 0) {
+                s.interactions.kArea = k;
+                s.interactions.areaForces = true;
+            } else
+                s.interactions.areaForces = false;
             break;
         }
         case OP_PARTICLE: {

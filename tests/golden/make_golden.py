@@ -214,6 +214,41 @@ def case_susp_mixed():
     return probes(sc, runs=(100, 200))
 
 
+def case_susp_area():
+    """Area springs (kArea > 0): disks drifting across the periodic boundary
+    in a solvent of a second type, deformed by random velocities; the
+    positions move triangle after triangle inside every force pass."""
+    verts, tris = S.hex_disk_mesh(3.0, 3, jitter=0.02, seed=81)
+    nv = verts.shape[0]
+    L = 24.0
+    rng = np.random.Generator(np.random.PCG64(82))
+    sc = S.Scene(meta=dict(workload="susp_area"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 2)
+    sc.add("set_pair_potential", [1.0, 1.0, 1.0, 1.0], [2.5, S.WCA_RC, S.WCA_RC, S.WCA_RC],
+           [S.lj_shift(2.5), 1.0, 1.0, 1.0])
+    sc.add("set_skin", 0.3).add("set_kBond", 80.0).add("set_youngs_modulus", 40.0)
+    sc.add("set_poisson_ratio", 0.3).add("set_elastomer_bonds", 1).add("set_kArea", 0.4)
+    centers = np.array([(20.8, 12.0), (12.0, 20.8), (5.0, 5.0)])
+    for c in centers:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 1, 0, 1.0, float(nv), True)
+    g = (np.stack(np.meshgrid(np.arange(18), np.arange(18), indexing="xy"), -1).reshape(-1, 2) + 0.5) * (L / 18)
+    d = g[:, None, :] - centers[None]
+    d -= L * np.round(d / L)
+    keep = ((d ** 2).sum(-1) > 4.3 ** 2).all(1)
+    p = g[keep] + rng.uniform(-0.05, 0.05, size=(int(keep.sum()), 2))
+    n = p.shape[0]
+    v = rng.normal(0, 1.0, size=(n, 2))
+    sc.add("add_particles", p[:, 0], p[:, 1], v[:, 0], v[:, 1], np.ones(n), np.ones(n), np.zeros(n, np.int32))
+    sc.add("init_neighbor_list")
+    vel = np.zeros((3 * nv + n, 2), np.float32)
+    vel[:3 * nv] = rng.normal(0, 1.5, size=(3 * nv, 2))
+    vel[:nv, 0] += 5.0
+    vel[nv:2 * nv, 1] += 5.0
+    vel[3 * nv:] = v
+    sc.add("set_velocities_array", vel)
+    return probes(sc, runs=(100, 250))
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 

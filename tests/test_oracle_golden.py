@@ -22,7 +22,8 @@ def test_oracle_matches_reference_bitwise(name):
 def test_golden_cases_cover_edge_cases():
     names = set(G.names())
     for required in ("lj_xy", "lj_multitype", "lj_xpbc", "lj_nopbc", "tiny_box", "susp_all", "susp_boundary",
-                     "susp_refdisk", "susp_crossing", "susp_mixed", "lj_nopbc_walls", "susp_xpbc_gravity"):
+                     "susp_refdisk", "susp_crossing", "susp_mixed", "lj_nopbc_walls", "susp_xpbc_gravity",
+                     "susp_area"):
         assert required in names
 
 
@@ -41,6 +42,20 @@ def test_crossing_case_crosses_the_boundary():
     x0, x1 = states[0]["pos"], states[-1]["pos"]
     # some vertices wrapped from near L to near 0 in x (or y)
     assert ((x0[:, 0] > 15) & (x1[:, 0] < 5)).any() or ((x0[:, 1] > 15) & (x1[:, 1] < 5)).any()
+
+
+def test_area_case_exercises_the_area_springs():
+    # the same scene without area springs ends elsewhere, and a disk crosses
+    # the periodic boundary during the runs
+    import femmd_old_gb300.scene as S
+    sc, ref = G.load("susp_area")
+    off = S.Scene(calls=[(n, (0.0,) if n == "set_kArea" else a) for n, a in sc.calls], meta=sc.meta)
+    o = Oracle(image_mode=0, log_mode=0)
+    off.replay(o)
+    states = [d for t, d in ref if t == "state"]
+    assert np.abs(o.positions() - states[-1]["pos"]).max() > 1e-3
+    x0, x1 = states[0]["pos"], states[-1]["pos"]
+    assert ((x0[:, 0] > 18) & (x1[:, 0] < 5)).any() or ((x0[:, 1] > 18) & (x1[:, 1] < 5)).any()
 
 
 def test_own_log_accuracy():
