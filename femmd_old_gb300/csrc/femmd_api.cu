@@ -28,6 +28,7 @@
 #include <numeric>
 #include <string>
 #include <thread>
+#include <map>
 #include <vector>
 
 #include "femmd.h"
@@ -125,7 +126,7 @@ struct femmd_ctx {
     bool bondForces = false, feaForces = false;
     float kBond = 0, E = 0, nu = 0.3f, lambda = 0, mu = 0, C1 = 0, C2 = 0, C3 = 0, gravity = 0, kArea = 0;
     float kWall = 10.0f;  // Interactions::init (interactions.cpp:22)
-    bool gravityForce = false;
+    bool gravityForce = false, areaForces = false;
     int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
     int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
     float skin = 0.4f;
@@ -159,6 +160,13 @@ struct femmd_ctx {
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF, triLame;
     DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta, wallSig;
     bool ownMaterial = false, materialDirty = false;
+    // area springs: kept positions and the per-mesh work list
+    DBuf<float2> posPre;
+    DBuf<int4> areaUnit, areaIdx;
+    DBuf<int> areaLane;
+    DBuf<float> areaA0;
+    int areaUnits = 0, areaSmem = 0;
+    std::string areaWhy;  // why the triangles cannot be scheduled ("" when they can)
     // observables: cluster ranges and masses, cluster of each particle, FP64 terms
     DBuf<int2> clRange;
     DBuf<float> clMass;
@@ -300,6 +308,8 @@ static void release_device(femmd_ctx *c) {
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
     c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
     c->triLame.release(); c->wallDelta.release(); c->wallSig.release();
+    c->posPre.release(); c->areaUnit.release(); c->areaIdx.release(); c->areaLane.release(); c->areaA0.release();
+    c->areaUnits = 0;
     c->clRange.release(); c->clMass.release(); c->clusterOf.release(); c->unf.release(); c->cmPos.release();
     c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
     auto &a = c->adj;
@@ -458,6 +468,16 @@ static DevSys make_sys(femmd_ctx *c) {
     s.wallRc = wall_range();
     s.gravity = c->gravityForce ? c->gravity : 0.0f;
     s.wallSig = (c->wallOn || c->pbc != FEMMD_XYPBC) ? c->wallSig.p : nullptr;
+    const bool area = c->areaForces && c->areaUnits > 0 && c->areaWhy.empty();
+    s.kArea = c->kArea;
+    s.areaUnits = area ? c->areaUnits : 0;
+    s.areaSmem = c->areaSmem;
+    s.areaUnit = c->areaUnit.p;
+    s.areaLane = c->areaLane.p;
+    s.areaIdx = c->areaIdx.p;
+    s.areaA0 = c->areaA0.p;
+    s.posPre = area ? c->posPre.p : nullptr;
+    s.nPre = area ? c->nBonded : 0;
     return s;
 }
 
@@ -529,6 +549,105 @@ static femmd_status upload_material(femmd_ctx *ctx) {
     }
     CK(cudaStreamSynchronize(s));
     ctx->materialDirty = false;
+    return FEMMD_OK;
+}
+
+// The area springs' work list (calcAreaForcesCPU, interactions.cpp:696-750).
+// Each elastomer's triangles keep the reference's order and run serially in
+// one lane.  Elastomers with the same mesh (vertex count and triangle list
+// inside the elastomer) share blocks of up to 32 lanes, as many as the
+// shared memory holds; A0 of every triangle is formed here from the
+// reference positions by the reference's float operations, per elastomer
+// (the rounding depends on where the elastomer was placed).
+static femmd_status upload_area_schedule(femmd_ctx *ctx) {
+    ctx->areaUnits = 0;
+    ctx->areaSmem = 0;
+    ctx->areaWhy.clear();
+    const int nt = (int)ctx->refVol.size(), ncl = (int)ctx->clusters.size();
+    if (nt == 0) return FEMMD_OK;
+    std::vector<std::vector<int>> byCl(ncl);
+    for (int t = 0; t < nt; t++) {
+        const int *v = &ctx->tri[3 * (size_t)t];
+        const int c = ctx->cluster[v[0]];
+        bool ok = c >= 0 && c < ncl;
+        for (int k = 0; ok && k < 3; k++)
+            ok = ctx->cluster[v[k]] == c && v[k] >= ctx->clusters[c].offset &&
+                 v[k] < ctx->clusters[c].offset + ctx->clusters[c].nv;
+        if (!ok) {
+            ctx->areaWhy = "a triangle's vertices lie in different elastomers";
+            return FEMMD_OK;
+        }
+        byCl[c].push_back(t);
+    }
+    // meshes
+    std::map<std::vector<int>, int> meshOf;
+    std::vector<int4> idx;
+    std::vector<int> meshBase, meshNt, meshNv;
+    std::vector<std::vector<int>> members;
+    for (int c = 0; c < ncl; c++) {
+        if (byCl[c].empty()) continue;
+        const int off = ctx->clusters[c].offset;
+        std::vector<int> key(1, ctx->clusters[c].nv);
+        for (int t : byCl[c])
+            for (int k = 0; k < 3; k++) key.push_back(ctx->tri[3 * (size_t)t + k] - off);
+        auto it = meshOf.find(key);
+        int m;
+        if (it == meshOf.end()) {
+            m = (int)meshBase.size();
+            meshOf.emplace(key, m);
+            meshBase.push_back((int)idx.size());
+            meshNt.push_back((int)byCl[c].size());
+            meshNv.push_back(ctx->clusters[c].nv);
+            members.emplace_back();
+            for (size_t k = 1; k < key.size(); k += 3) idx.push_back(make_int4(key[k], key[k + 1], key[k + 2], 0));
+        } else {
+            m = it->second;
+        }
+        members[m].push_back(c);
+    }
+    const size_t limit = 200 * 1024;
+    std::vector<int4> unit;
+    std::vector<int> lane;
+    std::vector<float> a0;
+    size_t smem = 0;
+    for (size_t m = 0; m < members.size(); m++) {
+        const size_t mnt = meshNt[m], mnv = meshNv[m];
+        auto bytes = [&](size_t nl) { return mnt * 16 + ((mnt * nl + 1) & ~(size_t)1) * 4 + mnv * (nl + 1) * 8; };
+        size_t W = 32;
+        while (W > 1 && bytes(W) > limit) W--;
+        if (bytes(W) > limit) {
+            ctx->areaWhy = "an elastomer's mesh does not fit one block's shared memory";
+            return FEMMD_OK;
+        }
+        for (size_t j0 = 0; j0 < members[m].size(); j0 += W) {
+            const int nl = (int)std::min(W, members[m].size() - j0);
+            unit.push_back(make_int4(meshBase[m], (int)mnt, (int)mnv, nl));
+            unit.push_back(make_int4((int)a0.size(), 0, 0, 0));
+            const size_t a0b = a0.size();
+            a0.resize(a0b + mnt * nl);
+            for (int j = 0; j < 32; j++) lane.push_back(j < nl ? ctx->clusters[members[m][j0 + j]].offset : 0);
+            for (int j = 0; j < nl; j++) {
+                const int c = members[m][j0 + j];
+                for (size_t k = 0; k < mnt; k++) {
+                    const int *v = &ctx->tri[3 * (size_t)byCl[c][k]];
+                    const float2 q0 = ctx->refPos[v[0]], q1 = ctx->refPos[v[1]], q2 = ctx->refPos[v[2]];
+                    a0[a0b + k * nl + j] = 0.5f * ((q2.y - q0.y) * (q1.x - q0.x) - (q1.y - q0.y) * (q2.x - q0.x));
+                }
+            }
+            smem = std::max(smem, bytes(nl));
+        }
+    }
+    if (smem > 48 * 1024) CK(area_smem_setup((int)smem));
+    cudaStream_t s = ctx->stream;
+    CK(ctx->areaUnit.ensure(unit.size())); CK(ctx->areaIdx.ensure(idx.size()));
+    CK(ctx->areaLane.ensure(lane.size())); CK(ctx->areaA0.ensure(std::max(a0.size(), (size_t)1)));
+    CK(ctx->posPre.ensure(std::max(ctx->nBonded, 1)));
+    CK(cudaMemcpyAsync(ctx->areaUnit.p, unit.data(), unit.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->areaIdx.p, idx.data(), idx.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->areaLane.p, lane.data(), lane.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->areaA0.p, a0.data(), a0.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    ctx->areaUnits = (int)unit.size() / 2;
+    ctx->areaSmem = (int)smem;
     return FEMMD_OK;
 }
 
@@ -653,6 +772,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->triIdx.p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     }
+    if ((st = upload_area_schedule(ctx))) return st;
     if ((st = upload_material(ctx))) return st;
     ctx->topoDirty = false;
     ctx->listBuilt = false;
@@ -741,6 +861,8 @@ static femmd_status prepare(femmd_ctx *ctx) {
     if (ctx->stateDirty && (st = upload_state(ctx))) return st;
     if (ctx->materialDirty && (st = upload_material(ctx))) return st;
     if (ctx->nbrCap == 0 && (st = size_list(ctx, 0))) return st;
+    if (ctx->areaForces && !ctx->areaWhy.empty())
+        return fail(ctx, FEMMD_UNSUPPORTED, "area springs: %s", ctx->areaWhy.c_str());
     return FEMMD_OK;
 }
 
@@ -1352,10 +1474,18 @@ femmd_status femmd_set_gravity(femmd_ctx *ctx, double g) {
     return FEMMD_OK;
 }
 
+// DukSystemSetKArea (interface.cpp:466-476): k > 0 sets and enables the area
+// springs, otherwise they are disabled (the stored value is kept)
 femmd_status femmd_set_karea(femmd_ctx *ctx, double k) {
     NEED(ctx);
-    ctx->kArea = k > 0 ? (float)k : 0.f;
-    if (k > 0) return fail(ctx, FEMMD_UNSUPPORTED, "area springs (positions moved inside the force loop) are not supported");
+    if (k > 0) {
+        ctx->kArea = (float)k;
+        ctx->areaForces = true;
+    } else {
+        ctx->areaForces = false;
+    }
+    ctx->forcesValid = false;
+    release_graphs(ctx);
     return FEMMD_OK;
 }
 
@@ -1739,6 +1869,7 @@ femmd_status femmd_calc_forces(femmd_ctx *ctx) {
     CK(enqueue_step(L, s, MODE_FORCES, ctx->cur, 0, 0));
     if ((st = read_scalars(ctx))) return st;
     ctx->staleMask |= kForce | kEnergy;
+    if (s.areaUnits > 0) ctx->staleMask |= kPos;  // the area springs moved the vertices
     ctx->forcesValid = true;
     if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a force became NaN or infinite");
     return FEMMD_OK;
@@ -2184,6 +2315,8 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
 static float wall_y_host(const femmd_ctx *ctx, int n) { return ctx->wallY0 - ctx->wallV * ((float)n * ctx->dt); }
 
 static femmd_status adj_supported(femmd_ctx *ctx) {
+    if (ctx->areaForces && !ctx->refVol.empty())
+        return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint does not implement the area springs");
     if (!ctx->wallOn && ctx->pbc != FEMMD_XYPBC)
         return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint implements the moving walls, not the reference's fixed walls");
     if (ctx->feaForces && !ctx->refVol.empty() && ctx->feaLaw != FEMMD_FEA_NEO_HOOKEAN)
@@ -2468,6 +2601,8 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
         if (c->device != b->device) return bfail(b, FEMMD_INVALID_ARG, "replicas must share the batch's device");
         if ((st = ensure_stream(c)) || (st = prepare(c)) || (st = ensure_obs(c, steps)))
             return bfail(b, st, "replica: %s", c->err.c_str());
+        if (c->areaForces && !c->refVol.empty())
+            return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel does not implement the area springs");
         // the replica's own uploads must land before the batch stream reads them
         BCK(cudaStreamSynchronize(c->stream));
     }

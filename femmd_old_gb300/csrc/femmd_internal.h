@@ -117,6 +117,19 @@ struct DevSys {
     int refWalls;
     float kWall, wallRc, gravity;
     const float *wallSig;  // sigma_i, with walls of either kind
+    // area springs (calcAreaForcesCPU, interactions.cpp:696-750): after the
+    // triangle forces the vertices are displaced in place, triangle by
+    // triangle; walls and bonds (earlier in the reference's force order) read
+    // the positions of [0, nPre) as they were before, kept in posPre
+    float kArea;
+    float2 *posPre;
+    int nPre;
+    int areaUnits;         // blocks of the area pass (0: area springs off)
+    int areaSmem;          // bytes of shared memory per block
+    const int4 *areaUnit;  // per block, 2 entries: {triangle list, triangles, vertices, lanes}, {A0 offset}
+    const int *areaLane;   // per block and lane (32): first vertex of the lane's elastomer
+    const int4 *areaIdx;   // per triangle of a mesh: its vertices inside the elastomer
+    const float *areaA0;   // per block: A0 of triangle k for lane l at [k * lanes + l]
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -141,6 +154,8 @@ cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
 // leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
+// Allow the area-spring kernel 'bytes' of dynamic shared memory.
+cudaError_t area_smem_setup(int bytes);
 
 // ---- adjoint (k_adjoint.cu)
 // Seed at the final positions: xbar += dJ/dx of cWall * wall stress + cFea *

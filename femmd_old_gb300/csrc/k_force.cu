@@ -10,6 +10,9 @@
 // Per step:
 //   k_tri_forces  thread per triangle: nodal forces of the triangle written to
 //                 triF[3t+slot] (no atomics), energy reduced in FP64.
+//   k_area_keep,  with area springs only: the positions of the bonded range
+//   k_area        kept for walls and bonds, then the vertices displaced in
+//                 place triangle by triangle (one lane per elastomer).
 //   k_step        thread per particle: gathers bond incidences (bond order),
 //                 triangle incidences (triangle order) and the Verlet list
 //                 (list order) -- the order in which the reference's CPU path
@@ -58,6 +61,104 @@ __global__ void __launch_bounds__(kBlock) k_tri_forces(DevSys s, int parity) {
             if (row < s.obsCap) atomicMax(&s.trace[(size_t)row * kTraceCols + 1], global_ns());
         }
     }
+}
+
+// ------------------------------------------------------------ area springs
+// calcAreaForcesCPU (interactions.cpp:696-750) moves positions, not forces,
+// and triangle t reads the positions the earlier triangles left: within an
+// elastomer the loop is serial (the hex-ring meshes chain every triangle to
+// the one before).  Elastomers share no vertices, so each is one lane: a
+// block of up to 32 lanes runs elastomers of the same mesh in lock step over
+// the mesh's triangle list, with the vertices, the triangle list and each
+// lane's reference areas A0 staged in shared memory.
+
+constexpr int kAreaLanes = 32;
+
+__global__ void __launch_bounds__(kBlock) k_area_keep(DevSys s, int parity) {
+    const float2 *pin = parity ? s.pos1 : s.pos0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s.nPre) s.posPre[i] = pin[i];
+}
+
+// One triangle of calcAreaForcesCPU on a lane's staged vertices (stride w
+// between consecutive vertices of the lane): r1 and r2 moved to r0's side by
+// the half-box rule on both axes (whatever the periodicity), the current area
+// A as float products halved (the reference halves in double, which is
+// exact), c = -kArea (A - A0) / A0 / 2 formed in double and rounded to float,
+// then f1 = c (y2 - y0, -(x2 - x0)), f2 = c (-(y1 - y0), x1 - x0),
+// f0 = -f1 - f2 added to the stored (unshifted) positions in vertex order.
+// Returns the energy 1/2 kArea (A - A0)^2 (in float: energies are sums
+// checked to a tolerance, positions bit for bit).
+__device__ __forceinline__ float area_tri(float2 *sv, int w, int4 t, float A0, float Lx, float Ly, float kA) {
+    float2 *p0 = sv + t.x * w, *p1 = sv + t.y * w, *p2 = sv + t.z * w;
+    const float2 r0 = *p0;
+    float2 r1 = *p1, r2 = *p2;
+    const float hx = 0.5f * Lx, hy = 0.5f * Ly;
+    const float dx01 = r0.x - r1.x, dx02 = r0.x - r2.x;
+    if (dx01 > hx) r1.x += Lx;
+    if (dx01 < -hx) r1.x -= Lx;
+    if (dx02 > hx) r2.x += Lx;
+    if (dx02 < -hx) r2.x -= Lx;
+    const float dy01 = r0.y - r1.y, dy02 = r0.y - r2.y;
+    if (dy01 > hy) r1.y += Ly;
+    if (dy01 < -hy) r1.y -= Ly;
+    if (dy02 > hy) r2.y += Ly;
+    if (dy02 < -hy) r2.y -= Ly;
+    const float A = 0.5f * ((r2.y - r0.y) * (r1.x - r0.x) - (r1.y - r0.y) * (r2.x - r0.x));
+    const float dA = A - A0;
+    const float c = __double2float_rn(-0.5 * (double)kA * (double)dA / (double)A0);
+    const float f1x = c * (r2.y - r0.y), f1y = -c * (r2.x - r0.x);
+    const float f2x = -c * (r1.y - r0.y), f2y = c * (r1.x - r0.x);
+    const float f0x = -f1x - f2x, f0y = -f1y - f2y;
+    float2 p = *p0;
+    *p0 = make_float2(p.x + f0x, p.y + f0y);
+    p = *p1;
+    *p1 = make_float2(p.x + f1x, p.y + f1y);
+    p = *p2;
+    *p2 = make_float2(p.x + f2x, p.y + f2y);
+    return 0.5f * kA * dA * dA;
+}
+
+__global__ void __launch_bounds__(kAreaLanes) k_area(DevSys s, int parity) {
+    extern __shared__ float4 smem4[];
+    float2 *pos = parity ? s.pos1 : s.pos0;
+    const int4 u = s.areaUnit[2 * blockIdx.x];  // triangle list, triangles, vertices, lanes
+    const int a0base = s.areaUnit[2 * blockIdx.x + 1].x;
+    const int nt = u.y, nv = u.z, nl = u.w, w = nl + 1;  // w: vertex stride (spreads the banks)
+    const int lane = threadIdx.x;
+    int4 *idx = reinterpret_cast<int4 *>(smem4);
+    float *a0 = reinterpret_cast<float *>(idx + nt);
+    float2 *sv = reinterpret_cast<float2 *>(a0 + (((size_t)nt * nl + 1) & ~(size_t)1));
+    for (int k = lane; k < nt; k += kAreaLanes) idx[k] = __ldg(s.areaIdx + u.x + k);
+    for (int k = lane; k < nt * nl; k += kAreaLanes) a0[k] = __ldg(s.areaA0 + a0base + k);
+    // coalesced over each elastomer's vertices, stored lane-minor
+    for (int j = 0; j < nl; j++) {
+        const int off = s.areaLane[blockIdx.x * kAreaLanes + j];
+        for (int v = lane; v < nv; v += kAreaLanes) sv[v * w + j] = pos[off + v];
+    }
+    __syncwarp();
+    double e = 0.0;
+    if (lane < nl) {
+        float2 *mine = sv + lane;
+        const float Lx = s.Lx, Ly = s.Ly, kA = s.kArea;
+        for (int k = 0; k < nt; k++) e += (double)area_tri(mine, w, idx[k], a0[k * nl + lane], Lx, Ly, kA);
+    }
+    __syncwarp();
+    for (int j = 0; j < nl; j++) {
+        const int off = s.areaLane[blockIdx.x * kAreaLanes + j];
+        for (int v = lane; v < nv; v += kAreaLanes) pos[off + v] = sv[v * w + j];
+    }
+    e = warp_sum(e);
+    if (lane == 0) {
+        bool bad = false;
+        unsigned long long q = to_fixed((float)e, bad);
+        if (bad) atomicOr(&s.sc->nonfinite, 2);
+        else if (q) atomicAdd(&s.sc->accU, q);
+    }
+}
+
+cudaError_t area_smem_setup(int bytes) {
+    return cudaFuncSetAttribute(k_area, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 // Resident blocks per SM the register allocation must allow: 16 (64 warps,
@@ -212,6 +313,10 @@ cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaG
     cudaError_t e;
     if (s.feaForces && s.ntri > 0) {
         if ((e = L.kernel(k_tri_forces, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, parity))) return e;
+    }
+    if (s.areaUnits > 0) {
+        if ((e = L.kernel(k_area_keep, dim3(force_blocks(s.nPre)), dim3(kBlock), 0, s, parity))) return e;
+        if ((e = L.kernel(k_area, dim3(s.areaUnits), dim3(kAreaLanes), (size_t)s.areaSmem, s, parity))) return e;
     }
     cudaEvent_t e0 = L.mark();
     if (s.numTypes > 1)

@@ -315,19 +315,24 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
     const float2 pi = pin[i];
     const float Lx = s.Lx, Ly = s.Ly;
     float fx = 0.0f, fy = 0.0f;
-    if (s.refWalls) ref_walls(s, i, pi, fx, fy, uwall);
+    // walls and bonds come before the area springs in the reference's force
+    // order: they see the positions from before that pass (posPre, for the
+    // particles of [0, nPre); pin without area springs)
+    if (s.refWalls) ref_walls(s, i, i < s.nPre ? s.posPre[i] : pi, fx, fy, uwall);
     if (s.gravity > 0.0f) fy -= s.mass[i] * s.gravity;
     if (i < s.nBonded) {
         if (s.bondForces) {
             // calcBondForcesCPU: f on the bond's first particle, -f on the second
+            const float2 *pb = s.nPre > 0 ? s.posPre : pin;
+            const float2 pw = s.nPre > 0 ? s.posPre[i] : pi;
             const int qb = s.bStart[i], qe = s.bStart[i + 1];
             for (int q = qb; q < qe; q++) {
                 int2 en = __ldg(s.bEnt + q);
                 const bool second = en.x < 0;
                 const int j = en.x & 0x7fffffff;
                 const float r0 = __int_as_float(en.y);
-                const float2 pj = RO ? __ldg(pin + j) : pin[j];
-                const float2 a = second ? pj : pi, b = second ? pi : pj;
+                const float2 pj = RO ? __ldg(pb + j) : pb[j];
+                const float2 a = second ? pj : pw, b = second ? pw : pj;
                 float dxr, dyr;
                 bool wr = false;
                 float dx = img<WX>(a.x, b.x, Lx, s.imageExact, dxr, wr);

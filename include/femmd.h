@@ -83,10 +83,12 @@ femmd_status femmd_set_youngs_modulus(femmd_ctx *ctx, double E);
 /* Interactions::nu (C++ only in the reference, interactions.h:22; default 0.3) */
 femmd_status femmd_set_poisson_ratio(femmd_ctx *ctx, double nu);
 /* System.set_gravity(g): interface.cpp:443-453 (g > 0 enables f_y -= m g,
- * calcGravityForces, interactions.cpp:111-126).  System.set_kArea:
- * interface.cpp:467-477; the reference's area springs move positions inside
- * the force loop in triangle order (interactions.cpp:691-750), so k > 0
- * returns FEMMD_UNSUPPORTED.  Boxes that are not periodic in y get the
+ * calcGravityForces, interactions.cpp:111-126).  System.set_kArea(k):
+ * interface.cpp:466-476 (k > 0 enables the area springs of calcAreaForcesCPU,
+ * interactions.cpp:696-750: after the triangle forces, each triangle in turn
+ * displaces its vertices towards its reference area, and the pair forces see
+ * the displaced positions; not available in the batched kernel or the
+ * adjoint, which return FEMMD_UNSUPPORTED).  Boxes that are not periodic in y get the
  * reference's fixed walls (NOPBC: LJ walls on every side; XPBC: harmonic top
  * and bottom with kWall = 10), unless femmd_set_moving_wall is set. */
 femmd_status femmd_set_gravity(femmd_ctx *ctx, double g);
