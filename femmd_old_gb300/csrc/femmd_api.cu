@@ -612,7 +612,7 @@ static femmd_status upload_area_schedule(femmd_ctx *ctx) {
     size_t smem = 0;
     for (size_t m = 0; m < members.size(); m++) {
         const size_t mnt = meshNt[m], mnv = meshNv[m];
-        auto bytes = [&](size_t nl) { return mnt * 16 + ((mnt * nl + 1) & ~(size_t)1) * 4 + mnv * (nl + 1) * 8; };
+        auto bytes = [&](size_t nl) { return mnt * 16 + ((mnt * nl + 3) & ~(size_t)3) * 4 + mnv * (nl + 1) * 8; };
         size_t W = 32;
         while (W > 1 && bytes(W) > limit) W--;
         if (bytes(W) > limit) {
@@ -624,7 +624,7 @@ static femmd_status upload_area_schedule(femmd_ctx *ctx) {
             unit.push_back(make_int4(meshBase[m], (int)mnt, (int)mnv, nl));
             unit.push_back(make_int4((int)a0.size(), 0, 0, 0));
             const size_t a0b = a0.size();
-            a0.resize(a0b + mnt * nl);
+            a0.resize(a0b + ((mnt * nl + 3) & ~(size_t)3));  // 16-byte ranges (copied in 16-byte pieces)
             for (int j = 0; j < 32; j++) lane.push_back(j < nl ? ctx->clusters[members[m][j0 + j]].offset : 0);
             for (int j = 0; j < nl; j++) {
                 const int c = members[m][j0 + j];

@@ -80,78 +80,151 @@ __global__ void __launch_bounds__(kBlock) k_area_keep(DevSys s, int parity) {
     if (i < s.nPre) s.posPre[i] = pin[i];
 }
 
-// One triangle of calcAreaForcesCPU on a lane's staged vertices (stride w
-// between consecutive vertices of the lane): r1 and r2 moved to r0's side by
-// the half-box rule on both axes (whatever the periodicity), the current area
-// A as float products halved (the reference halves in double, which is
-// exact), c = -kArea (A - A0) / A0 / 2 formed in double and rounded to float,
-// then f1 = c (y2 - y0, -(x2 - x0)), f2 = c (-(y1 - y0), x1 - x0),
-// f0 = -f1 - f2 added to the stored (unshifted) positions in vertex order.
-// Returns the energy 1/2 kArea (A - A0)^2 (in float: energies are sums
-// checked to a tolerance, positions bit for bit).
-__device__ __forceinline__ float area_tri(float2 *sv, int w, int4 t, float A0, float Lx, float Ly, float kA) {
-    float2 *p0 = sv + t.x * w, *p1 = sv + t.y * w, *p2 = sv + t.z * w;
-    const float2 r0 = *p0;
-    float2 r1 = *p1, r2 = *p2;
-    const float hx = 0.5f * Lx, hy = 0.5f * Ly;
-    const float dx01 = r0.x - r1.x, dx02 = r0.x - r2.x;
-    if (dx01 > hx) r1.x += Lx;
-    if (dx01 < -hx) r1.x -= Lx;
-    if (dx02 > hx) r2.x += Lx;
-    if (dx02 < -hx) r2.x -= Lx;
-    const float dy01 = r0.y - r1.y, dy02 = r0.y - r2.y;
-    if (dy01 > hy) r1.y += Ly;
-    if (dy01 < -hy) r1.y -= Ly;
-    if (dy02 > hy) r2.y += Ly;
-    if (dy02 < -hy) r2.y -= Ly;
-    const float A = 0.5f * ((r2.y - r0.y) * (r1.x - r0.x) - (r1.y - r0.y) * (r2.x - r0.x));
-    const float dA = A - A0;
-    const float c = __double2float_rn(-0.5 * (double)kA * (double)dA / (double)A0);
-    const float f1x = c * (r2.y - r0.y), f1y = -c * (r2.x - r0.x);
-    const float f2x = -c * (r1.y - r0.y), f2y = c * (r1.x - r0.x);
-    const float f0x = -f1x - f2x, f0y = -f1y - f2y;
-    float2 p = *p0;
-    *p0 = make_float2(p.x + f0x, p.y + f0y);
-    p = *p1;
-    *p1 = make_float2(p.x + f1x, p.y + f1y);
-    p = *p2;
-    *p2 = make_float2(p.x + f2x, p.y + f2y);
-    return 0.5f * kA * dA * dA;
+// c = -kArea (A - A0) / A0 / 2 as the reference forms it: the exact product
+// a b (a = -kArea/2, b = A - A0, 48 bits, exact in double) divided in double
+// and rounded to float.  With a 48-bit dividend and a 24-bit divisor the
+// double quotient never lands on or across a float rounding boundary that
+// the exact quotient q does not, so the result is q rounded to float once.
+// That is computed here without FP64 (slow on this part): y = ph / d from
+// ph = RN(a b), the exact remainder r = ph - y d (one FMA), q - y =
+// (r + pl) / d with pl = a b - ph (one FMA), and y moved by one unit when q
+// lies clearly in a neighbour's rounding interval.  Ties within 2^-20 of an
+// interval's half-width, and the corners of the float range, take the double
+// division itself (out of line, so that it is not evaluated on the common
+// path).  A zero product (the triangle kept its area) gives the signed zero
+// y, as the double quotient does.
+__device__ __noinline__ float area_coeff_f64(float a, float b, float d) {
+    return __double2float_rn((double)a * (double)b / (double)d);
+}
+
+__device__ __forceinline__ float area_coeff(float a, float b, float d) {
+    const float ph = __fmul_rn(a, b);
+    const float pl = __fmaf_rn(a, b, -ph);
+    const float y = __fdiv_rn(ph, d);
+    const float r = __fmaf_rn(-y, d, ph);
+    const unsigned ay = __float_as_uint(y) & 0x7fffffffu, aph = __float_as_uint(ph) & 0x7fffffffu,
+                   ad = __float_as_uint(d) & 0x7fffffffu;
+    // t = (|q| - |y|) |d|; |y| is kept while |t| < hb = ulp(y) |d| / 2
+    const float t = __fadd_rn(r, pl) * (((__float_as_uint(d) ^ __float_as_uint(y)) & 0x80000000u) ? -1.0f : 1.0f);
+    const float u = __uint_as_float((ay & 0x7f800000u) - (23u << 23));
+    const float hb = 0.5f * u * fabsf(d), m = hb * 0x1p-20f, h3 = 3.0f * hb;
+    const bool keep = fabsf(t) < hb - m;
+    const bool up = t > hb + m && t < h3 - m;
+    const bool down = t < -hb - m && t > -h3 + m;
+    const bool dok = ad >= (31u << 23) && ad < (220u << 23);
+    const bool fast = dok && aph >= (31u << 23) && aph < (220u << 23) && ay >= (31u << 23) && ay < (220u << 23) &&
+                      (ay & 0x7fffffu) >= 2u && (keep || up || down);
+    const float c = __uint_as_float(__float_as_uint(y) + (up ? 1u : 0u) - (down ? 1u : 0u));
+    if (fast) return c;
+    if (aph == 0u && dok) return y;
+    return area_coeff_f64(a, b, d);
+}
+
+// Asynchronous global -> shared copies (cp.async): a lane issues all of its
+// copies back to back and waits once, instead of one load latency per element.
+__device__ __forceinline__ void copy_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src));
+}
+__device__ __forceinline__ void copy_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src));
+}
+__device__ __forceinline__ void copy_async_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// The newest value of vertex v after a triangle (t) stored n0, n1, n2 in that
+// order; 'old' when the triangle did not touch v.
+__device__ __forceinline__ float2 area_latest(int v, int4 t, float2 n0, float2 n1, float2 n2, float2 old) {
+    return v == t.z ? n2 : v == t.y ? n1 : v == t.x ? n0 : old;
 }
 
 __global__ void __launch_bounds__(kAreaLanes) k_area(DevSys s, int parity) {
     extern __shared__ float4 smem4[];
     float2 *pos = parity ? s.pos1 : s.pos0;
-    const int4 u = s.areaUnit[2 * blockIdx.x];  // triangle list, triangles, vertices, lanes
+    const int4 un = s.areaUnit[2 * blockIdx.x];  // triangle list, triangles, vertices, lanes
     const int a0base = s.areaUnit[2 * blockIdx.x + 1].x;
-    const int nt = u.y, nv = u.z, nl = u.w, w = nl + 1;  // w: vertex stride (spreads the banks)
+    const int nt = un.y, nv = un.z, nl = un.w, w = nl + 1;  // w: vertex stride (spreads the banks)
     const int lane = threadIdx.x;
+    // shared memory: the mesh's triangle list, the lanes' A0 (padded to 16
+    // bytes; the host pads each block's A0 range alike), the vertices
     int4 *idx = reinterpret_cast<int4 *>(smem4);
     float *a0 = reinterpret_cast<float *>(idx + nt);
-    float2 *sv = reinterpret_cast<float2 *>(a0 + (((size_t)nt * nl + 1) & ~(size_t)1));
-    for (int k = lane; k < nt; k += kAreaLanes) idx[k] = __ldg(s.areaIdx + u.x + k);
-    for (int k = lane; k < nt * nl; k += kAreaLanes) a0[k] = __ldg(s.areaA0 + a0base + k);
+    const int na = (nt * nl + 3) & ~3;
+    float2 *sv = reinterpret_cast<float2 *>(a0 + na);
+    for (int k = lane; k < nt; k += kAreaLanes) copy_async16(idx + k, s.areaIdx + un.x + k);
+    for (int k = lane; k < na / 4; k += kAreaLanes) copy_async16(a0 + 4 * k, s.areaA0 + a0base + 4 * k);
     // coalesced over each elastomer's vertices, stored lane-minor
     for (int j = 0; j < nl; j++) {
         const int off = s.areaLane[blockIdx.x * kAreaLanes + j];
-        for (int v = lane; v < nv; v += kAreaLanes) sv[v * w + j] = pos[off + v];
+        for (int v = lane; v < nv; v += kAreaLanes) copy_async8(sv + v * w + j, pos + off + v);
     }
+    copy_async_wait();
     __syncwarp();
-    double e = 0.0;
-    if (lane < nl) {
+    float e = 0.0f;  // a float sum, as the reference's potEnergy
+    if (lane < nl && nt > 0) {
+        // The lane's elastomer, triangle after triangle (calcAreaForcesCPU
+        // order).  The next triangle's index, A0 and vertices are read before
+        // this one stores; the vertices this one moved are passed on in
+        // registers, so the chain from triangle to triangle is arithmetic only.
         float2 *mine = sv + lane;
-        const float Lx = s.Lx, Ly = s.Ly, kA = s.kArea;
-        for (int k = 0; k < nt; k++) e += (double)area_tri(mine, w, idx[k], a0[k * nl + lane], Lx, Ly, kA);
+        const float Lx = s.Lx, Ly = s.Ly, kA = s.kArea, ca = -0.5f * kA;
+        const float hx = 0.5f * Lx, hy = 0.5f * Ly;
+        int4 t = idx[0];
+        float A0 = a0[lane];
+        float2 v0 = mine[t.x * w], v1 = mine[t.y * w], v2 = mine[t.z * w];
+        for (int k = 0; k < nt; k++) {
+            const int kn = k + 1 < nt ? k + 1 : k;
+            const int4 tn = idx[kn];
+            const float A0n = a0[kn * nl + lane];
+            float2 u0 = mine[tn.x * w], u1 = mine[tn.y * w], u2 = mine[tn.z * w];
+            // r1 and r2 moved to r0's side by the half-box rule on both axes
+            // (whatever the periodicity); the area A as float products halved
+            // (the reference halves in double, which is exact)
+            const float2 r0 = v0;
+            float2 r1 = v1, r2 = v2;
+            const float dx01 = r0.x - r1.x, dx02 = r0.x - r2.x;
+            if (dx01 > hx) r1.x += Lx;
+            if (dx01 < -hx) r1.x -= Lx;
+            if (dx02 > hx) r2.x += Lx;
+            if (dx02 < -hx) r2.x -= Lx;
+            const float dy01 = r0.y - r1.y, dy02 = r0.y - r2.y;
+            if (dy01 > hy) r1.y += Ly;
+            if (dy01 < -hy) r1.y -= Ly;
+            if (dy02 > hy) r2.y += Ly;
+            if (dy02 < -hy) r2.y -= Ly;
+            const float A = 0.5f * ((r2.y - r0.y) * (r1.x - r0.x) - (r1.y - r0.y) * (r2.x - r0.x));
+            const float dA = A - A0;
+            const float c = area_coeff(ca, dA, A0);
+            const float f1x = c * (r2.y - r0.y), f1y = -c * (r2.x - r0.x);
+            const float f2x = -c * (r1.y - r0.y), f2y = c * (r1.x - r0.x);
+            const float f0x = -f1x - f2x, f0y = -f1y - f2y;
+            // pos[p] += f[p] for p = 0, 1, 2 in turn (a repeated vertex sees
+            // the earlier addition)
+            const float2 n0 = make_float2(v0.x + f0x, v0.y + f0y);
+            const float2 b1 = t.y == t.x ? n0 : v1;
+            const float2 n1 = make_float2(b1.x + f1x, b1.y + f1y);
+            const float2 b2 = t.z == t.y ? n1 : t.z == t.x ? n0 : v2;
+            const float2 n2 = make_float2(b2.x + f2x, b2.y + f2y);
+            mine[t.x * w] = n0;
+            mine[t.y * w] = n1;
+            mine[t.z * w] = n2;
+            e += 0.5f * kA * dA * dA;
+            v0 = area_latest(tn.x, t, n0, n1, n2, u0);
+            v1 = area_latest(tn.y, t, n0, n1, n2, u1);
+            v2 = area_latest(tn.z, t, n0, n1, n2, u2);
+            t = tn;
+            A0 = A0n;
+        }
     }
     __syncwarp();
     for (int j = 0; j < nl; j++) {
         const int off = s.areaLane[blockIdx.x * kAreaLanes + j];
         for (int v = lane; v < nv; v += kAreaLanes) pos[off + v] = sv[v * w + j];
     }
-    e = warp_sum(e);
+    e = warp_sum_f(e);
     if (lane == 0) {
         bool bad = false;
-        unsigned long long q = to_fixed((float)e, bad);
+        unsigned long long q = to_fixed(e, bad);
         if (bad) atomicOr(&s.sc->nonfinite, 2);
         else if (q) atomicAdd(&s.sc->accU, q);
     }
