@@ -192,6 +192,23 @@ class System:
         self._call("femmd_get_properties", out)
         return dict(zip(self.PROPERTY_NAMES, list(out)))
 
+    def set_property_averaging(self, on=True, step_avg=1000, step_equi=10000):
+        """Properties::compute after every step: sums of the properties, closed
+        into an average and standard deviation at steps past step_equi that
+        are multiples of step_avg."""
+        self._call("femmd_set_property_averaging", int(bool(on)), int(step_avg), int(step_equi))
+
+    def average_properties(self):
+        """The last closed window (avg, stdv), the last step's values (val),
+        the steps in the open window (count), the windows closed so far and
+        the step that closed the last one."""
+        a, sd, v = (C.c_double * 10)(), (C.c_double * 10)(), (C.c_double * 10)()
+        n, w, ls = C.c_int(), C.c_int(), C.c_int()
+        self._call("femmd_get_average_properties", a, sd, v, C.byref(n), C.byref(w), C.byref(ls))
+        names = self.PROPERTY_NAMES
+        return dict(avg=dict(zip(names, list(a))), stdv=dict(zip(names, list(sd))), val=dict(zip(names, list(v))),
+                    count=n.value, windows=w.value, last_step=ls.value)
+
     def adjoint_forward(self, steps, every=20):
         self._call("femmd_adjoint_forward", int(steps), int(every))
 

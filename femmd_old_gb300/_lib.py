@@ -47,6 +47,8 @@ SIGNATURES = {
     "femmd_set_moving_wall": (i_, [P, d_, d_, d_]),
     "femmd_get_wall_forces": (i_, [P, dp, dp]),
     "femmd_get_properties": (i_, [P, dp]),
+    "femmd_set_property_averaging": (i_, [P, i_, i_, i_]),
+    "femmd_get_average_properties": (i_, [P, dp, dp, dp, C.POINTER(i_), C.POINTER(i_), C.POINTER(i_)]),
     "femmd_set_trajectory": (i_, [P, C.c_char_p, i_, i_]),
     "femmd_flush_trajectory": (i_, [P, llp]),
     "femmd_adjoint_forward": (i_, [P, i_, i_]),

@@ -173,6 +173,13 @@ struct femmd_ctx {
     DBuf<int> clusterOf;
     DBuf<double2> unf, cmPos, cmVel;
     DBuf<double> clKin, feaVir, kinTerm, clVir;
+    // per-step property averaging (Properties::compute): on/off, window
+    // length, equilibration steps, the device accumulator and its copy at
+    // the start of a run (restored when the run is repeated)
+    bool propAvg = false, propsUploaded = false, propsReset = false;
+    int propAvgEvery = 1000, propEqui = 10000, propBlocks = 0;
+    DBuf<DevProps> props, propsCk;
+    DBuf<double> propPart;
     DBuf<int> dtype, dexcl, cellOf, rank, cellCount, cellStart, blockSums, unsorted, sortedIds, nbr, nbrCount, bStart, tStart,
         tEnt;
     DBuf<int2> bEnt;
@@ -312,6 +319,8 @@ static void release_device(femmd_ctx *c) {
     c->areaUnits = 0;
     c->clRange.release(); c->clMass.release(); c->clusterOf.release(); c->unf.release(); c->cmPos.release();
     c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
+    c->props.release(); c->propsCk.release(); c->propPart.release();
+    c->propsUploaded = false;
     auto &a = c->adj;
     a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
     a.xbar.release(); a.vbar.release(); a.w0.release(); a.w1.release(); a.triD.release();
@@ -773,6 +782,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     }
     if ((st = upload_area_schedule(ctx))) return st;
+    ctx->propsUploaded = false;
     if ((st = upload_material(ctx))) return st;
     ctx->topoDirty = false;
     ctx->listBuilt = false;
@@ -850,6 +860,8 @@ static femmd_status size_list(femmd_ctx *ctx, int min_cap) {
     return alloc_list(ctx, std::max(need, min_cap));
 }
 
+static femmd_status props_buffers(femmd_ctx *ctx);
+
 static femmd_status prepare(femmd_ctx *ctx) {
     femmd_status st;
     if (!ctx->nnInit) return fail(ctx, FEMMD_NOT_READY, "init_neighbor_list() has not been called");
@@ -863,6 +875,17 @@ static femmd_status prepare(femmd_ctx *ctx) {
     if (ctx->nbrCap == 0 && (st = size_list(ctx, 0))) return st;
     if (ctx->areaForces && !ctx->areaWhy.empty())
         return fail(ctx, FEMMD_UNSUPPORTED, "area springs: %s", ctx->areaWhy.c_str());
+    if (ctx->propAvg) {
+        if (!ctx->propsUploaded) {
+            if ((st = props_buffers(ctx))) return st;
+            release_graphs(ctx);
+        }
+        if (!ctx->props.p || ctx->propsReset) {
+            CK(ctx->props.ensure(1)); CK(ctx->propsCk.ensure(1));
+            CK(cudaMemsetAsync(ctx->props.p, 0, sizeof(DevProps), ctx->stream));
+            ctx->propsReset = false;
+        }
+    }
     return FEMMD_OK;
 }
 
@@ -877,7 +900,51 @@ static femmd_status ensure_obs(femmd_ctx *ctx, int rows) {
     return FEMMD_OK;
 }
 
-// Graph of 'units' x [MID step on parity p -> IF(rebuild on 1-p)] starting at parity p.
+// Cluster ranges, masses and the cluster of each particle, and the term
+// arrays of the observables kernels.
+static femmd_status props_buffers(femmd_ctx *ctx) {
+    const int N = (int)ctx->pos.size(), nt = (int)ctx->refVol.size(), ncl = (int)ctx->clusters.size();
+    cudaStream_t sm = ctx->stream;
+    if (ncl > 0) {
+        std::vector<int2> rg(ncl);
+        std::vector<float> ms(ncl);
+        for (int c = 0; c < ncl; c++) {
+            rg[c] = make_int2(ctx->clusters[c].offset, ctx->clusters[c].nv);
+            ms[c] = ctx->clusters[c].mass;
+        }
+        CK(ctx->clRange.ensure(ncl)); CK(ctx->clMass.ensure(ncl)); CK(ctx->clusterOf.ensure(N));
+        CK(ctx->cmPos.ensure(ncl)); CK(ctx->cmVel.ensure(ncl)); CK(ctx->clKin.ensure(ncl));
+        CK(ctx->feaVir.ensure(std::max(nt, 1)));
+        CK(cudaMemcpyAsync(ctx->clRange.p, rg.data(), ncl * sizeof(int2), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(ctx->clMass.p, ms.data(), ncl * sizeof(float), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(ctx->clusterOf.p, ctx->cluster.data(), N * sizeof(int), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemsetAsync(ctx->feaVir.p, 0, sizeof(double) * std::max(nt, 1), sm));
+    }
+    CK(ctx->unf.ensure(std::max(N, 1))); CK(ctx->kinTerm.ensure(std::max(N, 1))); CK(ctx->clVir.ensure(std::max(N, 1)));
+    // the accumulator's reduction: a fixed number of blocks per system size
+    ctx->propBlocks = std::max(1, std::min(304, (N + 4095) / 4096));
+    CK(ctx->propPart.ensure(3 * (size_t)ctx->propBlocks));
+    CK(cudaStreamSynchronize(sm));  // the host vectors above are not pinned
+    ctx->propsUploaded = true;
+    return FEMMD_OK;
+}
+
+// The observables of a step that ended with LAST (positions of 'parity'),
+// then their accumulation.
+static cudaError_t enqueue_step_props(femmd_ctx *ctx, Launch &L, const DevSys &s, int parity) {
+    const float2 *pc = parity ? s.pos1 : s.pos0;
+    const int ncl = (int)ctx->clusters.size(), nt = (int)ctx->refVol.size();
+    cudaError_t e = enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p,
+                                  ctx->cmPos.p, ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p,
+                                  ctx->clVir.p);
+    if (e) return e;
+    const bool tri = ncl > 0 && s.ntri > 0 && s.feaForces;
+    return enqueue_props_accum(L, s, ctx->props.p, ctx->propPart.p, ctx->propBlocks, ncl > 0 ? ctx->clKin.p : nullptr,
+                               ncl, tri ? ctx->feaVir.p : nullptr, nt, ctx->clVir.p, ctx->propAvgEvery, ctx->propEqui);
+}
+
+// Graph of 'units' x [MID step on parity p -> IF(rebuild on 1-p)] starting at
+// parity p (with property averaging: LAST, the properties, the drift).
 static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int units) {
     gs.release();
     CK(cudaGraphCreate(&gs.g, 0));
@@ -889,7 +956,15 @@ static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int un
     for (int u = 0; u < units; u++) {
         cudaGraphConditionalHandle h;
         CK(cudaGraphConditionalHandleCreate(&h, gs.g, 0, cudaGraphCondAssignDefault));
-        CK(enqueue_step(L, s, MODE_MID, p, h, 1));
+        if (ctx->propAvg) {
+            // the step ends (LAST), its properties are accumulated, then the
+            // next step's drift: the fused MID step's arithmetic, split
+            CK(enqueue_step(L, s, MODE_LAST, p, h, 1));
+            CK(enqueue_step_props(ctx, L, s, p));
+            CK(enqueue_drift_in_run(L, s, p));
+        } else {
+            CK(enqueue_step(L, s, MODE_MID, p, h, 1));
+        }
         Launch body;
         CK(L.begin_if(h, body));
         CK(enqueue_rebuild(body, s, 1 - p, 1));
@@ -910,7 +985,13 @@ static femmd_status launch_units(femmd_ctx *ctx, int units, bool use_graphs) {
             L.event_pool = &ctx->eventPool;
         }
         for (int u = 0; u < units; u++) {
-            CK(enqueue_step(L, s, MODE_MID, ctx->cur, 0, 0));
+            if (ctx->propAvg) {
+                CK(enqueue_step(L, s, MODE_LAST, ctx->cur, 0, 0));
+                CK(enqueue_step_props(ctx, L, s, ctx->cur));
+                CK(enqueue_drift_in_run(L, s, ctx->cur));
+            } else {
+                CK(enqueue_step(L, s, MODE_MID, ctx->cur, 0, 0));
+            }
             CK(enqueue_rebuild(L, s, 1 - ctx->cur, 1));
             ctx->cur ^= 1;
         }
@@ -1217,6 +1298,7 @@ static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
         Launch D = L;
         D.kernels = 0;
         CK(enqueue_step(D, s, MODE_LAST, ctx->cur, 0, 0));
+        if (ctx->propAvg) CK(enqueue_step_props(ctx, D, s, ctx->cur));
         if ((st = traj_snapshot(ctx, m, aborted))) return st;
         if (aborted) return FEMMD_OK;
         CK(enqueue_step(D, s, MODE_FIRST, ctx->cur, 0, 0));
@@ -1230,6 +1312,7 @@ static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
     Launch T2 = L;
     T2.kernels = 0;
     CK(enqueue_step(T2, s, MODE_LAST, ctx->cur, 0, 0));
+    if (ctx->propAvg) CK(enqueue_step_props(ctx, T2, s, ctx->cur));
     ctx->profKernels += T2.kernels;
     if (!frames.empty() && frames.back() == s0 + n && (st = traj_snapshot(ctx, s0 + n, aborted))) return st;
     return FEMMD_OK;
@@ -1773,6 +1856,8 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(ctx->ckPos.p, pc, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckVel.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckAcc.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (ctx->propAvg)
+            CK(cudaMemcpyAsync(ctx->propsCk.p, ctx->props.p, sizeof(DevProps), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));  // overflow, nonfinite, outside
         if (ctx->tracing)
             CK(cudaMemsetAsync(ctx->trace.p, 0, (size_t)ctx->obsCap * kTraceCols * sizeof(unsigned long long),
@@ -1801,6 +1886,8 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(pd, ctx->ckPos.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->dvel.p, ctx->ckVel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->dacc.p, ctx->ckAcc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (ctx->propAvg)
+            CK(cudaMemcpyAsync(ctx->props.p, ctx->propsCk.p, sizeof(DevProps), cudaMemcpyDeviceToDevice, ctx->stream));
         int need = std::max(ctx->hsc->maxCount, ctx->nbrCap + ctx->nbrCap / 2);
         if ((st = alloc_list(ctx, need + need / 4 + 8))) return st;
     }
@@ -1821,6 +1908,7 @@ femmd_status femmd_do_step(femmd_ctx *ctx) {
     ctx->cur ^= 1;
     CK(enqueue_rebuild(L, s, ctx->cur, 1));
     CK(enqueue_step(L, s, MODE_LAST, ctx->cur, 0, 0));
+    if (ctx->propAvg) CK(enqueue_step_props(ctx, L, s, ctx->cur));
     if ((st = read_scalars(ctx))) return st;
     ctx->steps++;
     ctx->staleMask |= kPos | kVel | kAcc | kForce;
@@ -2258,22 +2346,7 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
     for (int k = 0; k < 10; k++) out[k] = 0.0;
     if (N == 0) return FEMMD_OK;
     cudaStream_t sm = ctx->stream;
-    if (ncl > 0) {
-        std::vector<int2> rg(ncl);
-        std::vector<float> ms(ncl);
-        for (int c = 0; c < ncl; c++) {
-            rg[c] = make_int2(ctx->clusters[c].offset, ctx->clusters[c].nv);
-            ms[c] = ctx->clusters[c].mass;
-        }
-        CK(ctx->clRange.ensure(ncl)); CK(ctx->clMass.ensure(ncl)); CK(ctx->clusterOf.ensure(N));
-        CK(ctx->cmPos.ensure(ncl)); CK(ctx->cmVel.ensure(ncl)); CK(ctx->clKin.ensure(ncl));
-        CK(ctx->feaVir.ensure(std::max(nt, 1)));
-        CK(cudaMemcpyAsync(ctx->clRange.p, rg.data(), ncl * sizeof(int2), cudaMemcpyHostToDevice, sm));
-        CK(cudaMemcpyAsync(ctx->clMass.p, ms.data(), ncl * sizeof(float), cudaMemcpyHostToDevice, sm));
-        CK(cudaMemcpyAsync(ctx->clusterOf.p, ctx->cluster.data(), N * sizeof(int), cudaMemcpyHostToDevice, sm));
-        CK(cudaMemsetAsync(ctx->feaVir.p, 0, sizeof(double) * std::max(nt, 1), sm));
-    }
-    CK(ctx->unf.ensure(N)); CK(ctx->kinTerm.ensure(N)); CK(ctx->clVir.ensure(N));
+    if ((st = props_buffers(ctx))) return st;
     DevSys s = make_sys(ctx);
     const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
     Launch L;
@@ -2307,6 +2380,44 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
     out[7] = ncl > 0 ? 0.5 * clusterKin / ncl : 0.0;
     out[8] = clusterVirial;
     out[9] = 0.5 * clusterKin / V - 0.5 * clusterVirial / V;
+    return FEMMD_OK;
+}
+
+// Properties::compute (properties.cpp:85-95) at the end of every step of
+// run() and do_step(): with on != 0 the properties of femmd_get_properties
+// are evaluated after each step and accumulated; at steps past step_equi
+// that are multiples of step_avg the window's average and standard deviation
+// are kept and a new window starts (the reference's defaults: 1000, 10000).
+// Switching on (again) starts from empty sums.
+femmd_status femmd_set_property_averaging(femmd_ctx *ctx, int on, int step_avg, int step_equi) {
+    NEED(ctx);
+    if (on && (step_avg <= 0 || step_equi < 0))
+        return fail(ctx, FEMMD_INVALID_ARG, "step_avg must be > 0 and step_equi >= 0");
+    ctx->propAvg = on != 0;
+    if (on) {
+        ctx->propAvgEvery = step_avg;
+        ctx->propEqui = step_equi;
+        ctx->propsReset = true;
+    }
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_average_properties(femmd_ctx *ctx, double *avg, double *stdv, double *val, int *count,
+                                          int *windows, int *last_step) {
+    NEED(ctx);
+    if (!ctx->props.p || ctx->propsReset) return fail(ctx, FEMMD_NOT_READY, "no step has been averaged");
+    DevProps P;
+    CK(cudaMemcpyAsync(&P, ctx->props.p, sizeof(DevProps), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < kNumProps; k++) {
+        if (avg) avg[k] = P.avg[k];
+        if (stdv) stdv[k] = P.stdv[k];
+        if (val) val[k] = P.val[k];
+    }
+    if (count) *count = P.count;
+    if (windows) *windows = P.windows;
+    if (last_step) *last_step = P.lastStep;
     return FEMMD_OK;
 }
 

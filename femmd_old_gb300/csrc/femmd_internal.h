@@ -154,6 +154,9 @@ cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
 // leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
+// The same drift inside a run: the step counter advances by one (the drift
+// makes x_{n+1}) instead of being set from stepBase.
+cudaError_t enqueue_drift_in_run(Launch &L, const DevSys &s, int parity);
 // Allow the area-spring kernel 'bytes' of dynamic shared memory.
 cudaError_t area_smem_setup(int bytes);
 
@@ -171,6 +174,24 @@ cudaError_t enqueue_adj_step(Launch &L, const DevSys &s, const float2 *pos, cons
 
 // ---- observables (k_props.cu): cluster unfolding, centre of mass and
 // velocity, feaVirial and cluster-virial terms, m v^2 per particle
+// Properties::compute (properties.cpp:85-95) on the device: the values of
+// Properties::evaluate at the end of each step, their window sums, and the
+// last completed window's average and standard deviation (Prop,
+// properties.h:5-13).  Order of the values: uKinetic, uPotential, uTotal,
+// temperature, virial, feaVirial, pressure, clusterUKinetic, clusterVirial,
+// molPressure.
+constexpr int kNumProps = 10;
+struct DevProps {
+    double val[kNumProps], sum[kNumProps], sum2[kNumProps], avg[kNumProps], stdv[kNumProps];
+    int count, windows, lastStep;
+    unsigned ticket;
+};
+// After a step's LAST: reduce the term arrays of enqueue_props (fixed slices
+// per block, added in block order by the last block), evaluate, accumulate,
+// and close a window at steps past stepEqui that are multiples of stepAvg.
+cudaError_t enqueue_props_accum(Launch &L, const DevSys &s, DevProps *P, double *partials, int blocks,
+                                const double *clKin, int ncl, const double *feaVir, int ntri, const double *clVir,
+                                int stepAvg, int stepEqui);
 cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
                           const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
                           double *clKin, double *feaVir, double *kin, double *clVir);

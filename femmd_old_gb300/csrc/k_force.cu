@@ -340,12 +340,15 @@ __global__ void __launch_bounds__(kStepBlock, MT ? 16 : 12) k_step(DevSys s, int
     }
 }
 
-// leapFrogStep1 + applyPBC on their own (c_doStep entry)
-__global__ void __launch_bounds__(kBlock) k_drift(DevSys s, int parity) {
+// leapFrogStep1 + applyPBC on their own: the c_doStep entry (the step
+// counter becomes stepBase + 1), or inside a run after a step that ended with
+// LAST (the counter advances); the same float operations as the fused drift
+// of k_step
+__global__ void __launch_bounds__(kBlock) k_drift(DevSys s, int parity, int advance) {
     const float2 *pin = parity ? s.pos1 : s.pos0;
     float2 *pout = parity ? s.pos0 : s.pos1;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) s.sc->stepNow = s.stepBase + 1;
+    if (i == 0) s.sc->stepNow = advance ? s.sc->stepNow + 1 : s.stepBase + 1;
     if (i >= s.N) return;
     float2 v = s.vel[i], a = s.acc[i], p = pin[i];
     v.x += s.hdt * a.x;
@@ -404,7 +407,11 @@ cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaG
 }
 
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity) {
-    return L.kernel(k_drift, dim3(force_blocks(s.N)), dim3(kBlock), 0, s, parity);
+    return L.kernel(k_drift, dim3(force_blocks(s.N)), dim3(kBlock), 0, s, parity, 0);
+}
+
+cudaError_t enqueue_drift_in_run(Launch &L, const DevSys &s, int parity) {
+    return L.kernel(k_drift, dim3(force_blocks(s.N)), dim3(kBlock), 0, s, parity, 1);
 }
 
 }  // namespace femmd

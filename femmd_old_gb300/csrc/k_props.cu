@@ -193,6 +193,86 @@ __global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const f
     clVir[i] = cv;
 }
 
+// Properties::compute (properties.cpp:85-95) after a step: block b sums a
+// fixed slice of the cluster-virial, feaVirial and cluster-kinetic terms;
+// the grid's last block adds the slices in block order (the same result on
+// every run), forms Properties::evaluate (properties.cpp:15-36) with the
+// step's U, W and sum m v^2, then Properties::accumulate(1)
+// (properties.cpp:56-70) and, at steps past stepEqui that are multiples of
+// stepAvg, accumulate(2) and accumulate(0): the window's average and
+// standard deviation, sqrt(max(sum2/n - avg^2, 0)) (properties.h:11), and a
+// new window.
+__global__ void __launch_bounds__(kBlock) k_props_accum(DevSys s, DevProps *P, double *part, const double *clKin,
+                                                        int ncl, const double *feaVir, int ntri, const double *clVir,
+                                                        int stepAvg, int stepEqui) {
+    __shared__ double dscr[32];
+    __shared__ bool last;
+    const int nb = gridDim.x, b = blockIdx.x;
+    const int n3[3] = {s.N, feaVir ? ntri : 0, clKin ? ncl : 0};
+    const double *arr[3] = {clVir, feaVir, clKin};
+    for (int k = 0; k < 3; k++) {
+        const int per = (n3[k] + nb - 1) / nb, lo = min(n3[k], b * per), hi = min(n3[k], lo + per);
+        double a = 0.0;
+        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) a += arr[k][i];
+        a = block_sum_d(a, dscr);
+        if (threadIdx.x == 0) part[3 * b + k] = a;
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&P->ticket, 1u) == (unsigned)nb - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double cv = 0.0, fv = 0.0, ck = 0.0;
+    for (int q = 0; q < nb; q++) {
+        cv += part[3 * q];
+        fv += part[3 * q + 1];
+        ck += part[3 * q + 2];
+    }
+    const DevScalars *sc = s.sc;
+    const double N = (double)s.N, V = (double)s.Lx * (double)s.Ly, KE = sc->KE, W = sc->W;
+    double v[kNumProps];
+    v[0] = 0.5 * KE / N;
+    v[1] = sc->U / N;
+    v[2] = v[0] + v[1];
+    v[3] = v[0];
+    v[4] = W;
+    v[5] = fv;
+    v[6] = 0.5 * KE / V + 0.5 * (W + fv) / V;
+    v[7] = ncl > 0 ? 0.5 * ck / ncl : 0.0;
+    v[8] = cv;
+    v[9] = 0.5 * ck / V - 0.5 * cv / V;
+    P->count += 1;
+    for (int k = 0; k < kNumProps; k++) {
+        P->val[k] = v[k];
+        P->sum[k] += v[k];
+        P->sum2[k] += v[k] * v[k];
+    }
+    const int step = sc->stepNow;
+    if (step > stepEqui && stepAvg > 0 && step % stepAvg == 0) {
+        const double n = (double)P->count;
+        for (int k = 0; k < kNumProps; k++) {
+            const double a = P->sum[k] / n;
+            P->avg[k] = a;
+            P->stdv[k] = sqrt(fmax(P->sum2[k] / n - a * a, 0.0));
+            P->sum[k] = 0.0;
+            P->sum2[k] = 0.0;
+        }
+        P->count = 0;
+        P->windows += 1;
+        P->lastStep = step;
+    }
+    P->ticket = 0;
+}
+
+cudaError_t enqueue_props_accum(Launch &L, const DevSys &s, DevProps *P, double *partials, int blocks,
+                                const double *clKin, int ncl, const double *feaVir, int ntri, const double *clVir,
+                                int stepAvg, int stepEqui) {
+    return L.kernel(k_props_accum, dim3(blocks), dim3(kBlock), 0, s, P, partials, clKin, ncl, feaVir, ntri, clVir,
+                    stepAvg, stepEqui);
+}
+
 cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
                           const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
                           double *clKin, double *feaVir, double *kin, double *clVir) {

@@ -290,6 +290,22 @@ femmd_status femmd_flush_trajectory(femmd_ctx *ctx, long long *frames_written);
  * sums pairs of two cluster particles (the reference indexes clusters[-1] for
  * free particles). */
 femmd_status femmd_get_properties(femmd_ctx *ctx, double *out);
+/* Properties::compute (properties.cpp:85-95), run after every doStep
+ * (integrator.cpp:18): with on != 0 the ten values of femmd_get_properties
+ * are evaluated at the end of every step of run() and do_step() and summed;
+ * at steps past step_equi that are multiples of step_avg the window's
+ * average and standard deviation (Prop::avg, properties.h:11) are kept and a
+ * new window starts (accumulate(2), accumulate(0)).  The reference's
+ * defaults are step_avg 1000, step_equi 10000.  Switching on starts from
+ * empty sums.  Each averaged step costs the observables kernels on top of the
+ * step.  System.print_props (interface.cpp:270-286) prints the averages. */
+femmd_status femmd_set_property_averaging(femmd_ctx *ctx, int on, int step_avg, int step_equi);
+/* The last completed window's averages and standard deviations, the last
+ * step's values, the steps summed in the open window, the windows closed so
+ * far and the step that closed the last one (any pointer may be NULL; arrays
+ * of 10 in femmd_get_properties' order). */
+femmd_status femmd_get_average_properties(femmd_ctx *ctx, double *avg, double *stdv, double *val, int *count,
+                                          int *windows, int *last_step);
 
 /* ------------------------------------------------------------ adjoint */
 /* Gradients of an observable of the final state through the whole run, by the

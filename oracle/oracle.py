@@ -104,6 +104,39 @@ def _ptr(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
+class PropertyAverages:
+    """Properties::compute (src/properties.cpp:85-95) with Prop
+    (src/properties.h:5-13), for values given per step: accumulate(1) adds
+    val and val^2 and counts the step; at steps past step_equi that are
+    multiples of step_avg, accumulate(2) sets avgval = sum / n and
+    stdv = sqrt(max(sum2 / n - avgval^2, 0)), then accumulate(0) clears the
+    sums and the count.  (evalClusterRdf, also called there, is out of
+    scope.)"""
+
+    def __init__(self, names, step_avg=1000, step_equi=10000):
+        self.names, self.step_avg, self.step_equi = tuple(names), step_avg, step_equi
+        self.count, self.windows, self.last_step = 0, 0, 0
+        self.sum = dict.fromkeys(self.names, 0.0)
+        self.sum2 = dict.fromkeys(self.names, 0.0)
+        self.avg = dict.fromkeys(self.names, 0.0)
+        self.stdv = dict.fromkeys(self.names, 0.0)
+
+    def compute(self, step, vals):
+        self.count += 1
+        for k in self.names:
+            self.sum[k] += vals[k]
+            self.sum2[k] += vals[k] * vals[k]
+        if step > self.step_equi and step % self.step_avg == 0:
+            for k in self.names:
+                a = self.sum[k] / self.count
+                self.avg[k] = a
+                self.stdv[k] = max(self.sum2[k] / self.count - a * a, 0.0) ** 0.5
+                self.sum[k] = self.sum2[k] = 0.0
+            self.count = 0
+            self.windows += 1
+            self.last_step = step
+
+
 class Oracle:
     """CPU restatement of the reference timestep with the System method names.
 

@@ -66,3 +66,104 @@ def test_properties_disks_across_the_boundary():
 def test_properties_mixed_solvent():
     # free particles are left out of the cluster virial on both sides
     compare(S.mixed_replica(3000, 0.75, 1.0, seed=3), 60)
+
+
+# ------------------------------------------------------------- averaging
+#
+# femmd_set_property_averaging (Properties::compute after every step) against
+# the per-step values of femmd_get_properties fed through the oracle's
+# restatement of the reference's window logic (oracle.PropertyAverages).
+# The device sums m v^2 as float block sums in fixed point, the per-step
+# evaluation in FP64, so the kinetic terms differ by ~1e-7 relative: averages
+# within 1e-6 of the largest per-step magnitude of that property, variances
+# within 1e-5 of its square; counters exact.
+
+def _per_step_reference(sc, segments, step_avg, step_equi):
+    """The per-step values of a system stepped with do_step, each segment
+    started by run(0) as a run() call starts (forced rebuild, forces)."""
+    from oracle import PropertyAverages
+    b = F.System(0)
+    sc.replay(b)
+    b.run(0)
+    acc = PropertyAverages(F.System.PROPERTY_NAMES, step_avg, step_equi)
+    mags = dict.fromkeys(F.System.PROPERTY_NAMES, 0.0)
+    n = 0
+    for seg in segments:
+        b.run(0)
+        for _ in range(seg):
+            b.do_step()
+            n += 1
+            v = b.properties()
+            for k in mags:
+                mags[k] = max(mags[k], abs(v[k]))
+            acc.compute(n, v)
+    return acc, mags, b
+
+
+def _check(got, acc, mags):
+    assert got["windows"] == acc.windows and got["last_step"] == acc.last_step and got["count"] == acc.count
+    for k in acc.names:
+        m = mags[k] + 1e-300
+        assert abs(got["avg"][k] - acc.avg[k]) <= 1e-6 * m, (k, got["avg"][k], acc.avg[k])
+        assert abs(got["stdv"][k] ** 2 - acc.stdv[k] ** 2) <= 1e-5 * m * m, (k, got["stdv"][k], acc.stdv[k])
+
+
+def test_property_averages_match_per_step_evaluation():
+    sc = S.suspension(n_side=3, phi=0.62, center_jitter=0.3, T=0.3)
+    acc, mags, b = _per_step_reference(sc, (57, 43), 20, 30)
+    a = F.System(0)
+    sc.replay(a)
+    a.set_property_averaging(True, 20, 30)
+    a.run(0)
+    a.run(57)   # windows close at steps 40 and 60 (past 30, multiples of 20),
+    a.run(43)   # 80 and 100, across run() calls as in the reference
+    got = a.average_properties()
+    assert acc.windows == 4 and acc.last_step == 100
+    _check(got, acc, mags)
+    for k in ("virial", "feaVirial", "clusterVirial", "pressure"):
+        assert acc.stdv[k] > 0 and got["stdv"][k] > 0
+    # averaging splits each step (LAST, properties, drift) with the fused
+    # step's arithmetic: the trajectory is unchanged bit for bit
+    for x, y in zip(a.get_state(), b.get_state()):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    plain = F.System(0)
+    sc.replay(plain)
+    plain.run(0)
+    plain.run(57)
+    plain.run(43)
+    for x, y in zip(a.get_state(), plain.get_state()):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_property_averaging_survives_a_repeated_run():
+    # a run repeated after a list overflow restores the sums from its start
+    sc = S.lj_fluid(n_side=24)
+    acc, mags, _ = _per_step_reference(sc, (60,), 10, 0)
+    a = F.System(0)
+    sc.replay(a)
+    a.set_property_averaging(True, 10, 0)
+    a.run(0)
+    a.set_neighbor_capacity(2)
+    a.run(60)
+    assert a.neighbor_capacity() > 2
+    _check(a.average_properties(), acc, mags)
+
+
+def test_property_averaging_with_do_step_and_frames(tmp_path):
+    # do_step and trajectory frames end steps on their own paths; the open
+    # window's count and the last step's values follow them
+    sc = S.suspension(n_side=2, rings=3, T=0.3)
+    acc, mags, _ = _per_step_reference(sc, (35,), 1000, 10000)
+    a = F.System(0)
+    sc.replay(a)
+    a.set_property_averaging(True)
+    a.set_trajectory(str(tmp_path / "t.dump"), 7, 0)
+    a.run(0)
+    a.run(30)
+    for _ in range(5):
+        a.do_step()
+    got = a.average_properties()
+    assert got["count"] == 35 and got["windows"] == 0
+    last = a.properties()
+    for k in acc.names:
+        assert abs(got["val"][k] - last[k]) <= 1e-6 * (mags[k] + 1e-300), k
