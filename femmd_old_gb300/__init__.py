@@ -192,6 +192,15 @@ class System:
         self._call("femmd_get_properties", out)
         return dict(zip(self.PROPERTY_NAMES, list(out)))
 
+    def clusters(self):
+        """FeaElements::calcClusterProps: per elastomer the centre of mass and
+        its velocity (unfolded) and the periodic centroid, each (n, 2)."""
+        n = int(self.info()["nelastomers"])
+        cm, cv, ce = (np.zeros((max(n, 1), 2)) for _ in range(3))
+        if n:
+            self._call("femmd_get_clusters", _d(cm), _d(cv), _d(ce))
+        return dict(cm=cm[:n], cm_vel=cv[:n], centroid=ce[:n])
+
     def set_property_averaging(self, on=True, step_avg=1000, step_equi=10000):
         """Properties::compute after every step: sums of the properties, closed
         into an average and standard deviation at steps past step_equi that

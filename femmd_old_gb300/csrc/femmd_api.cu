@@ -171,7 +171,7 @@ struct femmd_ctx {
     DBuf<int2> clRange;
     DBuf<float> clMass;
     DBuf<int> clusterOf;
-    DBuf<double2> unf, cmPos, cmVel;
+    DBuf<double2> unf, cmPos, cmVel, centroid;
     DBuf<double> clKin, feaVir, kinTerm, clVir;
     // per-step property averaging (Properties::compute): on/off, window
     // length, equilibration steps, the device accumulator and its copy at
@@ -319,7 +319,7 @@ static void release_device(femmd_ctx *c) {
     c->areaUnits = 0;
     c->clRange.release(); c->clMass.release(); c->clusterOf.release(); c->unf.release(); c->cmPos.release();
     c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
-    c->props.release(); c->propsCk.release(); c->propPart.release();
+    c->props.release(); c->propsCk.release(); c->propPart.release(); c->centroid.release();
     c->propsUploaded = false;
     auto &a = c->adj;
     a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
@@ -2380,6 +2380,33 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
     out[7] = ncl > 0 ? 0.5 * clusterKin / ncl : 0.0;
     out[8] = clusterVirial;
     out[9] = 0.5 * clusterKin / V - 0.5 * clusterVirial / V;
+    return FEMMD_OK;
+}
+
+// FeaElements::calcClusterProps (feaElements.cpp:199-204) at the current
+// state: unfoldPos's centre of mass and its velocity per cluster, and the
+// periodic centroid of updateClustersCentroid; 2 doubles per cluster each
+// (NULL to skip).
+femmd_status femmd_get_clusters(femmd_ctx *ctx, double *cm, double *cm_vel, double *centroid) {
+    NEED(ctx);
+    femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    const int N = (int)ctx->pos.size(), ncl = (int)ctx->clusters.size();
+    if (N == 0 || ncl == 0) return FEMMD_OK;
+    if ((st = props_buffers(ctx))) return st;
+    CK(ctx->centroid.ensure(ncl));
+    DevSys s = make_sys(ctx);
+    const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
+    Launch L;
+    L.stream = ctx->stream;
+    CK(enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p, ctx->cmPos.p,
+                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p));
+    CK(enqueue_cluster_centroid(L, s, pc, ncl, ctx->clRange.p, ctx->centroid.p));
+    if (cm) CK(cudaMemcpyAsync(cm, ctx->cmPos.p, ncl * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    if (cm_vel) CK(cudaMemcpyAsync(cm_vel, ctx->cmVel.p, ncl * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    if (centroid)
+        CK(cudaMemcpyAsync(centroid, ctx->centroid.p, ncl * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return FEMMD_OK;
 }
 

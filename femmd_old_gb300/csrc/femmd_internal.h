@@ -180,6 +180,8 @@ cudaError_t enqueue_adj_step(Launch &L, const DevSys &s, const float2 *pos, cons
 // properties.h:5-13).  Order of the values: uKinetic, uPotential, uTotal,
 // temperature, virial, feaVirial, pressure, clusterUKinetic, clusterVirial,
 // molPressure.
+cudaError_t enqueue_cluster_centroid(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
+                                     double2 *centroid);
 constexpr int kNumProps = 10;
 struct DevProps {
     double val[kNumProps], sum[kNumProps], sum2[kNumProps], avg[kNumProps], stdv[kNumProps];

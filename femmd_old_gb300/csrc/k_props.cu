@@ -112,6 +112,43 @@ __global__ void k_props_cluster(DevSys s, const float2 *pos, const int2 *clRange
     }
 }
 
+// FeaElements::updateClustersCentroid (feaElements.cpp:162-197): the
+// centroid of a cluster in a periodic box from the mean of (cos, sin) of
+// 2 pi x / L per axis, x_c = L (atan2(-<sin>, -<cos>) + pi) / (2 pi).  In
+// FP64.  The reference averages the x sums again for y (feaElements.cpp:
+// 192-193); here each axis uses its own sums.
+__global__ void k_cluster_centroid(DevSys s, const float2 *pos, const int2 *clRange, double2 *centroid) {
+    __shared__ double dscr[32];
+    const int c = blockIdx.x;
+    const int off = clRange[c].x, n = clRange[c].y;
+    double cx = 0.0, sx = 0.0, cy = 0.0, sy = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 p = pos[off + k];
+        double sn, cs;
+        sincospi(2.0 * (double)p.x / (double)s.Lx, &sn, &cs);
+        cx += cs;
+        sx += sn;
+        sincospi(2.0 * (double)p.y / (double)s.Ly, &sn, &cs);
+        cy += cs;
+        sy += sn;
+    }
+    cx = block_sum_d(cx, dscr);
+    sx = block_sum_d(sx, dscr);
+    cy = block_sum_d(cy, dscr);
+    sy = block_sum_d(sy, dscr);
+    if (threadIdx.x == 0) {
+        const double pi = 3.14159265358979323846;
+        const double tx = atan2(-sx / n, -cx / n) + pi, ty = atan2(-sy / n, -cy / n) + pi;
+        centroid[c] = make_double2((double)s.Lx * tx / (2.0 * pi), (double)s.Ly * ty / (2.0 * pi));
+    }
+}
+
+cudaError_t enqueue_cluster_centroid(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
+                                     double2 *centroid) {
+    if (ncl <= 0) return cudaSuccess;
+    return L.kernel(k_cluster_centroid, dim3(ncl), dim3(128), 0, s, pos, clRange, centroid);
+}
+
 // feaVirial terms: per triangle sum over its vertices of f . unfolded position
 // (interactions.cpp:681), with the nodal forces of the last force evaluation.
 __global__ void __launch_bounds__(kBlock) k_props_tri(DevSys s, const double2 *unf, double *feaVir) {

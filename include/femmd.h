@@ -300,6 +300,13 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out);
  * empty sums.  Each averaged step costs the observables kernels on top of the
  * step.  System.print_props (interface.cpp:270-286) prints the averages. */
 femmd_status femmd_set_property_averaging(femmd_ctx *ctx, int on, int step_avg, int step_equi);
+/* FeaElements::calcClusterProps (feaElements.cpp:199-204) at the current
+ * state: per cluster (elastomer, in add order) the centre of mass of the
+ * unfolded vertices and its velocity (unfoldPos, :86-150) and the periodic
+ * centroid from the mean angle per axis (updateClustersCentroid, :162-197;
+ * the reference's y uses the x sums, here y uses its own).  2 doubles per
+ * cluster in each array; a NULL array is skipped. */
+femmd_status femmd_get_clusters(femmd_ctx *ctx, double *cm, double *cm_vel, double *centroid);
 /* The last completed window's averages and standard deviations, the last
  * step's values, the steps summed in the open window, the windows closed so
  * far and the step that closed the last one (any pointer may be NULL; arrays

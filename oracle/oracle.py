@@ -104,6 +104,36 @@ def _ptr(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
+def cluster_props(pos, vel, mass, ranges, Lx, Ly):
+    """FeaElements::calcClusterProps (src/feaElements.cpp:199-204) in FP64 on
+    float positions: unfoldPos (:86-150) -- a cluster wider than half the box
+    has its vertices beyond L/2 moved down by L, and all moved up by L again
+    when their mean is negative -- then the mass-weighted centre and
+    velocity; updateClustersCentroid (:162-197) -- L (atan2(-<sin>, -<cos>)
+    + pi) / (2 pi) of the angles 2 pi x / L -- with each axis on its own sums
+    (the reference reuses the x sums for y)."""
+    pos = np.asarray(pos, np.float32)
+    out = {"cm": [], "cm_vel": [], "centroid": []}
+    L = (np.float32(Lx), np.float32(Ly))
+    for off, n in ranges:
+        p, v, m = pos[off:off + n], np.asarray(vel[off:off + n], np.float64), np.asarray(mass[off:off + n], np.float64)
+        u = p.astype(np.float64)
+        for a in range(2):
+            if p[:, a].max() - p[:, a].min() > L[a] / np.float32(2):
+                u[:, a] = np.where(p[:, a] > L[a] / np.float32(2), u[:, a] - float(L[a]), u[:, a])
+                if u[:, a].sum() / n < 0:
+                    u[:, a] += float(L[a])
+        M = m.sum()
+        out["cm"].append((m[:, None] * u).sum(0) / M)
+        out["cm_vel"].append((m[:, None] * v).sum(0) / M)
+        c = []
+        for a in range(2):
+            t = 2.0 * np.pi * p[:, a].astype(np.float64) / float(L[a])
+            c.append(float(L[a]) * (np.arctan2(-np.sin(t).mean(), -np.cos(t).mean()) + np.pi) / (2.0 * np.pi))
+        out["centroid"].append(c)
+    return {k: np.array(v) for k, v in out.items()}
+
+
 class PropertyAverages:
     """Properties::compute (src/properties.cpp:85-95) with Prop
     (src/properties.h:5-13), for values given per step: accumulate(1) adds

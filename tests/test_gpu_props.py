@@ -167,3 +167,48 @@ def test_property_averaging_with_do_step_and_frames(tmp_path):
     last = a.properties()
     for k in acc.names:
         assert abs(got["val"][k] - last[k]) <= 1e-6 * (mags[k] + 1e-300), k
+
+
+# ------------------------------------------------------------- cluster props
+
+def _ranges(sc):
+    off, out = 0, []
+    for name, args in sc.calls:
+        if name == "add_elastomer":
+            n = len(args[0]) // 2 if np.ndim(args[0]) == 1 else len(args[0])
+            out.append((off, n))
+            off += n
+    return out
+
+
+@pytest.mark.parametrize("case", ["dense", "crossing"])
+def test_cluster_centres_and_centroids(case):
+    """femmd_get_clusters against the oracle's FP64 restatement on the same
+    float state: centres of mass and centroids within 1e-6 of the box, centre
+    velocities within 1e-6 of the largest vertex speed."""
+    from oracle import cluster_props
+    if case == "dense":
+        sc = S.suspension(n_side=3, phi=0.62, center_jitter=0.3, T=0.3)
+        steps = 200
+    else:
+        sc, _ = G.load("susp_crossing")
+        sc.calls = sc.calls[:[n for n, _ in sc.calls].index("dump_setup")]
+        steps = 300
+    s = F.System(0)
+    sc.replay(s)
+    s.run(0)
+    s.run(steps)
+    got = s.clusters()
+    Lx, Ly = sc.calls[0][1]
+    ref = cluster_props(s.positions(), s.velocities(), s.masses(), _ranges(sc), Lx, Ly)
+    L = np.array([Lx, Ly])
+    assert np.abs(got["cm"] - ref["cm"]).max() <= 1e-6 * L.max()
+    vmax = np.abs(s.velocities()).max()
+    assert np.abs(got["cm_vel"] - ref["cm_vel"]).max() <= 1e-6 * vmax
+    d = got["centroid"] - ref["centroid"]
+    d -= L * np.round(d / L)
+    assert np.abs(d).max() <= 1e-6 * L.max()
+    if case == "crossing":
+        # a disk straddles the edge: its centre lies within a radius of it
+        # and the unfold moved it, the centroid sits inside the box
+        assert ((got["centroid"] >= 0) & (got["centroid"] <= L)).all()
