@@ -173,25 +173,68 @@ __global__ void __launch_bounds__(kBlock) k_cell_place(DevSys s, int parity, int
 // take the particles in cell order (slot t of cellSorted), so the lanes of a
 // warp sit in the same or adjacent cells of one column and walk nearly the
 // same candidate ranges; each particle's list is still its own column.
+//
+// A warp whose 32 slots lie in one cell column, away from the y edges,
+// first copies the candidates of its three stencil columns (one contiguous
+// slot window per column) into shared memory with coalesced loads; its lanes
+// then walk their own ranges there, in the same order.  Other warps walk
+// cellSorted directly.
+constexpr int kWinCap = 256;  // staged candidates per warp (16 bytes each)
+
 __global__ void __launch_bounds__(kNnBlock) k_build_nn(DevSys s, int parity, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    __shared__ float4 win[kNnBlock / 32][kWinCap];
     const float2 *pos = parity ? s.pos1 : s.pos0;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool fast = fast_walk_ok(s);
+    const bool fast = fast_walk_ok(s);  // the same for the whole grid
     int k = 0;
-    if (t < s.N) {
-        if (fast) {
-            const float4 me = __ldg(s.cellSorted + t);  // position, tag and group of the slot's particle
-            const int i = __float_as_int(me.z) & kIdMask;
-            k = build_fast_at<true>(s, i, s.cellOf[i], make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
-                                    (size_t)s.Ncap);
-            s.nbrCount[i] = k;
-        } else {
-            const int i = t;
-            k = fast ? build_fast<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
-                     : build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
-            s.nbrCount[i] = k;
+    if (fast) {
+        const bool valid = t < s.N;
+        const float4 me = valid ? __ldg(s.cellSorted + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int i = __float_as_int(me.z) & kIdMask;
+        // the cell the binning gave the particle, from the same position
+        int ix, iy;
+        cell_xy(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
+        const int ncy = s.ncy;
+        int qb[3] = {0, 0, 0}, qe[3] = {0, 0, 0};
+        float sx[3] = {0.f, 0.f, 0.f};
+        if (valid && iy >= 1 && iy <= ncy - 2) stencil_columns(s, ix, iy, qb, qe, sx);
+        // slots are in cell order: ix and iy do not decrease along the warp,
+        // so lane 0's range starts and lane 31's range ends bound the windows
+        const unsigned all = __ballot_sync(0xffffffffu, valid);
+        const int ixa = __shfl_sync(0xffffffffu, ix, 0), ixb = __shfl_sync(0xffffffffu, ix, 31);
+        const int iya = __shfl_sync(0xffffffffu, iy, 0), iyb = __shfl_sync(0xffffffffu, iy, 31);
+        bool staged = all == 0xffffffffu && ixa == ixb && iya >= 1 && iyb <= ncy - 2;
+        int wb[3], wo[3], wl[3];
+        if (staged) {
+            int tot = 0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                wb[d] = __shfl_sync(0xffffffffu, qb[d], 0);
+                wl[d] = __shfl_sync(0xffffffffu, qe[d], 31) - wb[d];
+                wo[d] = tot;
+                tot += wl[d];
+            }
+            staged = tot <= kWinCap;  // the same on every lane
         }
+        if (staged) {
+            float4 *w = win[threadIdx.x >> 5];
+            const int lane = threadIdx.x & 31;
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                for (int q = lane; q < wl[d]; q += 32) w[wo[d] + q] = __ldg(s.cellSorted + wb[d] + q);
+            __syncwarp();
+            k = build_fast_staged(s, i, make_float2(me.x, me.y), __float_as_int(me.w), w, qb, qe, sx, wb, wo,
+                                  s.nbr + i, (size_t)s.Ncap);
+        } else if (valid) {
+            k = build_fast_at<true>(s, i, ix * ncy + iy, make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
+                                    (size_t)s.Ncap);
+        }
+        if (valid) s.nbrCount[i] = k;
+    } else if (t < s.N) {
+        const int i = t;
+        k = build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+        s.nbrCount[i] = k;
     }
     // build statistics and overflow
     int kmax = warp_max_int(k);

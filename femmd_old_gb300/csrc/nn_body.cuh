@@ -143,6 +143,76 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
     return k;
 }
 
+// The walk of build_fast_at over candidates staged in shared memory: for
+// stencil column d (dx = d - 1) the candidates of slots [wb[d], wb[d] +
+// wl[d]) sit at cand[wo[d] + slot - wb[d]].  Same ranges, same order, same
+// arithmetic as the walk over cellSorted.
+__device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float sy, float2 p, int i,
+                                            int gi, float R2, int cap, size_t stride, int *&out, int &k) {
+    int q = lb;
+    for (; q + 4 <= le; q += 4) {
+        float4 e[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) e[u] = cand[q + u];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
+                if (k < cap) {
+                    *out = __float_as_int(e[u].z);
+                    out += stride;
+                }
+                k++;
+            }
+        }
+    }
+    for (; q < le; q++) {
+        const float4 e = cand[q];
+        if (walk_hit(e, sx, sy, p, i, gi, R2)) {
+            if (k < cap) {
+                *out = __float_as_int(e.z);
+                out += stride;
+            }
+            k++;
+        }
+    }
+}
+
+// The stencil of a particle whose cell row has no y-wrap (1 <= iy <= ncy -
+// 2): per column d (dx = d - 1) the slot range [qb[d], qe[d]) of rows
+// iy - 1 .. iy + 1 and the image shift sx[d].  Returns the columns.
+__device__ __forceinline__ void stencil_columns(const DevSys &s, int ix, int iy, int *qb, int *qe, float *sx) {
+    const int ncx = s.ncx, ncy = s.ncy;
+    const float Lx = s.wrapx ? s.Lx : 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        int nx = ix + d - 1;
+        sx[d] = 0.0f;
+        if (nx < 0) {
+            nx = ncx - 1;
+            sx[d] = -Lx;
+        } else if (nx == ncx) {
+            nx = 0;
+            sx[d] = Lx;
+        }
+        const int col = nx * ncy;
+        qb[d] = __ldg(s.cellStart + col + iy - 1);
+        qe[d] = __ldg(s.cellStart + col + iy + 2);
+    }
+}
+
+// build_fast_at over the three column windows staged in shared memory
+// (column d's slots [wb[d], ...) at cand[wo[d] + slot - wb[d]]).
+__device__ __forceinline__ int build_fast_staged(const DevSys &s, int i, float2 p, int gi, const float4 *cand,
+                                                 const int *qb, const int *qe, const float *sx, const int *wb,
+                                                 const int *wo, int *out, size_t stride) {
+    int k = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        walk_staged(cand, wo[d] + qb[d] - wb[d], wo[d] + qe[d] - wb[d], sx[d], 0.0f, p, i, gi, s.nnRadiusSq,
+                    s.nbrCap, stride, out, k);
+    return k;
+}
+
 template <bool RO>
 __device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
     return build_fast_at<RO>(s, i, s.cellOf[i], pos[i], s.excl[i], out, stride);
