@@ -161,9 +161,20 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
     int kmax = 0;
     unsigned long long ksum = 0;
     if (!skip)
-        for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
-            int k = fast ? build_fast<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap)
-                         : build_general<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+        for (int t = threadIdx.x; t < s.N; t += blockDim.x) {
+            // the fast walk takes the particles in cell order (slot t of
+            // cellSorted): neighbouring lanes walk nearly the same ranges
+            int i, k;
+            if (fast) {
+                const float4 me = s.cellSorted[t];
+                i = __float_as_int(me.z) & kIdMask;
+                const int c = cell_col(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly);  // the binning's cell
+                k = build_fast_at<false>(s, i, c, make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
+                                         (size_t)s.Ncap);
+            } else {
+                i = t;
+                k = build_general<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+            }
             s.nbrCount[i] = k;
             kmax = max(kmax, k);
             ksum += (unsigned long long)k;
