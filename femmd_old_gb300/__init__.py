@@ -539,6 +539,10 @@ class Batch:
     def set_launch(self, threads, ctas_per_sm):
         self._call("femmd_batch_set_launch", int(threads), int(ctas_per_sm))
 
+    def set_split(self, on=True):
+        """Run replicas heavier than a CTA's average share on CTA pairs."""
+        self._call("femmd_batch_set_split", int(bool(on)))
+
     def launch(self):
         t, c, k = C.c_int(), C.c_int(), C.c_int()
         self._call("femmd_batch_get_launch", C.byref(t), C.byref(c), C.byref(k))

@@ -48,6 +48,7 @@ SIGNATURES = {
     "femmd_get_wall_forces": (i_, [P, dp, dp]),
     "femmd_get_properties": (i_, [P, dp]),
     "femmd_set_property_averaging": (i_, [P, i_, i_, i_]),
+    "femmd_batch_set_split": (i_, [P, i_]),
     "femmd_get_clusters": (i_, [P, dp, dp, dp]),
     "femmd_get_average_properties": (i_, [P, dp, dp, dp, C.POINTER(i_), C.POINTER(i_), C.POINTER(i_)]),
     "femmd_set_trajectory": (i_, [P, C.c_char_p, i_, i_]),

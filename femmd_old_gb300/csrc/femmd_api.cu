@@ -2708,7 +2708,8 @@ struct femmd_batch {
     GraphSet graph;
     int graphSteps = -1, graphThreads = 0, graphCtas = 0;
     const void *graphReps = nullptr;
-    int graphVariant = -1;
+    bool splitLarge = true;  // femmd_batch_set_split
+    int graphVariant = -1, graphNbig = -1;
     size_t graphSmem = 0;
     int ctas = 0;
 };
@@ -2781,8 +2782,8 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
     BCK(b->dreps.ensure(R));
     BCK(b->order.ensure(std::max<size_t>(ord.size(), 1)));
     if (!b->queue.p) {
-        BCK(b->queue.ensure(2));
-        BCK(cudaMemsetAsync(b->queue.p, 0, 2 * sizeof(int), b->stream));
+        BCK(b->queue.ensure(3));
+        BCK(cudaMemsetAsync(b->queue.p, 0, 3 * sizeof(int), b->stream));
     }
     BCK(b->parity.ensure(R));
     BCK(cudaMemcpyAsync(b->dreps.p, sys.data(), R * sizeof(DevSys), cudaMemcpyHostToDevice, b->stream));
@@ -2794,6 +2795,16 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
     bl.order = b->order.p;
     bl.queue = b->queue.p;
     bl.nwork = (int)ord.size();
+    // replicas heavier than a CTA's average share run on CTA pairs (a
+    // thread-block cluster of two), so that none sets the launch's length
+    // alone; pairs need an even grid
+    bl.nbig = 0;
+    if (b->splitLarge && ctas % 2 == 0 && ctas >= 2) {
+        double total = 0.0;
+        for (int r : ord) total += cost[r];
+        const double share = total / ctas;
+        while (bl.nbig < (int)ord.size() && cost[ord[bl.nbig]] > share) bl.nbig++;
+    }
     bl.minBlocks = b->ctasPerSm >= 2 && b->threads > 512 ? 2 : 1;
     bl.parity = b->parity.p;
     bl.steps = steps;
@@ -2813,7 +2824,7 @@ static femmd_status batch_launch(femmd_batch *b, const BatchLaunch &bl) {
     const int variant = bl.multiType | bl.sigmaByType << 1 | bl.sigmaOne << 2 | bl.wrapx << 3 | bl.wrapy << 4;
     const bool rebuild = !b->graph.x || b->graphSteps != bl.steps || b->graphThreads != bl.threads ||
                          b->graphCtas != bl.ctas || b->graphReps != (const void *)bl.reps ||
-                         b->graphVariant != variant || b->graphSmem != bl.smem;
+                         b->graphVariant != variant || b->graphSmem != bl.smem || b->graphNbig != bl.nbig;
     if (rebuild) {
         b->graph.release();
         BCK(cudaGraphCreate(&b->graph.g, 0));
@@ -2828,8 +2839,9 @@ static femmd_status batch_launch(femmd_batch *b, const BatchLaunch &bl) {
         b->graphReps = bl.reps;
         b->graphVariant = variant;
         b->graphSmem = bl.smem;
+        b->graphNbig = bl.nbig;
     }
-    BCK(cudaMemsetAsync(bl.queue, 0, 2 * sizeof(int), b->stream));
+    BCK(cudaMemsetAsync(bl.queue, 0, 3 * sizeof(int), b->stream));
     BCK(cudaGraphLaunch(b->graph.x, b->stream));
     return FEMMD_OK;
 }
@@ -2907,6 +2919,12 @@ femmd_status femmd_batch_set_launch(femmd_batch *b, int threads, int ctas_per_sm
         return bfail(b, FEMMD_INVALID_ARG, "threads must be a multiple of 32 in [32, 1024], CTAs per SM in [1, 32]");
     b->threads = threads;
     b->ctasPerSm = ctas_per_sm;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_batch_set_split(femmd_batch *b, int on) {
+    if (!b) return FEMMD_INVALID_ARG;
+    b->splitLarge = on != 0;
     return FEMMD_OK;
 }
 

@@ -202,8 +202,9 @@ cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl
 struct BatchLaunch {
     const DevSys *reps;
     const int *order, *parity;
-    int *queue;  // {next work index, finished CTAs}, zero before a launch
+    int *queue;  // {next work index, finished CTAs, next single-CTA index}, zero before a launch
     int nwork, minBlocks;
+    int nbig;    // the first nbig replicas of 'order' run on CTA pairs (0: none)
     int steps, ctas, threads;
     size_t smem;
     bool multiType, sigmaByType, sigmaOne, wrapx, wrapy, exact;

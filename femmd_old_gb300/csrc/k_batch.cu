@@ -15,6 +15,7 @@
 // nn_body.cuh, the same code as the single-system kernels, and the list order
 // is the same, so a replica's trajectory is bit-identical to running it alone.
 // Energies are reduced per replica in FP32 inside the block.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include "femmd_internal.h"
 #include "launch.h"
@@ -23,6 +24,8 @@
 #include "step_body.cuh"
 
 namespace femmd {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -76,16 +79,45 @@ __device__ __forceinline__ void block_reduce_step(float &a, float &b, float &c, 
     }
 }
 
+// The threads that work on one replica: one CTA (Solo), or the two CTAs of
+// a thread-block cluster (Pair).  Loops over particles, triangles and
+// candidates are strided over the team; sync() is __syncthreads or the
+// cluster barrier (release/acquire at cluster scope, so global writes made
+// by either CTA before it are seen by both after it).  Every sync() is
+// reached by every thread of the team the same number of times: no sync()
+// sits under a condition that could differ between the two CTAs.
+struct SoloTeam {
+    static constexpr int size = 1;
+    __device__ int rank() const { return 0; }
+    __device__ void sync() const { __syncthreads(); }
+    // combine one float/int partial per CTA in the leader (rank 0)
+    __device__ float *slot(float *x, int) const { return x; }
+};
+
+struct PairTeam {
+    static constexpr int size = 2;
+    int r;
+    __device__ int rank() const { return r; }
+    __device__ void sync() const { cg::this_cluster().sync(); }
+    // the leader's copy of a shared array, at this CTA's entries
+    __device__ float *slot(float *x, int per) const {
+        return cg::this_cluster().map_shared_rank(x, 0) + r * per;
+    }
+};
+
 // NeighborList::update branch + binning + Verlet build for one replica
-__device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *iscr) {
+template <class Team>
+__device__ __noinline__ void block_rebuild(const Team team, const DevSys &s, int parity, int *iscr, float *xch) {
     const float2 *pos = parity ? s.pos1 : s.pos0;
     const int lane = threadIdx.x & 31;
-    if (threadIdx.x == 0 && s.sc->rebuild) {
+    const int t0 = team.rank() * blockDim.x + threadIdx.x, tstride = Team::size * blockDim.x;
+    const bool lead = team.rank() == 0 && threadIdx.x == 0;
+    if (lead && s.sc->rebuild) {
         s.sc->totalUpdates += 1;
         s.sc->dispHi = 0.0f;
     }
     // counting sort: warp-aggregated histogram (warp-uniform loop for the match)
-    for (int base = threadIdx.x & ~31; base < s.N; base += blockDim.x) {
+    for (int base = t0 & ~31; base < s.N; base += tstride) {
         const int i = base + lane;
         const bool act = i < s.N;
         const unsigned active = __ballot_sync(0xffffffffu, act);
@@ -103,9 +135,10 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
             s.rank[i] = b + __popc(peers & ((1u << lane) - 1u));
         }
     }
-    __syncthreads();
-    // exclusive scan of the counts into cellStart, counts cleared
-    {
+    team.sync();
+    // exclusive scan of the counts into cellStart, counts cleared (the
+    // leading CTA alone; its barriers are its own)
+    if (team.rank() == 0) {
         const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         int carry = 0;
         for (int cb = 0; cb < s.ncells; cb += blockDim.x) {
@@ -143,25 +176,25 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
             s.sc->maxCount = 0;
         }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < s.N; i += blockDim.x) {
+    team.sync();
+    for (int i = t0; i < s.N; i += tstride) {
         int slot = s.cellStart[s.cellOf[i]] + s.rank[i];
         if (slot >= 0 && slot < s.N)
             s.unsorted[slot] = i;
         else
             atomicOr(&s.sc->overflow, 2);
     }
-    __syncthreads();
+    team.sync();
     // crowded cells after a blow-up or inconsistent counts: skip the quadratic parts
     const bool skip = s.sc->nonfinite != 0 || (s.sc->overflow & 2);
     if (!skip)
-        for (int i = threadIdx.x; i < s.N; i += blockDim.x) place_one<false>(s, pos, i, &s.sc->overflow);
-    __syncthreads();
+        for (int i = t0; i < s.N; i += tstride) place_one<false>(s, pos, i, &s.sc->overflow);
+    team.sync();
     const bool fast = fast_walk_ok(s);
     int kmax = 0;
     unsigned long long ksum = 0;
     if (!skip)
-        for (int t = threadIdx.x; t < s.N; t += blockDim.x) {
+        for (int t = t0; t < s.N; t += tstride) {
             // the fast walk takes the particles in cell order (slot t of
             // cellSorted): neighbouring lanes walk nearly the same ranges
             int i, k;
@@ -181,34 +214,59 @@ __device__ __noinline__ void block_rebuild(const DevSys &s, int parity, int *isc
         }
     if (ksum) atomicAdd(&s.sc->nbrSum, ksum);
     kmax = block_max_int(kmax, iscr);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0) *team.slot(xch, 1) = __int_as_float(kmax);
+    team.sync();
+    if (lead) {
+        for (int q = 1; q < Team::size; q++) kmax = max(kmax, __float_as_int(xch[q]));
         s.sc->maxCount = kmax;
         if (kmax > s.nbrCap) s.sc->overflow |= 1;
         s.sc->builds += 1ull;
     }
-    __syncthreads();
+    team.sync();
 }
 
 // one force evaluation + integration of a replica (k_tri_forces + k_step)
-template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
-__device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, int mode, int parity, float *fscr) {
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, class Team>
+__device__ __noinline__ void block_step(const Team team, const DevSys &s, const PairEntry *tab, int mode, int parity,
+                                        float *fscr, float *xch) {
     const float2 *pin = parity ? s.pos1 : s.pos0;
     float2 *pout = parity ? s.pos0 : s.pos1;
+    const int t0 = team.rank() * blockDim.x + threadIdx.x, tstride = Team::size * blockDim.x;
     float etri = 0.0f;
     if (s.feaForces && s.ntri > 0) {
-        for (int t = threadIdx.x; t < s.ntri; t += blockDim.x) etri += tri_force(s, pin, t);
-        __syncthreads();  // every nodal force written before the gathers
+        for (int t = t0; t < s.ntri; t += tstride) etri += tri_force(s, pin, t);
+        team.sync();  // every nodal force written before the gathers
     }
     float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
     bool bad = false;
-    for (int i = threadIdx.x; i < s.N; i += blockDim.x)
+    for (int i = t0; i < s.N; i += tstride)
         particle_step<MT, SG, WX, WY, SIG1, false>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
     int anybad = bad;
     block_reduce_step(etri, ue, we, ke, vvm, anybad, fscr);
-    const float te = etri, tu = ue, tw = we, tk = ke, tm = vvm;
+    // the team's partials, added in rank order by the leader (one CTA: as is)
     if (threadIdx.x == 0) {
+        float *x = team.slot(xch, 6);
+        x[0] = etri;
+        x[1] = ue;
+        x[2] = we;
+        x[3] = ke;
+        x[4] = vvm;
+        x[5] = anybad ? 1.0f : 0.0f;
+    }
+    team.sync();
+    if (team.rank() == 0 && threadIdx.x == 0) {
+        float te = xch[0], tu = xch[1], tw = xch[2], tk = xch[3], tm = xch[4];
+        bool nb = xch[5] != 0.0f;
+        for (int q = 1; q < Team::size; q++) {
+            te += xch[6 * q];
+            tu += xch[6 * q + 1];
+            tw += xch[6 * q + 2];
+            tk += xch[6 * q + 3];
+            tm = fmaxf(tm, xch[6 * q + 4]);
+            nb = nb || xch[6 * q + 5] != 0.0f;
+        }
         DevScalars *sc = s.sc;
-        if (anybad) sc->nonfinite |= 1;
+        if (nb) sc->nonfinite |= 1;
         const double U = (double)te + (double)tu, W = (double)tw, KE = (double)tk;
         sc->U = U;
         sc->W = W;
@@ -236,7 +294,51 @@ __device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, i
         sc->rebuild = reb;
         if (mode == MODE_FIRST || mode == MODE_MID) sc->stepNow += 1;
     }
+    team.sync();
+}
+
+// The reference's Integrator::run (integrator.cpp:31-57) for replica r on a
+// team: descriptor and pair table into shared memory, run start, forced
+// rebuild, first force pass, steps with the half-skin rule, last step.
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, class Team>
+__device__ __forceinline__ void run_replica(const Team team, const DevSys *reps, int r, const int *parity0, int steps,
+                                            DevSys &S, PairEntry *tab, float *fscr, int *iscr, float *xch) {
+    {
+        const int *src = (const int *)(reps + r);
+        int *dst = (int *)&S;
+        for (int w = threadIdx.x; w < (int)(sizeof(DevSys) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+    }
     __syncthreads();
+    const int nt = S.numTypes > 1 ? S.numTypes * S.numTypes : 1;
+    for (int w = threadIdx.x; w < nt; w += blockDim.x) tab[w] = S.pair[w];
+    if (team.rank() == 0 && threadIdx.x == 0) {
+        // run start: NeighborList::update(1)
+        DevScalars *c = S.sc;
+        c->rebuild = 1;
+        c->dispHi = 0.0f;
+        c->totalUpdates = 0;
+        c->obsRow = 0;
+        c->stepNow = S.stepBase;
+    }
+    team.sync();
+    int cur = parity0[r];
+    block_rebuild(team, S, cur, iscr, xch);
+    if (steps == 0) {
+        block_step<MT, SG, WX, WY, SIG1>(team, S, tab, MODE_INIT, cur, fscr, xch);
+    } else {
+        block_step<MT, SG, WX, WY, SIG1>(team, S, tab, MODE_FIRST, cur, fscr, xch);
+        cur ^= 1;
+        for (int k = 1; k < steps; k++) {
+            // the flag was written before the step's last sync(): the same
+            // value in every CTA of the team
+            if (S.sc->rebuild) block_rebuild(team, S, cur, iscr, xch);
+            block_step<MT, SG, WX, WY, SIG1>(team, S, tab, MODE_MID, cur, fscr, xch);
+            cur ^= 1;
+        }
+        if (S.sc->rebuild) block_rebuild(team, S, cur, iscr, xch);
+        block_step<MT, SG, WX, WY, SIG1>(team, S, tab, MODE_LAST, cur, fscr, xch);
+    }
+    team.sync();
 }
 
 }  // namespace
@@ -244,65 +346,77 @@ __device__ __noinline__ void block_step(const DevSys &s, const PairEntry *tab, i
 // Replicas are handed out from a queue: 'order' lists them heaviest first,
 // and each CTA takes the next one when it is free (greedy list scheduling,
 // which also balances CTAs that share an SM).  queue[0] is the next index,
-// queue[1] counts finished CTAs; the last CTA to finish resets both.
+// queue[1] counts finished CTAs; the last CTA to finish resets the queue.
 // MINB: resident CTAs per SM the register allocation must allow.
 template <bool MT, bool SG, bool WX, bool WY, bool SIG1, int MINB>
 __global__ void __launch_bounds__(1024, MINB) k_batch(const DevSys *__restrict__ reps, const int *__restrict__ order,
-                                                      int nwork, int *queue, const int *__restrict__ parity0,
+                                                      int nwork, int nbig, int *queue, const int *__restrict__ parity0,
                                                       int steps) {
     __shared__ DevSys S;
     __shared__ float fscr[6 * 32];
+    __shared__ float xch[6 * 2];
     __shared__ int iscr[33];
     __shared__ int next;
     extern __shared__ PairEntry tab[];
+    const SoloTeam team;
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(queue, 1);
         __syncthreads();
         const int q = next;
         __syncthreads();
         if (q >= nwork) break;
-        const int r = order[q];
-        // copy the replica's descriptor into shared memory
-        {
-            const int *src = (const int *)(reps + r);
-            int *dst = (int *)&S;
-            for (int w = threadIdx.x; w < (int)(sizeof(DevSys) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
-        }
-        __syncthreads();
-        const int nt = S.numTypes > 1 ? S.numTypes * S.numTypes : 1;
-        for (int w = threadIdx.x; w < nt; w += blockDim.x) tab[w] = S.pair[w];
-        if (threadIdx.x == 0) {
-            // run start: NeighborList::update(1)
-            DevScalars *c = S.sc;
-            c->rebuild = 1;
-            c->dispHi = 0.0f;
-            c->totalUpdates = 0;
-            c->obsRow = 0;
-            c->stepNow = S.stepBase;
-        }
-        __syncthreads();
-        int cur = parity0[r];
-        block_rebuild(S, cur, iscr);
-        if (steps == 0) {
-            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_INIT, cur, fscr);
-        } else {
-            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_FIRST, cur, fscr);
-            cur ^= 1;
-            for (int k = 1; k < steps; k++) {
-                if (S.sc->rebuild) block_rebuild(S, cur, iscr);
-                block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_MID, cur, fscr);
-                cur ^= 1;
-            }
-            if (S.sc->rebuild) block_rebuild(S, cur, iscr);
-            block_step<MT, SG, WX, WY, SIG1>(S, tab, MODE_LAST, cur, fscr);
-        }
-        __syncthreads();
+        run_replica<MT, SG, WX, WY, SIG1>(team, reps, order[q], parity0, steps, S, tab, fscr, iscr, xch);
     }
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
             queue[0] = 0;
             queue[1] = 0;
+            queue[2] = 0;
+        }
+    }
+}
+
+// The same with the CTAs in pairs (thread-block clusters of two): first the
+// order's nbig heaviest replicas, each run by a pair (particles, triangles
+// and candidates split between the two CTAs; the leader's pick of the queue
+// shared through its shared memory), then the rest one CTA each, from their
+// own counter queue[2].  A replica much larger than the average work of a
+// CTA then no longer sets the length of the whole launch.
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(1024, 1)
+    k_batch_pair(const DevSys *__restrict__ reps, const int *__restrict__ order, int nwork, int nbig, int *queue,
+                 const int *__restrict__ parity0, int steps) {
+    __shared__ DevSys S;
+    __shared__ float fscr[6 * 32];
+    __shared__ float xch[6 * 2];
+    __shared__ int iscr[33];
+    __shared__ int next;
+    extern __shared__ PairEntry tab[];
+    const PairTeam pair{(int)cg::this_cluster().block_rank()};
+    for (;;) {
+        if (pair.rank() == 0 && threadIdx.x == 0) next = atomicAdd(queue, 1);
+        pair.sync();
+        const int q = *cg::this_cluster().map_shared_rank(&next, 0);
+        pair.sync();  // both have read the leader's pick before it changes
+        if (q >= nbig) break;  // the same q in both CTAs
+        run_replica<MT, SG, WX, WY, SIG1>(pair, reps, order[q], parity0, steps, S, tab, fscr, iscr, xch);
+    }
+    const SoloTeam solo;
+    for (;;) {
+        if (threadIdx.x == 0) next = nbig + atomicAdd(queue + 2, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= nwork) break;
+        run_replica<MT, SG, WX, WY, SIG1>(solo, reps, order[q], parity0, steps, S, tab, fscr, iscr, xch);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+            queue[2] = 0;
         }
     }
 }
@@ -311,11 +425,14 @@ namespace {
 
 template <bool MT, bool SG, bool WX, bool WY, bool SIG1>
 cudaError_t launch_batch(Launch &L, const BatchLaunch &b) {
+    if (b.nbig > 0)
+        return L.kernel(k_batch_pair<MT, SG, WX, WY, SIG1>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
+                        b.nwork, b.nbig, b.queue, b.parity, b.steps);
     if (b.minBlocks >= 2)
         return L.kernel(k_batch<MT, SG, WX, WY, SIG1, 2>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
-                        b.nwork, b.queue, b.parity, b.steps);
+                        b.nwork, 0, b.queue, b.parity, b.steps);
     return L.kernel(k_batch<MT, SG, WX, WY, SIG1, 1>, dim3(b.ctas), dim3(b.threads), b.smem, b.reps, b.order,
-                    b.nwork, b.queue, b.parity, b.steps);
+                    b.nwork, 0, b.queue, b.parity, b.steps);
 }
 
 template <bool MT, bool SG, bool WX, bool WY>

@@ -250,6 +250,12 @@ int femmd_batch_size(const femmd_batch *b);
 femmd_status femmd_batch_run(femmd_batch *b, int steps);
 /* Launch shape: threads per CTA (multiple of 32, <= 1024) and CTAs per SM. */
 femmd_status femmd_batch_set_launch(femmd_batch *b, int threads, int ctas_per_sm);
+/* Replicas heavier than a CTA's average share of the batch (atoms +
+ * triangles) run on a pair of CTAs (a thread-block cluster of two) before
+ * the rest run one per CTA, so that the largest replica no longer sets the
+ * length of the launch alone; needs an even number of CTAs.  On by default;
+ * results are bit-identical either way. */
+femmd_status femmd_batch_set_split(femmd_batch *b, int on);
 femmd_status femmd_batch_get_launch(const femmd_batch *b, int *threads, int *ctas_per_sm, int *ctas);
 /* Times trial_steps on each candidate launch shape (states restored after each
  * trial) and keeps the fastest. */

@@ -152,3 +152,30 @@ def test_batch_autotune_lists_applies_the_choice():
         a.init_neighbor_list()
         a.run(40)
         assert same(s, a)
+
+
+@pytest.mark.parametrize("sizes,launch", [((8000, 600, 900, 1200, 700, 500), (1024, 1)),
+                                          ((6000, 5000, 700, 800), (512, 2)),
+                                          ((7000, 6500, 6000, 900, 400, 300), (256, 4))])
+def test_large_replicas_on_cta_pairs_match_alone(sizes, launch):
+    """Replicas heavier than a CTA's average share run on a pair of CTAs (a
+    thread-block cluster of two, particles split between them): still bit
+    for bit the replica run alone, split or not."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    scs = [S.mixed_replica(int(sz), float(rng.uniform(0.6, 0.85)), float(rng.uniform(0.1, 1.5)), seed=300 + k)
+           for k, sz in enumerate(sizes)]
+    for split in (True, False):
+        b = F.Batch(0)
+        systems = []
+        for sc in scs:
+            s = F.System(0)
+            sc.replay(s)
+            systems.append(s)
+            b.add(s)
+        b.set_launch(*launch)
+        b.set_split(split)
+        b.run(60)
+        b.run(0)
+        b.run(41)
+        for sc, s in zip(scs, systems):
+            assert same(s, alone(sc, [60, 0, 41])), (split, s.N)
