@@ -953,6 +953,7 @@ static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int un
     L.stream = ctx->stream;
     L.graph = gs.g;
     int p = parity;
+    cudaGraphNode_t prevStep = nullptr, prevIf = nullptr;
     for (int u = 0; u < units; u++) {
         cudaGraphConditionalHandle h;
         CK(cudaGraphConditionalHandleCreate(&h, gs.g, 0, cudaGraphCondAssignDefault));
@@ -963,11 +964,21 @@ static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int un
             CK(enqueue_step_props(ctx, L, s, p));
             CK(enqueue_drift_in_run(L, s, p));
         } else {
-            CK(enqueue_step(L, s, MODE_MID, p, h, 1));
+            // The triangle pass needs only the drifted positions: it depends
+            // on the previous step alone and runs beside that step's
+            // conditional rebuild (which writes cells and lists, not
+            // positions); the area springs and the step kernel wait for both.
+            L.deps.clear();
+            if (prevStep) L.deps.push_back(prevStep);
+            CK(enqueue_tri(L, s, p));
+            if (prevIf) L.deps.push_back(prevIf);
+            CK(enqueue_step_after_tri(L, s, MODE_MID, p, h, 1));
+            prevStep = L.deps.back();
         }
         Launch body;
         CK(L.begin_if(h, body));
         CK(enqueue_rebuild(body, s, 1 - p, 1));
+        prevIf = L.deps.back();
         p = 1 - p;
     }
     CK(cudaGraphInstantiate(&gs.x, gs.g, 0));

@@ -152,6 +152,11 @@ cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
 
 // ---- forces + integration (k_force.cu)
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);
+// enqueue_step in two parts: the triangle pass (reads positions only), then
+// the area springs and the step kernel.
+cudaError_t enqueue_tri(Launch &L, const DevSys &s, int parity);
+cudaError_t enqueue_step_after_tri(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                                   int use_h);
 // leapFrogStep1 + applyPBC alone (integrator.cpp:100-127): buffer parity -> 1-parity
 cudaError_t enqueue_drift(Launch &L, const DevSys &s, int parity);
 // The same drift inside a run: the step counter advances by one (the drift

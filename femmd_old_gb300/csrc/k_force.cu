@@ -385,11 +385,20 @@ static cudaError_t pick_image(Launch &L, const DevSys &s, int mode, int parity, 
     return pick_sig<MT, SG, false, false>(L, s, mode, parity, h, use_h);
 }
 
+cudaError_t enqueue_tri(Launch &L, const DevSys &s, int parity) {
+    if (s.feaForces && s.ntri > 0) return L.kernel(k_tri_forces, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, parity);
+    return cudaSuccess;
+}
+
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h) {
     cudaError_t e;
-    if (s.feaForces && s.ntri > 0) {
-        if ((e = L.kernel(k_tri_forces, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, parity))) return e;
-    }
+    if ((e = enqueue_tri(L, s, parity))) return e;
+    return enqueue_step_after_tri(L, s, mode, parity, h, use_h);
+}
+
+cudaError_t enqueue_step_after_tri(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                                   int use_h) {
+    cudaError_t e;
     if (s.areaUnits > 0) {
         if ((e = L.kernel(k_area_keep, dim3(force_blocks(s.nPre)), dim3(kBlock), 0, s, parity))) return e;
         if ((e = L.kernel(k_area, dim3(s.areaUnits), dim3(kAreaLanes), (size_t)s.areaSmem, s, parity))) return e;
