@@ -76,34 +76,11 @@ def parse():
 
 # ------------------------------------------------------------- distributed
 
-class Dist:
-    def __init__(self):
-        self.world = int(os.environ.get("WORLD_SIZE", "1"))
-        self.rank = int(os.environ.get("RANK", "0"))
-        self.local = int(os.environ.get("LOCAL_RANK", "0"))
-        self.pg = None
-        if self.world > 1:
-            import torch
-            import torch.distributed as dist
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
-            self.pg = dist
-
-    def barrier(self):
-        if self.pg:
-            self.pg.barrier()
-
-    def max(self, x: float) -> float:
-        if not self.pg:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{self.local}")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def close(self):
-        if self.pg:
-            self.pg.destroy_process_group()
+# one process per GPU, replicas only (femmd_old_gb300.replicas.Group: NCCL
+# barrier and max over ranks; nothing with one process)
+def Dist():
+    from femmd_old_gb300.replicas import Group
+    return Group()
 
 
 class _Solo:
