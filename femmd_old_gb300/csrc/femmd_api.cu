@@ -922,7 +922,7 @@ static femmd_status props_buffers(femmd_ctx *ctx) {
     }
     CK(ctx->unf.ensure(std::max(N, 1))); CK(ctx->kinTerm.ensure(std::max(N, 1))); CK(ctx->clVir.ensure(std::max(N, 1)));
     // the accumulator's reduction: a fixed number of blocks per system size
-    ctx->propBlocks = std::max(1, std::min(304, (N + 4095) / 4096));
+    ctx->propBlocks = std::max(1, std::min(1216, (N + 1023) / 1024));
     CK(ctx->propPart.ensure(3 * (size_t)ctx->propBlocks));
     CK(cudaStreamSynchronize(sm));  // the host vectors above are not pinned
     ctx->propsUploaded = true;

@@ -28,65 +28,65 @@ __device__ __forceinline__ double block_sum_d(double v, double *scr) {
     return scr[0];
 }
 
-__device__ __forceinline__ float block_min_f(float v, float *scr) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    __syncthreads();
-    if (lane == 0) scr[warp] = v;
-    __syncthreads();
-    float t = 3.0e38f;
-    if (threadIdx.x < 32) {
-        t = lane < nw ? scr[lane] : 3.0e38f;
-        for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) scr[0] = t;
-    __syncthreads();
-    return scr[0];
+// sum over the warp, the same value in every lane (butterfly: a fixed order)
+__device__ __forceinline__ double warp_sum_all(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 }  // namespace
 
-// One block per cluster (elastomer): unfold across the periodic boundary the
+// One warp per cluster (elastomer): unfold across the periodic boundary the
 // reference's way (a cluster wider than half the box has its vertices beyond
 // L/2 moved down by L, and all moved up by L again when their mean is
 // negative), then the mass-weighted centre of mass and velocity and the
-// cluster kinetic term M |v_cm|^2.
-__global__ void k_props_cluster(DevSys s, const float2 *pos, const int2 *clRange, const float *clMass, double2 *unf,
-                                double2 *cmPos, double2 *cmVel, double *clKin) {
-    __shared__ double dscr[32];
-    __shared__ float fscr[32];
-    const int c = blockIdx.x;
+// cluster kinetic term M |v_cm|^2.  Warp reductions only: min/max exact,
+// sums in FP64 in a fixed lane order.
+constexpr int kClusterWarps = 4;
+
+__global__ void __launch_bounds__(32 * kClusterWarps) k_props_cluster(DevSys s, const float2 *pos, int ncl,
+                                                                      const int2 *clRange, const float *clMass,
+                                                                      double2 *unf, double2 *cmPos, double2 *cmVel,
+                                                                      double *clKin) {
+    const int c = blockIdx.x * kClusterWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (c >= ncl) return;  // whole warps
     const int off = clRange[c].x, n = clRange[c].y;
-    float xmin = 3.0e38f, ymin = 3.0e38f, nxmax = 3.0e38f, nymax = 3.0e38f;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        float2 p = pos[off + k];
+    float xmin = 3.0e38f, ymin = 3.0e38f, xmax = -3.0e38f, ymax = -3.0e38f;
+    for (int k = lane; k < n; k += 32) {
+        const float2 p = pos[off + k];
         xmin = fminf(xmin, p.x);
         ymin = fminf(ymin, p.y);
-        nxmax = fminf(nxmax, -p.x);
-        nymax = fminf(nymax, -p.y);
+        xmax = fmaxf(xmax, p.x);
+        ymax = fmaxf(ymax, p.y);
     }
-    xmin = block_min_f(xmin, fscr);
-    ymin = block_min_f(ymin, fscr);
-    const float xmax = -block_min_f(nxmax, fscr), ymax = -block_min_f(nymax, fscr);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        xmin = fminf(xmin, __shfl_xor_sync(0xffffffffu, xmin, o));
+        ymin = fminf(ymin, __shfl_xor_sync(0xffffffffu, ymin, o));
+        xmax = fmaxf(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+        ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
+    }
     const bool ux = xmax - xmin > s.Lx / 2.0f;  // whatever the periodicity, as the reference
     const bool uy = ymax - ymin > s.Ly / 2.0f;
     double sx = 0.0, sy = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        float2 p = pos[off + k];
-        double x = p.x, y = p.y;
-        if (ux && p.x > s.Lx / 2.0f) x -= s.Lx;
-        if (uy && p.y > s.Ly / 2.0f) y -= s.Ly;
-        sx += x;
-        sy += y;
+    if (ux || uy) {
+        for (int k = lane; k < n; k += 32) {
+            const float2 p = pos[off + k];
+            double x = p.x, y = p.y;
+            if (ux && p.x > s.Lx / 2.0f) x -= s.Lx;
+            if (uy && p.y > s.Ly / 2.0f) y -= s.Ly;
+            sx += x;
+            sy += y;
+        }
+        sx = warp_sum_all(sx);
+        sy = warp_sum_all(sy);
     }
-    sx = block_sum_d(sx, dscr);
-    sy = block_sum_d(sy, dscr);
     const bool upx = ux && sx / n < 0.0, upy = uy && sy / n < 0.0;
     double mx = 0.0, my = 0.0, mvx = 0.0, mvy = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = lane; k < n; k += 32) {
         const int i = off + k;
-        float2 p = pos[i], v = s.vel[i];
+        const float2 p = pos[i], v = s.vel[i];
         double x = p.x, y = p.y;
         if (ux && p.x > s.Lx / 2.0f) x -= s.Lx;
         if (uy && p.y > s.Ly / 2.0f) y -= s.Ly;
@@ -99,11 +99,11 @@ __global__ void k_props_cluster(DevSys s, const float2 *pos, const int2 *clRange
         mvx += m * v.x;
         mvy += m * v.y;
     }
-    mx = block_sum_d(mx, dscr);
-    my = block_sum_d(my, dscr);
-    mvx = block_sum_d(mvx, dscr);
-    mvy = block_sum_d(mvy, dscr);
-    if (threadIdx.x == 0) {
+    mx = warp_sum_all(mx);
+    my = warp_sum_all(my);
+    mvx = warp_sum_all(mvx);
+    mvy = warp_sum_all(mvy);
+    if (lane == 0) {
         const double M = clMass[c];
         cmPos[c] = make_double2(mx / M, my / M);
         const double vx = mvx / M, vy = mvy / M;
@@ -259,14 +259,15 @@ __global__ void __launch_bounds__(kBlock) k_props_accum(DevSys s, DevProps *P, d
         last = atomicAdd(&P->ticket, 1u) == (unsigned)nb - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last) return;
     __threadfence();
-    double cv = 0.0, fv = 0.0, ck = 0.0;
-    for (int q = 0; q < nb; q++) {
-        cv += part[3 * q];
-        fv += part[3 * q + 1];
-        ck += part[3 * q + 2];
-    }
+    // the slices' sums: a fixed share per thread, then the block's fixed tree
+    double pv[3] = {0.0, 0.0, 0.0};
+    for (int q = threadIdx.x; q < nb; q += blockDim.x)
+        for (int k = 0; k < 3; k++) pv[k] += part[3 * q + k];
+    for (int k = 0; k < 3; k++) pv[k] = block_sum_d(pv[k], dscr);
+    if (threadIdx.x != 0) return;
+    const double cv = pv[0], fv = pv[1], ck = pv[2];
     const DevScalars *sc = s.sc;
     const double N = (double)s.N, V = (double)s.Lx * (double)s.Ly, KE = sc->KE, W = sc->W;
     double v[kNumProps];
@@ -315,7 +316,8 @@ cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl
                           double *clKin, double *feaVir, double *kin, double *clVir) {
     cudaError_t e;
     if (ncl > 0) {
-        if ((e = L.kernel(k_props_cluster, dim3(ncl), dim3(128), 0, s, pos, clRange, clMass, unf, cmPos, cmVel, clKin)))
+        if ((e = L.kernel(k_props_cluster, dim3((ncl + kClusterWarps - 1) / kClusterWarps), dim3(32 * kClusterWarps), 0,
+                          s, pos, ncl, clRange, clMass, unf, cmPos, cmVel, clKin)))
             return e;
         if (s.ntri > 0 && s.feaForces) {
             if ((e = L.kernel(k_props_tri, dim3(tri_blocks(s.ntri)), dim3(kBlock), 0, s, (const double2 *)unf, feaVir)))
