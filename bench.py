@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--probe", default=None,
+                    choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras"],
+                    help="run one small fixed workload for a profiler capture and exit (no JSON line)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched and adjoint measurements added to the default line")
@@ -543,8 +546,92 @@ def adjoint_ratio(dev, reps=3, steps=200, every=20):
             "gradients": "initial positions and velocities, per-disk E and nu, log eps, log sigma"}
 
 
+# ------------------------------------------------------------------ probes
+#
+# Small fixed workloads for profiler captures (the commands in profiles/):
+# each runs once on cuda:0, prints "ok" and no JSON line.
+
+def probe(name):
+    import femmd_old_gb300 as F
+    import torch
+    if name == "midrun_rebuild":
+        # one neighbour rebuild of the large mixed system after 200 steps,
+        # inside the NVTX range "midrun", then run(12) launched directly
+        s = F.System()
+        S.large_mixed().replay(s)
+        s.run(0)
+        s.run(200)
+        s.sync()
+        torch.cuda.nvtx.range_push("midrun")
+        s.build_nn()
+        s.set_profiling(True)
+        s.run(12)
+        s.sync()
+        torch.cuda.nvtx.range_pop()
+    elif name in ("batch_run10", "batch_run10_single"):
+        # the 512-replica ensemble, run(0) then run(10) in one launch each:
+        # 1024 threads x 2 CTAs per SM with the heaviest replicas on CTA
+        # pairs, or 1024 x 1 with every replica on one CTA
+        b = F.Batch(0)
+        keep = []
+        for sc in S.batched_ensemble():
+            s = F.System(0)
+            sc.replay(s)
+            keep.append(s)
+            b.add(s)
+        if name == "batch_run10":
+            b.set_launch(1024, 2)
+        else:
+            b.set_launch(1024, 1)
+            b.set_split(False)
+        b.run(0)
+        b.run(10)
+        keep[0].sync()
+    elif name == "adjoint":
+        # config 5: forward with checkpoints every 20 steps, then the backward
+        c = F.System()
+        S.compression().replay(c)
+        c.run(0)
+        c.adjoint_forward(200, 20)
+        c.adjoint_observable()
+        c.adjoint_backward()
+        c.sync()
+    elif name == "extras":
+        # area springs (kArea 0.3) on the large mixed system: run(4), the
+        # observables, the cluster getter and three averaged steps; then the
+        # compression case through adjoint_forward(40, 20) and the backward
+        sc = S.large_mixed()
+        calls = []
+        for n, a in sc.calls:
+            calls.append((n, a))
+            if n == "set_elastomer_bonds":
+                calls.append(("set_kArea", (0.3,)))
+        s = F.System()
+        S.Scene(calls=calls, meta=sc.meta).replay(s)
+        s.run(0)
+        s.run(4)
+        s.properties()
+        s.clusters()
+        s.set_property_averaging(True, 5, 0)
+        s.run(3)
+        s.sync()
+        del s
+        c = F.System()
+        S.compression().replay(c)
+        c.adjoint_forward(40, 20)
+        c.adjoint_observable()
+        c.adjoint_backward()
+        c.sync()
+    else:
+        raise SystemExit(f"unknown probe {name}")
+    print("ok", flush=True)
+
+
 def main():
     args = parse()
+    if args.probe:
+        probe(args.probe)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":
