@@ -208,6 +208,7 @@ struct femmd_ctx {
         bool ready = false;
         int every = 0, endStep = 0, maxLen = 0;
         std::vector<int> segStart, segLen;
+        std::vector<std::vector<char>> segReb;  // per segment: a rebuild followed MID unit u
         DBuf<float2> ckX, ckV, slots, finalX, finalV, finalA, xbar, vbar, w0, w1, triD;
         DBuf<double> gMu, gLam, epsAcc, sigAcc;
     } adj;
@@ -2489,6 +2490,7 @@ femmd_status femmd_adjoint_forward(femmd_ctx *ctx, int steps, int every) {
     a.every = every;
     a.segStart.assign(nseg, 0);
     a.segLen.assign(nseg, 0);
+    a.segReb.assign(nseg, std::vector<char>());
     CK(a.ckX.ensure((size_t)nseg * N));
     CK(a.ckV.ensure((size_t)nseg * N));
     for (int g = 0; g < nseg; g++) {
@@ -2500,6 +2502,15 @@ femmd_status femmd_adjoint_forward(femmd_ctx *ctx, int steps, int every) {
         a.segStart[g] = ctx->steps;
         a.segLen[g] = len;
         if ((st = femmd_run(ctx, len))) return st;
+        // the run's MID unit u (forces at x_u) wrote observable row u-1, whose
+        // last column says whether a rebuild followed it
+        a.segReb[g].assign(len, 0);
+        if (len > 1) {
+            std::vector<double> o((size_t)(len - 1) * kObsCols);
+            CK(cudaMemcpyAsync(o.data(), ctx->obs.p, o.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            for (int u = 1; u < len; u++) a.segReb[g][u] = o[(size_t)(u - 1) * kObsCols + 5] != 0.0;
+        }
     }
     a.maxLen = std::min(every, steps);
     a.endStep = ctx->steps;
@@ -2555,7 +2566,9 @@ static femmd_status adj_recompute(femmd_ctx *ctx, int g, std::vector<int> &rebui
         CK(enqueue_step(L, s, MODE_MID, cur, 0, 0));
         float2 *pout = cur ? ctx->dpos0.p : ctx->dpos1.p;
         CK(cudaMemcpyAsync(a.slots.p + (size_t)(u + 1) * N, pout, N * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-        CK(enqueue_rebuild(L, s, 1 - cur, 1));
+        // the rebuild kernels only where the forward rebuilt (elsewhere
+        // their check would return at once); a disagreement is caught below
+        if (a.segReb[g][u]) CK(enqueue_rebuild(L, s, 1 - cur, 1));
         cur ^= 1;
     }
     femmd_status e;
@@ -2571,8 +2584,12 @@ static femmd_status adj_recompute(femmd_ctx *ctx, int g, std::vector<int> &rebui
         std::vector<double> o((size_t)rows * kObsCols);
         CK(cudaMemcpyAsync(o.data(), ctx->obs.p, o.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        for (int u = 1; u < K; u++)
-            if (o[(size_t)(u - 1) * kObsCols + 5] != 0.0) rebuilt.push_back(u + 1);
+        for (int u = 1; u < K; u++) {
+            const bool reb = o[(size_t)(u - 1) * kObsCols + 5] != 0.0;
+            if (reb != (a.segReb[g][u] != 0))
+                return fail(ctx, FEMMD_NOT_READY, "the recomputed segment's rebuilds differ from the forward pass");
+            if (reb) rebuilt.push_back(u + 1);
+        }
     }
     return FEMMD_OK;
 }
