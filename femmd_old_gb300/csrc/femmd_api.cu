@@ -1293,8 +1293,8 @@ static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
     // trajectory frames at the steps m in (s0, s0 + n] that are multiples of
     // 'every' (the reference's steps % trajectorySteps == 0).  Unit u of the
     // run computes the forces at x_{s0+u}; a frame inside the run replaces
-    // its unit by LAST (completes v_m), the copy, and FIRST (the same forces
-    // again, first half kick and drift) followed by the rebuild check, which
+    // its unit by LAST (completes v_m, keeps a_m), the copy, and the drift
+    // (half kick with a_m, drift, wrap) followed by the rebuild check, which
     // is the unit's work bit for bit.
     const int s0 = ctx->steps;
     std::vector<int> frames;
@@ -1313,7 +1313,9 @@ static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
         if (ctx->propAvg) CK(enqueue_step_props(ctx, D, s, ctx->cur));
         if ((st = traj_snapshot(ctx, m, aborted))) return st;
         if (aborted) return FEMMD_OK;
-        CK(enqueue_step(D, s, MODE_FIRST, ctx->cur, 0, 0));
+        // the rest of the fused step: half kick with the stored a_m and drift
+        // (a second force pass would repeat the area springs' displacement)
+        CK(enqueue_drift_in_run(D, s, ctx->cur));
         ctx->cur ^= 1;
         CK(enqueue_rebuild(D, s, ctx->cur, 1));
         ctx->profKernels += D.kernels;

@@ -112,3 +112,31 @@ def test_xyz_and_vtk_layouts(tmp_path):
     text = open(os.path.join(tmp_path, files[-1])).read()
     nt = s.counts()["triangles"]
     assert f"POINTS {n} FLOAT" in text and f"CELLS {nt} {4 * nt}" in text and "VECTORS Velocity FLOAT" in text
+
+
+def test_frames_and_averaging_leave_area_spring_runs_unchanged(tmp_path):
+    """With area springs (positions moved inside every force pass), a run
+    with trajectory frames and one with property averaging end bit for bit
+    where the plain run ends: the split step adds no second force pass."""
+    base = S.suspension(n_side=3, rings=6, bonds="boundary", T=0.6, center_jitter=0.3, phi=0.5)
+    calls = []
+    for n, a in base.calls:
+        calls.append((n, a))
+        if n == "set_elastomer_bonds":
+            calls.append(("set_kArea", (0.3,)))
+    sc = S.Scene(calls=calls, meta=dict(base.meta))
+    plain = system(sc)
+    plain.run(0)
+    plain.run(120)
+    framed = system(sc)
+    framed.run(0)
+    framed.set_trajectory(str(tmp_path / "a.dump"), 25, 0)
+    framed.run(120)
+    assert framed.flush_trajectory() == 4
+    averaged = system(sc)
+    averaged.set_property_averaging(True, 40, 0)
+    averaged.run(0)
+    averaged.run(120)
+    for other in (framed, averaged):
+        for x, y in zip(other.get_state(), plain.get_state()):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
