@@ -2355,7 +2355,20 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
     NEED(ctx);
     if (!out) return fail(ctx, FEMMD_INVALID_ARG, "null output");
     femmd_status st;
+    if ((st = prepare(ctx))) return st;
+    // the force pass of an evaluation must not move anything: with area
+    // springs it displaces the vertices, so the positions are put back
+    const bool area = ctx->areaForces && ctx->areaUnits > 0 && !ctx->pos.empty();
+    const size_t np = ctx->pos.size();
+    if (area) {
+        CK(ctx->ckPos.ensure(np));
+        CK(cudaMemcpyAsync(ctx->ckPos.p, ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, np * sizeof(float2),
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     if ((st = femmd_calc_forces(ctx))) return st;
+    if (area)
+        CK(cudaMemcpyAsync(ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, ctx->ckPos.p, np * sizeof(float2),
+                           cudaMemcpyDeviceToDevice, ctx->stream));
     const int N = (int)ctx->pos.size(), nt = (int)ctx->refVol.size(), ncl = (int)ctx->clusters.size();
     for (int k = 0; k < 10; k++) out[k] = 0.0;
     if (N == 0) return FEMMD_OK;

@@ -140,3 +140,11 @@ def test_frames_and_averaging_leave_area_spring_runs_unchanged(tmp_path):
     for other in (framed, averaged):
         for x, y in zip(other.get_state(), plain.get_state()):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    # evaluating the properties moves nothing either, and the run continues
+    # as if it had not been called
+    before = plain.positions().copy()
+    plain.properties()
+    assert np.array_equal(plain.positions().view(np.uint32), before.view(np.uint32))
+    plain.run(30)
+    averaged.run(30)
+    assert np.array_equal(plain.positions().view(np.uint32), averaged.positions().view(np.uint32))
