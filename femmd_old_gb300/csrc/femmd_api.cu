@@ -2785,6 +2785,10 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
             return bfail(b, st, "replica: %s", c->err.c_str());
         if (c->areaForces && !c->refVol.empty())
             return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel does not implement the area springs");
+        if (c->traj.on)
+            return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel does not write trajectory frames");
+        if (c->propAvg)
+            return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel does not average properties");
         // the replica's own uploads must land before the batch stream reads them
         BCK(cudaStreamSynchronize(c->stream));
     }

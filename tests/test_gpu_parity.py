@@ -185,6 +185,14 @@ def test_area_springs_outside_the_batch_and_adjoint():
     assert "UNSUPPORTED" in str(e.value)
     s.set_kArea(0.0)  # off again: the system runs in the batch
     b.run(5)
+    # trajectory frames and property averaging are not done by the batched
+    # kernel either: refused, not silently skipped
+    s.set_property_averaging(True, 10, 0)
+    with pytest.raises(F.FemmdError) as e:
+        b.run(5)
+    assert "UNSUPPORTED" in str(e.value)
+    s.set_property_averaging(False)
+    b.run(5)
 
 
 # ------------------------------------------------------------- FP64 checks
