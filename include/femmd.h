@@ -239,8 +239,10 @@ femmd_status femmd_get_profile(femmd_ctx *ctx, double *force_kernel_ms, long lon
  * running them one by one -- with one CTA per group of replicas
  * (longest-processing-time assignment) and no per-step launches.  Replicas
  * must share the number of types, the sigma mode, the periodicity and the
- * image mode.  A replica's results are read with the usual getters on its
- * context.  The batch does not own the contexts. */
+ * image mode; a replica with area springs, trajectory frames or property
+ * averaging on makes femmd_batch_run return FEMMD_UNSUPPORTED (the batched
+ * kernel does none of them).  A replica's results are read with the usual
+ * getters on its context.  The batch does not own the contexts. */
 typedef struct femmd_batch femmd_batch;
 femmd_status femmd_batch_create(int device, femmd_batch **out);
 void femmd_batch_destroy(femmd_batch *b);
