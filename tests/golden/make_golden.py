@@ -249,6 +249,27 @@ def case_susp_area():
     return probes(sc, runs=(100, 250))
 
 
+def case_susp_area_xpbc():
+    """Area springs in an XPBC box under gravity: the reference's fixed
+    top/bottom walls and gravity act on the positions from before the area
+    pass, the pairs on those after it."""
+    verts, tris = S.hex_disk_mesh(2.5, 3, jitter=0.02, seed=91)
+    nv = verts.shape[0]
+    L = 22.0
+    sc = S.Scene(meta=dict(workload="susp_area_xpbc"))
+    sc.add("init", L, L).add("PBC", 1).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [S.WCA_RC], [1.0]).add("set_skin", 0.3)
+    sc.add("set_kBond", 80.0).add("set_youngs_modulus", 40.0).add("set_poisson_ratio", 0.3)
+    sc.add("set_elastomer_bonds", 1).add("set_gravity", 2.0).add("set_kArea", 0.5)
+    for c in [(5.0, 3.2), (12.0, 3.4), (18.5, 9.0), (8.0, 18.9)]:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 0, 0, 1.0, float(nv), True)
+    sc.add("init_neighbor_list")
+    sc.add("set_capacity", 64, 256)
+    rng = np.random.Generator(np.random.PCG64(92))
+    sc.add("set_velocities_array", rng.normal(0, 0.6, size=(4 * nv, 2)).astype(np.float32))
+    return probes(sc, runs=(150, 300))
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 

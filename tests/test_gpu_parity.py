@@ -31,7 +31,7 @@ from oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 FEA_CASES = {"susp_all", "susp_boundary", "susp_refdisk", "susp_crossing", "susp_mixed", "susp_xpbc_gravity",
-             "susp_area"}
+             "susp_area", "susp_area_xpbc"}
 F_IMAGE_REFERENCE = 0
 F_IMAGE_EXACT = 1
 STATE_FIELDS = ("pos", "vel", "acc", "force")

@@ -23,7 +23,7 @@ def test_golden_cases_cover_edge_cases():
     names = set(G.names())
     for required in ("lj_xy", "lj_multitype", "lj_xpbc", "lj_nopbc", "tiny_box", "susp_all", "susp_boundary",
                      "susp_refdisk", "susp_crossing", "susp_mixed", "lj_nopbc_walls", "susp_xpbc_gravity",
-                     "susp_area"):
+                     "susp_area", "susp_area_xpbc"):
         assert required in names
 
 
