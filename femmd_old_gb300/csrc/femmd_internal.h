@@ -34,12 +34,13 @@ constexpr int kTraceCols = 6;      // per-step trace row (ns): tri start/end, st
 // Per type-pair constants, all formed on the host with the reference's float
 // operations (interactionsCuda.cu:43-55, 79-88) so that the kernel's per-pair
 // arithmetic reproduces the reference bit for bit.
-struct PairEntry {
+// The four values the pair loop reads first share one aligned 16 bytes.
+struct __align__(16) PairEntry {
     float rcut2;  // (rc*rc)*sigma_ij*sigma_ij      (sigma by type)
-    float sig2;   // sigma_ij*sigma_ij              (sigma by type)
     float c;      // 48*eps/(sigma_ij*sigma_ij)     (sigma by type)
     float eps4;   // 4*eps
     float us;     // uShift
+    float sig2;   // sigma_ij*sigma_ij              (sigma by type)
     float rc;     // rc (units of sigma_ij)
     float eps48;  // 48*eps
     float pad;
