@@ -923,7 +923,7 @@ static femmd_status props_buffers(femmd_ctx *ctx) {
     }
     CK(ctx->unf.ensure(std::max(N, 1))); CK(ctx->kinTerm.ensure(std::max(N, 1))); CK(ctx->clVir.ensure(std::max(N, 1)));
     // the accumulator's reduction: a fixed number of blocks per system size
-    ctx->propBlocks = std::max(1, std::min(1216, (N + 1023) / 1024));
+    ctx->propBlocks = std::max(1, std::min(304, (N + 4095) / 4096));
     CK(ctx->propPart.ensure(3 * (size_t)ctx->propBlocks));
     CK(cudaStreamSynchronize(sm));  // the host vectors above are not pinned
     ctx->propsUploaded = true;
@@ -935,13 +935,16 @@ static femmd_status props_buffers(femmd_ctx *ctx) {
 static cudaError_t enqueue_step_props(femmd_ctx *ctx, Launch &L, const DevSys &s, int parity) {
     const float2 *pc = parity ? s.pos1 : s.pos0;
     const int ncl = (int)ctx->clusters.size(), nt = (int)ctx->refVol.size();
+    // the cluster virial lives on the elastomers' particles, the first ones
+    const int ncp = ncl > 0 ? ctx->clusters.back().offset + ctx->clusters.back().nv : 0;
     cudaError_t e = enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p,
                                   ctx->cmPos.p, ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p,
-                                  ctx->clVir.p);
+                                  ctx->clVir.p, ncp);
     if (e) return e;
     const bool tri = ncl > 0 && s.ntri > 0 && s.feaForces;
     return enqueue_props_accum(L, s, ctx->props.p, ctx->propPart.p, ctx->propBlocks, ncl > 0 ? ctx->clKin.p : nullptr,
-                               ncl, tri ? ctx->feaVir.p : nullptr, nt, ctx->clVir.p, ctx->propAvgEvery, ctx->propEqui);
+                               ncl, tri ? ctx->feaVir.p : nullptr, nt, ctx->clVir.p, ncp, ctx->propAvgEvery,
+                               ctx->propEqui);
 }
 
 // Graph of 'units' x [MID step on parity p -> IF(rebuild on 1-p)] starting at
@@ -2379,7 +2382,7 @@ femmd_status femmd_get_properties(femmd_ctx *ctx, double *out) {
     Launch L;
     L.stream = sm;
     CK(enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p, ctx->cmPos.p,
-                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p));
+                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p, N));
     std::vector<double> kin(N), cv(N), fv(std::max(nt, 1), 0.0), ck(std::max(ncl, 1), 0.0);
     CK(cudaMemcpyAsync(kin.data(), ctx->kinTerm.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
     CK(cudaMemcpyAsync(cv.data(), ctx->clVir.p, N * sizeof(double), cudaMemcpyDeviceToHost, sm));
@@ -2427,7 +2430,7 @@ femmd_status femmd_get_clusters(femmd_ctx *ctx, double *cm, double *cm_vel, doub
     Launch L;
     L.stream = ctx->stream;
     CK(enqueue_props(L, s, pc, ncl, ctx->clRange.p, ctx->clMass.p, ctx->clusterOf.p, ctx->unf.p, ctx->cmPos.p,
-                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p));
+                     ctx->cmVel.p, ctx->clKin.p, ctx->feaVir.p, ctx->kinTerm.p, ctx->clVir.p, N));
     CK(enqueue_cluster_centroid(L, s, pc, ncl, ctx->clRange.p, ctx->centroid.p));
     if (cm) CK(cudaMemcpyAsync(cm, ctx->cmPos.p, ncl * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
     if (cm_vel) CK(cudaMemcpyAsync(cm_vel, ctx->cmVel.p, ncl * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));

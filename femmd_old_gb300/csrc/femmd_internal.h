@@ -199,10 +199,12 @@ struct DevProps {
 // and close a window at steps past stepEqui that are multiples of stepAvg.
 cudaError_t enqueue_props_accum(Launch &L, const DevSys &s, DevProps *P, double *partials, int blocks,
                                 const double *clKin, int ncl, const double *feaVir, int ntri, const double *clVir,
-                                int stepAvg, int stepEqui);
+                                int nvir, int stepAvg, int stepEqui);
 cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
                           const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
-                          double *clKin, double *feaVir, double *kin, double *clVir);
+                          double *clKin, double *feaVir, double *kin, double *clVir, int npart);
+// (kin and clVir of particles [0, npart); the cluster virial is zero beyond
+// the elastomers, which come first)
 
 // ---- batched replicas (k_batch.cu): one persistent launch over many systems
 struct BatchLaunch {

@@ -28,6 +28,18 @@ __device__ __forceinline__ double block_sum_d(double v, double *scr) {
     return scr[0];
 }
 
+// three block sums in one pass (a fixed tree); valid in thread 0
+__device__ __forceinline__ void block_sum3_d(double *v, double *scr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < 3; k++) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < 3; k++) scr[3 * warp + k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 32)
+        for (int k = 0; k < 3; k++) v[k] = warp_sum(lane < nw ? scr[3 * lane + k] : 0.0);
+}
+
 // sum over the warp, the same value in every lane (butterfly: a fixed order)
 __device__ __forceinline__ double warp_sum_all(double v) {
 #pragma unroll
@@ -166,17 +178,18 @@ __global__ void __launch_bounds__(kBlock) k_props_tri(DevSys s, const double2 *u
     feaVir[t] = acc;
 }
 
-// Per particle: m v^2 and the cluster virial 1/2 f_ij . (R_ci - R_cj)
-// (nearest image) over its Verlet list, for pairs of two cluster particles.
+// Per particle of [0, n): m v^2 and the cluster virial 1/2 f_ij . (R_ci -
+// R_cj) (nearest image) over its Verlet list, for pairs of two cluster
+// particles.
 template <bool WX, bool WY>
-__global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const float2 *pos, const int *clusterOf,
+__global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const float2 *pos, int n, const int *clusterOf,
                                                               const double2 *cmPos, double *kin, double *clVir) {
     extern __shared__ PairEntry tab[];
     const int nt2 = s.numTypes > 1 ? s.numTypes * s.numTypes : 1;
     for (int k = threadIdx.x; k < nt2; k += blockDim.x) tab[k] = s.pair[k];
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.N) return;
+    if (i >= n) return;
     const float2 vi = s.vel[i];
     kin[i] = (double)s.mass[i] * ((double)vi.x * vi.x + (double)vi.y * vi.y);
     double cv = 0.0;
@@ -241,19 +254,31 @@ __global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const f
 // new window.
 __global__ void __launch_bounds__(kBlock) k_props_accum(DevSys s, DevProps *P, double *part, const double *clKin,
                                                         int ncl, const double *feaVir, int ntri, const double *clVir,
-                                                        int stepAvg, int stepEqui) {
-    __shared__ double dscr[32];
+                                                        int nvir, int stepAvg, int stepEqui) {
+    __shared__ double dscr[3 * 32];
     __shared__ bool last;
     const int nb = gridDim.x, b = blockIdx.x;
-    const int n3[3] = {s.N, feaVir ? ntri : 0, clKin ? ncl : 0};
+    const int n3[3] = {nvir, feaVir ? ntri : 0, clKin ? ncl : 0};
     const double *arr[3] = {clVir, feaVir, clKin};
+    double sums[3];
     for (int k = 0; k < 3; k++) {
         const int per = (n3[k] + nb - 1) / nb, lo = min(n3[k], b * per), hi = min(n3[k], lo + per);
-        double a = 0.0;
-        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) a += arr[k][i];
-        a = block_sum_d(a, dscr);
-        if (threadIdx.x == 0) part[3 * b + k] = a;
+        // four independent sums per thread (the loads overlap), then added
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        const int st = blockDim.x;
+        int i = lo + threadIdx.x;
+        for (; i + 3 * st < hi; i += 4 * st) {
+            a0 += arr[k][i];
+            a1 += arr[k][i + st];
+            a2 += arr[k][i + 2 * st];
+            a3 += arr[k][i + 3 * st];
+        }
+        for (; i < hi; i += st) a0 += arr[k][i];
+        sums[k] = (a0 + a1) + (a2 + a3);
     }
+    block_sum3_d(sums, dscr);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; k++) part[3 * b + k] = sums[k];
     if (threadIdx.x == 0) {
         __threadfence();
         last = atomicAdd(&P->ticket, 1u) == (unsigned)nb - 1;
@@ -265,7 +290,8 @@ __global__ void __launch_bounds__(kBlock) k_props_accum(DevSys s, DevProps *P, d
     double pv[3] = {0.0, 0.0, 0.0};
     for (int q = threadIdx.x; q < nb; q += blockDim.x)
         for (int k = 0; k < 3; k++) pv[k] += part[3 * q + k];
-    for (int k = 0; k < 3; k++) pv[k] = block_sum_d(pv[k], dscr);
+    __syncthreads();  // dscr was used by this block's own slice sums
+    block_sum3_d(pv, dscr);
     if (threadIdx.x != 0) return;
     const double cv = pv[0], fv = pv[1], ck = pv[2];
     const DevScalars *sc = s.sc;
@@ -306,14 +332,14 @@ __global__ void __launch_bounds__(kBlock) k_props_accum(DevSys s, DevProps *P, d
 
 cudaError_t enqueue_props_accum(Launch &L, const DevSys &s, DevProps *P, double *partials, int blocks,
                                 const double *clKin, int ncl, const double *feaVir, int ntri, const double *clVir,
-                                int stepAvg, int stepEqui) {
+                                int nvir, int stepAvg, int stepEqui) {
     return L.kernel(k_props_accum, dim3(blocks), dim3(kBlock), 0, s, P, partials, clKin, ncl, feaVir, ntri, clVir,
-                    stepAvg, stepEqui);
+                    nvir, stepAvg, stepEqui);
 }
 
 cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl, const int2 *clRange,
                           const float *clMass, const int *clusterOf, double2 *unf, double2 *cmPos, double2 *cmVel,
-                          double *clKin, double *feaVir, double *kin, double *clVir) {
+                          double *clKin, double *feaVir, double *kin, double *clVir, int npart) {
     cudaError_t e;
     if (ncl > 0) {
         if ((e = L.kernel(k_props_cluster, dim3((ncl + kClusterWarps - 1) / kClusterWarps), dim3(32 * kClusterWarps), 0,
@@ -324,13 +350,14 @@ cudaError_t enqueue_props(Launch &L, const DevSys &s, const float2 *pos, int ncl
                 return e;
         }
     }
-    dim3 g(step_blocks(s.N)), b(kStepBlock);
+    dim3 g(step_blocks(npart)), b(kStepBlock);
     size_t smt = sizeof(PairEntry) * (size_t)(s.numTypes > 1 ? s.numTypes * s.numTypes : 1);
     const int *co = ncl > 0 ? clusterOf : nullptr;
     if (s.wrapx && s.wrapy)
-        return L.kernel(k_props_particle<true, true>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
-    if (s.wrapx) return L.kernel(k_props_particle<true, false>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
-    return L.kernel(k_props_particle<false, false>, g, b, smt, s, pos, co, (const double2 *)cmPos, kin, clVir);
+        return L.kernel(k_props_particle<true, true>, g, b, smt, s, pos, npart, co, (const double2 *)cmPos, kin, clVir);
+    if (s.wrapx)
+        return L.kernel(k_props_particle<true, false>, g, b, smt, s, pos, npart, co, (const double2 *)cmPos, kin, clVir);
+    return L.kernel(k_props_particle<false, false>, g, b, smt, s, pos, npart, co, (const double2 *)cmPos, kin, clVir);
 }
 
 }  // namespace femmd
