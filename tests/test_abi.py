@@ -87,3 +87,27 @@ def test_info_matches_reference_fields():
     assert info["nbonds"] == 2 * setup["bonds"].shape[0]  # bondList.size(), interface.cpp:575
     assert info["ntrigs"] == setup["tris"].shape[0]
     assert info["nelastomers"] == 9
+
+
+def test_argument_limits_without_gpu():
+    """Host-side checks at the limits, before any GPU work: type count in
+    [1, 32] (five tag bits in the list entries), averaging windows, cell
+    factor in [1, 8], a negative skin."""
+    s = F.System()
+    s.init(10, 10)
+    s.set_numTypes(32)
+    with pytest.raises(F.FemmdError) as e:
+        s.set_numTypes(33)
+    assert "INVALID_ARG" in str(e.value)
+    s.set_numTypes(1)
+    with pytest.raises(F.FemmdError):
+        s.set_property_averaging(True, 0, 10)
+    with pytest.raises(F.FemmdError):
+        s.set_property_averaging(True, 10, -1)
+    s.set_property_averaging(False)  # off needs no window
+    for bad in (0.5, 9.0):
+        with pytest.raises(F.FemmdError):
+            s.set_cell_factor(bad)
+    s.set_cell_factor(2.0)
+    with pytest.raises(F.FemmdError):
+        s.set_skin(-0.1)
