@@ -174,14 +174,43 @@ class System:
         self._call("femmd_get_wall_forces", C.byref(t), C.byref(b))
         return t.value, b.value
 
+    # layouts of femmd_set_trajectory / femmd_save_frame
+    FRAME_DUMP, FRAME_XYZ, FRAME_VTK, FRAME_VTF, FRAME_CLUSTER_VTF, FRAME_VTU, FRAME_VTU_BIN = range(7)
+
     def set_trajectory(self, path, every, fmt=0):
-        """Frames every 'every' steps of run(): fmt 0 dump, 1 xyz, 2 vtk."""
+        """Frames every 'every' steps of run(), in layout fmt (FRAME_*)."""
         self._call("femmd_set_trajectory", None if path is None else str(path).encode(), int(every), int(fmt))
 
     def flush_trajectory(self):
         n = C.c_longlong()
         self._call("femmd_flush_trajectory", C.byref(n))
         return n.value
+
+    def save_frame(self, path, fmt, append=0):
+        """The current state written now in layout fmt; append 0 starts the file anew."""
+        self._call("femmd_save_frame", str(path).encode(), int(fmt), int(append))
+
+    # the reference's writers by their script names (interface.cpp:664-668)
+    def save_vtk(self, name):
+        self.save_frame(name, self.FRAME_VTK)
+
+    def save_vtf(self, name, flag):
+        self.save_frame(name, self.FRAME_VTF, flag)
+
+    def save_cluster_vtf(self, name, flag):
+        self.save_frame(name, self.FRAME_CLUSTER_VTF, flag)
+
+    def save_cluster_xyz(self, name, flag):
+        self.save_frame(name, self.FRAME_DUMP, flag)
+
+    def save_xyz(self, name, flag):
+        self.save_frame(name, self.FRAME_XYZ, flag)
+
+    def save_vtk_xml(self, name, binary=False):
+        self.save_frame(name, self.FRAME_VTU_BIN if binary else self.FRAME_VTU)
+
+    def set_scale(self, scale):
+        self._call("femmd_set_scale", float(scale))
 
     PROPERTY_NAMES = ("uKinetic", "uPotential", "uTotal", "temperature", "virial", "feaVirial", "pressure",
                       "clusterUKinetic", "clusterVirial", "molPressure")

@@ -53,6 +53,8 @@ SIGNATURES = {
     "femmd_get_average_properties": (i_, [P, dp, dp, dp, C.POINTER(i_), C.POINTER(i_), C.POINTER(i_)]),
     "femmd_set_trajectory": (i_, [P, C.c_char_p, i_, i_]),
     "femmd_flush_trajectory": (i_, [P, llp]),
+    "femmd_save_frame": (i_, [P, C.c_char_p, i_, i_]),
+    "femmd_set_scale": (i_, [P, d_]),
     "femmd_adjoint_forward": (i_, [P, i_, i_]),
     "femmd_adjoint_backward": (i_, [P, d_, d_, fp, fp, fp, fp, dp, dp, dp, dp]),
     "femmd_adjoint_observable": (i_, [P, dp, dp]),

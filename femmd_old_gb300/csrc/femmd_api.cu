@@ -89,10 +89,24 @@ struct TrajFrame {
     int step, slot;
 };
 
+// What a frame is formatted with: the layout, the file, and the topology
+// (copied from the context when it changes, so that the writer thread never
+// reads the context).
+struct FrameMeta {
+    std::string path;
+    int format = 0;
+    std::vector<int> type, tri, bond;
+    std::vector<float> mass, sigma;
+    std::vector<int2> clusters;  // (offset, vertices)
+    std::vector<float> clusterMass;
+    float Lx = 0, Ly = 0, scale = 1;
+};
+
 struct Trajectory {
     bool on = false;
-    std::string path;
-    int every = 0, format = 0;
+    FrameMeta meta;
+    bool headerDone = false;  // the VTF layouts write their header with the first frame
+    int every = 0;
     long long lastCommitted = LLONG_MIN;
     int N = 0;
     std::vector<float2 *> pos, vel;  // pinned slots
@@ -106,12 +120,6 @@ struct Trajectory {
     bool stop = false;
     std::string error;
     long long written = 0;
-    // metadata the writer formats with (copied when the topology is uploaded)
-    std::vector<int> type, tri;
-    std::vector<float> mass;
-    std::vector<int2> clusters;  // (offset, vertices)
-    std::vector<float> clusterMass;
-    float Lx = 0, Ly = 0;
 };
 
 struct femmd_ctx {
@@ -126,6 +134,7 @@ struct femmd_ctx {
     bool bondForces = false, feaForces = false;
     float kBond = 0, E = 0, nu = 0.3f, lambda = 0, mu = 0, C1 = 0, C2 = 0, C3 = 0, gravity = 0, kArea = 0;
     float kWall = 10.0f;  // Interactions::init (interactions.cpp:22)
+    float scale = 1.0f;   // MDSystem::scale (set_scale): the cluster VTF radius is 0.5 scale + 0.5
     bool gravityForce = false, areaForces = false;
     int feaLaw = FEMMD_FEA_NEO_HOOKEAN, bondKMode = FEMMD_BONDK_KBOND, imageMode = FEMMD_IMAGE_EXACT;
     int bondMode = FEMMD_ELASTOMER_BONDS_ALL;
@@ -1064,34 +1073,62 @@ static void unfold_cluster(const float2 *p, float *ux, float *uy, int off, int n
     }
 }
 
-// One frame in the reference's layouts: 0 = saveClusterXYZ's dump
-// (md3dsystem.cpp:248-273, every particle), 1 = saveXYZ (:232-246),
-// 2 = saveVtk (:275-328, one file per frame, clusters unfolded).
-static bool write_frame(Trajectory &T, int step, const float2 *p, const float2 *v, std::string &err) {
-    const int N = T.N;
-    if (T.format == 2) {
-        if (T.clusters.empty()) return true;  // saveVtk writes nothing without elastomers
-        char name[1024];
-        snprintf(name, sizeof name, "%s%.9d.vtk", T.path.c_str(), step);
-        FILE *f = fopen(name, "w");
-        if (!f) {
-            err = std::string("cannot open ") + name;
-            return false;
-        }
-        std::vector<float> ux(N), uy(N);
-        for (int i = 0; i < N; i++) {
-            ux[i] = p[i].x;
-            uy[i] = p[i].y;
-        }
-        for (const int2 &c : T.clusters) unfold_cluster(p, ux.data() + c.x, uy.data() + c.x, c.x, c.y, T.Lx, T.Ly);
+// Positions with every elastomer unfolded (FeaElements::unfoldPos,
+// feaElements.cpp:86-150); the other particles keep their wrapped positions.
+// (The reference reads unfoldedPos past the elastomers' vertices, which it
+// never sizes for; here those particles are written where they are.)
+static void unfolded_positions(const FrameMeta &M, int N, const float2 *p, std::vector<float> &ux,
+                               std::vector<float> &uy) {
+    ux.resize(N);
+    uy.resize(N);
+    for (int i = 0; i < N; i++) {
+        ux[i] = p[i].x;
+        uy[i] = p[i].y;
+    }
+    for (const int2 &c : M.clusters) unfold_cluster(p, ux.data() + c.x, uy.data() + c.x, c.x, c.y, M.Lx, M.Ly);
+}
+
+// The VTF type name of particle type t (md3dsystem.cpp:333: 'A' for type 0
+// on; the reference's table ends at 'F', later letters continue it).
+static char type_letter(int t) { return t >= 0 && t < 26 ? (char)('A' + t) : '?'; }
+
+static FILE *open_out(const std::string &name, const char *mode, std::string &err) {
+    FILE *f = fopen(name.c_str(), mode);
+    if (!f) err = "cannot open " + name;
+    return f;
+}
+
+// The per-frame file '<path><step, 9 digits><ext>' of saveVtk and saveVtkXML.
+static std::string step_file(const FrameMeta &M, int step, const char *ext) {
+    char num[32];
+    snprintf(num, sizeof num, "%.9d", step);
+    return M.path + num + ext;
+}
+
+// One frame in the reference's layouts (md3dsystem.cpp):
+//   0 saveClusterXYZ's dump (:248-273; every particle), 1 saveXYZ (:232-246),
+//   2 saveVtk (:275-328), 3 saveVTF (:330-353), 4 saveClusterVTF (:355-378),
+//   5 saveVtkXML (:381-443), 6 saveVtkXMLBin (:451-522).
+// Layouts 0, 1, 3 and 4 add to 'path' (started anew with 'truncate'; 'header'
+// writes the VTF structure block first, as the reference does for s == 0);
+// 2, 5 and 6 write one file per frame named by the step count.
+static bool write_frame(const FrameMeta &M, int N, int step, const float2 *p, const float2 *v, bool truncate,
+                        bool header, std::string &err) {
+    const int nt = (int)M.tri.size() / 3;
+    const int ncl = (int)M.clusters.size();
+    if (M.format == 2) {
+        if (M.clusters.empty()) return true;  // saveVtk writes nothing without elastomers
+        FILE *f = open_out(step_file(M, step, ".vtk"), "w", err);
+        if (!f) return false;
+        std::vector<float> ux, uy;
+        unfolded_positions(M, N, p, ux, uy);
         fprintf(f, "# vtk DataFile Version 3.1\nReally cool data\nASCII\nDATASET UNSTRUCTURED_GRID\n\n");
         fprintf(f, "POINTS %d FLOAT\n", N);
         for (int i = 0; i < N; i++) fprintf(f, "%f %f %f\n", ux[i], uy[i], 0.0f);
         fprintf(f, "\n");
-        const int nt = (int)T.tri.size() / 3;
         if (nt > 0) {
             fprintf(f, "CELLS %d %d\n", nt, 4 * nt);
-            for (int t = 0; t < nt; t++) fprintf(f, "%d %d %d %d\n", 3, T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2]);
+            for (int t = 0; t < nt; t++) fprintf(f, "%d %d %d %d\n", 3, M.tri[3 * t], M.tri[3 * t + 1], M.tri[3 * t + 2]);
             fprintf(f, "\nCELL_TYPES %d\n", nt);
             for (int t = 0; t < nt; t++) fprintf(f, "%d ", 5);
             fprintf(f, "\n\n");
@@ -1103,23 +1140,133 @@ static bool write_frame(Trajectory &T, int step, const float2 *p, const float2 *
         fclose(f);
         return true;
     }
-    FILE *f = fopen(T.path.c_str(), "a");
-    if (!f) {
-        err = "cannot open " + T.path;
-        return false;
+    if (M.format == 5 || M.format == 6) {
+        FILE *f = open_out(step_file(M, step, ".vtu"), M.format == 6 ? "wb" : "w", err);
+        if (!f) return false;
+        std::vector<float> ux, uy;
+        unfolded_positions(M, N, p, ux, uy);
+        if (M.format == 5) fprintf(f, "<?xml version=\"1.0\"?>\n");
+        fprintf(f, "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n");
+        fprintf(f, "\t<UnstructuredGrid>\n\t\t<Piece NumberOfPoints=\"%d\" NumberOfCells=\"%d\">\n", N, nt);
+        if (M.format == 5) {
+            fprintf(f, "\t\t\t<PointData Scalars=\"scalars\">\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" format=\"ascii\" Name=\"VelocitySquared\">\n");
+            for (int i = 0; i < N; i++) fprintf(f, "%f ", v[i].x * v[i].x + v[i].y * v[i].y);
+            fprintf(f, "\n\t\t\t\t</DataArray>\n\t\t\t</PointData>\n");
+            fprintf(f, "\t\t\t<Points>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" format=\"ascii\" NumberOfComponents=\"3\">\n");
+            for (int i = 0; i < N; i++) fprintf(f, "%f %f %f ", ux[i], uy[i], 0.0f);
+            fprintf(f, "\n\t\t\t\t</DataArray>\n\t\t\t</Points>\n");
+            fprintf(f, "\t\t\t<Cells>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n");
+            for (int t = 0; t < nt; t++) fprintf(f, "%d %d %d ", M.tri[3 * t], M.tri[3 * t + 1], M.tri[3 * t + 2]);
+            fprintf(f, "\n\t\t\t\t</DataArray>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Int32\" format=\"ascii\" Name=\"offsets\">\n");
+            for (int t = 0; t < nt; t++) fprintf(f, "%d ", 3 * (t + 1));
+            fprintf(f, "\n\t\t\t\t</DataArray>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Int32\" format=\"ascii\" Name=\"types\">\n");
+            for (int t = 0; t < nt; t++) fprintf(f, "%d ", 5);
+            fprintf(f, "\n\t\t\t\t</DataArray>\n\t\t\t</Cells>\n");
+            fprintf(f, "\t\t</Piece>\n\t</UnstructuredGrid>\n</VTKFile>");
+        } else {
+            // appended raw arrays, each behind a 4-byte little-endian byte count;
+            // the offsets count from the byte after '_'
+            const uint32_t nVv = 4u * N, nPts = 12u * N, nCon = 12u * nt, nOff = 4u * nt, nTyp = (uint32_t)nt;
+            const uint32_t oPts = nVv + 4, oCon = oPts + nPts + 4, oOff = oCon + nCon + 4, oTyp = oOff + nOff + 4;
+            fprintf(f, "\t\t\t<PointData Scalars=\"scalars\">\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" format=\"appended\" Name=\"VelocitySquared\" offset=\"%d\"/>\n", 0);
+            fprintf(f, "\t\t\t</PointData>\n\t\t\t<Points>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" format=\"appended\" NumberOfComponents=\"3\" offset=\"%u\"/>\n",
+                    oPts);
+            fprintf(f, "\t\t\t</Points>\n\t\t\t<Cells>\n");
+            fprintf(f, "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"appended\" offset=\"%u\"/>\n", oCon);
+            fprintf(f, "\t\t\t\t<DataArray type=\"UInt32\" Name=\"offsets\" Format=\"appended\" offset=\"%u\"/>\n", oOff);
+            fprintf(f, "\t\t\t\t<DataArray type=\"UInt8\" Name=\"types\" Format=\"appended\" offset=\"%u\"/>\n", oTyp);
+            fprintf(f, "\t\t\t</Cells>\n\t\t</Piece>\n\t</UnstructuredGrid>\n");
+            fprintf(f, "\t<AppendedData encoding=\"raw\">\n\t_");
+            // the arrays are laid out in host memory and written with explicit
+            // little-endian byte counts, so the file is the same on any host
+            std::vector<unsigned char> raw;
+            raw.reserve(20 + nVv + nPts + nCon + nOff + nTyp);
+            auto put32 = [&](uint32_t w) {
+                for (int b = 0; b < 4; b++) raw.push_back((unsigned char)(w >> (8 * b)));
+            };
+            auto putf = [&](float x) {
+                uint32_t w;
+                memcpy(&w, &x, 4);
+                put32(w);
+            };
+            put32(nVv);
+            for (int i = 0; i < N; i++) putf(v[i].x * v[i].x + v[i].y * v[i].y);
+            put32(nPts);
+            for (int i = 0; i < N; i++) {
+                putf(ux[i]);
+                putf(uy[i]);
+                putf(0.0f);
+            }
+            put32(nCon);
+            for (int t = 0; t < 3 * nt; t++) put32((uint32_t)M.tri[t]);
+            put32(nOff);
+            for (int t = 0; t < nt; t++) put32(3u * (t + 1));
+            put32(nTyp);
+            for (int t = 0; t < nt; t++) raw.push_back(5);
+            fwrite(raw.data(), 1, raw.size(), f);
+            fprintf(f, "\n\t</AppendedData>\n</VTKFile>");
+        }
+        const bool ok = !ferror(f);
+        fclose(f);
+        if (!ok) err = "write failed";
+        return ok;
     }
-    if (T.format == 1) {
+    FILE *f = open_out(M.path, truncate ? "w" : "a", err);
+    if (!f) return false;
+    if (M.format == 1) {
         fprintf(f, "%d\n\n", N);
         for (int i = 0; i < N; i++) fprintf(f, "A\t%f\t%f\t%f\n", p[i].x, p[i].y, 0.0f);
+    } else if (M.format == 3) {
+        if (header) {
+            // radius = sigma / 2 (Particles::addParticle, particles.cpp:218)
+            for (int i = 0; i < N; i++)
+                fprintf(f, "atom %d type %c radius %f\n", i, type_letter(M.type[i]), (double)M.sigma[i] / 2.0);
+            for (size_t b = 0; 2 * b + 1 < M.bond.size(); b++) fprintf(f, "bond %d:%d\n", M.bond[2 * b], M.bond[2 * b + 1]);
+            fprintf(f, "pbc %f %f %f\n", (double)M.Lx, (double)M.Ly, 1.0);
+        }
+        fprintf(f, "timestep\n");
+        for (int i = 0; i < N; i++) fprintf(f, "%f %f %f\n", p[i].x, p[i].y, 0.0f);
+    } else if (M.format == 4) {
+        if (header) {
+            // one atom per elastomer; the reference names atom i by the type
+            // of particle i (md3dsystem.cpp:361), kept as it is
+            for (int c = 0; c < ncl; c++)
+                fprintf(f, "atom %d type %c radius %f\n", c, type_letter(c < N ? M.type[c] : 0),
+                        0.5 * (double)M.scale + 0.5);
+            fprintf(f, "pbc %f %f %f\n", (double)M.Lx, (double)M.Ly, 1.0);
+        }
+        fprintf(f, "timestep\n");
+        // centre of mass of the unfolded elastomer, float sums in vertex
+        // order (FeaElements::unfoldPos, feaElements.cpp:135-147)
+        std::vector<float> ux, uy;
+        unfolded_positions(M, N, p, ux, uy);
+        for (int c = 0; c < ncl; c++) {
+            const int off = M.clusters[c].x, nv = M.clusters[c].y;
+            float xc = 0, yc = 0;
+            for (int k = 0; k < nv; k++) {
+                xc += M.mass[off + k] * ux[off + k];
+                yc += M.mass[off + k] * uy[off + k];
+            }
+            fprintf(f, "%f %f %f\n", xc / M.clusterMass[c], yc / M.clusterMass[c], 0.0f);
+        }
     } else {
         fprintf(f, "ITEM: TIMESTEP\n%d\nITEM: NUMBER OF ATOMS\n%d\n", step, N);
-        fprintf(f, "ITEM: BOX BOUNDS pp pp pp\n%f %f\n%f %f\n%f %f\n", 0.0, (double)T.Lx, 0.0, (double)T.Ly, 0.0, 0.0);
+        fprintf(f, "ITEM: BOX BOUNDS pp pp pp\n%f %f\n%f %f\n%f %f\n", 0.0, (double)M.Lx, 0.0, (double)M.Ly, 0.0, 0.0);
         fprintf(f, "ITEM: ATOMS id type x y z vx vy vz\n");
         for (int i = 0; i < N; i++)
-            fprintf(f, "%d %d %f %f %f %f %f %f\n", i, T.type[i], p[i].x, p[i].y, 0.0f, v[i].x, v[i].y, 0.0f);
+            fprintf(f, "%d %d %f %f %f %f %f %f\n", i, M.type[i], p[i].x, p[i].y, 0.0f, v[i].x, v[i].y, 0.0f);
     }
+    const bool ok = !ferror(f);
     fclose(f);
-    return true;
+    if (!ok) err = "write failed on " + M.path;
+    return ok;
 }
 
 static void traj_writer(Trajectory *T) {
@@ -1132,7 +1279,8 @@ static void traj_writer(Trajectory *T) {
             fr = T->queue.front();
         }
         std::string err;
-        const bool ok = write_frame(*T, fr.step, T->pos[fr.slot], T->vel[fr.slot], err);
+        const bool ok = write_frame(T->meta, T->N, fr.step, T->pos[fr.slot], T->vel[fr.slot], false, !T->headerDone, err);
+        T->headerDone = true;
         {
             std::lock_guard<std::mutex> lk(T->mu);
             T->queue.pop_front();
@@ -1257,21 +1405,29 @@ static femmd_status traj_snapshot(femmd_ctx *ctx, int m, bool &aborted) {
     return FEMMD_OK;
 }
 
+// The topology a frame is formatted with, from the context.
+static void frame_meta(const femmd_ctx *ctx, FrameMeta &M) {
+    M.type = ctx->type;
+    M.tri = ctx->tri;
+    M.bond = ctx->bond;
+    M.mass = ctx->mass;
+    M.sigma = ctx->sigma;
+    M.clusters.clear();
+    M.clusterMass.clear();
+    for (const Cluster &c : ctx->clusters) {
+        M.clusters.push_back(make_int2(c.offset, c.nv));
+        M.clusterMass.push_back(c.mass);
+    }
+    M.Lx = ctx->Lx;
+    M.Ly = ctx->Ly;
+    M.scale = ctx->scale;
+}
+
 static void traj_refresh_meta(femmd_ctx *ctx) {
     Trajectory &T = ctx->traj;
     if (!T.on) return;
     traj_drain(T);
-    T.type = ctx->type;
-    T.tri = ctx->tri;
-    T.mass = ctx->mass;
-    T.clusters.clear();
-    T.clusterMass.clear();
-    for (const Cluster &c : ctx->clusters) {
-        T.clusters.push_back(make_int2(c.offset, c.nv));
-        T.clusterMass.push_back(c.mass);
-    }
-    T.Lx = ctx->Lx;
-    T.Ly = ctx->Ly;
+    frame_meta(ctx, T.meta);
 }
 
 static femmd_status run_once(femmd_ctx *ctx, int n, bool &aborted) {
@@ -2318,15 +2474,16 @@ femmd_status femmd_set_trajectory(femmd_ctx *ctx, const char *path, int every, i
     traj_stop(T);
     T.on = false;
     if (!path || every <= 0) return FEMMD_OK;
-    if (format < 0 || format > 2) return fail(ctx, FEMMD_INVALID_ARG, "format must be 0 (dump), 1 (xyz) or 2 (vtk)");
-    T.path = path;
+    if (format < 0 || format > 6) return fail(ctx, FEMMD_INVALID_ARG, "format must be in 0..6 (femmd.h)");
+    T.meta.path = path;
+    T.meta.format = format;
     T.every = every;
-    T.format = format;
+    T.headerDone = false;
     T.error.clear();
     T.written = 0;
     T.N = 0;
     T.lastCommitted = (long long)ctx->steps;  // frames from the next step on
-    if (format != 2) {
+    if (format <= 1 || format == 3 || format == 4) {
         FILE *f = fopen(path, "w");  // a new trajectory starts a new file
         if (!f) return fail(ctx, FEMMD_INVALID_ARG, "cannot create %s", path);
         fclose(f);
@@ -2334,6 +2491,34 @@ femmd_status femmd_set_trajectory(femmd_ctx *ctx, const char *path, int every, i
     T.on = true;
     traj_refresh_meta(ctx);
     T.th = std::thread(traj_writer, &T);
+    return FEMMD_OK;
+}
+
+// save_vtk / save_vtf / save_cluster_vtf / save_cluster_xyz
+// (interface.cpp:301-330) and the reference's other writers: the current
+// state, now, in layout 'format' of femmd_set_trajectory.
+femmd_status femmd_save_frame(femmd_ctx *ctx, const char *path, int format, int append) {
+    NEED(ctx);
+    if (!path) return fail(ctx, FEMMD_INVALID_ARG, "null path");
+    if (format < 0 || format > 6) return fail(ctx, FEMMD_INVALID_ARG, "format must be in 0..6 (femmd.h)");
+    femmd_status st;
+    if ((st = download_state(ctx, kPos | kVel))) return st;
+    FrameMeta M;
+    frame_meta(ctx, M);
+    M.path = path;
+    M.format = format;
+    std::string err;
+    if (!write_frame(M, (int)ctx->pos.size(), ctx->steps, ctx->pos.data(), ctx->vel.data(), append == 0, append == 0,
+                     err))
+        return fail(ctx, FEMMD_INVALID_ARG, "%s", err.c_str());
+    return FEMMD_OK;
+}
+
+// MDSystem::scale (DukSystemSetScale, interface.cpp:365-369).
+femmd_status femmd_set_scale(femmd_ctx *ctx, double scale) {
+    NEED(ctx);
+    ctx->scale = (float)scale;  // real scale (md3dsystem.h:40)
+    traj_refresh_meta(ctx);
     return FEMMD_OK;
 }
 

@@ -26,7 +26,7 @@ import numpy as np
 OP = dict(END=0, INIT=1, PBC=2, DT=3, NUMTYPES=4, PAIR=5, KBOND=6, YOUNG=7, NU=8, SKIN=9,
           ELASTOMER=10, PARTICLE=11, BOND=12, INITNN=13, CAPACITY=14, RUN=15, STEP=16,
           BUILDNN=17, FORCES=18, ELASTOMER_BONDS=19, DUMP_STATE=20, DUMP_NN=21, DUMP_SETUP=22,
-          SETVEL=23, GRAVITY=24, KAREA=25)
+          SETVEL=23, GRAVITY=24, KAREA=25, SAVE=26, SCALE=27)
 
 WCA_RC = 2.0 ** (1.0 / 6.0)
 
@@ -121,6 +121,13 @@ class Scene:
                 w(struct.pack("<i", OP["DUMP_NN"]))
             elif name == "dump_setup":
                 w(struct.pack("<i", OP["DUMP_SETUP"]))
+            elif name == "save_frame":
+                # (file name, layout, append): the name is relative to where the frames go
+                nm = str(a[0]).encode()
+                w(struct.pack("<iiii", OP["SAVE"], int(a[1]), int(a[2]), len(nm)))
+                w(nm)
+            elif name == "set_scale":
+                w(struct.pack("<id", OP["SCALE"], a[0]))
             elif name in ("allocate_cuda", "DEV", "set_fea_law", "set_bond_k_mode", "set_image_mode"):
                 continue
             else:
@@ -198,6 +205,12 @@ class Scene:
                 pend_particles.append(take("ddddddi"))
             elif name == "BOND":
                 sc.add("create_bond", *take("ii"))
+            elif name == "SAVE":
+                layout, append, n = take("iii")
+                nm = bytes(take_arr(np.uint8, n)).decode()
+                sc.add("save_frame", nm, layout, append)
+            elif name == "SCALE":
+                sc.add("set_scale", *take("d"))
             elif name == "SETVEL":
                 n = sum(len(a[0]) for nm, a in sc.calls if nm == "add_particles") + \
                     sum(len(a[0]) // 2 for nm, a in sc.calls if nm == "add_elastomer") + \

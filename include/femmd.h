@@ -279,15 +279,32 @@ femmd_status femmd_batch_event_elapsed(femmd_batch *b, int slot_a, int slot_b, f
  * during femmd_run, every 'every' steps (at step counts that are multiples of
  * it, as Integrator::doStep, integrator.cpp:20-26) the positions and
  * velocities are copied to pinned host memory and written by a host thread
- * while the run goes on.  format 0: the layout of saveClusterXYZ
- * (md3dsystem.cpp:248-273; that routine lists only the first NC particles,
- * every particle is listed here), appended to 'path'; 1: saveXYZ
- * (:232-246); 2: saveVtk (:275-328), one file '<path><step, 9 digits>.vtk'
- * per frame with the clusters unfolded.  The run's results are bit for bit
- * those without frames.  path NULL or every <= 0 stops writing. */
+ * while the run goes on.  Layouts of the reference's writers
+ * (md3dsystem.cpp), the first four appended to 'path', the others one file
+ * '<path><step, 9 digits>.<ext>' per frame, elastomers unfolded:
+ *   0  saveClusterXYZ (:248-273; that routine lists only the first NC
+ *      particles, every particle is listed here)
+ *   1  saveXYZ (:232-246)
+ *   2  saveVtk (:275-328), legacy VTK '.vtk' (nothing without elastomers)
+ *   3  saveVTF (:330-353), the structure block (atoms, bonds, pbc) before the first frame
+ *   4  saveClusterVTF (:355-378), one atom per elastomer at its centre of mass
+ *   5  saveVtkXML (:381-443), VTK XML '.vtu', ascii
+ *   6  saveVtkXMLBin (:451-522), VTK XML '.vtu', raw appended arrays
+ * The run's results are bit for bit those without frames.  path NULL or
+ * every <= 0 stops writing. */
 femmd_status femmd_set_trajectory(femmd_ctx *ctx, const char *path, int every, int format);
 /* Wait until every captured frame is on disk; the count written so far. */
 femmd_status femmd_flush_trajectory(femmd_ctx *ctx, long long *frames_written);
+/* save_vtk / save_vtf / save_cluster_vtf / save_cluster_xyz
+ * (interface.cpp:301-330, and the reference's saveXYZ, saveVtkXML and
+ * saveVtkXMLBin): the current state written now in layout 'format' above,
+ * named by the current step count where the layout makes one file per frame.
+ * append = 0 starts the file anew (and writes the VTF structure block), as
+ * the reference's s = 0; otherwise the frame is added to it. */
+femmd_status femmd_save_frame(femmd_ctx *ctx, const char *path, int format, int append);
+/* set_scale (interface.cpp:365-369): the cluster VTF atoms' radius is
+ * 0.5 scale + 0.5.  1 until set (the reference leaves it unset). */
+femmd_status femmd_set_scale(femmd_ctx *ctx, double scale);
 
 /* -------------------------------------------------------- observables */
 /* Properties::evaluate (properties.cpp:15-36) at the current state, FP64

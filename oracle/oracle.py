@@ -231,6 +231,14 @@ class Oracle:
     def set_kArea(self, k):
         self.L.orc_set_karea(self.h, float(k))
 
+    # File writers are outside the restated timestep: the product's frames are
+    # compared with the files the reference itself wrote.
+    def save_frame(self, name, fmt, append):
+        pass
+
+    def set_scale(self, scale):
+        pass
+
     def set_elastomer_material(self, e, E, nu):
         if self.L.orc_set_elastomer_material(self.h, int(e), float(E), float(nu)):
             raise ValueError(f"no elastomer {e}")
@@ -474,9 +482,11 @@ def logf_own(x: float) -> float:
 
 # ------------------------------------------------------ reference harness
 
-def run_reference(scene, timeout=600):
+def run_reference(scene, timeout=600, files=None):
     """Replay a scene on the compiled reference; returns the list of dumps
-    (('state'|'nn'|'setup', dict)) in the order the scene requested them."""
+    (('state'|'nn'|'setup', dict)) in the order the scene requested them.
+    With a dict 'files', the frames the scene saved (save_frame) are added to
+    it as {file name: bytes}."""
     if not os.path.exists(REF_BIN):
         raise FileNotFoundError("reference harness not built (make -C oracle ref)")
     with tempfile.TemporaryDirectory() as d:
@@ -487,6 +497,11 @@ def run_reference(scene, timeout=600):
         if r.returncode != 0:
             raise RuntimeError("reference harness failed: " + r.stderr[-2000:])
         buf = open(cout, "rb").read()
+        if files is not None:
+            for name in sorted(os.listdir(d)):
+                if name not in ("cmd.bin", "out.bin"):
+                    with open(os.path.join(d, name), "rb") as f:
+                        files[name] = f.read()
     return parse_dumps(buf)
 
 

@@ -3,8 +3,9 @@
 // the reference sources by oracle/Makefile into oracle/_ref/ref_harness.  It
 // replays a scene (the same setup calls a reference script makes through
 // System.*, src/interface.cpp:229-563) on MDSystem in CPU mode and dumps
-// setup arrays, cell/neighbour sets, forces and trajectories, which
-// tests/golden/make_golden.py stores as golden fixtures.  It stands in for the
+// setup arrays, cell/neighbour sets, forces and trajectories, and has the
+// reference's file writers (md3dsystem.cpp:232-522) write frames beside the
+// output file; tests/golden/make_golden.py stores both as golden fixtures.  It stands in for the
 // reference's Duktape front end (src/interface.cpp:712-756) so that skin and
 // capacities can be set from C++, which the script surface cannot do.
 //
@@ -15,6 +16,7 @@
 #include <cstdint>
 #include <vector>
 #include <algorithm>
+#include <string>
 #include "md3dsystem.h"
 
 enum Op {
@@ -22,7 +24,7 @@ enum Op {
     OP_YOUNG = 7, OP_NU = 8, OP_SKIN = 9, OP_ELASTOMER = 10, OP_PARTICLE = 11, OP_BOND = 12,
     OP_INITNN = 13, OP_CAPACITY = 14, OP_RUN = 15, OP_STEP = 16, OP_BUILDNN = 17, OP_FORCES = 18,
     OP_ELASTOMER_BONDS = 19, OP_DUMP_STATE = 20, OP_DUMP_NN = 21, OP_DUMP_SETUP = 22, OP_SETVEL = 23,
-    OP_GRAVITY = 24, OP_KAREA = 25
+    OP_GRAVITY = 24, OP_KAREA = 25, OP_SAVE = 26, OP_SCALE = 27
 };
 
 // Bond set of an elastomer: 0 keeps the reference's bonds on every triangle
@@ -137,6 +139,10 @@ int main(int argc, char **argv) {
     MDSystem *sp = new MDSystem(0);
     MDSystem &s = *sp;
     s.DEV = CPU;
+    s.scale = 1;  // MDSystem leaves scale unset until set_scale
+    // frames (OP_SAVE) are written beside the output file
+    std::string dir = argv[2];
+    dir = dir.find('/') == std::string::npos ? std::string(".") : dir.substr(0, dir.rfind('/'));
     for (;;) {
         int32_t op = rd<int32_t>();
         if (op == OP_END) break;
@@ -227,6 +233,32 @@ int main(int argc, char **argv) {
         case OP_DUMP_STATE: dump_state(s); break;
         case OP_DUMP_NN: dump_nn(s); break;
         case OP_DUMP_SETUP: dump_setup(s); break;
+        case OP_SCALE: s.scale = rd<double>(); break;  // DukSystemSetScale (interface.cpp:365-369)
+        case OP_SAVE: {
+            // the writers print what the last property evaluation left: the
+            // unfolded positions and centres of mass (calc_cluster_props,
+            // interface.cpp:332-335) and v^2, as evalProps sets it
+            // (md3dsystem.cpp:162-163; evalProps itself also adds to dispHi,
+            // which would move the next list rebuild)
+            int layout = rd<int32_t>(), append = rd<int32_t>(), n = rd<int32_t>();
+            std::string name(n, '\0');
+            if (n > 0 && fread(&name[0], 1, n, fin) != (size_t)n) { fprintf(stderr, "ref_harness: short name\n"); return 3; }
+            std::string path = dir + "/" + name;
+            if (!s.particles.feaElements.clusters.empty()) s.particles.feaElements.calcClusterProps();
+            for (int i = 0; i < s.N; i++)
+                s.particles.vv[i] = s.particles.vel[i].x * s.particles.vel[i].x + s.particles.vel[i].y * s.particles.vel[i].y;
+            switch (layout) {
+            case 0: s.saveClusterXYZ(path.c_str(), append); break;
+            case 1: s.saveXYZ(path.c_str(), append); break;
+            case 2: s.saveVtk(path.c_str()); break;
+            case 3: s.saveVTF(path.c_str(), append); break;
+            case 4: s.saveClusterVTF(path.c_str(), append); break;
+            case 5: s.saveVtkXML(path.c_str()); break;
+            case 6: s.saveVtkXMLBin(path.c_str()); break;
+            default: fprintf(stderr, "ref_harness: unknown layout %d\n", layout); return 3;
+            }
+            break;
+        }
         default: fprintf(stderr, "ref_harness: unknown op %d\n", op); return 3;
         }
     }

@@ -273,6 +273,100 @@ def case_susp_area_xpbc():
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 
+# ------------------------------------------------------- writer fixtures
+# The reference's file writers (md3dsystem.cpp:232-522) run on scenes with the
+# FEA forces off (E = 0, the disks held by edge bonds), whose runs are bit-exact
+# with the reference, so every frame can be compared byte for byte.  The
+# legacy dump (layout 0) is left out: the reference lists only the first NC
+# particles in it.  Fixtures go to tests/golden/frames/<case>.npz.
+
+def _saves(sc: S.Scene, first: bool, vtk: bool):
+    a = 0 if first else 1
+    sc.add("save_frame", "f.xyz", 1, a).add("save_frame", "f.vtf", 3, a).add("save_frame", "c.vtf", 4, a)
+    if vtk:
+        sc.add("save_frame", "v", 2, 0).add("save_frame", "x", 5, 0).add("save_frame", "b", 6, 0)
+    return sc
+
+
+def frames_elastomers():
+    """Disks only (the VTK writers read unfolded positions, which the
+    reference holds for elastomer vertices alone), held by bonds on every
+    mesh edge, drifting across the periodic boundary; every layout at the
+    start and after two runs."""
+    verts, tris = S.hex_disk_mesh(3.0, 3, jitter=0.02, seed=111)
+    nv = verts.shape[0]
+    L = 20.0
+    rng = np.random.Generator(np.random.PCG64(112))
+    sc = S.Scene(meta=dict(workload="frames_elastomers"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [S.WCA_RC], [1.0]).add("set_skin", 0.3)
+    sc.add("set_kBond", 80.0).add("set_youngs_modulus", 0.0).add("set_elastomer_bonds", 0)
+    for c in [(16.6, 10.0), (10.0, 16.6), (4.0, 4.0)]:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 0, 0, 1.0, float(nv), True)
+    sc.add("init_neighbor_list")
+    vel = rng.normal(0, 0.3, size=(3 * nv, 2))
+    vel[:nv, 0] += 6.0
+    vel[nv:2 * nv, 1] += 6.0
+    vel[2 * nv:] -= 6.0
+    sc.add("set_velocities_array", vel.astype(np.float32))
+    sc.add("set_scale", 0.8)
+    _saves(sc, True, True)
+    for n in (40, 60):
+        sc.add("run", n).add("dump_state")
+        _saves(sc, False, True)
+    return sc
+
+
+def frames_mixed():
+    """Disks of type 1 among free particles of type 0 (sigma 0.9) with bonds
+    between free neighbours: the VTF structure block (type letters, radii,
+    bond list, box) and one cluster VTF atom per disk."""
+    verts, tris = S.hex_disk_mesh(2.5, 2, jitter=0.02, seed=121)
+    nv = verts.shape[0]
+    L = 16.0
+    rng = np.random.Generator(np.random.PCG64(122))
+    sc = S.Scene(meta=dict(workload="frames_mixed"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 2)
+    sc.add("set_pair_potential", [1.0, 1.0, 1.0, 1.0], [2.5, S.WCA_RC, S.WCA_RC, S.WCA_RC],
+           [S.lj_shift(2.5), 1.0, 1.0, 1.0])
+    sc.add("set_skin", 0.3).add("set_kBond", 60.0).add("set_youngs_modulus", 0.0).add("set_elastomer_bonds", 0)
+    centers = np.array([(4.0, 4.0), (12.0, 4.0), (4.0, 12.0), (12.0, 12.0)])
+    for c in centers:
+        sc.add("add_elastomer", verts, tris, float(c[0]), float(c[1]), 1, 0, 1.0, float(nv), True)
+    g = (np.stack(np.meshgrid(np.arange(12), np.arange(12), indexing="xy"), -1).reshape(-1, 2) + 0.5) * (L / 12)
+    d = g[:, None, :] - centers[None]
+    d -= L * np.round(d / L)
+    keep = ((d ** 2).sum(-1) > 3.6 ** 2).all(1)
+    p = g[keep] + rng.uniform(-0.05, 0.05, size=(int(keep.sum()), 2))
+    n = p.shape[0]
+    v = rng.normal(0, 0.8, size=(n, 2))
+    sc.add("add_particles", p[:, 0], p[:, 1], v[:, 0], v[:, 1], np.ones(n), np.full(n, 0.9), np.zeros(n, np.int32))
+    base = 4 * nv
+    for k in range(0, n - 1, 5):
+        sc.add("create_bond", base + k, base + k + 1)
+    sc.add("init_neighbor_list")
+    _saves(sc, True, False)
+    for n_ in (50, 50):
+        sc.add("run", n_).add("dump_state")
+        _saves(sc, False, False)
+    return sc
+
+
+FRAME_CASES = {k[7:]: v for k, v in globals().items() if k.startswith("frames_")}
+
+
+def save_frames(name: str, sc: S.Scene, dumps, files):
+    blob = {"scene": np.frombuffer(sc.to_bytes(), np.uint8)}
+    for k, (tag, d) in enumerate(dumps):
+        for key, val in d.items():
+            blob[f"d{k:02d}_{tag}_{key}"] = np.asarray(val)
+    blob["frame_names"] = np.array(sorted(files), dtype="U64")
+    for k, fname in enumerate(sorted(files)):
+        blob[f"frame{k:03d}"] = np.frombuffer(files[fname], np.uint8)
+    os.makedirs(os.path.join(OUT, "frames"), exist_ok=True)
+    np.savez_compressed(os.path.join(OUT, "frames", f"{name}.npz"), **blob)
+
+
 def save(name: str, sc: S.Scene, dumps):
     blob = {"scene": np.frombuffer(sc.to_bytes(), np.uint8)}
     for k, (tag, d) in enumerate(dumps):
@@ -291,6 +385,14 @@ def main(names=None):
         dumps = O.run_reference(sc)
         save(name, sc, dumps)
         print(f"{name}: {len(dumps)} dumps, {os.path.getsize(os.path.join(OUT, name + '.npz'))} bytes")
+    for name, fn in FRAME_CASES.items():
+        if names and "frames_" + name not in names:
+            continue
+        sc = fn()
+        files = {}
+        dumps = O.run_reference(sc, files=files)
+        save_frames(name, sc, dumps, files)
+        print(f"frames {name}: {len(files)} files, {os.path.getsize(os.path.join(OUT, 'frames', name + '.npz'))} bytes")
 
 
 if __name__ == "__main__":

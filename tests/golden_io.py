@@ -16,12 +16,25 @@ def names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
 
 
+def frame_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "frames", "*.npz")))
+
+
+def load_frames(name):
+    """A writer fixture: the scene, its state dumps, and {file name: bytes}
+    of every frame the reference's writers produced."""
+    sc, dumps = load(os.path.join("frames", name))
+    z = np.load(os.path.join(GOLDEN, "frames", name + ".npz"))
+    files = {str(n): z[f"frame{k:03d}"].tobytes() for k, n in enumerate(z["frame_names"])}
+    return sc, dumps, files
+
+
 def load(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     sc = Scene.from_bytes(z["scene"].tobytes())
     dumps = {}
     for key in z.files:
-        if key == "scene":
+        if key == "scene" or key.startswith("frame"):
             continue
         idx, tag, field = key.split("_", 2)
         k = int(idx[1:])

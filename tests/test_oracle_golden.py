@@ -19,6 +19,42 @@ def test_oracle_matches_reference_bitwise(name):
     assert not bad, "\n".join(bad)
 
 
+@pytest.mark.parametrize("name", G.frame_names())
+def test_oracle_matches_reference_on_writer_scenes(name):
+    """The scenes of the writer fixtures (FEA off, edge bonds) step bit for
+    bit as the reference's, so their frames can be compared byte for byte."""
+    sc, ref, _ = G.load_frames(name)
+    o = Oracle(image_mode=0, log_mode=0)
+    sc.replay(o)
+    bad = G.diff_report(ref, o.dumps)
+    assert not bad, "\n".join(bad)
+
+
+def test_writer_fixtures_hold_every_layout():
+    """Scene streams with frame saves round-trip, and the reference's raw VTK
+    XML frames have the appended arrays their offsets announce."""
+    assert set(G.frame_names()) == {"elastomers", "mixed"}
+    sc, _, files = G.load_frames("elastomers")
+    assert sc.to_bytes() == type(sc).from_bytes(sc.to_bytes()).to_bytes()
+    assert ("set_scale", (0.8,)) in sc.calls
+    exts = {n.split(".")[-1] for n in files}
+    assert exts == {"xyz", "vtf", "vtk", "vtu"}
+    for n, b in files.items():
+        if not n.startswith("b"):
+            continue
+        head, raw = b.split(b"\t_", 1)
+        txt = head.decode()
+        npts = int(txt.split('NumberOfPoints="')[1].split('"')[0])
+        ncell = int(txt.split('NumberOfCells="')[1].split('"')[0])
+        offs = [int(x.split('"')[0]) for x in txt.split('offset="')[1:]]
+        sizes = [4 * npts, 12 * npts, 12 * ncell, 4 * ncell, ncell]
+        assert offs == list(np.cumsum([0] + [s + 4 for s in sizes[:-1]]))
+        for o, size in zip(offs, sizes):
+            assert int.from_bytes(raw[o:o + 4], "little") == size
+        assert raw[offs[-1] + 4:offs[-1] + 4 + ncell] == bytes([5]) * ncell
+        assert raw[offs[-1] + 4 + ncell:] == b"\n\t</AppendedData>\n</VTKFile>"
+
+
 def test_golden_cases_cover_edge_cases():
     names = set(G.names())
     for required in ("lj_xy", "lj_multitype", "lj_xpbc", "lj_nopbc", "tiny_box", "susp_all", "susp_boundary",
