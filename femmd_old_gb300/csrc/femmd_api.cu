@@ -845,9 +845,10 @@ static femmd_status read_scalars(femmd_ctx *ctx) {
     return FEMMD_OK;
 }
 
-// Neighbour-list storage for capacity 'cap' per particle.
+// Neighbour-list storage for capacity 'cap' per particle (rounded up to the
+// list's groups of four).
 static femmd_status alloc_list(femmd_ctx *ctx, int cap) {
-    cap = std::max(1, cap);
+    cap = (std::max(1, cap) + 3) / 4 * 4;
     CK(ctx->nbr.ensure((size_t)cap * ctx->Ncap));
     ctx->nbrCap = cap;
     release_graphs(ctx);
@@ -2319,7 +2320,7 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
         if (nbr_start) nbr_start[i] = (int)k;
         int c = std::min(cnt[i], ctx->nbrCap);
         for (int q = 0; q < c; q++) {
-            if (nbr_list) nbr_list[k] = raw[(size_t)q * ctx->Ncap + i] & kIdMask;
+            if (nbr_list) nbr_list[k] = raw[nbr_at(q, i, ctx->Ncap)] & kIdMask;
             k++;
         }
     }

@@ -11,7 +11,8 @@
 //   cells   column-major cell index c = ix*ncy + iy (so the three cells of one stencil
 //           column are adjacent), cellStart[ncells+1], sortedIds[N] (ascending id
 //           inside a cell), cellSorted float4[N] = (x, y, id|type<<27, excl)
-//   nbr     int[cap][Ncap] neighbour-major list (entry = id | type<<27), nbrCount[N]
+//   nbr     int4[cap/4][Ncap] Verlet lists (entry = id | type<<27), nbrCount[N]: entries
+//           4g..4g+3 of particle i share the int4 at [g][i] (nbr_at)
 //   bonds   per-particle incidence CSR (bStart, bEnt = {partner|sign<<31, r0 bits})
 //   tris    triIdx int4[nt], triGeo float4[2nt] (neo-Hookean: Bm, vol0; Green: xm rows 1-2, area),
 //           tStart/tEnt vertex->triangle incidence (t*4+slot), triF float2[3nt] per-step nodal forces
@@ -51,6 +52,15 @@ struct __align__(16) PairEntry {
 // exact and order-independent, so the totals are deterministic and no FP64
 // work sits on the per-step path (GB300's FP64 pipe is narrow).
 constexpr int kFixFrac = 24;
+
+// Verlet list layout: entry k of particle i at nbr[nbr_at(k, i, Ncap)].
+// Four consecutive entries of a particle share 16 bytes, and group g of every
+// particle forms a row of Ncap int4, so the 32 lanes of a warp read a group
+// of their particles with one coalesced 512-byte load and the list build
+// stores one int4 per four entries.  The capacity is a multiple of 4.
+__host__ __device__ __forceinline__ size_t nbr_at(int k, int i, int Ncap) {
+    return ((size_t)(k >> 2) * Ncap + i) * 4 + (k & 3);
+}
 
 struct DevScalars {
     double U, W, KE, Ufea;          // last force evaluation (FP64 from the fixed-point sums)

@@ -195,12 +195,11 @@ __global__ void __launch_bounds__(kStepBlock) k_adj_step(DevSys s, const float2 
     double ea = 0.0, sa = 0.0;
     {
         const int cnt = min(s.nbrCount[i], s.nbrCap);
-        const int *lst = s.nbr + i;
         const int ti = s.numTypes > 1 ? s.typeId[i] : 0;
         const float si = s.sigmaByType ? 0.0f : s.sigma[i];
         float fex = 0.0f, fey = 0.0f, fsx = 0.0f, fsy = 0.0f;
         for (int k = 0; k < cnt; k++) {
-            const int tag = lst[(size_t)k * s.Ncap];
+            const int tag = s.nbr[nbr_at(k, i, s.Ncap)];
             const int j = tag & kIdMask;
             const float2 pj = pos[j];
             float dxr, dyr;

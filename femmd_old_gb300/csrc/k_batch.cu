@@ -202,11 +202,14 @@ __device__ __noinline__ void block_rebuild(const Team team, const DevSys &s, int
                 const float4 me = s.cellSorted[t];
                 i = __float_as_int(me.z) & kIdMask;
                 const int c = cell_col(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly);  // the binning's cell
-                k = build_fast_at<false>(s, i, c, make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
-                                         (size_t)s.Ncap);
+                ListOut o = list_out(s, i);
+                k = build_fast_at<false>(s, i, c, make_float2(me.x, me.y), __float_as_int(me.w), o);
+                o.finish(k, s.nbrCap);
             } else {
                 i = t;
-                k = build_general<false>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+                ListOut o = list_out(s, i);
+                k = build_general<false>(s, pos, i, o);
+                o.finish(k, s.nbrCap);
             }
             s.nbrCount[i] = k;
             kmax = max(kmax, k);

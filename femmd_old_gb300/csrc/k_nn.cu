@@ -16,8 +16,8 @@
 // The list build visits the 3x3 cells in the reference's order (cx outer,
 // cy inner, both axes wrapped as applyCellBC does, nnCuda.cu:26-36), keeps
 // j != i outside i's exclusion group with the reference's float
-// dr2 <= (rc+skin)^2, and writes the neighbour-major layout nbr[k*Ncap + i]
-// (coalesced for the force kernel).  Counts beyond the capacity raise an
+// dr2 <= (rc+skin)^2, and writes the packed layout of nbr_at (16-byte
+// groups of four entries, coalesced for the force kernel).  Counts beyond the capacity raise an
 // overflow flag; the host grows the list and repeats the steps.
 #include "femmd_internal.h"
 #include "launch.h"
@@ -224,16 +224,20 @@ __global__ void __launch_bounds__(kNnBlock) k_build_nn(DevSys s, int parity, int
             for (int d = 0; d < 3; d++)
                 for (int q = lane; q < wl[d]; q += 32) w[wo[d] + q] = __ldg(s.cellSorted + wb[d] + q);
             __syncwarp();
-            k = build_fast_staged(s, i, make_float2(me.x, me.y), __float_as_int(me.w), w, qb, qe, sx, wb, wo,
-                                  s.nbr + i, (size_t)s.Ncap);
+            ListOut o = list_out(s, i);
+            k = build_fast_staged(s, i, make_float2(me.x, me.y), __float_as_int(me.w), w, qb, qe, sx, wb, wo, o);
+            o.finish(k, s.nbrCap);
         } else if (valid) {
-            k = build_fast_at<true>(s, i, ix * ncy + iy, make_float2(me.x, me.y), __float_as_int(me.w), s.nbr + i,
-                                    (size_t)s.Ncap);
+            ListOut o = list_out(s, i);
+            k = build_fast_at<true>(s, i, ix * ncy + iy, make_float2(me.x, me.y), __float_as_int(me.w), o);
+            o.finish(k, s.nbrCap);
         }
         if (valid) s.nbrCount[i] = k;
     } else if (t < s.N) {
         const int i = t;
-        k = build_general<true>(s, pos, i, s.nbr + i, (size_t)s.Ncap);
+        ListOut o = list_out(s, i);
+        k = build_general<true>(s, pos, i, o);
+        o.finish(k, s.nbrCap);
         s.nbrCount[i] = k;
     }
     // build statistics and overflow

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kStepBlock) k_props_particle(DevSys s, const f
         const float si = s.sigmaByType ? 0.0f : s.sigma[i];
         const double2 Ri = cmPos[ci];
         for (int k = 0; k < cnt; k++) {
-            const int tag = s.nbr[(size_t)k * s.Ncap + i];
+            const int tag = s.nbr[nbr_at(k, i, s.Ncap)];
             const int j = tag & kIdMask;
             const int cj = clusterOf[j];
             if (cj < 0) continue;

@@ -48,6 +48,47 @@ __device__ __forceinline__ bool fast_walk_ok(const DevSys &s) {
     return (s.wrapx ? s.ncx >= 5 : s.ncx >= 3) && (s.wrapy ? s.ncy >= 5 : s.ncy >= 3) && !s.sc->outside;
 }
 
+// One particle's list while it is written, in the packed layout of
+// nbr_at: entries collect in 'buf' and leave as one 16-byte store per four
+// (a quarter of the store requests of one word per entry).  Entries beyond
+// the capacity (a multiple of 4) are counted by the caller, not written.
+struct ListOut {
+    int4 *p;     // the particle's current group of four
+    int4 buf;    // the entries of the group so far, last in .w
+    size_t row;  // int4 from one group of a particle to its next (Ncap)
+    __device__ __forceinline__ void push(int tag, int k, int cap) {
+        if (k < cap) {
+            buf.x = buf.y;
+            buf.y = buf.z;
+            buf.z = buf.w;
+            buf.w = tag;
+            if ((k & 3) == 3) {
+                *p = buf;
+                p += row;
+            }
+        }
+    }
+    // Store the last, partial group of a list of k entries (its unused
+    // words are zero; readers stop at the count).
+    __device__ __forceinline__ void finish(int k, int cap) {
+        const int r = min(k, cap) & 3;
+        if (r == 1)
+            *p = make_int4(buf.w, 0, 0, 0);
+        else if (r == 2)
+            *p = make_int4(buf.z, buf.w, 0, 0);
+        else if (r == 3)
+            *p = make_int4(buf.y, buf.z, buf.w, 0);
+    }
+};
+
+__device__ __forceinline__ ListOut list_out(const DevSys &s, int i) {
+    ListOut o;
+    o.p = reinterpret_cast<int4 *>(s.nbr) + i;
+    o.buf = make_int4(0, 0, 0, 0);
+    o.row = (size_t)s.Ncap;
+    return o;
+}
+
 // One contiguous candidate range with a known image shift (sx, sy): the
 // reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
 // Candidates are taken four at a time: the four loads are issued before any
@@ -63,7 +104,7 @@ __device__ __forceinline__ bool walk_hit(float4 e, float sx, float sy, float2 p,
 
 template <bool RO>
 __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int i,
-                                           int gi, float R2, int cap, size_t stride, int *&out, int &k) {
+                                           int gi, float R2, int cap, ListOut &out, int &k) {
     int q = qb;
     for (; q + 4 <= qe; q += 4) {
         float4 e[4];
@@ -72,10 +113,7 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
-                if (k < cap) {
-                    *out = __float_as_int(e[u].z);
-                    out += stride;
-                }
+                out.push(__float_as_int(e[u].z), k, cap);
                 k++;
             }
         }
@@ -83,23 +121,20 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
     for (; q < qe; q++) {
         const float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
         if (walk_hit(e, sx, sy, p, i, gi, R2)) {
-            if (k < cap) {
-                *out = __float_as_int(e.z);
-                out += stride;
-            }
+            out.push(__float_as_int(e.z), k, cap);
             k++;
         }
     }
 }
 
-// Verlet list of particle i in the reference's order, written to out[k *
-// stride]; returns its length (entries beyond the capacity are counted, not
-// written).  RO: the cell arrays are read through the read-only path
-// (written by an earlier kernel); the batched kernel rewrites them in the
-// same launch (coherent loads).
+// Verlet list of particle i in the reference's order, written through out
+// (the caller stores the last group with out.finish); returns its length
+// (entries beyond the capacity are counted, not written).  RO: the cell
+// arrays are read through the read-only path (written by an earlier
+// kernel); the batched kernel rewrites them in the same launch (coherent
+// loads).
 template <bool RO>
-__device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, float2 p, int gi, int *out,
-                                             size_t stride) {
+__device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, float2 p, int gi, ListOut &out) {
     const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
     const float R2 = s.nnRadiusSq;
     const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
@@ -121,23 +156,23 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
         if (iy > 0 && iy < ncy - 1) {
             const int qb = RO ? __ldg(cs + col + iy - 1) : cs[col + iy - 1];
             const int qe = RO ? __ldg(cs + col + iy + 2) : cs[col + iy + 2];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
         } else if (iy == 0) {
             // dy = -1 wraps to the top cell, then dy = 0, +1
             int qb = RO ? __ldg(cs + col + ncy - 1) : cs[col + ncy - 1];
             int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
-            walk_range<RO>(s, qb, qe, sx, -Ly, p, i, gi, R2, cap, stride, out, k);
+            walk_range<RO>(s, qb, qe, sx, -Ly, p, i, gi, R2, cap, out, k);
             qb = RO ? __ldg(cs + col) : cs[col];
             qe = RO ? __ldg(cs + col + 2) : cs[col + 2];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
         } else {
             // dy = -1, 0, then dy = +1 wraps to the bottom cell
             int qb = RO ? __ldg(cs + col + ncy - 2) : cs[col + ncy - 2];
             int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, stride, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
             qb = RO ? __ldg(cs + col) : cs[col];
             qe = RO ? __ldg(cs + col + 1) : cs[col + 1];
-            walk_range<RO>(s, qb, qe, sx, Ly, p, i, gi, R2, cap, stride, out, k);
+            walk_range<RO>(s, qb, qe, sx, Ly, p, i, gi, R2, cap, out, k);
         }
     }
     return k;
@@ -148,7 +183,7 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
 // wl[d]) sit at cand[wo[d] + slot - wb[d]].  Same ranges, same order, same
 // arithmetic as the walk over cellSorted.
 __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float sy, float2 p, int i,
-                                            int gi, float R2, int cap, size_t stride, int *&out, int &k) {
+                                            int gi, float R2, int cap, ListOut &out, int &k) {
     int q = lb;
     for (; q + 4 <= le; q += 4) {
         float4 e[4];
@@ -157,10 +192,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
-                if (k < cap) {
-                    *out = __float_as_int(e[u].z);
-                    out += stride;
-                }
+                out.push(__float_as_int(e[u].z), k, cap);
                 k++;
             }
         }
@@ -168,10 +200,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
     for (; q < le; q++) {
         const float4 e = cand[q];
         if (walk_hit(e, sx, sy, p, i, gi, R2)) {
-            if (k < cap) {
-                *out = __float_as_int(e.z);
-                out += stride;
-            }
+            out.push(__float_as_int(e.z), k, cap);
             k++;
         }
     }
@@ -204,25 +233,25 @@ __device__ __forceinline__ void stencil_columns(const DevSys &s, int ix, int iy,
 // (column d's slots [wb[d], ...) at cand[wo[d] + slot - wb[d]]).
 __device__ __forceinline__ int build_fast_staged(const DevSys &s, int i, float2 p, int gi, const float4 *cand,
                                                  const int *qb, const int *qe, const float *sx, const int *wb,
-                                                 const int *wo, int *out, size_t stride) {
+                                                 const int *wo, ListOut &out) {
     int k = 0;
 #pragma unroll
     for (int d = 0; d < 3; d++)
         walk_staged(cand, wo[d] + qb[d] - wb[d], wo[d] + qe[d] - wb[d], sx[d], 0.0f, p, i, gi, s.nnRadiusSq,
-                    s.nbrCap, stride, out, k);
+                    s.nbrCap, out, k);
     return k;
 }
 
 template <bool RO>
-__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
-    return build_fast_at<RO>(s, i, s.cellOf[i], pos[i], s.excl[i], out, stride);
+__device__ __forceinline__ int build_fast(const DevSys &s, const float2 *pos, int i, ListOut &out) {
+    return build_fast_at<RO>(s, i, s.cellOf[i], pos[i], s.excl[i], out);
 }
 
 // The general walk: any grid (1 or 2 cells along an axis visit the same cell
 // more than once, as the reference does), any position, the minimum image
 // decided per pair.
 template <bool RO>
-__device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos, int i, int *out, size_t stride) {
+__device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos, int i, ListOut &out) {
     int k = 0;
     const int ncx = s.ncx, ncy = s.ncy, cap = s.nbrCap;
     const bool wx = s.wrapx, wy = s.wrapy;
@@ -251,7 +280,7 @@ __device__ __forceinline__ int build_general(const DevSys &s, const float2 *pos,
                     image_axis(p.y, e.y, Ly, wy, false, dyr, dyo);
                     const float dr2 = dxr * dxr + dyr * dyr;
                     if (dr2 <= R2) {
-                        if (k < cap) out[(size_t)k * stride] = tag;
+                        out.push(tag, k, cap);
                         k++;
                     }
                 }

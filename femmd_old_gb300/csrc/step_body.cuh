@@ -363,55 +363,47 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             }
         }
     }
-    if constexpr (PIPE > 0) {
-        // pairForce over the Verlet list, in list order, software-pipelined:
-        // the list words of the next chunk of PIPE entries are in flight while
-        // the neighbour positions of the current chunk are gathered and its
-        // pair terms added in order.
-        constexpr int D = PIPE;
+    {
+        // pairForce over the Verlet list, in list order.  The list comes in
+        // 16-byte groups of four entries (nbr_at); the next group is in
+        // flight while the current one is worked.  PIPE > 0: the four
+        // neighbour positions of a group are gathered before its pair terms
+        // are added in order; otherwise each is gathered at its turn (fewer
+        // live registers, for the kernels whose occupancy needs them).
         const int cnt = min(s.nbrCount[i], s.nbrCap);
-        const int *__restrict__ lst = s.nbr + i;
-        const size_t stride = (size_t)s.Ncap;
+        const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
+        const size_t row = (size_t)s.Ncap;
         const int ti = MT ? s.typeId[i] : 0;
         const float si = SG ? s.sigma[i] : 0.0f;
         const PairEntry pe0 = tab[0];
-        int cur[D];
+        const int4 zero4 = make_int4(0, 0, 0, 0);
+        int4 g = cnt > 0 ? (RO ? __ldg(lst) : *lst) : zero4;
+        for (int base = 0; base < cnt; base += 4) {
+            lst += row;
+            const int4 gn = base + 4 < cnt ? (RO ? __ldg(lst) : *lst) : zero4;
+            const int tags[4] = {g.x, g.y, g.z, g.w};
+            if constexpr (PIPE > 0) {
+                float2 q[4];
 #pragma unroll
-        for (int u = 0; u < D; u++) cur[u] = u < cnt ? (RO ? __ldg(lst + u * stride) : lst[u * stride]) : 0;
-        for (int base = 0; base < cnt; base += D) {
-            int nxt[D];
+                for (int u = 0; u < 4; u++) {
+                    const int j = tags[u] & kIdMask;
+                    q[u] = base + u < cnt ? (RO ? __ldg(pin + j) : pin[j]) : make_float2(0.0f, 0.0f);
+                }
 #pragma unroll
-            for (int u = 0; u < D; u++) {
-                const int k = base + D + u;
-                nxt[u] = k < cnt ? (RO ? __ldg(lst + k * stride) : lst[k * stride]) : 0;
+                for (int u = 0; u < 4; u++)
+                    if (base + u < cnt)
+                        lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tags[u], q[u], fx, fy, ue, we);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (base + u < cnt) {
+                        const int j = tags[u] & kIdMask;
+                        lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tags[u], RO ? __ldg(pin + j) : pin[j],
+                                                      fx, fy, ue, we);
+                    }
+                }
             }
-            float2 q[D];
-#pragma unroll
-            for (int u = 0; u < D; u++) {
-                const int j = cur[u] & kIdMask;
-                q[u] = base + u < cnt ? (RO ? __ldg(pin + j) : pin[j]) : make_float2(0.0f, 0.0f);
-            }
-#pragma unroll
-            for (int u = 0; u < D; u++)
-                if (base + u < cnt) lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, cur[u], q[u], fx, fy, ue, we);
-#pragma unroll
-            for (int u = 0; u < D; u++) cur[u] = nxt[u];
-        }
-    } else {
-        // pairForce over the Verlet list, in list order (next entry prefetched)
-        const int cnt = min(s.nbrCount[i], s.nbrCap);
-        const int *__restrict__ lst = s.nbr + i;
-        const int stride = s.Ncap;
-        const int ti = MT ? s.typeId[i] : 0;
-        const float si = SG ? s.sigma[i] : 0.0f;
-        const PairEntry pe0 = tab[0];
-        int tag = cnt > 0 ? (RO ? __ldg(lst) : *lst) : 0;
-        for (int k = 1; k <= cnt; k++) {
-            lst += stride;
-            const int tnext = k < cnt ? (RO ? __ldg(lst) : *lst) : 0;
-            const int j = tag & kIdMask;
-            lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tag, RO ? __ldg(pin + j) : pin[j], fx, fy, ue, we);
-            tag = tnext;
+            g = gn;
         }
     }
     ue *= 0.5f;
