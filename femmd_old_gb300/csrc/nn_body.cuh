@@ -57,19 +57,18 @@ struct ListOut {
     int4 buf;    // the entries of the group so far, last in .w
     size_t row;  // int4 from one group of a particle to its next (Ncap)
     __device__ __forceinline__ void push(int tag, int k, int cap) {
-        if (k < cap) {
-            buf.x = buf.y;
-            buf.y = buf.z;
-            buf.z = buf.w;
-            buf.w = tag;
-            if ((k & 3) == 3) {
-                *p = buf;
-                p += row;
-            }
+        buf.x = buf.y;
+        buf.y = buf.z;
+        buf.z = buf.w;
+        buf.w = tag;
+        if ((k & 3) == 3 && k < cap) {
+            *p = buf;
+            p += row;
         }
     }
     // Store the last, partial group of a list of k entries (its unused
-    // words are zero; readers stop at the count).
+    // words are zero; readers stop at the count).  With k > cap (a multiple
+    // of 4) every group that fits is already stored.
     __device__ __forceinline__ void finish(int k, int cap) {
         const int r = min(k, cap) & 3;
         if (r == 1)
@@ -93,17 +92,26 @@ __device__ __forceinline__ ListOut list_out(const DevSys &s, int i) {
 // reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
 // Candidates are taken four at a time: the four loads are issued before any
 // test, then the hits are appended in candidate order.
-__device__ __forceinline__ bool walk_hit(float4 e, float sx, float sy, float2 p, int i, int gi, float R2) {
+// A candidate is kept when within the list radius, not the particle itself
+// (its tag is the particle's own: id and type), and not in the particle's
+// exclusion group: gi == -1 || gj == -1 || gi != gj, which is gi == -1 ||
+// gi != gj.
+__device__ __forceinline__ bool walk_hit(float4 e, float sx, float sy, float2 p, int tagi, int gi, float R2) {
     const float dx = (p.x - e.x) - sx;
     const float dy = (p.y - e.y) - sy;
     const float dr2 = dx * dx + dy * dy;
     const int tag = __float_as_int(e.z);
     const int gj = __float_as_int(e.w);
-    return dr2 <= R2 && (tag & kIdMask) != i && (gi == -1 || gj == -1 || gi != gj);
+    return dr2 <= R2 && tag != tagi && (gi == -1 || gi != gj);
+}
+
+// The tag cellSorted holds for particle i (place_one).
+__device__ __forceinline__ int own_tag(const DevSys &s, int i) {
+    return i | (s.numTypes > 1 ? (s.typeId[i] << kIdBits) : 0);
 }
 
 template <bool RO>
-__device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int i,
+__device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int tagi,
                                            int gi, float R2, int cap, ListOut &out, int &k) {
     int q = qb;
     for (; q + 4 <= qe; q += 4) {
@@ -112,7 +120,7 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
         for (int u = 0; u < 4; u++) e[u] = RO ? __ldg(s.cellSorted + q + u) : s.cellSorted[q + u];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
+            if (walk_hit(e[u], sx, sy, p, tagi, gi, R2)) {
                 out.push(__float_as_int(e[u].z), k, cap);
                 k++;
             }
@@ -120,7 +128,7 @@ __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, floa
     }
     for (; q < qe; q++) {
         const float4 e = RO ? __ldg(s.cellSorted + q) : s.cellSorted[q];
-        if (walk_hit(e, sx, sy, p, i, gi, R2)) {
+        if (walk_hit(e, sx, sy, p, tagi, gi, R2)) {
             out.push(__float_as_int(e.z), k, cap);
             k++;
         }
@@ -139,6 +147,7 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
     const float R2 = s.nnRadiusSq;
     const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
     const int ix = c / ncy, iy = c - ix * ncy;
+    const int tagi = own_tag(s, i);
     int k = 0;
     const int *cs = s.cellStart;
 #pragma unroll 1
@@ -156,23 +165,23 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
         if (iy > 0 && iy < ncy - 1) {
             const int qb = RO ? __ldg(cs + col + iy - 1) : cs[col + iy - 1];
             const int qe = RO ? __ldg(cs + col + iy + 2) : cs[col + iy + 2];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, tagi, gi, R2, cap, out, k);
         } else if (iy == 0) {
             // dy = -1 wraps to the top cell, then dy = 0, +1
             int qb = RO ? __ldg(cs + col + ncy - 1) : cs[col + ncy - 1];
             int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
-            walk_range<RO>(s, qb, qe, sx, -Ly, p, i, gi, R2, cap, out, k);
+            walk_range<RO>(s, qb, qe, sx, -Ly, p, tagi, gi, R2, cap, out, k);
             qb = RO ? __ldg(cs + col) : cs[col];
             qe = RO ? __ldg(cs + col + 2) : cs[col + 2];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, tagi, gi, R2, cap, out, k);
         } else {
             // dy = -1, 0, then dy = +1 wraps to the bottom cell
             int qb = RO ? __ldg(cs + col + ncy - 2) : cs[col + ncy - 2];
             int qe = RO ? __ldg(cs + col + ncy) : cs[col + ncy];
-            walk_range<RO>(s, qb, qe, sx, 0.0f, p, i, gi, R2, cap, out, k);
+            walk_range<RO>(s, qb, qe, sx, 0.0f, p, tagi, gi, R2, cap, out, k);
             qb = RO ? __ldg(cs + col) : cs[col];
             qe = RO ? __ldg(cs + col + 1) : cs[col + 1];
-            walk_range<RO>(s, qb, qe, sx, Ly, p, i, gi, R2, cap, out, k);
+            walk_range<RO>(s, qb, qe, sx, Ly, p, tagi, gi, R2, cap, out, k);
         }
     }
     return k;
@@ -182,7 +191,7 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
 // stencil column d (dx = d - 1) the candidates of slots [wb[d], wb[d] +
 // wl[d]) sit at cand[wo[d] + slot - wb[d]].  Same ranges, same order, same
 // arithmetic as the walk over cellSorted.
-__device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float sy, float2 p, int i,
+__device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float sy, float2 p, int tagi,
                                             int gi, float R2, int cap, ListOut &out, int &k) {
     int q = lb;
     for (; q + 4 <= le; q += 4) {
@@ -191,7 +200,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
         for (int u = 0; u < 4; u++) e[u] = cand[q + u];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            if (walk_hit(e[u], sx, sy, p, i, gi, R2)) {
+            if (walk_hit(e[u], sx, sy, p, tagi, gi, R2)) {
                 out.push(__float_as_int(e[u].z), k, cap);
                 k++;
             }
@@ -199,7 +208,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
     }
     for (; q < le; q++) {
         const float4 e = cand[q];
-        if (walk_hit(e, sx, sy, p, i, gi, R2)) {
+        if (walk_hit(e, sx, sy, p, tagi, gi, R2)) {
             out.push(__float_as_int(e.z), k, cap);
             k++;
         }
@@ -235,9 +244,10 @@ __device__ __forceinline__ int build_fast_staged(const DevSys &s, int i, float2 
                                                  const int *qb, const int *qe, const float *sx, const int *wb,
                                                  const int *wo, ListOut &out) {
     int k = 0;
+    const int tagi = own_tag(s, i);
 #pragma unroll
     for (int d = 0; d < 3; d++)
-        walk_staged(cand, wo[d] + qb[d] - wb[d], wo[d] + qe[d] - wb[d], sx[d], 0.0f, p, i, gi, s.nnRadiusSq,
+        walk_staged(cand, wo[d] + qb[d] - wb[d], wo[d] + qe[d] - wb[d], sx[d], 0.0f, p, tagi, gi, s.nnRadiusSq,
                     s.nbrCap, out, k);
     return k;
 }
