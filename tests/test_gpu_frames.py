@@ -98,3 +98,37 @@ def _frames(text, fmt):
             k += 2 + n
         return out
     return text.split("timestep\n")[1:]
+
+
+def test_writer_arguments_are_checked(tmp_path):
+    """Layouts outside 0..6 and files that cannot be opened come back as
+    errors with a message, from the one-shot save and from the trajectory."""
+    sc, _, _ = G.load_frames("mixed")
+    s = F.System()
+    for n, a in sc.calls:
+        if n not in ("save_frame", "run", "dump_state"):
+            getattr(s, n)(*a)
+    for bad in (-1, 7):
+        with pytest.raises(F.FemmdError):
+            s.save_frame(str(tmp_path / "x"), bad)
+        with pytest.raises(F.FemmdError):
+            s.set_trajectory(str(tmp_path / "t"), 10, bad)
+    with pytest.raises(F.FemmdError, match="cannot open"):
+        s.save_frame(str(tmp_path / "no_such_dir" / "f.vtf"), F.System.FRAME_VTF)
+    with pytest.raises(F.FemmdError, match="cannot"):
+        s.set_trajectory(str(tmp_path / "no_such_dir" / "t.xyz"), 10, F.System.FRAME_XYZ)
+    # a per-frame layout into a missing folder fails at the frame, reported by the flush
+    s.set_trajectory(str(tmp_path / "no_such_dir" / "v"), 5, F.System.FRAME_VTU)
+    s.run(10)
+    with pytest.raises(F.FemmdError, match="cannot open"):
+        s.flush_trajectory()
+    s.set_trajectory(None, 0)
+    # append = 0 starts a file anew; append = 1 adds a frame after it
+    p = tmp_path / "two.vtf"
+    s.save_frame(str(p), F.System.FRAME_VTF, 0)
+    one = p.read_text()
+    s.save_frame(str(p), F.System.FRAME_VTF, 1)
+    two = p.read_text()
+    assert two.startswith(one) and two.count("timestep\n") == 2 and one.count("timestep\n") == 1
+    s.save_frame(str(p), F.System.FRAME_VTF, 0)
+    assert p.read_text() == one
