@@ -105,6 +105,19 @@ __device__ __forceinline__ bool walk_hit(float4 e, float sx, float sy, float2 p,
     return dr2 <= R2 && tag != tagi && (gi == -1 || gi != gj);
 }
 
+// walk_hit specialised for a staged warp: EX, some lane of the warp is in an
+// exclusion group (else only the self test remains); SX, the column is
+// shifted by an image (else d - 0 is d itself, the same value).  Both are
+// the same on every lane of a staged warp, so the warp runs one version.
+template <bool EX, bool SX>
+__device__ __forceinline__ bool walk_hit_t(float4 e, float sx, float2 p, int tagi, int gi, float R2) {
+    const float dx = SX ? (p.x - e.x) - sx : p.x - e.x;
+    const float dy = p.y - e.y;
+    const float dr2 = dx * dx + dy * dy;
+    const int tag = __float_as_int(e.z);
+    return dr2 <= R2 && tag != tagi && (!EX || gi == -1 || gi != __float_as_int(e.w));
+}
+
 // The tag cellSorted holds for particle i (place_one).
 __device__ __forceinline__ int own_tag(const DevSys &s, int i) {
     return i | (s.numTypes > 1 ? (s.typeId[i] << kIdBits) : 0);
@@ -190,9 +203,11 @@ __device__ __forceinline__ int build_fast_at(const DevSys &s, int i, int c, floa
 // The walk of build_fast_at over candidates staged in shared memory: for
 // stencil column d (dx = d - 1) the candidates of slots [wb[d], wb[d] +
 // wl[d]) sit at cand[wo[d] + slot - wb[d]].  Same ranges, same order, same
-// arithmetic as the walk over cellSorted.
-__device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float sy, float2 p, int tagi,
-                                            int gi, float R2, int cap, ListOut &out, int &k) {
+// arithmetic as the walk over cellSorted (the rows of a staged warp never
+// wrap in y: sy = 0).
+template <bool EX, bool SX>
+__device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, float sx, float2 p, int tagi, int gi,
+                                            float R2, int cap, ListOut &out, int &k) {
     int q = lb;
     for (; q + 4 <= le; q += 4) {
         float4 e[4];
@@ -200,7 +215,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
         for (int u = 0; u < 4; u++) e[u] = cand[q + u];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            if (walk_hit(e[u], sx, sy, p, tagi, gi, R2)) {
+            if (walk_hit_t<EX, SX>(e[u], sx, p, tagi, gi, R2)) {
                 out.push(__float_as_int(e[u].z), k, cap);
                 k++;
             }
@@ -208,7 +223,7 @@ __device__ __forceinline__ void walk_staged(const float4 *cand, int lb, int le, 
     }
     for (; q < le; q++) {
         const float4 e = cand[q];
-        if (walk_hit(e, sx, sy, p, tagi, gi, R2)) {
+        if (walk_hit_t<EX, SX>(e, sx, p, tagi, gi, R2)) {
             out.push(__float_as_int(e.z), k, cap);
             k++;
         }
@@ -245,10 +260,26 @@ __device__ __forceinline__ int build_fast_staged(const DevSys &s, int i, float2 
                                                  const int *wo, ListOut &out) {
     int k = 0;
     const int tagi = own_tag(s, i);
+    const float R2 = s.nnRadiusSq;
+    const int cap = s.nbrCap;
+    // warp-uniform choices (the caller's staged warps are whole)
+    const bool ex = __any_sync(0xffffffffu, gi != -1);
 #pragma unroll
-    for (int d = 0; d < 3; d++)
-        walk_staged(cand, wo[d] + qb[d] - wb[d], wo[d] + qe[d] - wb[d], sx[d], 0.0f, p, tagi, gi, s.nnRadiusSq,
-                    s.nbrCap, out, k);
+    for (int d = 0; d < 3; d++) {
+        const int lb = wo[d] + qb[d] - wb[d], le = wo[d] + qe[d] - wb[d];
+        const bool shifted = sx[d] != 0.0f;  // the same on every lane: one cell column
+        if (ex) {
+            if (shifted)
+                walk_staged<true, true>(cand, lb, le, sx[d], p, tagi, gi, R2, cap, out, k);
+            else
+                walk_staged<true, false>(cand, lb, le, sx[d], p, tagi, gi, R2, cap, out, k);
+        } else {
+            if (shifted)
+                walk_staged<false, true>(cand, lb, le, sx[d], p, tagi, gi, R2, cap, out, k);
+            else
+                walk_staged<false, false>(cand, lb, le, sx[d], p, tagi, gi, R2, cap, out, k);
+        }
+    }
     return k;
 }
 
