@@ -88,10 +88,6 @@ __device__ __forceinline__ ListOut list_out(const DevSys &s, int i) {
     return o;
 }
 
-// One contiguous candidate range with a known image shift (sx, sy): the
-// reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
-// Candidates are taken four at a time: the four loads are issued before any
-// test, then the hits are appended in candidate order.
 // A candidate is kept when within the list radius, not the particle itself
 // (its tag is the particle's own: id and type), and not in the particle's
 // exclusion group: gi == -1 || gj == -1 || gi != gj, which is gi == -1 ||
@@ -123,6 +119,10 @@ __device__ __forceinline__ int own_tag(const DevSys &s, int i) {
     return i | (s.numTypes > 1 ? (s.typeId[i] << kIdBits) : 0);
 }
 
+// One contiguous candidate range with a known image shift (sx, sy): the
+// reference's d - L / d + L is d - sx with sx = +L / -L, and d - 0 = d.
+// Candidates are taken four at a time: the four loads are issued before any
+// test, then the hits are appended in candidate order.
 template <bool RO>
 __device__ __forceinline__ void walk_range(const DevSys &s, int qb, int qe, float sx, float sy, float2 p, int tagi,
                                            int gi, float R2, int cap, ListOut &out, int &k) {
