@@ -316,6 +316,30 @@ def test_overflowing_capacity_is_grown_and_run_repeated():
     assert np.array_equal(G.bits(a.positions()), G.bits(b.positions()))
 
 
+@pytest.mark.parametrize("cap", [16, 17, 18, 19])
+def test_list_groups_at_every_capacity_remainder(cap):
+    """The lists are stored in groups of four entries: a capacity is rounded
+    up to a multiple of 4, and lists ending anywhere inside a group (counts
+    of every remainder, some beyond a small capacity) read back in the
+    reference's order, with the same trajectory as the default capacity."""
+    sc, ref = G.load("susp_mixed")
+    s = product(F_IMAGE_REFERENCE)
+    first = next(k for k, (n, _) in enumerate(sc.calls) if n == "dump_setup")
+    for n, a in sc.calls[:first]:
+        getattr(s, n)(*a)
+    s.set_neighbor_capacity(cap)
+    assert s.neighbor_capacity() % 4 == 0 and s.neighbor_capacity() >= cap
+    for n, a in sc.calls[first:]:
+        getattr(s, n)(*a)
+    assert not nn_diffs(ref, s.dumps)
+    start, nbr = s.neighbors()
+    counts = np.diff(start)
+    assert set(np.unique(counts % 4)) == {0, 1, 2, 3}
+    o = Oracle(image_mode=0, log_mode=1)
+    sc.replay(o)
+    assert not state_diffs(o.dumps, s.dumps)
+
+
 def test_graph_and_direct_launches_agree():
     sc = S.suspension(n_side=4, rings=4)
     a = product(F_IMAGE_EXACT)
