@@ -382,7 +382,22 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             lst += row;
             const int4 gn = base + 4 < cnt ? (RO ? __ldg(lst) : *lst) : zero4;
             const int tags[4] = {g.x, g.y, g.z, g.w};
-            if constexpr (PIPE > 0) {
+            if constexpr (PIPE == 2) {
+                // two gathers in flight at a time
+#pragma unroll
+                for (int h = 0; h < 4; h += 2) {
+                    float2 q[2];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int j = tags[h + u] & kIdMask;
+                        q[u] = base + h + u < cnt ? (RO ? __ldg(pin + j) : pin[j]) : make_float2(0.0f, 0.0f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 2; u++)
+                        if (base + h + u < cnt)
+                            lj_pair<MT, SG, WX, WY, SIG1>(s, tab, pe0, ti, si, pi, tags[h + u], q[u], fx, fy, ue, we);
+                }
+            } else if constexpr (PIPE > 0) {
                 float2 q[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
