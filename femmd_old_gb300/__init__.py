@@ -298,6 +298,16 @@ class System:
     def set_image_mode(self, m):
         self._call("femmd_set_image_mode", int(m))
 
+    def set_force_mode(self, m):
+        """0: reference-exact arithmetic and list order; 1: fast (same sets,
+        forces within 1e-5 of FP64, free particles stored in cell order)."""
+        self._call("femmd_set_force_mode", int(m))
+
+    def force_mode(self):
+        m = C.c_int()
+        self._call("femmd_get_force_mode", C.byref(m))
+        return m.value
+
     def set_elastomer_bonds(self, m):
         self._call("femmd_set_elastomer_bonds", int(m))
 

@@ -63,6 +63,8 @@ SIGNATURES = {
     "femmd_set_fea_law": (i_, [P, i_]),
     "femmd_set_bond_k_mode": (i_, [P, i_]),
     "femmd_set_image_mode": (i_, [P, i_]),
+    "femmd_set_force_mode": (i_, [P, i_]),
+    "femmd_get_force_mode": (i_, [P, ip]),
     "femmd_set_elastomer_bonds": (i_, [P, i_]),
     "femmd_add_particle": (i_, [P, d_, d_, d_, d_, d_, d_, i_]),
     "femmd_add_particles": (i_, [P, i_, dp, dp, dp, dp, dp, dp, ip]),

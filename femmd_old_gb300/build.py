@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 SRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libfemmd.so")
-SOURCES = ["k_nn.cu", "k_force.cu", "k_batch.cu", "k_adjoint.cu", "k_props.cu", "femmd_api.cu", "k_bin_noalloc.cu"]
+SOURCES = ["k_nn.cu", "k_force.cu", "k_fast.cu", "k_batch.cu", "k_adjoint.cu", "k_props.cu", "femmd_api.cu", "k_bin_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                 "-I" + os.path.join(ROOT, "include"), "-I" + SRC]

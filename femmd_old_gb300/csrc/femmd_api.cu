@@ -167,7 +167,7 @@ struct femmd_ctx {
     int cur = 0;
     int nbrCap = 0, Ncap = 0, nBonded = 0, sigmaByType = 1, sigmaOne = 0;
     DBuf<float2> dpos0, dpos1, dvel, dacc, dforce, dref, ckPos, ckVel, ckAcc, triF, triLame;
-    DBuf<float> dmass, dsigma, denergy, triE, partialsMax, wallDelta, wallSig;
+    DBuf<float> dmass, dsigma, denergy, triE, wallDelta, wallSig;
     bool ownMaterial = false, materialDirty = false;
     // area springs: kept positions and the per-mesh work list
     DBuf<float2> posPre;
@@ -195,7 +195,7 @@ struct femmd_ctx {
     DBuf<int4> triIdx;
     DBuf<float4> triGeo, cellSorted;
     DBuf<PairEntry> pair;
-    DBuf<double> partials, obs;
+    DBuf<double> obs;
     DBuf<unsigned long long> trace;
     bool tracing = false;
     DBuf<DevScalars> sc;
@@ -223,6 +223,15 @@ struct femmd_ctx {
     } adj;
     double lastMeanNbr = 0;
     int lastMaxNbr = 0;
+    // fast force mode: the storage order of the free particles (perm), the
+    // rebuild's scratch, the id-order constants, the run-start copy of perm,
+    // the step blocks' windows
+    int forceMode = FEMMD_FORCE_REFERENCE;
+    DBuf<int> perm, sPerm, fBlockSums, ckPerm, idType, newCell;
+    DBuf<int4> blockWin;
+    DBuf<float2> sPos, sVel, sAcc;
+    DBuf<float> idMass, idSigma, idWallDelta, idWallSig, xfer1;
+    float imgD = 0;
 };
 
 // ------------------------------------------------------------------ errors
@@ -318,12 +327,12 @@ static void release_device(femmd_ctx *c) {
     release_graphs(c);
     c->dpos0.release(); c->dpos1.release(); c->dvel.release(); c->dacc.release(); c->dforce.release();
     c->dref.release(); c->ckPos.release(); c->ckVel.release(); c->ckAcc.release(); c->triF.release();
-    c->dmass.release(); c->dsigma.release(); c->denergy.release(); c->triE.release(); c->partialsMax.release();
+    c->dmass.release(); c->dsigma.release(); c->denergy.release(); c->triE.release();
     c->dtype.release(); c->dexcl.release(); c->cellOf.release(); c->rank.release(); c->cellCount.release();
     c->cellStart.release(); c->blockSums.release(); c->sortedIds.release(); c->unsorted.release(); c->nbr.release();
     c->nbrCount.release(); c->bStart.release(); c->tStart.release(); c->tEnt.release(); c->bEnt.release();
     c->triIdx.release(); c->triGeo.release(); c->cellSorted.release(); c->pair.release();
-    c->partials.release(); c->obs.release(); c->trace.release(); c->sc.release();
+    c->obs.release(); c->trace.release(); c->sc.release();
     c->triLame.release(); c->wallDelta.release(); c->wallSig.release();
     c->posPre.release(); c->areaUnit.release(); c->areaIdx.release(); c->areaLane.release(); c->areaA0.release();
     c->areaUnits = 0;
@@ -331,6 +340,9 @@ static void release_device(femmd_ctx *c) {
     c->cmVel.release(); c->clKin.release(); c->feaVir.release(); c->kinTerm.release(); c->clVir.release();
     c->props.release(); c->propsCk.release(); c->propPart.release(); c->centroid.release();
     c->propsUploaded = false;
+    c->perm.release(); c->sPerm.release(); c->fBlockSums.release(); c->ckPerm.release(); c->idType.release();
+    c->newCell.release(); c->blockWin.release(); c->sPos.release(); c->sVel.release(); c->sAcc.release();
+    c->idMass.release(); c->idSigma.release(); c->idWallDelta.release(); c->idWallSig.release(); c->xfer1.release();
     auto &a = c->adj;
     a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
     a.xbar.release(); a.vbar.release(); a.w0.release(); a.w1.release(); a.triD.release();
@@ -469,8 +481,6 @@ static DevSys make_sys(femmd_ctx *c) {
     s.C1 = c->C1;
     s.C2 = c->C2;
     s.C3 = c->C3;
-    s.partials = c->partials.p;
-    s.partialsMax = c->partialsMax.p;
     s.sc = c->sc.p;
     s.obs = c->obs.p;
     s.obsCap = c->obsCap;
@@ -497,7 +507,51 @@ static DevSys make_sys(femmd_ctx *c) {
     s.areaA0 = c->areaA0.p;
     s.posPre = area ? c->posPre.p : nullptr;
     s.nPre = area ? c->nBonded : 0;
+    s.fast = c->forceMode == FEMMD_FORCE_FAST;
+    if (s.fast) {
+        s.imgD = c->imgD;
+        s.perm = c->perm.p;
+        s.sPos = c->sPos.p;
+        s.sVel = c->sVel.p;
+        s.sAcc = c->sAcc.p;
+        s.sPerm = c->sPerm.p;
+        s.fBlockSums = c->fBlockSums.p;
+        s.idMass = c->idMass.p;
+        s.idType = c->idType.p;
+        s.idSigma = c->idSigma.p;
+        s.idWallDelta = s.wallDelta ? c->idWallDelta.p : nullptr;
+        s.idWallSig = s.wallSig ? c->idWallSig.p : nullptr;
+        s.newCell = c->newCell.p;
+        s.blockWin = c->blockWin.p;
+    }
     return s;
+}
+
+// Fast force mode: the device stores particles in its own order (perm[s] =
+// id at slot s).  Host arrays are in id order; these convert on the way in
+// and out through the rebuild's scratch arrays.
+static bool fast_mode(const femmd_ctx *c) { return c->forceMode == FEMMD_FORCE_FAST; }
+
+// Device array 'in' (storage order) to host 'out' (id order), N float2.
+static cudaError_t fast_download2(femmd_ctx *c, const float2 *in, void *out) {
+    const int N = (int)c->pos.size();
+    DevSys s = make_sys(c);
+    Launch L;
+    L.stream = c->stream;
+    cudaError_t e = enqueue_unpermute2(L, s, in, c->sPos.p);
+    if (e) return e;
+    return cudaMemcpyAsync(out, c->sPos.p, N * sizeof(float2), cudaMemcpyDeviceToHost, c->stream);
+}
+
+// Host 'in' (id order) to device array 'out' (storage order), N float2.
+static cudaError_t fast_upload2(femmd_ctx *c, const void *in, float2 *out) {
+    const int N = (int)c->pos.size();
+    cudaError_t e = cudaMemcpyAsync(c->sPos.p, in, N * sizeof(float2), cudaMemcpyHostToDevice, c->stream);
+    if (e) return e;
+    DevSys s = make_sys(c);
+    Launch L;
+    L.stream = c->stream;
+    return enqueue_permute2(L, s, c->sPos.p, out);
 }
 
 static femmd_status ensure_stream(femmd_ctx *ctx) {
@@ -565,6 +619,23 @@ static femmd_status upload_material(femmd_ctx *ctx) {
         CK(ctx->wallSig.ensure(N));
         CK(cudaMemcpyAsync(ctx->wallDelta.p, dl.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->wallSig.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+        if (fast_mode(ctx)) {
+            // id-order originals, then the storage-order copies through perm
+            CK(ctx->idWallDelta.ensure(N));
+            CK(ctx->idWallSig.ensure(N));
+            CK(cudaMemcpyAsync(ctx->idWallDelta.p, dl.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(ctx->idWallSig.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+            if (!ctx->topoDirty && !ctx->stateDirty) {
+                DevSys ds = make_sys(ctx);
+                ds.wallDelta = ctx->wallDelta.p;
+                ds.wallSig = ctx->wallSig.p;
+                ds.idWallDelta = ctx->idWallDelta.p;
+                ds.idWallSig = ctx->idWallSig.p;
+                Launch L;
+                L.stream = s;
+                CK(enqueue_perm_consts(L, ds));
+            }
+        }
     }
     CK(cudaStreamSynchronize(s));
     ctx->materialDirty = false;
@@ -710,17 +781,16 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->pair.p, tab.data(), tab.size() * sizeof(PairEntry), cudaMemcpyHostToDevice,
                            ctx->stream));
     }
-    CK(ctx->dpos0.ensure(N)); CK(ctx->dpos1.ensure(N)); CK(ctx->dvel.ensure(N)); CK(ctx->dacc.ensure(N));
+    // positions hold one more slot: the ghost that pads the fast mode's lists
+    CK(ctx->dpos0.ensure(N + 1)); CK(ctx->dpos1.ensure(N + 1)); CK(ctx->dvel.ensure(N)); CK(ctx->dacc.ensure(N));
     CK(ctx->dforce.ensure(N)); CK(ctx->denergy.ensure(N)); CK(ctx->dref.ensure(N));
     CK(ctx->ckPos.ensure(N)); CK(ctx->ckVel.ensure(N)); CK(ctx->ckAcc.ensure(N));
     CK(ctx->dmass.ensure(N)); CK(ctx->dtype.ensure(N)); CK(ctx->dexcl.ensure(N));
-    CK(ctx->dsigma.ensure(ctx->sigmaByType ? 1 : N));
+    CK(ctx->dsigma.ensure(ctx->sigmaByType ? 1 : N + 1));  // + the ghost slot
     CK(ctx->cellOf.ensure(N)); CK(ctx->rank.ensure(N)); CK(ctx->sortedIds.ensure(N)); CK(ctx->unsorted.ensure(N));
     CK(ctx->cellSorted.ensure(N)); CK(ctx->nbrCount.ensure(N));
     CK(ctx->cellCount.ensure(ctx->ncells)); CK(ctx->cellStart.ensure(ctx->ncells + 1));
     CK(ctx->blockSums.ensure(scan_blocks(ctx->ncells)));
-    int fb = std::max(force_blocks(N), step_blocks(N));
-    CK(ctx->partials.ensure(3 * (size_t)std::max(fb, 1))); CK(ctx->partialsMax.ensure(std::max(fb, 1)));
     CK(ctx->sc.ensure(1));
     cudaStream_t s = ctx->stream;
     if (N > 0) {
@@ -728,8 +798,11 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->dtype.p, ctx->type.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->dexcl.p, ctx->excl.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->dref.p, ctx->refPos.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
-        if (!ctx->sigmaByType)
+        if (!ctx->sigmaByType) {
+            static const float one = 1.0f;
             CK(cudaMemcpyAsync(ctx->dsigma.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(ctx->dsigma.p + N, &one, sizeof(float), cudaMemcpyHostToDevice, s));
+        }
     }
     CK(cudaMemsetAsync(ctx->cellCount.p, 0, sizeof(int) * std::max(ctx->ncells, 1), s));
     CK(cudaMemsetAsync(ctx->sc.p, 0, sizeof(DevScalars), s));
@@ -791,6 +864,24 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->triIdx.p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->triGeo.p, tg.data(), tg.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     }
+    if (fast_mode(ctx) && N > 0) {
+        CK(ctx->perm.ensure(N)); CK(ctx->sPerm.ensure(N)); CK(ctx->ckPerm.ensure(N)); CK(ctx->xfer1.ensure(N));
+        CK(ctx->sPos.ensure(N)); CK(ctx->sVel.ensure(N)); CK(ctx->sAcc.ensure(N));
+        CK(ctx->fBlockSums.ensure((N + 1023) / 1024));
+        CK(ctx->newCell.ensure(N));
+        CK(ctx->blockWin.ensure(4 * (size_t)((N + kFastBlock - 1) / kFastBlock)));
+        CK(ctx->idMass.ensure(N)); CK(ctx->idType.ensure(N)); CK(ctx->idSigma.ensure(ctx->sigmaByType ? 1 : N));
+        CK(cudaMemcpyAsync(ctx->idMass.p, ctx->mass.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->idType.p, ctx->type.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (!ctx->sigmaByType)
+            CK(cudaMemcpyAsync(ctx->idSigma.p, ctx->sigma.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
+        // the largest pair cutoff in length units: a particle farther than
+        // that from every periodic edge has no interacting pair across it
+        float rmax = ctx->nnRadius, smax = 0.0f;
+        for (int i = 0; i < N; i++) smax = std::max(smax, ctx->sigma[i]);
+        for (size_t q = 0; q < ctx->rc.size(); q++) rmax = std::max(rmax, ctx->rc[q] * smax);
+        ctx->imgD = rmax + 1e-3f;
+    }
     if ((st = upload_area_schedule(ctx))) return st;
     ctx->propsUploaded = false;
     if ((st = upload_material(ctx))) return st;
@@ -808,6 +899,19 @@ static femmd_status upload_state(femmd_ctx *ctx) {
         CK(cudaMemcpyAsync(ctx->dvel.p, ctx->vel.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->dacc.p, ctx->acc.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->dforce.p, ctx->force.data(), N * sizeof(float2), cudaMemcpyHostToDevice, s));
+        // the ghost slot N, far outside the box (the fast mode's list
+        // padding): its distance to any particle is beyond every cutoff, its
+        // square finite
+        static const float2 ghost = make_float2(3.0e15f, 3.0e15f);
+        CK(cudaMemcpyAsync(ctx->dpos0.p + N, &ghost, sizeof(float2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->dpos1.p + N, &ghost, sizeof(float2), cudaMemcpyHostToDevice, s));
+        if (fast_mode(ctx)) {
+            // the state arrives in id order: storage order = id order
+            DevSys ds = make_sys(ctx);
+            Launch L;
+            L.stream = s;
+            CK(enqueue_perm_identity(L, ds));
+        }
     }
     ctx->cur = 0;
     ctx->stateDirty = false;
@@ -823,7 +927,20 @@ static femmd_status download_state(femmd_ctx *ctx, unsigned what) {
     if (!what) return FEMMD_OK;
     const int N = (int)ctx->pos.size();
     cudaStream_t s = ctx->stream;
-    if (N > 0) {
+    if (N > 0 && fast_mode(ctx)) {
+        if (what & kPos) CK(fast_download2(ctx, ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, ctx->pos.data()));
+        if (what & kVel) CK(fast_download2(ctx, ctx->dvel.p, ctx->vel.data()));
+        if (what & kAcc) CK(fast_download2(ctx, ctx->dacc.p, ctx->acc.data()));
+        if (what & kForce) CK(fast_download2(ctx, ctx->dforce.p, ctx->force.data()));
+        if (what & kEnergy) {
+            DevSys ds = make_sys(ctx);
+            Launch L;
+            L.stream = s;
+            CK(enqueue_unpermute1(L, ds, ctx->denergy.p, ctx->xfer1.p));
+            CK(cudaMemcpyAsync(ctx->energy.data(), ctx->xfer1.p, N * sizeof(float), cudaMemcpyDeviceToHost, s));
+        }
+        CK(cudaStreamSynchronize(s));
+    } else if (N > 0) {
         if (what & kPos)
             CK(cudaMemcpyAsync(ctx->pos.data(), ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, N * sizeof(float2),
                                cudaMemcpyDeviceToHost, s));
@@ -849,7 +966,9 @@ static femmd_status read_scalars(femmd_ctx *ctx) {
 // list's groups of four).
 static femmd_status alloc_list(femmd_ctx *ctx, int cap) {
     cap = (std::max(1, cap) + 3) / 4 * 4;
-    CK(ctx->nbr.ensure((size_t)cap * ctx->Ncap));
+    // at least two groups of storage: the fast step kernel loads a
+    // particle's first two groups before it knows the list's length
+    CK(ctx->nbr.ensure((size_t)std::max(cap, 8) * ctx->Ncap));
     ctx->nbrCap = cap;
     release_graphs(ctx);
     return FEMMD_OK;
@@ -1400,8 +1519,13 @@ static femmd_status traj_snapshot(femmd_ctx *ctx, int m, bool &aborted) {
         T.busy[slot] = 1;
     }
     const float2 *pc = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
-    CK(cudaMemcpyAsync(T.pos[slot], pc, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(T.vel[slot], ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+    if (fast_mode(ctx)) {
+        CK(fast_download2(ctx, pc, T.pos[slot]));
+        CK(fast_download2(ctx, ctx->dvel.p, T.vel[slot]));
+    } else {
+        CK(cudaMemcpyAsync(T.pos[slot], pc, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(T.vel[slot], ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));
+    }
     T.pending.push_back({m, slot});
     return FEMMD_OK;
 }
@@ -1811,6 +1935,24 @@ femmd_status femmd_set_image_mode(femmd_ctx *ctx, int mode) {
     return FEMMD_OK;
 }
 
+femmd_status femmd_set_force_mode(femmd_ctx *ctx, int mode) {
+    NEED(ctx);
+    if (mode != FEMMD_FORCE_REFERENCE && mode != FEMMD_FORCE_FAST)
+        return fail(ctx, FEMMD_INVALID_ARG, "unknown force mode %d", mode);
+    if (mode == ctx->forceMode) return FEMMD_OK;
+    HOSTSYNC(ctx);  // the state comes home in id order, then goes up again in the new layout
+    ctx->forceMode = mode;
+    mark_topology(ctx);
+    release_graphs(ctx);
+    return FEMMD_OK;
+}
+
+femmd_status femmd_get_force_mode(const femmd_ctx *ctx, int *mode) {
+    if (!ctx || !mode) return FEMMD_INVALID_ARG;
+    *mode = ctx->forceMode;
+    return FEMMD_OK;
+}
+
 femmd_status femmd_set_elastomer_bonds(femmd_ctx *ctx, int mode) {
     NEED(ctx);
     if (mode < 0 || mode > 2) return fail(ctx, FEMMD_INVALID_ARG, "unknown elastomer bond mode %d", mode);
@@ -2030,6 +2172,8 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(ctx->ckPos.p, pc, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckVel.p, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->ckAcc.p, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (fast_mode(ctx))
+            CK(cudaMemcpyAsync(ctx->ckPerm.p, ctx->perm.p, N * sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
         if (ctx->propAvg)
             CK(cudaMemcpyAsync(ctx->propsCk.p, ctx->props.p, sizeof(DevProps), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, 3 * sizeof(int), ctx->stream));  // overflow, nonfinite, outside
@@ -2060,6 +2204,14 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         CK(cudaMemcpyAsync(pd, ctx->ckPos.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->dvel.p, ctx->ckVel.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->dacc.p, ctx->ckAcc.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (fast_mode(ctx)) {
+            // the checkpoint's storage order and the constants in that order
+            CK(cudaMemcpyAsync(ctx->perm.p, ctx->ckPerm.p, N * sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
+            DevSys ds = make_sys(ctx);
+            Launch L;
+            L.stream = ctx->stream;
+            CK(enqueue_perm_consts(L, ds));
+        }
         if (ctx->propAvg)
             CK(cudaMemcpyAsync(ctx->props.p, ctx->propsCk.p, sizeof(DevProps), cudaMemcpyDeviceToDevice, ctx->stream));
         int need = std::max(ctx->hsc->maxCount, ctx->nbrCap + ctx->nbrCap / 2);
@@ -2279,7 +2431,17 @@ femmd_status femmd_get_cells(femmd_ctx *ctx, int *cell_start, int *cell_ids) {
     CK(cudaMemcpyAsync(start.data(), ctx->cellStart.p, (ctx->ncells + 1) * sizeof(int), cudaMemcpyDeviceToHost,
                        ctx->stream));
     if (N) CK(cudaMemcpyAsync(ids.data(), ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<int> perm;
+    if (fast_mode(ctx) && N) {
+        perm.resize(N);
+        CK(cudaMemcpyAsync(perm.data(), ctx->perm.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
+    if (!perm.empty()) {
+        // storage slots to ids, ascending inside each cell as the reference's
+        for (int &v : ids) v = perm[v];
+        for (int c = 0; c < ctx->ncells; c++) std::sort(ids.begin() + start[c], ids.begin() + start[c + 1]);
+    }
     int at = 0;
     for (int iy = 0; iy < ctx->ncy; iy++)
         for (int ix = 0; ix < ctx->ncx; ix++) {
@@ -2310,17 +2472,48 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     const int N = (int)ctx->pos.size();
     std::vector<int> cnt(N);
     std::vector<int> raw((size_t)ctx->nbrCap * ctx->Ncap);
+    std::vector<int> perm, slot, cellIds;
+    std::vector<int4> bw;
     if (N) {
         CK(cudaMemcpyAsync(cnt.data(), ctx->nbrCount.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(raw.data(), ctx->nbr.p, raw.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        if (fast_mode(ctx)) {
+            perm.resize(N);
+            cellIds.resize(N);
+            bw.resize(4 * (size_t)((N + kFastBlock - 1) / kFastBlock));
+            CK(cudaMemcpyAsync(perm.data(), ctx->perm.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(cellIds.data(), ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+            CK(cudaMemcpyAsync(bw.data(), ctx->blockWin.p, bw.size() * sizeof(int4), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        }
         CK(cudaStreamSynchronize(ctx->stream));
     }
+    if (!perm.empty()) {
+        // rows by particle id, entries as ids (the fast mode's list order
+        // inside a row is not the reference's; the sets are)
+        slot.resize(N);
+        for (int q = 0; q < N; q++) slot[perm[q]] = q;
+    }
+    // fast mode: entry q of the particle at storage slot r, as a storage slot
+    // (a windowed block's entry is an index into its window's cell slots)
+    auto fast_entry = [&](int r, int q) -> int {
+        const int4 *b = &bw[4 * (size_t)(r / kFastBlock)];
+        const int w = raw[nbr_at(q, r, ctx->Ncap)];
+        if (b[0].x < 0) return w & kIdMask;
+        const int st[6] = {b[0].y, b[0].z, b[0].w, b[1].x, b[1].y, b[1].z};
+        const int off[7] = {b[1].w, b[2].x, b[2].y, b[2].z, b[2].w, b[3].x, b[3].y};
+        int p = 0;
+        while (p < 5 && w >= off[p + 1]) p++;
+        return cellIds[st[p] + (w - off[p])];
+    };
     long long k = 0;
     for (int i = 0; i < N; i++) {
         if (nbr_start) nbr_start[i] = (int)k;
-        int c = std::min(cnt[i], ctx->nbrCap);
+        const int r = perm.empty() ? i : slot[i];
+        int c = std::min(cnt[r], ctx->nbrCap);
         for (int q = 0; q < c; q++) {
-            if (nbr_list) nbr_list[k] = raw[nbr_at(q, i, ctx->Ncap)] & kIdMask;
+            if (nbr_list) nbr_list[k] = perm.empty() ? raw[nbr_at(q, r, ctx->Ncap)] & kIdMask : perm[fast_entry(r, q)];
             k++;
         }
     }
@@ -2362,8 +2555,13 @@ femmd_status femmd_set_state(femmd_ctx *ctx, const float *p, const float *v) {
         // device copy current: copy the caller's arrays straight to the device;
         // the host copies become stale.  The next run starts with a forced rebuild.
         float2 *pd = ctx->cur ? ctx->dpos1.p : ctx->dpos0.p;
-        if (p) CK(cudaMemcpyAsync(pd, p, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
-        if (v) CK(cudaMemcpyAsync(ctx->dvel.p, v, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+        if (fast_mode(ctx)) {
+            if (p) CK(fast_upload2(ctx, p, pd));
+            if (v) CK(fast_upload2(ctx, v, ctx->dvel.p));
+        } else {
+            if (p) CK(cudaMemcpyAsync(pd, p, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+            if (v) CK(cudaMemcpyAsync(ctx->dvel.p, v, N * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+        }
         CK(cudaStreamSynchronize(ctx->stream));
         ctx->listBuilt = false;
         if (p) ctx->staleMask |= kPos;
@@ -2384,18 +2582,23 @@ femmd_status femmd_get_state(femmd_ctx *ctx, float *p, float *v, float *a) {
     // device-current arrays go straight into the caller's buffers
     unsigned dev = ctx->staleMask;
     cudaStream_t s = ctx->stream;
+    // device arrays in storage order pass through the unpermute (fast mode)
+    auto d2h = [&](void *out, const float2 *in) -> cudaError_t {
+        if (fast_mode(ctx)) return fast_download2(ctx, in, out);
+        return cudaMemcpyAsync(out, in, N * sizeof(float2), cudaMemcpyDeviceToHost, s);
+    };
     if (p) {
         if (dev & kPos)
-            CK(cudaMemcpyAsync(p, ctx->cur ? ctx->dpos1.p : ctx->dpos0.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+            CK(d2h(p, ctx->cur ? ctx->dpos1.p : ctx->dpos0.p));
         else
             memcpy(p, ctx->pos.data(), N * sizeof(float2));
     }
     if (v) {
-        if (dev & kVel) CK(cudaMemcpyAsync(v, ctx->dvel.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        if (dev & kVel) CK(d2h(v, ctx->dvel.p));
         else memcpy(v, ctx->vel.data(), N * sizeof(float2));
     }
     if (a) {
-        if (dev & kAcc) CK(cudaMemcpyAsync(a, ctx->dacc.p, N * sizeof(float2), cudaMemcpyDeviceToHost, s));
+        if (dev & kAcc) CK(d2h(a, ctx->dacc.p));
         else memcpy(a, ctx->acc.data(), N * sizeof(float2));
     }
     if (dev && s) CK(cudaStreamSynchronize(s));
@@ -2669,6 +2872,8 @@ femmd_status femmd_get_average_properties(femmd_ctx *ctx, double *avg, double *s
 static float wall_y_host(const femmd_ctx *ctx, int n) { return ctx->wallY0 - ctx->wallV * ((float)n * ctx->dt); }
 
 static femmd_status adj_supported(femmd_ctx *ctx) {
+    if (fast_mode(ctx))
+        return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint replays the reference-exact force mode; set it first");
     if (ctx->areaForces && !ctx->refVol.empty())
         return fail(ctx, FEMMD_UNSUPPORTED, "the adjoint does not implement the area springs");
     if (!ctx->wallOn && ctx->pbc != FEMMD_XYPBC)
@@ -2972,6 +3177,8 @@ static femmd_status batch_prepare(femmd_batch *b, int steps, BatchLaunch &bl, st
         if (c->device != b->device) return bfail(b, FEMMD_INVALID_ARG, "replicas must share the batch's device");
         if ((st = ensure_stream(c)) || (st = prepare(c)) || (st = ensure_obs(c, steps)))
             return bfail(b, st, "replica: %s", c->err.c_str());
+        if (fast_mode(c))
+            return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel runs the reference-exact force mode");
         if (c->areaForces && !c->refVol.empty())
             return bfail(b, FEMMD_UNSUPPORTED, "the batched kernel does not implement the area springs");
         if (c->traj.on)

@@ -107,8 +107,6 @@ struct DevSys {
     float *triE;
     const float2 *refPos;
     float kBond, E, mu, lambda, C1, C2, C3;
-    double *partials;      // 3 doubles per block (kept for diagnostics; the sums use fixed point)
-    float *partialsMax;
     DevScalars *sc;
     double *obs;
     int obsCap;
@@ -141,7 +139,34 @@ struct DevSys {
     const int *areaLane;   // per block and lane (32): first vertex of the lane's elastomer
     const int4 *areaIdx;   // per triangle of a mesh: its vertices inside the elastomer
     const float *areaA0;   // per block: A0 of triangle k for lane l at [k * lanes + l]
+    // Fast force mode (femmd_set_force_mode): every rebuild stores the free
+    // particles [nBonded, N) in cell order; perm[s] is the id of the particle
+    // at storage slot s (slots below nBonded never move).  The per-particle
+    // arrays above (state, mass, type, sigma, wall ranges, lists) are then in
+    // storage order; the id-order originals of the constant ones are kept in
+    // idMass..idWallSig.  imgD: a warp whose particles all lie at least imgD
+    // inside every periodic edge has no pair that crosses the boundary.
+    int fast;
+    float imgD;
+    int *perm;
+    float2 *sPos, *sVel, *sAcc;  // rebuild scratch: the state in the new order
+    int *sPerm;
+    int *fBlockSums;             // free particles per block of cell slots
+    const float *idMass, *idSigma, *idWallDelta, *idWallSig;
+    const int *idType;
+    // The step kernel's blocks of kFastBlock storage slots: a block of free
+    // particles inside one cell column stages the positions of its stencil
+    // window (up to six cell-slot ranges: per stencil column the rows around
+    // the block, and the row across the y edge) in shared memory, and its
+    // lists hold window indices instead of storage slots.  blockWin[4b..4b+3]
+    // = {len, start[6], off[7], groups, -} (len < 0: the block reads global
+    // slots; groups: list groups of the block's longest list).
+    int *newCell;   // cell of the particle at each storage slot
+    int4 *blockWin;
 };
+
+constexpr int kFastBlock = 128;  // storage slots per block of the fast step kernel
+constexpr int kWinMax = 1024;    // window entries per block (the last one the ghost)
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -160,6 +185,26 @@ cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check_fl
 // Run start (NeighborList::update(1), nn.cpp:114-134): forced rebuild,
 // dispHi = 0, totalUpdates = 1, per-step observable rows restart.
 cudaError_t enqueue_run_start(Launch &L, const DevSys &s);
+
+// The binning part of a rebuild (rebuild bookkeeping, counting, scan,
+// scatter): cellOf, rank, cellStart and the unsorted slots.
+cudaError_t enqueue_bin(Launch &L, const DevSys &s, int parity, int check);
+
+// ---- fast force mode (k_fast.cu)
+// Rebuild: binning, then the free particles stored in cell order and the
+// Verlet lists built in the new storage order.
+cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int check);
+// The step kernel of the fast mode (same modes and outputs as enqueue_step_after_tri).
+cudaError_t enqueue_step_fast(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                              int use_h);
+// Storage order <-> particle id: out[perm[s]] = in[s] (float2 / float
+// arrays), out[s] = in[perm[s]], perm = identity with the constants copied
+// from the id-order originals, and the constants gathered through perm.
+cudaError_t enqueue_unpermute2(Launch &L, const DevSys &s, const float2 *in, float2 *out);
+cudaError_t enqueue_unpermute1(Launch &L, const DevSys &s, const float *in, float *out);
+cudaError_t enqueue_permute2(Launch &L, const DevSys &s, const float2 *in, float2 *out);
+cudaError_t enqueue_perm_identity(Launch &L, const DevSys &s);
+cudaError_t enqueue_perm_consts(Launch &L, const DevSys &s);
 
 // ---- forces + integration (k_force.cu)
 cudaError_t enqueue_step(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h, int use_h);

@@ -1,0 +1,912 @@
+// k_fast.cu -- the fast force mode of the femmd2D timestep.
+//
+// The reference-exact mode (k_force.cu, k_nn.cu) reproduces the reference's
+// float operations and list order so that trajectories match it bit for bit.
+// The fast mode keeps what the contract fixes -- the same cell and neighbour
+// SETS, forces, energies and virial within 1e-5 of FP64 -- and drops what only
+// the bit-exact trajectory needs:
+//   * storage order: every rebuild stores the free particles [nBonded, N) in
+//     cell order (column-major cells, ascending id inside a cell), so a
+//     warp's particles are neighbours in space and a block's neighbours lie
+//     in a few contiguous cell-slot ranges; perm[s] keeps the id of the
+//     particle at slot s (bonded particles never move, so bonds, triangles
+//     and area springs keep their indices);
+//   * windows: a step block of free particles inside one cell column stages
+//     the current positions of its stencil window in shared memory once per
+//     step, and its lists name window entries, so the pair loop gathers from
+//     shared memory;
+//   * pair arithmetic: fused multiply-adds, the hardware reciprocal
+//     (rcp.approx, 1 ulp) for 1/r^2, and energies summed per particle as
+//     sum s6^2, sum s6 and the number of pairs inside the cutoff (one type);
+//   * minimum image: a warp whose particles all lie at least imgD inside every
+//     periodic edge has no interacting pair across the boundary and does no
+//     image work; the warps at an edge take the image per pair, with the
+//     difference rounded once from its exact value (TwoSum), as the exact
+//     image mode of the reference-exact path.
+// Cutoff decisions of the list (dr^2 <= (rc + skin)^2) use the reference's
+// own float expression (this file, like the others, is compiled without
+// contraction; the pair loop asks for its fused multiply-adds explicitly).
+//
+// Reference: pairForce/ljforce (femmd2D/src/interactionsCuda.cu:43-100),
+// calcPairForcesNN (interactions.cpp:347-389), updateCellsCPU / buildNNCPUSerial
+// (nn.cpp:8-62), NeighborList::update (nn.cpp:114-134), the leapfrog of
+// Integrator::doStep (integrator.cpp:8-29, 100-135).
+#include <cuda_runtime.h>
+#include "femmd_internal.h"
+#include "launch.h"
+#include "device_common.cuh"
+#include "nn_body.cuh"
+#include "step_body.cuh"
+
+namespace femmd {
+
+constexpr int kPermBlock = 1024;  // cell slots per block of the storage reorder
+
+// ================================================================ rebuild
+
+// Placement inside the cell by ascending particle id (the counting sort's
+// atomics gave arbitrary ranks): sortedIds[t] = old slot.  The new storage
+// order is then a function of the positions and ids alone -- the reference's
+// cell order -- whatever order the particles were stored in before.
+__global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.N) return;
+    const int c = s.cellOf[i];
+    const int b = s.cellStart[c], e = s.cellStart[c + 1];
+    const int id = s.perm[i];
+    int r = 0;
+    for (int q = b; q < e; q++) r += __ldg(s.perm + __ldg(s.unsorted + q)) < id;
+    const int slot = b + r;
+    if (slot >= e) {  // inconsistent cell contents: never write outside the cell
+        atomicOr(&s.sc->overflow, 2);
+        return;
+    }
+    s.sortedIds[slot] = i;
+}
+
+// Free particles among each block's cell slots (only with bonded particles).
+__global__ void __launch_bounds__(kPermBlock) k_ffree_count(DevSys s, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    __shared__ int red[kPermBlock / 32];
+    const int t = blockIdx.x * kPermBlock + threadIdx.x;
+    int v = (t < s.N && __ldg(s.sortedIds + t) >= s.nBonded) ? 1 : 0;
+    v = warp_sum_int(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int w = red[threadIdx.x];
+        w = warp_sum_int(w);
+        if (threadIdx.x == 0) s.fBlockSums[blockIdx.x] = w;
+    }
+}
+
+// New storage slot of every particle: bonded ones keep theirs, free ones take
+// nBonded + their rank among the free particles in cell order.  Writes the
+// cell-ordered candidate copy (tags are the new slots), the new slots in
+// cell order (sortedIds), the cell of each new slot, and the free particles'
+// state in the new order into the scratch arrays.
+__global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    __shared__ int wsum[kPermBlock / 32];
+    __shared__ int prefix;
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    const int t = blockIdx.x * kPermBlock + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int old = t < s.N ? __ldg(s.sortedIds + t) : -1;
+    const bool fr = old >= s.nBonded;
+    int ns = t;
+    if (s.nBonded > 0) {
+        // prefix of the earlier blocks (fixed order), then the block's own scan
+        int acc = 0;
+        for (int b = threadIdx.x; b < (int)blockIdx.x; b += kPermBlock) acc += s.fBlockSums[b];
+        acc = warp_sum_int(acc);
+        if (lane == 0) wsum[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int p = 0;
+            for (int w = 0; w < kPermBlock / 32; w++) p += wsum[w];
+            prefix = p;
+        }
+        __syncthreads();
+        const unsigned bal = __ballot_sync(0xffffffffu, fr);
+        const int before = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        if (warp == 0) {
+            const int w = wsum[lane];
+            int z = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z - w;
+        }
+        __syncthreads();
+        ns = fr ? s.nBonded + prefix + wsum[warp] + before : old;
+    }
+    if (t >= s.N) return;
+    const float2 p = pos[old];
+    const int tag = ns | (s.numTypes > 1 ? (s.typeId[old] << kIdBits) : 0);
+    s.cellSorted[t] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[old]));
+    s.sortedIds[t] = ns;
+    s.newCell[ns] = s.cellOf[old];
+    if (fr) {
+        s.sPos[ns] = p;
+        s.sVel[ns] = s.vel[old];
+        s.sAcc[ns] = s.acc[old];
+        s.sPerm[ns] = s.perm[old];
+    }
+}
+
+// The window of every step-kernel block (one thread per block).  A block of
+// free particles whose first and last slot lie in one cell column (rows r0 ..
+// r1) gets, per stencil column d (dx = d - 1, wrapped as the list walk
+// wraps), the cell-slot range of rows r0 - 1 .. r1 + 1 inside the grid (piece
+// 2d) and, where the block touches a y edge, the row across it (piece 2d + 1).
+// Every candidate the list build walks for the block's particles lies in one
+// of these pieces, so a list entry is the candidate's offset in the
+// concatenated pieces.  Other blocks (bonded particles, blocks across two
+// columns, windows too large, grids the fast walk does not cover) keep global
+// storage slots.  The block's longest list (in groups) is gathered by the
+// list build into blockWin[4b+3].z.
+__global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nblk = (s.N + kFastBlock - 1) / kFastBlock;
+    if (b >= nblk) return;
+    int4 *out = s.blockWin + 4 * (size_t)b;
+    const int f = b * kFastBlock, l = min(f + kFastBlock, s.N) - 1;
+    const int ncy = s.ncy, ncx = s.ncx;
+    bool ok = f >= s.nBonded && fast_walk_ok(s) && ncy >= 3;
+    int st[6] = {0, 0, 0, 0, 0, 0}, off[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (ok) {
+        const int cf = s.newCell[f], cl = s.newCell[l];
+        const int ix = cf / ncy, r0 = cf - ix * ncy, r1 = cl - ix * ncy;
+        ok = cl / ncy == ix && !(r0 == 0 && r1 == ncy - 1);
+        if (ok) {
+            const int lo = max(r0 - 1, 0), hi = min(r1 + 1, ncy - 1);
+            int acc = 0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                int nx = ix + d - 1;
+                if (nx < 0) nx = ncx - 1;
+                else if (nx == ncx) nx = 0;
+                const int col = nx * ncy;
+                const int a = s.cellStart[col + lo], e = s.cellStart[col + hi + 1];
+                st[2 * d] = a;
+                off[2 * d] = acc;
+                acc += e - a;
+                int wa = 0, we = 0;
+                if (r0 == 0) {
+                    wa = s.cellStart[col + ncy - 1];
+                    we = s.cellStart[col + ncy];
+                } else if (r1 == ncy - 1) {
+                    wa = s.cellStart[col];
+                    we = s.cellStart[col + 1];
+                }
+                st[2 * d + 1] = wa;
+                off[2 * d + 1] = acc;
+                acc += we - wa;
+            }
+            off[6] = acc;
+            ok = acc + 1 <= kWinMax;
+        }
+    }
+    out[0] = make_int4(ok ? off[6] : -1, st[0], st[1], st[2]);
+    out[1] = make_int4(st[3], st[4], st[5], off[0]);
+    out[2] = make_int4(off[1], off[2], off[3], off[4]);
+    out[3] = make_int4(off[5], off[6], 0, 0);
+}
+
+// The list build of the fast mode.  One thread per cell slot t builds the
+// list of the particle stored there (storage slot = its tag).  An entry is
+// the neighbour's storage slot, or -- for a particle of a windowed step
+// block -- the neighbour's index in that block's window.  Every candidate
+// writes the lane's column of a per-warp shared-memory stage ([entry][lane]:
+// conflict-free whatever the entry index): at its next entry when it is a
+// hit, in a spare row when it is not, so the candidate loop has no branch.
+// At the end the warp copies the stage to the list one 16-byte group of
+// every lane per store (the force kernel's own read pattern).  A lane whose
+// list outgrows the stage walks again and writes the rest directly.  Unused
+// words of a list's last group name the ghost (slot N, or the window's last
+// entry), whose position lies far outside the box, so the force loop needs
+// no count test per entry.
+constexpr int kLBlock = 128;  // threads per block of the list build
+constexpr int kLWin = 256;    // staged candidates per warp
+constexpr int kLStage = 48;   // list entries per lane staged in shared memory (a multiple of 4)
+
+struct StagePut {
+    int (*st)[32];  // [kLStage + 1][32]; row kLStage takes the misses
+    int lane;
+    __device__ __forceinline__ void put(bool hit, int val, int &k) const {
+        st[(hit && k < kLStage) ? k : kLStage][lane] = val;
+        k += hit ? 1 : 0;
+    }
+};
+
+// Entries from kLStage on, written straight to the list.
+struct DirectPut {
+    int *nbr;
+    int slot, cap, Ncap;
+    __device__ __forceinline__ void put(bool hit, int val, int &k) const {
+        if (hit) {
+            if (k >= kLStage && k < cap) nbr[nbr_at(k, slot, Ncap)] = val;
+            k++;
+        }
+    }
+};
+
+// Candidate e (position, tag, group) of the particle at p (group gi) with
+// the column's image shift (sx, sy): inside the list radius by the
+// reference's float dr^2 (no contraction), not the particle itself (cell
+// slot q != self) and not in its exclusion group.
+template <bool EX>
+__device__ __forceinline__ bool fhit(float4 e, float sx, float sy, float2 p, int gi, float R2, int q, int self) {
+    const float dx = (p.x - e.x) - sx;
+    const float dy = (p.y - e.y) - sy;
+    const float dr2 = dx * dx + dy * dy;
+    return dr2 <= R2 && q != self && (!EX || gi == -1 || gi != __float_as_int(e.w));
+}
+
+// Candidates [qb, qe) of cand (cell slots qbase + q).  The entry written is
+// the candidate's tag, or q + dv with win (its window index).
+template <bool EX, bool SX, bool RO, class Put>
+__device__ __forceinline__ void fwalk(const float4 *cand, int qb, int qe, int qbase, float sx, float sy, float2 p,
+                                      int gi, float R2, int self, bool win, int dv, const Put &out, int &k) {
+    int q = qb;
+#pragma unroll 1
+    for (; q + 4 <= qe; q += 4) {
+        float4 e[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) e[u] = RO ? __ldg(cand + q + u) : cand[q + u];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            out.put(fhit<EX>(e[u], SX ? sx : 0.0f, sy, p, gi, R2, qbase + q + u, self),
+                    win ? q + u + dv : __float_as_int(e[u].z), k);
+    }
+#pragma unroll 1
+    for (; q < qe; q++) {
+        const float4 e = RO ? __ldg(cand + q) : cand[q];
+        out.put(fhit<EX>(e, SX ? sx : 0.0f, sy, p, gi, R2, qbase + q, self), win ? q + dv : __float_as_int(e.z), k);
+    }
+}
+
+// The window deltas of a lane: entry = cell slot + dm[d] for the main rows
+// of stencil column d, + dw[d] for the row across the y edge.
+struct WinDelta {
+    bool win;
+    int len;
+    int dm[3], dw[3];
+};
+
+__device__ __forceinline__ WinDelta win_delta(const DevSys &s, int slot) {
+    WinDelta w;
+    const int4 *bw = s.blockWin + 4 * (size_t)(slot / kFastBlock);
+    const int4 a = bw[0], b = bw[1], c = bw[2], d = bw[3];
+    const int st[6] = {a.y, a.z, a.w, b.x, b.y, b.z};
+    const int off[6] = {b.w, c.x, c.y, c.z, c.w, d.x};
+    w.win = a.x >= 0;
+    w.len = a.x;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        w.dm[q] = off[2 * q] - st[2 * q];
+        w.dw[q] = off[2 * q + 1] - st[2 * q + 1];
+    }
+    return w;
+}
+
+// The particle at cell slot t over the column ranges of its stencil (every
+// periodic axis with >= 5 cells, every position inside the box:
+// fast_walk_ok), straight from cellSorted.  Cell indices wrap on every axis
+// as applyCellBC does (nnCuda.cu:26-36); the image shift only where the box
+// is periodic.
+template <bool EX, class Put>
+__device__ __forceinline__ void flist_columns(const DevSys &s, int ix, int iy, float2 p, int gi, int t,
+                                              const WinDelta &wd, const Put &out, int &k) {
+    const int ncx = s.ncx, ncy = s.ncy;
+    const float R2 = s.nnRadiusSq;
+    const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
+    const int *cs = s.cellStart;
+    const float4 *cand = s.cellSorted;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        int nx = ix + d - 1;
+        float sx = 0.0f;
+        if (nx < 0) {
+            nx = ncx - 1;
+            sx = -Lx;
+        } else if (nx == ncx) {
+            nx = 0;
+            sx = Lx;
+        }
+        const int col = nx * ncy;
+        const bool w = wd.win;
+        if (iy > 0 && iy < ncy - 1) {
+            fwalk<EX, true, true>(cand, __ldg(cs + col + iy - 1), __ldg(cs + col + iy + 2), 0, sx, 0.0f, p, gi, R2,
+                                  t, w, wd.dm[d], out, k);
+        } else if (iy == 0) {
+            fwalk<EX, true, true>(cand, __ldg(cs + col + ncy - 1), __ldg(cs + col + ncy), 0, sx, -Ly, p, gi, R2, t,
+                                  w, wd.dw[d], out, k);
+            fwalk<EX, true, true>(cand, __ldg(cs + col), __ldg(cs + col + 2), 0, sx, 0.0f, p, gi, R2, t, w,
+                                  wd.dm[d], out, k);
+        } else {
+            fwalk<EX, true, true>(cand, __ldg(cs + col + ncy - 2), __ldg(cs + col + ncy), 0, sx, 0.0f, p, gi, R2, t,
+                                  w, wd.dm[d], out, k);
+            fwalk<EX, true, true>(cand, __ldg(cs + col), __ldg(cs + col + 1), 0, sx, Ly, p, gi, R2, t, w, wd.dw[d],
+                                  out, k);
+        }
+    }
+}
+
+// Any grid and any position: the reference's 3x3 walk with both axes
+// wrapped (a grid of one or two cells along an axis visits a cell more than
+// once, as the reference does) and the float minimum image per candidate.
+// Blocks are never windowed here: entries are storage slots.
+template <class Put>
+__device__ __forceinline__ void flist_general(const DevSys &s, int ix, int iy, float2 p, int gi, int t,
+                                              const Put &out, int &k) {
+    const int ncx = s.ncx, ncy = s.ncy;
+    const float R2 = s.nnRadiusSq;
+    for (int dx = -1; dx <= 1; dx++) {
+        int nx = ix + dx;
+        if (nx < 0) nx = ncx - 1; else if (nx == ncx) nx = 0;
+        for (int dy = -1; dy <= 1; dy++) {
+            int ny = iy + dy;
+            if (ny < 0) ny = ncy - 1; else if (ny == ncy) ny = 0;
+            const int nc = nx * ncy + ny;
+            const int qb = __ldg(s.cellStart + nc), qe = __ldg(s.cellStart + nc + 1);
+            for (int q = qb; q < qe; q++) {
+                const float4 e = __ldg(s.cellSorted + q);
+                const int gj = __float_as_int(e.w);
+                float dxr, dxo, dyr, dyo;
+                image_axis(p.x, e.x, s.Lx, s.wrapx, false, dxr, dxo);
+                image_axis(p.y, e.y, s.Ly, s.wrapy, false, dyr, dyo);
+                const float dr2 = dxr * dxr + dyr * dyr;
+                out.put(q != t && (gi == -1 || gj == -1 || gi != gj) && dr2 <= R2, __float_as_int(e.z), k);
+            }
+        }
+    }
+}
+
+// The whole walk of one lane through a Put.  staged: the warp's candidates
+// are in w (build window offsets wo, cell slots wb) and the lane's ranges
+// are qb..qe; otherwise the column walk or the general walk.
+template <class Put>
+__device__ __forceinline__ void flist_walk(const DevSys &s, bool fastw, bool staged, bool valid, bool ex, int ix,
+                                           int iy, float2 p, int gi, int t, const WinDelta &wd, const float4 *w,
+                                           const int *qb, const int *qe, const float *sx, const int *wb,
+                                           const int *wo, const Put &out, int &k) {
+    if (fastw) {
+        if (staged) {
+            const float R2 = s.nnRadiusSq;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                // window index q is cell slot q - wo[d] + wb[d] of column d;
+                // the staged rows never cross a y edge (main rows only)
+                const int lb = wo[d] + qb[d] - wb[d], le = wo[d] + qe[d] - wb[d];
+                const int qbase = wb[d] - wo[d];
+                const int dv = qbase + wd.dm[d];
+                // the same shift on every lane: one cell column
+                if (sx[d] != 0.0f) {
+                    if (ex) fwalk<true, true, false>(w, lb, le, qbase, sx[d], 0.0f, p, gi, R2, t, wd.win, dv, out, k);
+                    else fwalk<false, true, false>(w, lb, le, qbase, sx[d], 0.0f, p, gi, R2, t, wd.win, dv, out, k);
+                } else {
+                    if (ex) fwalk<true, false, false>(w, lb, le, qbase, 0.0f, 0.0f, p, gi, R2, t, wd.win, dv, out, k);
+                    else fwalk<false, false, false>(w, lb, le, qbase, 0.0f, 0.0f, p, gi, R2, t, wd.win, dv, out, k);
+                }
+            }
+        } else if (valid) {
+            if (ex) flist_columns<true>(s, ix, iy, p, gi, t, wd, out, k);
+            else flist_columns<false>(s, ix, iy, p, gi, t, wd, out, k);
+        }
+    } else if (valid) {
+        flist_general(s, ix, iy, p, gi, t, out, k);
+    }
+}
+
+// One thread per cell slot t: the Verlet list of the particle stored there,
+// written to its storage column.  A warp whose 32 slots lie in one cell
+// column away from the y edges stages its three stencil column windows in
+// shared memory first.  The free particles' state then moves from the
+// scratch arrays to their new slots, with the constant arrays gathered from
+// the id-order originals.
+__global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    __shared__ float4 win[kLBlock / 32][kLWin];
+    __shared__ int stage[kLBlock / 32][kLStage + 1][32];
+    float2 *pos = parity ? s.pos1 : s.pos0;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool valid = t < s.N;
+    const float4 me = valid ? __ldg(s.cellSorted + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int gi = __float_as_int(me.w);
+    const int ns = valid ? (__float_as_int(me.z) & kIdMask) : 0;
+    const float2 p = make_float2(me.x, me.y);
+    int ix, iy;
+    cell_xy(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
+    const bool ex = __any_sync(0xffffffffu, valid && gi != -1);
+    const bool fastw = fast_walk_ok(s);
+    const WinDelta wd = win_delta(s, ns);
+    int qb[3] = {0, 0, 0}, qe[3] = {0, 0, 0}, wb[3] = {0, 0, 0}, wo[3] = {0, 0, 0}, wl[3] = {0, 0, 0};
+    float sx[3] = {0.f, 0.f, 0.f};
+    bool staged = false;
+    if (fastw) {
+        const int ncy = s.ncy;
+        if (valid && iy >= 1 && iy <= ncy - 2) stencil_columns(s, ix, iy, qb, qe, sx);
+        const unsigned all = __ballot_sync(0xffffffffu, valid);
+        const int ixa = __shfl_sync(0xffffffffu, ix, 0), ixb = __shfl_sync(0xffffffffu, ix, 31);
+        const int iya = __shfl_sync(0xffffffffu, iy, 0), iyb = __shfl_sync(0xffffffffu, iy, 31);
+        staged = all == 0xffffffffu && ixa == ixb && iya >= 1 && iyb <= ncy - 2;
+        if (staged) {
+            int tot = 0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                wb[d] = __shfl_sync(0xffffffffu, qb[d], 0);
+                wl[d] = __shfl_sync(0xffffffffu, qe[d], 31) - wb[d];
+                wo[d] = tot;
+                tot += wl[d];
+            }
+            staged = tot <= kLWin;
+        }
+        if (staged) {
+            float4 *w = win[wid];
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                for (int q = lane; q < wl[d]; q += 32) w[wo[d] + q] = __ldg(s.cellSorted + wb[d] + q);
+            __syncwarp();
+        }
+    }
+    StagePut sp;
+    sp.st = stage[wid];
+    sp.lane = lane;
+    int k = 0;
+    flist_walk(s, fastw, staged, valid, ex, ix, iy, p, gi, t, wd, win[wid], qb, qe, sx, wb, wo, sp, k);
+    const int cap = s.nbrCap;
+    if (__any_sync(0xffffffffu, valid && k > kLStage && cap > kLStage)) {
+        // the rest of an outgrown stage, straight to the list
+        DirectPut dp;
+        dp.nbr = s.nbr;
+        dp.slot = ns;
+        dp.cap = cap;
+        dp.Ncap = s.Ncap;
+        int k2 = 0;
+        flist_walk(s, fastw, staged, valid && k > kLStage, ex, ix, iy, p, gi, t, wd, win[wid], qb, qe, sx, wb, wo, dp,
+                   k2);
+    }
+    // the stage to the list: group g of every lane in one store per g; the
+    // unused words of the last group name the ghost
+    const int ghost = wd.win ? wd.len : s.N;
+    const int kk = valid ? min(k, cap) : 0;
+    const int ng = (kk + 3) >> 2;
+    const int ngs = min(ng, kLStage / 4);
+    const int gmax = __reduce_max_sync(0xffffffffu, ngs);
+    __syncwarp();
+    int4 *out = reinterpret_cast<int4 *>(s.nbr) + ns;
+    for (int g = 0; g < gmax; g++) {
+        if (g < ngs) {
+            int v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = 4 * g + u < kk ? stage[wid][4 * g + u][lane] : ghost;
+            out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+        }
+    }
+    if (valid && kk > kLStage && (kk & 3)) {
+        // a last group past the stage: its unused words
+        for (int q = kk; q < 4 * ng; q++) s.nbr[nbr_at(q, ns, s.Ncap)] = ghost;
+    }
+    if (valid) {
+        s.nbrCount[ns] = k;
+        if (wd.win) atomicMax(&s.blockWin[4 * (size_t)(ns / kFastBlock) + 3].z, ng);
+        if (ns >= s.nBonded) {
+            const int id = s.sPerm[ns];
+            pos[ns] = s.sPos[ns];
+            s.vel[ns] = s.sVel[ns];
+            s.acc[ns] = s.sAcc[ns];
+            s.perm[ns] = id;
+            const_cast<float *>(s.mass)[ns] = __ldg(s.idMass + id);
+            if (s.numTypes > 1) const_cast<int *>(s.typeId)[ns] = __ldg(s.idType + id);
+            if (!s.sigmaByType) const_cast<float *>(s.sigma)[ns] = __ldg(s.idSigma + id);
+            if (s.wallDelta) const_cast<float *>(s.wallDelta)[ns] = __ldg(s.idWallDelta + id);
+            if (s.wallSig) const_cast<float *>(s.wallSig)[ns] = __ldg(s.idWallSig + id);
+        }
+    }
+    const int kmax = __reduce_max_sync(0xffffffffu, valid ? k : 0);
+    const int ksum = __reduce_add_sync(0xffffffffu, valid ? k : 0);
+    if (lane == 0) {
+        if (ksum) atomicAdd(&s.sc->nbrSum, (unsigned long long)ksum);
+        if (kmax > 0) atomicMax(&s.sc->maxCount, kmax);
+        if (kmax > s.nbrCap) atomicOr(&s.sc->overflow, 1);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
+    if (s.trace && lane == 0) {
+        const int row = s.sc->obsRow - 1;
+        if (row >= 0 && row < s.obsCap) atomicMax(&s.trace[(size_t)row * kTraceCols + 5], global_ns());
+    }
+}
+
+cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int check) {
+    cudaError_t e;
+    if ((e = enqueue_bin(L, s, parity, check))) return e;
+    const int pb = (s.N + kBlock - 1) / kBlock;
+    const int permb = (s.N + kPermBlock - 1) / kPermBlock;
+    if ((e = L.kernel(k_fplace, dim3(pb), dim3(kBlock), 0, s, check))) return e;
+    if (s.nBonded > 0 && (e = L.kernel(k_ffree_count, dim3(permb), dim3(kPermBlock), 0, s, check))) return e;
+    if ((e = L.kernel(k_fperm, dim3(permb), dim3(kPermBlock), 0, s, parity, check))) return e;
+    const int fb = (s.N + kFastBlock - 1) / kFastBlock;
+    if ((e = L.kernel(k_fwindows, dim3((fb + kBlock - 1) / kBlock), dim3(kBlock), 0, s, check))) return e;
+    const int nb = (s.N + kLBlock - 1) / kLBlock;
+    return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check);
+}
+
+// ============================================================ step kernel
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The pair difference on one axis.  IMG: the particle lies within imgD of
+// a periodic edge, so an interacting pair may cross it: a difference of
+// more than half the box is moved by one box length, rounded once from its
+// exact value.
+template <bool WRAP, bool IMG>
+__device__ __forceinline__ float fdiff(float a, float b, float L) {
+    float d = a - b;
+    if (WRAP && IMG && fabsf(d) > 0.5f * L) {
+        const float sh = d > 0.0f ? L : -L;
+        d = (d - sh) + two_sum_err(a, -b, d);
+    }
+    return d;
+}
+
+// One Lennard-Jones pair of particle i (type ti, sigma si) with neighbour
+// position q, tag/type tj and sigma sj, added into the running sums.  The
+// cutoff test selects the terms (no branch per pair).  One type with sigma
+// from the table: A += s6^2, B += s6, n += 1 inside the cutoff; otherwise
+// the doubled energy u2 and virial w2 per pair.
+template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG>
+__device__ __forceinline__ void fpair(const DevSys &s, const PairEntry *tab, const PairEntry &pe0, int ti, float si,
+                                      float2 pi, float qx, float qy, int tj, float sj, float &fx, float &fy, float &A,
+                                      float &B, float &n, float &u2, float &w2) {
+    const float dx = fdiff<WX, IMG>(pi.x, qx, s.Lx);
+    const float dy = fdiff<WY, IMG>(pi.y, qy, s.Ly);
+    const float r2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+    float rcut2, c, sig2, eps4, us;
+    {
+        const PairEntry pe = MT ? tab[ti * s.numTypes + tj] : pe0;
+        eps4 = pe.eps4;
+        us = pe.us;
+        if (SG) {
+            const float sij = (si + sj) * 0.5f;
+            sig2 = sij * sij;
+            rcut2 = pe.rc * pe.rc * sig2;
+            c = pe.eps48 * rcp_approx(sig2);
+        } else {
+            rcut2 = pe.rcut2;
+            c = pe.c;
+            sig2 = pe.sig2;
+        }
+    }
+    const bool in = r2 < rcut2;
+    const float ir2 = in ? ((SIG1 && !SG) ? rcp_approx(r2) : sig2 * rcp_approx(r2)) : 0.0f;
+    const float ir4 = ir2 * ir2, ir6 = ir4 * ir2, ir8 = ir4 * ir4;
+    const float fc = ir8 * __fmaf_rn(c, ir6, -0.5f * c);
+    fx = __fmaf_rn(fc, dx, fx);
+    fy = __fmaf_rn(fc, dy, fy);
+    if (MT || SG) {
+        u2 += in ? __fmaf_rn(eps4, __fmaf_rn(ir6, ir6, -ir6), us) : 0.0f;
+        w2 = __fmaf_rn(fc, r2, w2);
+    } else {
+        A = __fmaf_rn(ir6, ir6, A);
+        B += ir6;
+        n += in ? 1.0f : 0.0f;
+    }
+}
+
+// Lennard-Jones forces of particle i over its list (cnt entries; its first
+// two 16-byte groups g0, g1 loaded by the caller; the group two ahead in
+// flight while the current one is worked).  WIN: the entries index the
+// block's staged window (wpos, wtyp, wsig); otherwise they are storage slots
+// gathered from pin.  Unused words of the last group name the ghost, so no
+// entry needs a count test.  Energy and virial come back doubled (per
+// ordered pair), as the reference-exact kernel's.
+template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG, bool WIN>
+__device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt, int4 g0,
+                                           int4 g1, const float2 *__restrict__ pin, const float2 *wpos,
+                                           const int *wtyp, const float *wsig, float &fx, float &fy, float &ue2,
+                                           float &we2) {
+    const int ng = (cnt + 3) >> 2;
+    const size_t row = (size_t)s.Ncap;
+    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i + 2 * row;
+    const int ti = MT ? s.typeId[i] : 0;
+    const float si = SG ? s.sigma[i] : 0.0f;
+    const PairEntry pe0 = tab[0];
+    float A = 0.0f, B = 0.0f, n = 0.0f, u2 = 0.0f, w2 = 0.0f;
+#pragma unroll 1
+    for (int gi = 0; gi < ng; gi++) {
+        const int4 g2 = gi + 2 < ng ? __ldg(lst) : make_int4(0, 0, 0, 0);
+        lst += row;
+        int e[4] = {g0.x, g0.y, g0.z, g0.w};
+        float2 q[4];
+        int tj[4] = {0, 0, 0, 0};
+        float sj[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (WIN) {
+                // masked to the window: a stray entry can name a wrong
+                // window slot but never one outside the shared arrays
+                e[u] &= kWinMax - 1;
+                q[u] = wpos[e[u]];
+                if (MT) tj[u] = wtyp[e[u]];
+                if (SG) sj[u] = wsig[e[u]];
+            } else {
+                const int j = MT ? (e[u] & kIdMask) : e[u];
+                q[u] = __ldg(pin + j);
+                if (MT) tj[u] = (unsigned)e[u] >> kIdBits;
+                if (SG) sj[u] = __ldg(s.sigma + j);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            fpair<MT, SG, SIG1, WX, WY, IMG>(s, tab, pe0, ti, si, pi, q[u].x, q[u].y, tj[u], sj[u], fx, fy, A, B, n,
+                                             u2, w2);
+        g0 = g1;
+        g1 = g2;
+    }
+    if (MT || SG) {
+        ue2 += u2;
+        we2 += w2;
+    } else {
+        ue2 += __fmaf_rn(pe0.eps4, A - B, pe0.us * n);
+        we2 += pe0.eps48 * __fmaf_rn(-0.5f, B, A);
+    }
+}
+
+// x wrapped into [0, L): one box length added or taken away, the reference's
+// r - floor(r/L) L for every |r| < 2L (the same single rounding), the full
+// expression beyond.
+__device__ __forceinline__ float fast_wrap(float x, float L) {
+    if (x < 0.0f) x += L;
+    else if (x >= L) x -= L;
+    if (!(x >= 0.0f && x < L)) x = wrap_coord(x, L);
+    return x;
+}
+
+// The rest of particle i's step in the fast mode: finish_particle with the
+// divisions replaced by the hardware reciprocal (a = f / m), the one-box
+// wrap, and the mass and velocity loaded by the caller.
+template <bool WX, bool WY>
+__device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, float2 pi, float m, float2 v,
+                                            float2 *pout, float fx, float fy, float ue, float we, float utri,
+                                            float uwall, float &ue_out, float &we_out, float &ke, float &vvm,
+                                            bool &bad) {
+    ue *= 0.5f;
+    we *= 0.5f;
+    ue += uwall;
+    if (s.wallOn) {
+        const float yw = wall_y(s, s.sc->stepNow);
+        const float dl = s.wallDelta[i];
+        const float ht = (pi.y + dl) - yw;
+        if (ht > 0.0f) {
+            fy -= s.wallK * ht;
+            ue += 0.5f * s.wallK * ht * ht;
+        }
+        const float hb = dl - pi.y;
+        if (hb > 0.0f) {
+            fy += s.wallK * hb;
+            ue += 0.5f * s.wallK * hb * hb;
+        }
+    }
+    bad = bad || !(isfinite(fx) && isfinite(fy));
+    const float im = rcp_approx(m);
+    const float ax = fx * im, ay = fy * im;
+    const float dt = s.dt, hdt = s.hdt;
+    if (mode == MODE_FORCES) {
+        s.forceOut[i] = make_float2(fx, fy);
+        s.energyOut[i] = ue + utri;
+    } else if (mode == MODE_INIT) {
+        s.acc[i] = make_float2(ax, ay);
+        s.forceOut[i] = make_float2(fx, fy);
+    } else {
+        if (mode == MODE_MID || mode == MODE_LAST) {
+            v.x = __fmaf_rn(hdt, ax, v.x);
+            v.y = __fmaf_rn(hdt, ay, v.y);
+            const float vv = __fmaf_rn(v.x, v.x, __fmul_rn(v.y, v.y));
+            vvm = fmaxf(vvm, vv);
+            ke = __fmaf_rn(m, vv, ke);
+        }
+        if (mode == MODE_LAST) {
+            s.vel[i] = v;
+            s.acc[i] = make_float2(ax, ay);
+            s.forceOut[i] = make_float2(fx, fy);
+        } else {
+            v.x = __fmaf_rn(hdt, ax, v.x);
+            v.y = __fmaf_rn(hdt, ay, v.y);
+            float2 x = make_float2(__fmaf_rn(dt, v.x, pi.x), __fmaf_rn(dt, v.y, pi.y));
+            if (WX) x.x = fast_wrap(x.x, s.Lx);
+            if (WY) x.y = fast_wrap(x.y, s.Ly);
+            pout[i] = x;
+            s.vel[i] = v;
+        }
+    }
+    ue_out += ue;
+    we_out += we;
+}
+
+// Resident blocks per SM the register allocation must allow (kFastBlock
+// threads each).
+#ifndef FEMMD_FAST_MINB
+#define FEMMD_FAST_MINB 10
+#endif
+constexpr int kFastMinBlocks = FEMMD_FAST_MINB;
+
+template <bool MT, bool SG, bool SIG1, bool WX, bool WY>
+__global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, int mode, int parity,
+                                                                     cudaGraphConditionalHandle h, int use_h) {
+    const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
+    float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
+    extern __shared__ float4 smem_f4[];
+    const int nt = s.numTypes;
+    const int ntab = MT ? nt * nt : 1;
+    PairEntry *tab = reinterpret_cast<PairEntry *>(smem_f4);
+    float2 *wpos = reinterpret_cast<float2 *>(tab + ntab);
+    int *wtyp = reinterpret_cast<int *>(wpos + kWinMax);
+    float *wsig = reinterpret_cast<float *>(wtyp + (MT ? kWinMax : 0));
+    // the particle's own data and its first two list groups, issued first so
+    // that their latency overlaps the staging of the window
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < s.N;
+    const int ic = act ? i : 0;
+    const float2 pi = pin[ic];
+    const int cnt = act ? min(s.nbrCount[ic], s.nbrCap) : 0;
+    const int4 *lst0 = reinterpret_cast<const int4 *>(s.nbr) + ic;
+    const int4 g0 = __ldg(lst0), g1 = __ldg(lst0 + s.Ncap);
+    const float m = s.mass[ic];
+    const float2 v = (mode != MODE_FORCES && mode != MODE_INIT) ? s.vel[ic] : make_float2(0.0f, 0.0f);
+    if (MT) {
+        for (int q = threadIdx.x; q < nt * nt; q += blockDim.x) tab[q] = s.pair[q];
+    } else if (threadIdx.x == 0) {
+        tab[0] = s.pair[0];
+    }
+    if (s.trace && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int row = s.sc->obsRow;
+        if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
+    }
+    // the block's window: the current positions (types, sigmas) of the cell
+    // slots of its pieces, and the ghost after them
+    const int4 *bw = s.blockWin + 4 * (size_t)blockIdx.x;
+    const int len = bw[0].x;
+    if (len >= 0) {
+        const int4 a = bw[0], b = bw[1], c = bw[2], d = bw[3];
+        const int st[6] = {a.y, a.z, a.w, b.x, b.y, b.z};
+        const int off[7] = {b.w, c.x, c.y, c.z, c.w, d.x, d.y};
+#pragma unroll
+        for (int p = 0; p < 6; p++) {
+            const int n = off[p + 1] - off[p];
+            for (int w = threadIdx.x; w < n; w += kFastBlock) {
+                const int j = __ldg(s.sortedIds + st[p] + w);
+                wpos[off[p] + w] = __ldg(pin + j);
+                if (MT) wtyp[off[p] + w] = s.typeId[j];
+                if (SG) wsig[off[p] + w] = s.sigma[j];
+            }
+        }
+        if (threadIdx.x == 0) {
+            wpos[len] = __ldg(pin + s.N);  // the ghost slot's far position
+            if (MT) wtyp[len] = 0;
+            if (SG) wsig[len] = 1.0f;
+        }
+    }
+    __syncthreads();
+    float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
+    bool bad = false;
+    float fx = 0.0f, fy = 0.0f, ue2 = 0.0f, we2 = 0.0f, utri = 0.0f, uwall = 0.0f;
+    if (act) bonded_forces<WX, WY, true>(s, i, mode, pin, pi, fx, fy, ue2, utri, uwall);
+    const float D = s.imgD;
+    const bool near = act && ((WX && (pi.x < D || pi.x > s.Lx - D)) || (WY && (pi.y < D || pi.y > s.Ly - D)));
+    const bool img = __any_sync(0xffffffffu, near);
+    if (act) {
+        if (len >= 0) {
+            if (img)
+                fast_pairs<MT, SG, SIG1, WX, WY, true, true>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
+                                                             fy, ue2, we2);
+            else
+                fast_pairs<MT, SG, SIG1, WX, WY, false, true>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
+                                                              fy, ue2, we2);
+        } else {
+            if (img)
+                fast_pairs<MT, SG, SIG1, WX, WY, true, false>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
+                                                              fy, ue2, we2);
+            else
+                fast_pairs<MT, SG, SIG1, WX, WY, false, false>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig,
+                                                               fx, fy, ue2, we2);
+        }
+        fast_finish<WX, WY>(s, i, mode, pi, m, v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke, vvm, bad);
+    }
+    step_reduce<kFastBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
+}
+
+template <bool MT, bool SG, bool SIG1, bool WX, bool WY>
+static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                                int use_h) {
+    const dim3 g((s.N + kFastBlock - 1) / kFastBlock), b(kFastBlock);
+    const size_t smt = sizeof(PairEntry) * (size_t)(MT ? s.numTypes * s.numTypes : 1) +
+                       (size_t)kWinMax * (sizeof(float2) + (MT ? sizeof(int) : 0) + (SG ? sizeof(float) : 0));
+    return L.kernel(k_fstep<MT, SG, SIG1, WX, WY>, g, b, smt, s, mode, parity, h, use_h);
+}
+
+template <bool MT, bool SG, bool SIG1>
+static cudaError_t fstep_image(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                               int use_h) {
+    if (s.wrapx && s.wrapy) return launch_fstep<MT, SG, SIG1, true, true>(L, s, mode, parity, h, use_h);
+    if (s.wrapx) return launch_fstep<MT, SG, SIG1, true, false>(L, s, mode, parity, h, use_h);
+    return launch_fstep<MT, SG, SIG1, false, false>(L, s, mode, parity, h, use_h);
+}
+
+cudaError_t enqueue_step_fast(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                              int use_h) {
+    const bool mt = s.numTypes > 1, sg = !s.sigmaByType;
+    if (mt) return sg ? fstep_image<true, true, false>(L, s, mode, parity, h, use_h)
+                      : fstep_image<true, false, false>(L, s, mode, parity, h, use_h);
+    if (sg) return fstep_image<false, true, false>(L, s, mode, parity, h, use_h);
+    return s.sigmaOne ? fstep_image<false, false, true>(L, s, mode, parity, h, use_h)
+                      : fstep_image<false, false, false>(L, s, mode, parity, h, use_h);
+}
+
+// =================================================== storage order <-> ids
+
+__global__ void __launch_bounds__(kBlock) k_unperm2(const int *perm, const float2 *in, float2 *out, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) out[__ldg(perm + i)] = in[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_unperm1(const int *perm, const float *in, float *out, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) out[__ldg(perm + i)] = in[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_perm2(const int *perm, const float2 *in, float2 *out, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) out[i] = in[__ldg(perm + i)];
+}
+
+// The constant arrays in storage order from the id-order originals (with
+// ident: the storage order becomes the id order).
+__global__ void __launch_bounds__(kBlock) k_perm_consts(DevSys s, int ident) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.N) return;
+    int id = i;
+    if (ident)
+        s.perm[i] = i;
+    else
+        id = s.perm[i];
+    const_cast<float *>(s.mass)[i] = s.idMass[id];
+    if (s.numTypes > 1) const_cast<int *>(s.typeId)[i] = s.idType[id];
+    if (!s.sigmaByType) const_cast<float *>(s.sigma)[i] = s.idSigma[id];
+    if (s.wallDelta) const_cast<float *>(s.wallDelta)[i] = s.idWallDelta[id];
+    if (s.wallSig) const_cast<float *>(s.wallSig)[i] = s.idWallSig[id];
+}
+
+cudaError_t enqueue_unpermute2(Launch &L, const DevSys &s, const float2 *in, float2 *out) {
+    return L.kernel(k_unperm2, dim3(force_blocks(s.N)), dim3(kBlock), 0, (const int *)s.perm, in, out, s.N);
+}
+
+cudaError_t enqueue_unpermute1(Launch &L, const DevSys &s, const float *in, float *out) {
+    return L.kernel(k_unperm1, dim3(force_blocks(s.N)), dim3(kBlock), 0, (const int *)s.perm, in, out, s.N);
+}
+
+cudaError_t enqueue_permute2(Launch &L, const DevSys &s, const float2 *in, float2 *out) {
+    return L.kernel(k_perm2, dim3(force_blocks(s.N)), dim3(kBlock), 0, (const int *)s.perm, in, out, s.N);
+}
+
+cudaError_t enqueue_perm_identity(Launch &L, const DevSys &s) {
+    return L.kernel(k_perm_consts, dim3(force_blocks(s.N)), dim3(kBlock), 0, s, 1);
+}
+
+cudaError_t enqueue_perm_consts(Launch &L, const DevSys &s) {
+    return L.kernel(k_perm_consts, dim3(force_blocks(s.N)), dim3(kBlock), 0, s, 0);
+}
+
+}  // namespace femmd

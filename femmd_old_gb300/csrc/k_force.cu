@@ -9,7 +9,8 @@
 //
 // Per step:
 //   k_tri_forces  thread per triangle: nodal forces of the triangle written to
-//                 triF[3t+slot] (no atomics), energy reduced in FP64.
+//                 triF[3t+slot] (no atomics); the block's energy in FP32, added
+//                 across blocks as 64-bit fixed point.
 //   k_area_keep,  with area springs only: the positions of the bonded range
 //   k_area        kept for walls and bonds, then the vertices displaced in
 //                 place triangle by triangle (one lane per elastomer).
@@ -19,9 +20,10 @@
 //                 adds into force[i] -- then a = f/m and the leapfrog, fused:
 //                 kick to v(t) and, unless it is the last step of a run, the
 //                 next half kick and the drift into the other position buffer.
-//                 FP32 per-particle sums, FP64 warp/block/grid reductions of
-//                 U, W and sum m v^2 finished by the last block in fixed order
-//                 (deterministic), which also updates dispHi and raises the
+//                 FP32 per-particle and per-block sums of U, W and sum m v^2,
+//                 added across blocks as 64-bit fixed point with integer
+//                 atomics (exact, order-independent, so deterministic); the
+//                 last block converts them, updates dispHi and raises the
 //                 rebuild flag / graph condition for the next step.
 #include <cuda_runtime.h>
 #include "femmd_internal.h"
@@ -245,8 +247,6 @@ __global__ void __launch_bounds__(kStepBlock, MT ? 16 : 12) k_step(DevSys s, int
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
     extern __shared__ PairEntry tab[];  // numTypes^2 entries (1 without types)
-    __shared__ float red[3][kStepBlock / 32];
-    __shared__ float redm[kStepBlock / 32];
     const int nt = s.numTypes;
     if (MT) {
         for (int q = threadIdx.x; q < nt * nt; q += blockDim.x) tab[q] = s.pair[q];
@@ -269,77 +269,7 @@ __global__ void __launch_bounds__(kStepBlock, MT ? 16 : 12) k_step(DevSys s, int
     // four at a time)
     if (i < s.N) particle_step<MT, SG, WX, WY, SIG1, true, MT ? 2 : 4>(s, tab, i, mode, pin, pout, ue, we, ke, vvm, bad);
 
-    // ---- reductions: FP32 within the block, 64-bit fixed-point atomics across
-    // blocks (exact, order-independent); the last block converts and finishes.
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke);
-    float mx = warp_max(vvm);
-    unsigned anybad = __ballot_sync(0xffffffffu, bad);
-    if (lane == 0) {
-        red[0][warp] = su;
-        red[1][warp] = sw;
-        red[2][warp] = sk;
-        redm[warp] = mx;
-        if (anybad) atomicOr(&s.sc->nonfinite, 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float a = 0.0f, b = 0.0f, c = 0.0f, m = 0.0f;
-        for (int w = 0; w < kStepBlock / 32; w++) {
-            a += red[0][w];
-            b += red[1][w];
-            c += red[2][w];
-            m = fmaxf(m, redm[w]);
-        }
-        bool ob = false;
-        unsigned long long qa = to_fixed(a, ob), qb = to_fixed(b, ob), qc = to_fixed(c, ob);
-        DevScalars *sc = s.sc;
-        if (ob) atomicOr(&sc->nonfinite, 2);
-        if (qa) atomicAdd(&sc->accU, qa);
-        if (qb) atomicAdd(&sc->accW, qb);
-        if (qc) atomicAdd(&sc->accK, qc);
-        if (m > 0.0f) atomicMax(&sc->vvMaxBits, __float_as_uint(m));
-        __threadfence();
-        if (atomicAdd(&sc->ticket, 1u) == gridDim.x - 1) {
-            __threadfence();
-            // the grid's last block: every block's atomics are visible
-            double U = from_fixed(atomicExch(&sc->accU, 0ull));
-            double W = from_fixed(atomicExch(&sc->accW, 0ull));
-            double KE = from_fixed(atomicExch(&sc->accK, 0ull));
-            float vm2 = __uint_as_float(atomicExch(&sc->vvMaxBits, 0u));
-            sc->U = U;
-            sc->W = W;
-            int reb;
-            if (mode == MODE_MID || mode == MODE_LAST) {
-                sc->KE = KE;
-                sc->vvMax = vm2;
-                float d = sc->dispHi + sqrtf(vm2) * s.dt;  // md3dsystem.cpp:177
-                reb = (double)d > s.halfSkin;               // nn.cpp:118
-                int row = sc->obsRow;
-                if (s.obs && row < s.obsCap) {
-                    double *o = s.obs + (size_t)row * kObsCols;
-                    o[0] = U;
-                    o[1] = W;
-                    o[2] = KE;
-                    o[3] = (double)vm2;
-                    o[4] = (double)d;
-                    o[5] = (double)reb;
-                }
-                sc->obsRow = row + 1;
-                sc->dispHi = d;  // a rebuild (k_rebuild_begin) restarts it and counts the update
-            } else {
-                reb = (double)sc->dispHi > s.halfSkin;
-            }
-            sc->rebuild = reb;
-            if (mode == MODE_FIRST || mode == MODE_MID) sc->stepNow += 1;  // the drift made x_{n+1}
-            if (use_h) cudaGraphSetConditional(h, reb ? 1u : 0u);
-            sc->ticket = 0;
-            if (s.trace) {
-                int row = sc->obsRow - ((mode == MODE_MID || mode == MODE_LAST) ? 1 : 0);
-                if (row >= 0 && row < s.obsCap) s.trace[(size_t)row * kTraceCols + 3] = global_ns();
-            }
-        }
-    }
+    step_reduce<kStepBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
 }
 
 // leapFrogStep1 + applyPBC on their own: the c_doStep entry (the step
@@ -406,7 +336,9 @@ cudaError_t enqueue_step_after_tri(Launch &L, const DevSys &s, int mode, int par
         if ((e = L.kernel(k_area, dim3(s.areaUnits), dim3(kAreaLanes), (size_t)s.areaSmem, s, parity))) return e;
     }
     cudaEvent_t e0 = L.mark();
-    if (s.numTypes > 1)
+    if (s.fast)
+        e = enqueue_step_fast(L, s, mode, parity, h, use_h);
+    else if (s.numTypes > 1)
         e = s.sigmaByType ? pick_image<true, false>(L, s, mode, parity, h, use_h)
                           : pick_image<true, true>(L, s, mode, parity, h, use_h);
     else

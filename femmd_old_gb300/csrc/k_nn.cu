@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kNnBlock) k_build_nn(DevSys s, int parity, int
 
 int scan_blocks(int ncells) { return (ncells + kScanBlock - 1) / kScanBlock; }
 
-cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
+cudaError_t enqueue_bin(Launch &L, const DevSys &s, int parity, int check) {
     cudaError_t e;
     int pb = (s.N + kBlock - 1) / kBlock;
     int nsb = scan_blocks(s.ncells);
@@ -265,7 +265,14 @@ cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
     if ((e = L.kernel(k_cells_count, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     if ((e = L.kernel(k_scan_blocks, dim3(nsb), dim3(kScanBlock), 0, s, check))) return e;
     if ((e = L.kernel(k_scan_apply, dim3(nsb), dim3(kScanBlock), 0, s, nsb, check))) return e;
-    if ((e = L.kernel(k_scatter, dim3(pb), dim3(kBlock), 0, s, check))) return e;
+    return L.kernel(k_scatter, dim3(pb), dim3(kBlock), 0, s, check);
+}
+
+cudaError_t enqueue_rebuild(Launch &L, const DevSys &s, int parity, int check) {
+    if (s.fast) return enqueue_rebuild_fast(L, s, parity, check);
+    cudaError_t e;
+    int pb = (s.N + kBlock - 1) / kBlock;
+    if ((e = enqueue_bin(L, s, parity, check))) return e;
     if ((e = L.kernel(k_cell_place, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
     const int nb = (s.N + kNnBlock - 1) / kNnBlock;
     if ((e = L.kernel(k_build_nn, dim3(nb), dim3(kNnBlock), 0, s, parity, check))) return e;

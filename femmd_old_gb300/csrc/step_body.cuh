@@ -301,20 +301,15 @@ __device__ __forceinline__ void lj_pair(const DevSys &s, const PairEntry *tab, c
     }
 }
 
-// One particle's step: bond, triangle and pair forces gathered in the order the
-// reference's CPU path adds them into force[i], then the mode's integration.
-// ue/we (doubled energy and virial), ke and vvm are accumulated by the caller.
-// RO: the list and the neighbours' positions are read through the read-only
-// path (written by an earlier kernel); the batched kernel rewrites both in the
-// same launch and reads them with coherent loads (RO = false).
-template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true, int PIPE = 0>
-__device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *tab, int i, int mode,
-                                              const float2 *pin, float2 *pout, float &ue_out,
-                                              float &we_out, float &ke, float &vvm, bool &bad) {
-    float ue = 0.0f, we = 0.0f, utri = 0.0f, uwall = 0.0f;
-    const float2 pi = pin[i];
+// The forces that come before the pair forces in the reference's CPU order
+// for particle i at position pi: the fixed walls and gravity, then (bonded
+// particles) the bond incidences in bond order and the triangles' nodal forces
+// in triangle order.  ue collects the doubled bond energy, utri the triangle
+// energy (MODE_FORCES only), uwall the wall energy.
+template <bool WX, bool WY, bool RO>
+__device__ __forceinline__ void bonded_forces(const DevSys &s, int i, int mode, const float2 *pin, float2 pi,
+                                              float &fx, float &fy, float &ue, float &utri, float &uwall) {
     const float Lx = s.Lx, Ly = s.Ly;
-    float fx = 0.0f, fy = 0.0f;
     // walls and bonds come before the area springs in the reference's force
     // order: they see the positions from before that pass (posPre, for the
     // particles of [0, nPre); pin without area springs)
@@ -363,6 +358,88 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             }
         }
     }
+}
+
+// The rest of particle i's step once its force (fx, fy) is complete: halve
+// the doubled energy and virial, add the wall energy and the moving walls,
+// then the integration of the mode (kick, observables, next half kick and
+// drift into pout) and the outputs of MODE_FORCES / MODE_INIT / MODE_LAST.
+template <bool WX, bool WY>
+__device__ __forceinline__ void finish_particle(const DevSys &s, int i, int mode, float2 pi, float2 *pout, float fx,
+                                                float fy, float ue, float we, float utri, float uwall, float &ue_out,
+                                                float &we_out, float &ke, float &vvm, bool &bad) {
+    const float Lx = s.Lx, Ly = s.Ly;
+    ue *= 0.5f;
+    we *= 0.5f;
+    ue += uwall;
+    if (s.wallOn) {
+        // harmonic walls after the pair forces: top wall at y_w(n), bottom at 0
+        const float yw = wall_y(s, s.sc->stepNow);
+        const float dl = s.wallDelta[i];
+        const float ht = (pi.y + dl) - yw;
+        if (ht > 0.0f) {
+            fy -= s.wallK * ht;
+            ue += 0.5f * s.wallK * ht * ht;
+        }
+        const float hb = dl - pi.y;
+        if (hb > 0.0f) {
+            fy += s.wallK * hb;
+            ue += 0.5f * s.wallK * hb * hb;
+        }
+    }
+    bad = bad || !(isfinite(fx) && isfinite(fy));
+    const float m = s.mass[i];
+    const float ax = fx / m, ay = fy / m;
+    const float dt = s.dt, hdt = s.hdt;
+    if (mode == MODE_FORCES) {
+        s.forceOut[i] = make_float2(fx, fy);
+        s.energyOut[i] = ue + utri;
+    } else if (mode == MODE_INIT) {
+        s.acc[i] = make_float2(ax, ay);
+        s.forceOut[i] = make_float2(fx, fy);
+    } else {
+        float2 v = s.vel[i];
+        if (mode == MODE_MID || mode == MODE_LAST) {
+            // leapFrogStep2 then evalProps
+            v.x += hdt * ax;
+            v.y += hdt * ay;
+            float vv = v.x * v.x + v.y * v.y;
+            vvm = fmaxf(vvm, vv);
+            ke += m * vv;
+        }
+        if (mode == MODE_LAST) {
+            s.vel[i] = v;
+            s.acc[i] = make_float2(ax, ay);
+            s.forceOut[i] = make_float2(fx, fy);
+        } else {
+            // next step's leapFrogStep1 + applyPBC
+            v.x += hdt * ax;
+            v.y += hdt * ay;
+            float2 x = make_float2(pi.x + dt * v.x, pi.y + dt * v.y);
+            if (WX) x.x = wrap_coord(x.x, Lx);
+            if (WY) x.y = wrap_coord(x.y, Ly);
+            pout[i] = x;
+            s.vel[i] = v;
+        }
+    }
+    ue_out += ue;
+    we_out += we;
+}
+
+// One particle's step: bond, triangle and pair forces gathered in the order the
+// reference's CPU path adds them into force[i], then the mode's integration.
+// ue/we (doubled energy and virial), ke and vvm are accumulated by the caller.
+// RO: the list and the neighbours' positions are read through the read-only
+// path (written by an earlier kernel); the batched kernel rewrites both in the
+// same launch and reads them with coherent loads (RO = false).
+template <bool MT, bool SG, bool WX, bool WY, bool SIG1, bool RO = true, int PIPE = 0>
+__device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *tab, int i, int mode,
+                                              const float2 *pin, float2 *pout, float &ue_out,
+                                              float &we_out, float &ke, float &vvm, bool &bad) {
+    float ue = 0.0f, we = 0.0f, utri = 0.0f, uwall = 0.0f;
+    const float2 pi = pin[i];
+    float fx = 0.0f, fy = 0.0f;
+    bonded_forces<WX, WY, RO>(s, i, mode, pin, pi, fx, fy, ue, utri, uwall);
     {
         // pairForce over the Verlet list, in list order.  The list comes in
         // 16-byte groups of four entries (nbr_at); the next group is in
@@ -421,61 +498,88 @@ __device__ __forceinline__ void particle_step(const DevSys &s, const PairEntry *
             g = gn;
         }
     }
-    ue *= 0.5f;
-    we *= 0.5f;
-    ue += uwall;
-    if (s.wallOn) {
-        // harmonic walls after the pair forces: top wall at y_w(n), bottom at 0
-        const float yw = wall_y(s, s.sc->stepNow);
-        const float dl = s.wallDelta[i];
-        const float ht = (pi.y + dl) - yw;
-        if (ht > 0.0f) {
-            fy -= s.wallK * ht;
-            ue += 0.5f * s.wallK * ht * ht;
+    finish_particle<WX, WY>(s, i, mode, pi, pout, fx, fy, ue, we, utri, uwall, ue_out, we_out, ke, vvm, bad);
+}
+
+// End of a step kernel: the block's energy, virial, kinetic and max-speed
+// sums in FP32, added across blocks as 64-bit fixed point with integer
+// atomics (exact, order-independent); the grid's last block converts them,
+// updates dispHi (md3dsystem.cpp:177), writes the observable row, sets the
+// rebuild flag by the reference's test (nn.cpp:118) and the graph condition.
+template <int BLOCK>
+__device__ __forceinline__ void step_reduce(const DevSys &s, int mode, float ue, float we, float ke, float vvm,
+                                            bool bad, cudaGraphConditionalHandle h, int use_h) {
+    __shared__ float red[3][BLOCK / 32];
+    __shared__ float redm[BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke);
+    float mx = warp_max(vvm);
+    unsigned anybad = __ballot_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        red[0][warp] = su;
+        red[1][warp] = sw;
+        red[2][warp] = sk;
+        redm[warp] = mx;
+        if (anybad) atomicOr(&s.sc->nonfinite, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.0f, b = 0.0f, c = 0.0f, m = 0.0f;
+        for (int w = 0; w < BLOCK / 32; w++) {
+            a += red[0][w];
+            b += red[1][w];
+            c += red[2][w];
+            m = fmaxf(m, redm[w]);
         }
-        const float hb = dl - pi.y;
-        if (hb > 0.0f) {
-            fy += s.wallK * hb;
-            ue += 0.5f * s.wallK * hb * hb;
+        bool ob = false;
+        unsigned long long qa = to_fixed(a, ob), qb = to_fixed(b, ob), qc = to_fixed(c, ob);
+        DevScalars *sc = s.sc;
+        if (ob) atomicOr(&sc->nonfinite, 2);
+        if (qa) atomicAdd(&sc->accU, qa);
+        if (qb) atomicAdd(&sc->accW, qb);
+        if (qc) atomicAdd(&sc->accK, qc);
+        if (m > 0.0f) atomicMax(&sc->vvMaxBits, __float_as_uint(m));
+        __threadfence();
+        if (atomicAdd(&sc->ticket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            // the grid's last block: every block's atomics are visible
+            double U = from_fixed(atomicExch(&sc->accU, 0ull));
+            double W = from_fixed(atomicExch(&sc->accW, 0ull));
+            double KE = from_fixed(atomicExch(&sc->accK, 0ull));
+            float vm2 = __uint_as_float(atomicExch(&sc->vvMaxBits, 0u));
+            sc->U = U;
+            sc->W = W;
+            int reb;
+            if (mode == MODE_MID || mode == MODE_LAST) {
+                sc->KE = KE;
+                sc->vvMax = vm2;
+                float d = sc->dispHi + sqrtf(vm2) * s.dt;  // md3dsystem.cpp:177
+                reb = (double)d > s.halfSkin;               // nn.cpp:118
+                int row = sc->obsRow;
+                if (s.obs && row < s.obsCap) {
+                    double *o = s.obs + (size_t)row * kObsCols;
+                    o[0] = U;
+                    o[1] = W;
+                    o[2] = KE;
+                    o[3] = (double)vm2;
+                    o[4] = (double)d;
+                    o[5] = (double)reb;
+                }
+                sc->obsRow = row + 1;
+                sc->dispHi = d;  // a rebuild (k_rebuild_begin) restarts it and counts the update
+            } else {
+                reb = (double)sc->dispHi > s.halfSkin;
+            }
+            sc->rebuild = reb;
+            if (mode == MODE_FIRST || mode == MODE_MID) sc->stepNow += 1;  // the drift made x_{n+1}
+            if (use_h) cudaGraphSetConditional(h, reb ? 1u : 0u);
+            sc->ticket = 0;
+            if (s.trace) {
+                int row = sc->obsRow - ((mode == MODE_MID || mode == MODE_LAST) ? 1 : 0);
+                if (row >= 0 && row < s.obsCap) s.trace[(size_t)row * kTraceCols + 3] = global_ns();
+            }
         }
     }
-    bad = bad || !(isfinite(fx) && isfinite(fy));
-    const float m = s.mass[i];
-    const float ax = fx / m, ay = fy / m;
-    const float dt = s.dt, hdt = s.hdt;
-    if (mode == MODE_FORCES) {
-        s.forceOut[i] = make_float2(fx, fy);
-        s.energyOut[i] = ue + utri;
-    } else if (mode == MODE_INIT) {
-        s.acc[i] = make_float2(ax, ay);
-        s.forceOut[i] = make_float2(fx, fy);
-    } else {
-        float2 v = s.vel[i];
-        if (mode == MODE_MID || mode == MODE_LAST) {
-            // leapFrogStep2 then evalProps
-            v.x += hdt * ax;
-            v.y += hdt * ay;
-            float vv = v.x * v.x + v.y * v.y;
-            vvm = fmaxf(vvm, vv);
-            ke += m * vv;
-        }
-        if (mode == MODE_LAST) {
-            s.vel[i] = v;
-            s.acc[i] = make_float2(ax, ay);
-            s.forceOut[i] = make_float2(fx, fy);
-        } else {
-            // next step's leapFrogStep1 + applyPBC
-            v.x += hdt * ax;
-            v.y += hdt * ay;
-            float2 x = make_float2(pi.x + dt * v.x, pi.y + dt * v.y);
-            if (WX) x.x = wrap_coord(x.x, Lx);
-            if (WY) x.y = wrap_coord(x.y, Ly);
-            pout[i] = x;
-            s.vel[i] = v;
-        }
-    }
-    ue_out += ue;
-    we_out += we;
 }
 
 }  // namespace femmd

@@ -46,6 +46,7 @@ enum { FEMMD_FEA_NEO_HOOKEAN = 0, FEMMD_FEA_GREEN_LINEAR = 1 }; /* interactions.
 enum { FEMMD_BONDK_KBOND = 0, FEMMD_BONDK_E_OVER_R0 = 1 };      /* interactions.cpp:161 / interactionsCuda.cu:238 */
 enum { FEMMD_IMAGE_REFERENCE = 0, FEMMD_IMAGE_EXACT = 1 };
 enum { FEMMD_ELASTOMER_BONDS_ALL = 0, FEMMD_ELASTOMER_BONDS_BOUNDARY = 1, FEMMD_ELASTOMER_BONDS_NONE = 2 };
+enum { FEMMD_FORCE_REFERENCE = 0, FEMMD_FORCE_FAST = 1 };
 
 /* ----------------------------------------------------------- lifecycle */
 /* MDSystem(0) + setDevice(GPU): femmd2D/src/md3dsystem.h:58-84.  device is the CUDA ordinal. */
@@ -124,6 +125,21 @@ femmd_status femmd_get_neighbor_capacity(const femmd_ctx *ctx, int *cap);
 femmd_status femmd_set_fea_law(femmd_ctx *ctx, int law);
 femmd_status femmd_set_bond_k_mode(femmd_ctx *ctx, int mode);
 femmd_status femmd_set_image_mode(femmd_ctx *ctx, int mode);
+/* Force mode (default FEMMD_FORCE_REFERENCE).  The reference mode reproduces
+ * the reference's float operations and list order, so trajectories follow
+ * the reference's bit for bit (in FEMMD_IMAGE_REFERENCE) or the oracle's.
+ * FEMMD_FORCE_FAST keeps the same cell and neighbour sets and forces,
+ * energies and virial within 1e-5 of an FP64 evaluation, but sums with fused
+ * multiply-adds and the hardware reciprocal and stores the free particles in
+ * cell order on the device (renewed with every neighbour list); trajectories
+ * then agree with the reference-exact ones to rounding, not bit for bit.
+ * Getters and setters keep the particle ids either way.  The batched kernel
+ * and the adjoint run the reference mode only (FEMMD_UNSUPPORTED in fast
+ * mode).  Changing the mode re-uploads the system at the next run.  No
+ * counterpart in the reference, whose CPU and GPU paths each fix one
+ * arithmetic. */
+femmd_status femmd_set_force_mode(femmd_ctx *ctx, int mode);
+femmd_status femmd_get_force_mode(const femmd_ctx *ctx, int *mode);
 /* Which edges of each later add_elastomer become bonds (default: every
  * triangle edge, interior edges twice, as particles.cpp:335-337). */
 femmd_status femmd_set_elastomer_bonds(femmd_ctx *ctx, int mode);
