@@ -26,7 +26,7 @@ import numpy as np
 OP = dict(END=0, INIT=1, PBC=2, DT=3, NUMTYPES=4, PAIR=5, KBOND=6, YOUNG=7, NU=8, SKIN=9,
           ELASTOMER=10, PARTICLE=11, BOND=12, INITNN=13, CAPACITY=14, RUN=15, STEP=16,
           BUILDNN=17, FORCES=18, ELASTOMER_BONDS=19, DUMP_STATE=20, DUMP_NN=21, DUMP_SETUP=22,
-          SETVEL=23, GRAVITY=24, KAREA=25, SAVE=26, SCALE=27)
+          SETVEL=23, GRAVITY=24, KAREA=25, SAVE=26, SCALE=27, FEA_CPU1=28)
 
 WCA_RC = 2.0 ** (1.0 / 6.0)
 
@@ -115,6 +115,8 @@ class Scene:
                 w(struct.pack("<i", OP["BUILDNN"]))
             elif name == "calc_forces":
                 w(struct.pack("<i", OP["FORCES"]))
+            elif name == "fea_cpu1":
+                w(struct.pack("<i", OP["FEA_CPU1"]))
             elif name == "dump_state":
                 w(struct.pack("<i", OP["DUMP_STATE"]))
             elif name == "dump_nn":
@@ -228,6 +230,8 @@ class Scene:
                 sc.add("build_nn")
             elif name == "FORCES":
                 sc.add("calc_forces")
+            elif name == "FEA_CPU1":
+                sc.add("fea_cpu1")
             elif name == "DUMP_STATE":
                 sc.add("dump_state")
             elif name == "DUMP_NN":

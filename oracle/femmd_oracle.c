@@ -897,6 +897,79 @@ static float tri_green(const orc *s, int t, float *f) {
     return eneVal;
 }
 
+static void fea_forces(orc *s);
+
+/* Interactions::calcFeaForcesCPU1 (src/interactions.cpp:411-530), the
+ * reference's CPU twin of the GPU kernel's Green-strain / linear-C law, alone
+ * after Integrator::zeroStuff: FEA forces and energy only, with the
+ * reference's own mix of precisions -- positions, strains, energy and the
+ * scatter in float; the half-box tests against box / 2.0, the area's and
+ * e01's halving and the nodal force sums (-2.0 * Cxxxx * ...) in double,
+ * rounded to float once.  xm and the reference positions are the setup
+ * arrays (src/particles.cpp:340-352); FeaElements::offset is 0
+ * (src/feaElements.cpp:9). */
+void orc_fea_cpu1(orc *s) {
+    orc_zero_stuff(s);
+    const float Lx = s->Lx, Ly = s->Ly;
+    for (int t = 0; t < s->ntri; t++) {
+        int p[3];
+        float rx[3], ry[3], X[3], Y[3];
+        for (int i = 0; i < 3; i++) {
+            p[i] = s->tri[3 * t + i];
+            rx[i] = s->px[p[i]]; ry[i] = s->py[p[i]];
+            X[i] = s->refx[p[i]]; Y[i] = s->refy[p[i]];
+        }
+        const float dx01 = rx[0] - rx[1];
+        if (dx01 > (double)Lx / 2.0) rx[1] += Lx;
+        if (dx01 < -(double)Lx / 2.0) rx[1] -= Lx;
+        const float dx02 = rx[0] - rx[2];
+        if (dx02 > (double)Lx / 2.0) rx[2] += Lx;
+        if (dx02 < -(double)Lx / 2.0) rx[2] -= Lx;
+        const float dy01 = ry[0] - ry[1];
+        if (dy01 > (double)Ly / 2.0) ry[1] += Ly;
+        if (dy01 < -(double)Ly / 2.0) ry[1] -= Ly;
+        const float dy02 = ry[0] - ry[2];
+        if (dy02 > (double)Ly / 2.0) ry[2] += Ly;
+        if (dy02 < -(double)Ly / 2.0) ry[2] -= Ly;
+        float vol = (float)(0.5 * (double)((Y[2] - Y[0]) * (X[1] - X[0]) - (Y[1] - Y[0]) * (X[2] - X[0])));
+        vol = fabsf(vol);
+        const float *m = s->xm + 9 * (size_t)t;
+        float ux[3], uy[3], a[3], b[3];
+        for (int i = 0; i < 3; i++) { ux[i] = rx[i] - X[i]; uy[i] = ry[i] - Y[i]; a[i] = b[i] = 0.0f; }
+        for (int j = 0; j < 3; j++)
+            for (int i = 0; i < 3; i++) {
+                a[i] = a[i] + m[3 * i + j] * ux[j];
+                b[i] = b[i] + m[3 * i + j] * uy[j];
+            }
+        const float e00 = a[1] + 0.5f * (a[1] * a[1] + b[1] * b[1]);
+        const float e11 = b[2] + 0.5f * (a[2] * a[2] + b[2] * b[2]);
+        const float e01 = (float)(0.5 * (double)(a[2] + b[1] + a[1] * a[2] + b[1] * b[2]));
+        const float c1 = s->Cxxxx, c2 = s->Cxxyy, c3 = s->Cxyxy;
+        const float pesum = c1 * (e00 * e00 + e11 * e11) + 2.0f * c2 * (e00 * e11) + 4.0f * c3 * (e01 * e01);
+        s->potEnergy += pesum * vol;
+        for (int i = 0; i < 3; i++) {
+            const int j = p[i];
+            const double m1 = m[3 + i], m2 = m[6 + i];
+            const float fxsum = (float)(-2.0 * c1 * e00 * m1 * (1.0 + a[1]) - 2.0 * c1 * e11 * m2 * a[2]
+                                        - 2.0 * c2 * e00 * m2 * a[2] - 2.0 * c2 * e11 * m1 * (1.0 + a[1])
+                                        - 4.0 * c3 * e01 * m2 * (1.0 + a[1]) - 4.0 * c3 * e01 * m1 * a[2]);
+            const float fysum = (float)(-2.0 * c1 * e00 * m1 * b[1] - 2.0 * c1 * e11 * m2 * (1.0 + b[2])
+                                        - 2.0 * c2 * e00 * m2 * (1.0 + b[2]) - 2.0 * c2 * e11 * m1 * b[1]
+                                        - 4.0 * c3 * e01 * m1 * (1.0 + b[2]) - 4.0 * c3 * e01 * m2 * b[1]);
+            s->fx[j] += fxsum * vol;
+            s->fy[j] += fysum * vol;
+        }
+    }
+}
+
+/* The FEA forces and energy alone, after zeroStuff, by the law in use (the
+ * float law of the GPU kernel for fea_law 1), for comparison with
+ * orc_fea_cpu1. */
+void orc_fea_only(orc *s) {
+    orc_zero_stuff(s);
+    fea_forces(s);
+}
+
 static void fea_forces(orc *s) {
     if (s->ncl > 0) unfold_pos(s);
     for (int t = 0; t < s->ntri; t++) {

@@ -36,9 +36,10 @@ def build(quiet: bool = True) -> str:
 
 
 def build_reference() -> str | None:
-    """Compile the reference harness from the reference sources, when present."""
-    src = os.environ.get("FEMMD_REF_SRC", "/root/reference/femmd2D/src")
-    if not os.path.isdir(src):
+    """Compile the reference harness from the reference sources named by
+    FEMMD_REF_SRC (the checkout's femmd2D/src), when they exist."""
+    src = os.environ.get("FEMMD_REF_SRC")
+    if not src or not os.path.isdir(src):
         return None
     out = subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={src}", "-j8"], capture_output=True, text=True)
     if out.returncode != 0:
@@ -72,6 +73,7 @@ def lib():
             "orc_init_neighbor_list": (C.c_int, [P]), "orc_build_nn": (None, [P]),
             "orc_update_nn": (None, [P, C.c_int]), "orc_zero_stuff": (None, [P]),
             "orc_calc_forces": (None, [P]), "orc_run": (None, [P, C.c_int]), "orc_do_step": (None, [P]),
+            "orc_fea_cpu1": (None, [P]), "orc_fea_only": (None, [P]),
             "orc_forces_f64": (None, [P, dp, dp, dp, dp, dp]),
             "orc_n": (C.c_int, [P]), "orc_nref": (C.c_int, [P]), "orc_nbonds": (C.c_int, [P]), "orc_ntri": (C.c_int, [P]),
             "orc_steps": (C.c_int, [P]), "orc_total_updates": (C.c_int, [P]), "orc_ncells": (C.c_int, [P]),
@@ -375,6 +377,16 @@ class Oracle:
     def calc_forces(self):
         self.L.orc_zero_stuff(self.h)
         self.L.orc_calc_forces(self.h)
+
+    def fea_cpu1(self):
+        """zeroStuff, then Interactions::calcFeaForcesCPU1 alone (the
+        reference's CPU Green-strain / linear-C law, with its double-precision
+        force sums)."""
+        self.L.orc_fea_cpu1(self.h)
+
+    def fea_only(self):
+        """zeroStuff, then the FEA forces alone by the oracle's law in use."""
+        self.L.orc_fea_only(self.h)
 
     # ---------------------------------------- dumps (same records as the harness)
     dumps: list

@@ -24,7 +24,7 @@ enum Op {
     OP_YOUNG = 7, OP_NU = 8, OP_SKIN = 9, OP_ELASTOMER = 10, OP_PARTICLE = 11, OP_BOND = 12,
     OP_INITNN = 13, OP_CAPACITY = 14, OP_RUN = 15, OP_STEP = 16, OP_BUILDNN = 17, OP_FORCES = 18,
     OP_ELASTOMER_BONDS = 19, OP_DUMP_STATE = 20, OP_DUMP_NN = 21, OP_DUMP_SETUP = 22, OP_SETVEL = 23,
-    OP_GRAVITY = 24, OP_KAREA = 25, OP_SAVE = 26, OP_SCALE = 27
+    OP_GRAVITY = 24, OP_KAREA = 25, OP_SAVE = 26, OP_SCALE = 27, OP_FEA_CPU1 = 28
 };
 
 // Bond set of an elastomer: 0 keeps the reference's bonds on every triangle
@@ -230,6 +230,9 @@ int main(int argc, char **argv) {
         case OP_STEP: s.integrator.doStep(); break;
         case OP_BUILDNN: s.neighborlist.buildNN(); break;
         case OP_FORCES: s.integrator.zeroStuff(); s.interactions.calcForces(); break;
+        // the Green-strain / linear-C law of the reference's CPU path alone
+        // (Interactions::calcFeaForcesCPU1, public, src/interactions.h:51)
+        case OP_FEA_CPU1: s.integrator.zeroStuff(); s.interactions.calcFeaForcesCPU1(); break;
         case OP_DUMP_STATE: dump_state(s); break;
         case OP_DUMP_NN: dump_nn(s); break;
         case OP_DUMP_SETUP: dump_setup(s); break;

@@ -6,8 +6,10 @@ own C++ classes, compiled from the reference sources (oracle/Makefile target
 neighbour sets, forces, energies and trajectory snapshots; this script stores
 the scene command stream and every dump in tests/golden/<case>.npz.
 
-Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py
+Run where the reference checkout exists, naming its source and mesh
+directories:
+    FEMMD_REF_SRC=<checkout>/femmd2D/src FEMMD_REF_MESHES=<checkout>/femmd2D/meshes \
+        python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -25,7 +27,9 @@ from femmd_old_gb300 import scene as S  # noqa: E402
 import oracle as O  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-MESHES = os.environ.get("FEMMD_REF_MESHES", "/root/reference/femmd2D/meshes")
+# the reference's meshes directory (femmd2D/meshes of its checkout), needed
+# by the case that uses the reference's own disk mesh
+MESHES = os.environ.get("FEMMD_REF_MESHES", "")
 
 
 def probes(sc: S.Scene, runs=(50, 200)) -> S.Scene:
@@ -160,6 +164,8 @@ def case_susp_boundary():
 
 
 def case_susp_refdisk():
+    if not MESHES:
+        raise SystemExit("set FEMMD_REF_MESHES to the meshes directory of the reference checkout (femmd2D/meshes)")
     v, t = S.load_mesh(os.path.join(MESHES, "diskVertices.txt"), os.path.join(MESHES, "diskTriangles.txt"))
     sc = S.suspension(n_side=3, radius=4.0, mesh=(v * 8.0, t), bonds="all", T=0.3, center_jitter=0.2, phi=0.4)
     return probes(sc, runs=(100, 200))
@@ -355,6 +361,35 @@ def frames_mixed():
 FRAME_CASES = {k[7:]: v for k, v in globals().items() if k.startswith("frames_")}
 
 
+def green_susp_cpu1():
+    """The reference's CPU Green-strain / linear-C law
+    (Interactions::calcFeaForcesCPU1, interactions.cpp:411-530), called alone
+    after zeroStuff at positions the reference's own run (neo-Hookean, no
+    bonds) deformed: six hex-ring disks, apart from each other (no pair
+    inside the WCA cutoff), three across the periodic edges."""
+    verts, tris = S.hex_disk_mesh(3.0, 3, jitter=0.03, seed=81)
+    nv = verts.shape[0]
+    L = 30.0
+    sc = S.Scene(meta=dict(workload="green_cpu1"))
+    sc.add("init", L, L).add("PBC", 2).add("set_dt", 0.002).add("set_numTypes", 1)
+    sc.add("set_pair_potential", [1.0], [S.WCA_RC], [1.0]).add("set_skin", 0.3)
+    sc.add("set_kBond", 0.0).add("set_youngs_modulus", 45.0).add("set_poisson_ratio", 0.3)
+    sc.add("set_elastomer_bonds", 2)
+    centers = [(0.4, 7.0), (15.0, 0.2), (29.6, 29.5), (8.0, 20.0), (21.0, 12.0), (14.5, 23.0)]
+    for c in centers:
+        sc.add("add_elastomer", verts, tris, c[0], c[1], 0, 0, 1.0, float(nv), True)
+    sc.add("init_neighbor_list")
+    rng = np.random.Generator(np.random.PCG64(82))
+    sc.add("set_velocities_array", rng.normal(0, 0.6, size=(len(centers) * nv, 2)).astype(np.float32))
+    sc.add("dump_setup")
+    for n in (60, 90):
+        sc.add("run", n).add("dump_state").add("fea_cpu1").add("dump_state")
+    return sc
+
+
+GREEN_CASES = {k[6:]: v for k, v in globals().items() if k.startswith("green_")}
+
+
 def save_frames(name: str, sc: S.Scene, dumps, files):
     blob = {"scene": np.frombuffer(sc.to_bytes(), np.uint8)}
     for k, (tag, d) in enumerate(dumps):
@@ -377,7 +412,7 @@ def save(name: str, sc: S.Scene, dumps):
 
 def main(names=None):
     if O.build_reference() is None:
-        raise SystemExit("reference checkout not found; golden fixtures are generated where it exists")
+        raise SystemExit("reference sources not found: set FEMMD_REF_SRC to the checkout's femmd2D/src")
     for name, fn in CASES.items():
         if names and name not in names:
             continue
@@ -385,6 +420,14 @@ def main(names=None):
         dumps = O.run_reference(sc)
         save(name, sc, dumps)
         print(f"{name}: {len(dumps)} dumps, {os.path.getsize(os.path.join(OUT, name + '.npz'))} bytes")
+    for name, fn in GREEN_CASES.items():
+        if names and "green_" + name not in names:
+            continue
+        sc = fn()
+        dumps = O.run_reference(sc)
+        os.makedirs(os.path.join(OUT, "green"), exist_ok=True)
+        save(os.path.join("green", name), sc, dumps)
+        print(f"green {name}: {len(dumps)} dumps")
     for name, fn in FRAME_CASES.items():
         if names and "frames_" + name not in names:
             continue

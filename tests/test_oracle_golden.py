@@ -103,3 +103,59 @@ def test_own_log_accuracy():
     ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
     err = np.abs(got - ref) / np.maximum(ulp, np.finfo(np.float32).tiny)
     assert err.max() <= 2.0, err.max()
+
+
+# ------------------------------------------- the Green-strain / linear-C law
+
+def _green_dumps():
+    sc, ref = G.load("green/susp_cpu1")
+    return sc, ref, [d for t, d in ref if t == "state"]
+
+
+def test_green_law_cpu1_matches_reference_bitwise():
+    """The reference's own CPU Green-strain / linear-C law
+    (Interactions::calcFeaForcesCPU1, interactions.cpp:411-530), called alone
+    after zeroStuff at positions the reference's run deformed: the oracle's
+    restatement of it (its double-precision force sums included) reproduces
+    every dumped array bit for bit -- positions, forces and the FEA energy."""
+    sc, ref, _ = _green_dumps()
+    assert sum(n == "fea_cpu1" for n, _ in sc.calls) == 2
+    o = Oracle(image_mode=0, log_mode=0)
+    sc.replay(o)
+    bad = G.diff_report(ref, o.dumps)
+    assert not bad, "\n".join(bad)
+
+
+def test_green_law_float_restatement_within_rounding_of_cpu1():
+    """The float restatement of the same law (the reference's GPU kernel
+    computeFeaForcesGPU, interactionsCuda.cu:312-451, which the product's
+    tri_green follows bit for bit) against the reference's CPU twin at the
+    same positions: every nodal force within 1e-6 of the largest FEA force
+    (the CPU twin sums the nodal force terms in double, the kernel in float;
+    measured 1.9e-7), the energy within 1e-6 relative (measured equal).  The
+    disks are apart (no pair inside the WCA cutoff, so the full force pass
+    is the FEA pass) and some straddle the periodic edges."""
+    sc, ref, states = _green_dumps()
+    o = Oracle(image_mode=0, log_mode=0, fea_law=1)
+    first = next(k for k, (n, _) in enumerate(sc.calls) if n == "run")
+    for n, a in sc.calls[:first]:
+        if n.startswith("dump"):
+            continue
+        getattr(o, n)(*a)
+    crossed = False
+    for k in (0, 2):
+        pos, cpu1 = states[k]["pos"], states[k + 1]
+        o.set_positions_array(pos)
+        o.fea_only()
+        f = o.forces().astype(np.float64)
+        g = cpu1["force"].astype(np.float64)
+        scale = np.abs(g).max()
+        assert scale > 1.0
+        assert np.abs(f - g).max() <= 1e-6 * scale, np.abs(f - g).max() / scale
+        u, uref = float(o.scalars()[0]), float(cpu1["scalars"][0])
+        assert abs(u - uref) <= 1e-6 * abs(uref)
+        o.build_nn()
+        o.calc_forces()
+        assert np.array_equal(G.bits(o.forces()), G.bits(f.astype(np.float32)))
+        crossed = crossed or (np.abs(np.diff(pos[:37, 0])).max() > 15.0)
+    assert crossed  # the first disk straddles x = 0
