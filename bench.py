@@ -52,7 +52,10 @@ WORKLOADS = {
     "suspension": ("elastomer suspension: 256 hex-ring disks (127 vertices), E=50, nu=0.3, boundary bonds k=100, "
                    "WCA, phi=0.5, T=0.1, dt=0.002, skin 0.3", lambda: S.suspension()),
     "lj_fluid": ("plain LJ fluid: N=4096, rho=0.8, rc=2.5, skin 0.3, dt=0.005", lambda: S.lj_fluid()),
+    "lj_1m": ("plain LJ fluid, the solvent class of the large mixed system: N=1,000,000 (1000x1000 jittered "
+              "lattice), rho=0.8, rc=2.5, skin 0.3, dt=0.005, T=1", lambda: S.lj_fluid(n_side=1000)),
 }
+FORCE_MODES = {"fast": 1, "reference": 0}
 BATCHED_DESC = ("batched ensemble: 512 independent LJ+elastomer replicas, atom counts log-uniform in [500, 20000] "
                 "(seed 8), density U(0.6, 0.85) and T U(0.1, 1.5) (seed 9), 90 % solvent + hex-ring disks, "
                 "dt=0.005, skin 0.3, one persistent launch per run() under a CUDA graph, autotuned block shape")
@@ -67,9 +70,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--force-mode", default="fast", choices=sorted(FORCE_MODES),
+                    help="fast: same sets, forces within 1e-5 of FP64, cell-ordered storage (default); "
+                         "reference: the reference's float operations and list order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--probe", default=None,
-                    choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras"],
+                    choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras", "lj_1m"],
                     help="run one small fixed workload for a profiler capture and exit (no JSON line)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
@@ -191,40 +197,45 @@ def reference_arm(args, dist):
         o = O.Oracle(image_mode=0, log_mode=0, threads=threads)
         sc.replay(o)
         systems.append(o)
+    # every bench step is the repo arm's run(S): one forced rebuild and initial
+    # force pass per S leapfrog steps, the same schedule; the number of timed
+    # steps is cut so that the whole arm ends within about two minutes
+    md = args.md_steps
     t0 = time.perf_counter()
     for o in systems:
         o.run(1)
-    per = time.perf_counter() - t0
-    # each bench step: a run(m) sample sized so the whole K+W run stays ~2 minutes
-    m = max(1, min(args.md_steps, int(120.0 / max(per, 1e-6) / max(args.steps + args.warmup, 1))))
-    for _ in range(args.warmup):
+    per_run = (time.perf_counter() - t0) * md
+    steps = max(1, min(args.steps, int(120.0 / max(per_run, 1e-6))))
+    warmup = min(args.warmup, 1) if per_run < 30.0 else 0
+    for _ in range(warmup):
         for o in systems:
-            o.run(m)
+            o.run(md)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         for o in systems:
-            o.run(m)
+            o.run(md)
     dt = time.perf_counter() - t0
-    value = natoms * m * args.steps / dt
-    what = (f"{len(scenes)} replicas ({natoms} atoms) each run({m}) in turn" if len(scenes) > 1 else
-            f"run({m}) of the {natoms}-atom system")
+    value = natoms * md * steps / dt
+    what = (f"{len(scenes)} replicas ({natoms} atoms) each run({md}) in turn" if len(scenes) > 1 else
+            f"run({md}) of the {natoms}-atom system")
     return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "impl": "reference",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "description": desc, "atoms": natoms, "md_steps_per_step": m,
-                       "parallelism": "replicas"},
+            "config": {"workload": args.workload, "description": desc, "atoms": natoms, "md_steps_per_step": md,
+                       "parallelism": "replicas" if len(scenes) > 1 else "single"},
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{what} per step; the reference's own binary (oracle/_ref) is built "
-                                       "for x86 and cannot run on this host"},
+                             "sample": f"{what} per step, {steps} timed steps of the requested {args.steps}; the "
+                                       "reference's own binary (oracle/_ref) is built for x86 and cannot run on "
+                                       "this host"},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 # ---------------------------------------------------------------- GPU arm
 
-def load_traffic(workload):
-    """DRAM bytes per k_step launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"k_step_{workload}.md")
+def load_traffic(kernel, workload):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -259,6 +270,7 @@ def ours(args, dist):
     sc.meta["types"] = max([a[0] for nm, a in sc.calls if nm == "set_numTypes"] or [1])
     dev = dist.local
     s = F.System(dev)
+    s.set_force_mode(FORCE_MODES[args.force_mode])
     sc.replay(s)
     n = s.N
     md = args.md_steps
@@ -338,9 +350,14 @@ def ours(args, dist):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = kbytes / (kms / 1e3) / 1e9
-    traffic = load_traffic(args.workload)
+    fast = args.force_mode == "fast"
+    kname = "k_fstep" if fast else "k_step"
+    traffic = load_traffic(kname, args.workload)
+    what = ("fast mode: cell-ordered storage, windows in shared memory, fused multiply-adds, hardware "
+            "reciprocal" if fast else "reference-exact arithmetic and list order")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_step (fused LJ+bond+triangle gather, leapfrog, fixed-point energy sums)",
+                "traffic": traffic,
+                "kernel": f"{kname} (fused LJ+bond+triangle gather, leapfrog, fixed-point energy sums; {what})",
                 "algorithmic_bytes_per_launch": kbytes, "mean_launch_ms": kms,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
 
@@ -359,7 +376,7 @@ def ours(args, dist):
                        "parallelism": "replicas" if dist.world > 1 else "single",
                        "l2": "L2 flushed between timed steps" if flush is not None else
                              "inputs larger than L2 (state + lists > 129 MB)",
-                       "image_mode": "exact", "fea_law": "neo-Hookean"},
+                       "image_mode": "exact", "fea_law": "neo-Hookean", "force_mode": args.force_mode},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     return line
 
@@ -551,7 +568,7 @@ def adjoint_ratio(dev, reps=3, steps=200, every=20):
 # Small fixed workloads for profiler captures (the commands in profiles/):
 # each runs once on cuda:0, prints "ok" and no JSON line.
 
-def probe(name):
+def probe(name, mode="fast"):
     import femmd_old_gb300 as F
     import torch
     if name == "midrun_rebuild":
@@ -587,6 +604,21 @@ def probe(name):
         b.run(0)
         b.run(10)
         keep[0].sync()
+    elif name == "lj_1m":
+        # the 1M-atom LJ fluid in the force mode of --force-mode: run(0),
+        # run(50), then run(12) launched directly (no graph) inside the NVTX
+        # range "steps"
+        s = F.System()
+        s.set_force_mode(FORCE_MODES[mode])
+        S.lj_fluid(n_side=1000).replay(s)
+        s.run(0)
+        s.run(50)
+        s.sync()
+        torch.cuda.nvtx.range_push("steps")
+        s.set_profiling(True)
+        s.run(12)
+        s.sync()
+        torch.cuda.nvtx.range_pop()
     elif name == "adjoint":
         # config 5: forward with checkpoints every 20 steps, then the backward
         c = F.System()
@@ -630,7 +662,7 @@ def probe(name):
 def main():
     args = parse()
     if args.probe:
-        probe(args.probe)
+        probe(args.probe, args.force_mode)
         return
     dist = Dist()
     try:
@@ -642,6 +674,18 @@ def main():
             line = ours(args, dist)
             if dist.rank == 0 and args.workload == "large_mixed" and not args.no_extras:
                 dev = dist.local
+                # the 1M-atom LJ fluid (the solvent class, where the HBM-roofline
+                # target is stated) and the headline system in the other force mode
+                keep = ("value", "unit", "ms_per_step", "roofline", "e2e", "gpu_launches", "clocks")
+                for key, wl, mode in (("lj_1m", "lj_1m", args.force_mode),
+                                      ("other_mode", "large_mixed",
+                                       "reference" if args.force_mode == "fast" else "fast")):
+                    sub = argparse.Namespace(**vars(args))
+                    sub.workload, sub.force_mode = wl, mode
+                    sub.steps, sub.warmup, sub.no_cpu_baseline = max(3, min(args.steps, 10)), 3, True
+                    r = ours(sub, _Solo())
+                    line[key] = {k: r[k] for k in keep}
+                    line[key]["config"] = r["config"]
                 line["adjoint"] = adjoint_ratio(dev)
                 sub = argparse.Namespace(**vars(args))
                 sub.steps, sub.warmup, sub.md_steps, sub.no_cpu_baseline = 3, 3, 100, True
