@@ -228,7 +228,7 @@ struct femmd_ctx {
     // the step blocks' windows
     int forceMode = FEMMD_FORCE_REFERENCE;
     DBuf<int> perm, sPerm, fBlockSums, ckPerm, idType, newCell;
-    DBuf<int4> blockWin;
+    DBuf<int> blockWin;
     DBuf<float2> sPos, sVel, sAcc;
     DBuf<float> idMass, idSigma, idWallDelta, idWallSig, xfer1;
     float imgD = 0;
@@ -869,7 +869,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(ctx->sPos.ensure(N)); CK(ctx->sVel.ensure(N)); CK(ctx->sAcc.ensure(N));
         CK(ctx->fBlockSums.ensure((N + 1023) / 1024));
         CK(ctx->newCell.ensure(N));
-        CK(ctx->blockWin.ensure(4 * (size_t)((N + kFastBlock - 1) / kFastBlock)));
+        CK(ctx->blockWin.ensure(kWinInts * (size_t)((N + kFastBlock - 1) / kFastBlock)));
         CK(ctx->idMass.ensure(N)); CK(ctx->idType.ensure(N)); CK(ctx->idSigma.ensure(ctx->sigmaByType ? 1 : N));
         CK(cudaMemcpyAsync(ctx->idMass.p, ctx->mass.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->idType.p, ctx->type.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -2185,6 +2185,8 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         if ((st = collect_profile(ctx))) return st;
         if ((st = read_scalars(ctx))) return st;
         if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
+        if (ctx->hsc->overflow & 8)
+            return fail(ctx, FEMMD_TIMEOUT, "a step block's copy to shared memory did not complete in time");
         if (!ctx->hsc->overflow && !aborted) {
             traj_commit(ctx->traj);
             ctx->steps += steps;
@@ -2238,6 +2240,8 @@ femmd_status femmd_do_step(femmd_ctx *ctx) {
     if ((st = read_scalars(ctx))) return st;
     ctx->steps++;
     ctx->staleMask |= kPos | kVel | kAcc | kForce;
+    if (ctx->hsc->overflow & 8)
+        return fail(ctx, FEMMD_TIMEOUT, "a step block's copy to shared memory did not complete in time");
     if (ctx->hsc->overflow) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "neighbour list overflow in do_step; run() grows it");
     if (ctx->hsc->nonfinite) return fail(ctx, FEMMD_NONFINITE, "a force became NaN or infinite");
     return FEMMD_OK;
@@ -2280,8 +2284,11 @@ femmd_status femmd_calc_forces(femmd_ctx *ctx) {
     CK(cudaMemsetAsync(&ctx->sc.p->nonfinite, 0, sizeof(int), ctx->stream));
     ctx->hsc->stepNow = ctx->steps;
     CK(cudaMemcpyAsync(&ctx->sc.p->stepNow, &ctx->hsc->stepNow, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(&ctx->sc.p->overflow, 0, sizeof(int), ctx->stream));
     CK(enqueue_step(L, s, MODE_FORCES, ctx->cur, 0, 0));
     if ((st = read_scalars(ctx))) return st;
+    if (ctx->hsc->overflow & 8)
+        return fail(ctx, FEMMD_TIMEOUT, "a step block's copy to shared memory did not complete in time");
     ctx->staleMask |= kForce | kEnergy;
     if (s.areaUnits > 0) ctx->staleMask |= kPos;  // the area springs moved the vertices
     ctx->forcesValid = true;
@@ -2472,19 +2479,18 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     const int N = (int)ctx->pos.size();
     std::vector<int> cnt(N);
     std::vector<int> raw((size_t)ctx->nbrCap * ctx->Ncap);
-    std::vector<int> perm, slot, cellIds;
-    std::vector<int4> bw;
+    std::vector<int> perm, slot, cellIds, bw;
     if (N) {
         CK(cudaMemcpyAsync(cnt.data(), ctx->nbrCount.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(raw.data(), ctx->nbr.p, raw.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         if (fast_mode(ctx)) {
             perm.resize(N);
             cellIds.resize(N);
-            bw.resize(4 * (size_t)((N + kFastBlock - 1) / kFastBlock));
+            bw.resize(kWinInts * (size_t)((N + kFastBlock - 1) / kFastBlock));
             CK(cudaMemcpyAsync(perm.data(), ctx->perm.p, N * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(cellIds.data(), ctx->sortedIds.p, N * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
-            CK(cudaMemcpyAsync(bw.data(), ctx->blockWin.p, bw.size() * sizeof(int4), cudaMemcpyDeviceToHost,
+            CK(cudaMemcpyAsync(bw.data(), ctx->blockWin.p, bw.size() * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
         }
         CK(cudaStreamSynchronize(ctx->stream));
@@ -2498,14 +2504,12 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     // fast mode: entry q of the particle at storage slot r, as a storage slot
     // (a windowed block's entry is an index into its window's cell slots)
     auto fast_entry = [&](int r, int q) -> int {
-        const int4 *b = &bw[4 * (size_t)(r / kFastBlock)];
+        const int *b = &bw[kWinInts * (size_t)(r / kFastBlock)];
         const int w = raw[nbr_at(q, r, ctx->Ncap)];
-        if (b[0].x < 0) return w & kIdMask;
-        const int st[6] = {b[0].y, b[0].z, b[0].w, b[1].x, b[1].y, b[1].z};
-        const int off[7] = {b[1].w, b[2].x, b[2].y, b[2].z, b[2].w, b[3].x, b[3].y};
-        int p = 0;
-        while (p < 5 && w >= off[p + 1]) p++;
-        return cellIds[st[p] + (w - off[p])];
+        if (b[0] < 0) return w & kIdMask;
+        for (int p = 0; p < 6; p++)
+            if (w >= b[7 + p] && w < b[7 + p] + b[13 + p]) return cellIds[b[1 + p] + (w - b[7 + p])];
+        return -1;  // not an entry of the window: a mismatch the set comparison exposes
     };
     long long k = 0;
     for (int i = 0; i < N; i++) {
@@ -2513,7 +2517,14 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
         const int r = perm.empty() ? i : slot[i];
         int c = std::min(cnt[r], ctx->nbrCap);
         for (int q = 0; q < c; q++) {
-            if (nbr_list) nbr_list[k] = perm.empty() ? raw[nbr_at(q, r, ctx->Ncap)] & kIdMask : perm[fast_entry(r, q)];
+            if (nbr_list) {
+                if (perm.empty()) {
+                    nbr_list[k] = raw[nbr_at(q, r, ctx->Ncap)] & kIdMask;
+                } else {
+                    const int e = fast_entry(r, q);
+                    nbr_list[k] = e >= 0 ? perm[e] : -1;
+                }
+            }
             k++;
         }
     }

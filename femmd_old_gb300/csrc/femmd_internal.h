@@ -158,15 +158,18 @@ struct DevSys {
     // particles inside one cell column stages the positions of its stencil
     // window (up to six cell-slot ranges: per stencil column the rows around
     // the block, and the row across the y edge) in shared memory, and its
-    // lists hold window indices instead of storage slots.  blockWin[4b..4b+3]
-    // = {len, start[6], off[7], groups, -} (len < 0: the block reads global
-    // slots; groups: list groups of the block's longest list).
+    // lists hold window indices instead of storage slots.  blockWin holds
+    // kWinInts ints per block: {len, start[6], off[6], count[6], groups, -}:
+    // piece p's cell slots start[p] .. start[p] + count[p] - 1 sit at window
+    // entries off[p] ..; len is the ghost's entry (len < 0: the block reads
+    // global slots); groups: 16-byte list groups of the block's longest list.
     int *newCell;   // cell of the particle at each storage slot
-    int4 *blockWin;
+    int *blockWin;
 };
 
 constexpr int kFastBlock = 128;  // storage slots per block of the fast step kernel
-constexpr int kWinMax = 1024;    // window entries per block (the last one the ghost)
+constexpr int kWinMax = 768;     // window entries per block (the ghost included)
+constexpr int kWinInts = 24;     // ints of window data per block
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

@@ -146,58 +146,68 @@ __global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int 
 // wraps), the cell-slot range of rows r0 - 1 .. r1 + 1 inside the grid (piece
 // 2d) and, where the block touches a y edge, the row across it (piece 2d + 1).
 // Every candidate the list build walks for the block's particles lies in one
-// of these pieces, so a list entry is the candidate's offset in the
-// concatenated pieces.  Other blocks (bonded particles, blocks across two
-// columns, windows too large, grids the fast walk does not cover) keep global
-// storage slots.  The block's longest list (in groups) is gathered by the
-// list build into blockWin[4b+3].z.
+// of these pieces, so a list entry is the candidate's index in the block's
+// window.  A piece starting at cell slot a takes window entries from an even
+// base, with a & 1 entries before it and its end padded to an even count, so
+// that its positions can be copied straight from the storage array in
+// 16-byte units when cell slots and storage slots coincide.  Other blocks
+// (bonded particles, blocks across two columns, windows too large, grids the
+// fast walk does not cover) keep global storage slots.  The block's longest
+// list (in groups) is gathered by the list build.
 __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int nblk = (s.N + kFastBlock - 1) / kFastBlock;
     if (b >= nblk) return;
-    int4 *out = s.blockWin + 4 * (size_t)b;
+    int *out = s.blockWin + kWinInts * (size_t)b;
     const int f = b * kFastBlock, l = min(f + kFastBlock, s.N) - 1;
     const int ncy = s.ncy, ncx = s.ncx;
     bool ok = f >= s.nBonded && fast_walk_ok(s) && ncy >= 3;
-    int st[6] = {0, 0, 0, 0, 0, 0}, off[7] = {0, 0, 0, 0, 0, 0, 0};
+    int st[6] = {0, 0, 0, 0, 0, 0}, off[6] = {0, 0, 0, 0, 0, 0}, cnt[6] = {0, 0, 0, 0, 0, 0};
+    int acc = 0;
     if (ok) {
         const int cf = s.newCell[f], cl = s.newCell[l];
         const int ix = cf / ncy, r0 = cf - ix * ncy, r1 = cl - ix * ncy;
         ok = cl / ncy == ix && !(r0 == 0 && r1 == ncy - 1);
         if (ok) {
             const int lo = max(r0 - 1, 0), hi = min(r1 + 1, ncy - 1);
-            int acc = 0;
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 int nx = ix + d - 1;
                 if (nx < 0) nx = ncx - 1;
                 else if (nx == ncx) nx = 0;
                 const int col = nx * ncy;
-                const int a = s.cellStart[col + lo], e = s.cellStart[col + hi + 1];
-                st[2 * d] = a;
-                off[2 * d] = acc;
-                acc += e - a;
-                int wa = 0, we = 0;
+                int a[2], e[2];
+                a[0] = s.cellStart[col + lo];
+                e[0] = s.cellStart[col + hi + 1];
+                a[1] = e[1] = 0;
                 if (r0 == 0) {
-                    wa = s.cellStart[col + ncy - 1];
-                    we = s.cellStart[col + ncy];
+                    a[1] = s.cellStart[col + ncy - 1];
+                    e[1] = s.cellStart[col + ncy];
                 } else if (r1 == ncy - 1) {
-                    wa = s.cellStart[col];
-                    we = s.cellStart[col + 1];
+                    a[1] = s.cellStart[col];
+                    e[1] = s.cellStart[col + 1];
                 }
-                st[2 * d + 1] = wa;
-                off[2 * d + 1] = acc;
-                acc += we - wa;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int p = 2 * d + h;
+                    st[p] = a[h];
+                    cnt[p] = e[h] - a[h];
+                    off[p] = acc + (a[h] & 1);
+                    if (cnt[p] > 0) acc += ((e[h] + 1) & ~1) - (a[h] & ~1);
+                }
             }
-            off[6] = acc;
             ok = acc + 1 <= kWinMax;
         }
     }
-    out[0] = make_int4(ok ? off[6] : -1, st[0], st[1], st[2]);
-    out[1] = make_int4(st[3], st[4], st[5], off[0]);
-    out[2] = make_int4(off[1], off[2], off[3], off[4]);
-    out[3] = make_int4(off[5], off[6], 0, 0);
+    out[0] = ok ? acc : -1;
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+        out[1 + p] = st[p];
+        out[7 + p] = off[p];
+        out[13 + p] = cnt[p];
+    }
+    out[19] = 0;
 }
 
 // The list build of the fast mode.  One thread per cell slot t builds the
@@ -283,16 +293,13 @@ struct WinDelta {
 
 __device__ __forceinline__ WinDelta win_delta(const DevSys &s, int slot) {
     WinDelta w;
-    const int4 *bw = s.blockWin + 4 * (size_t)(slot / kFastBlock);
-    const int4 a = bw[0], b = bw[1], c = bw[2], d = bw[3];
-    const int st[6] = {a.y, a.z, a.w, b.x, b.y, b.z};
-    const int off[6] = {b.w, c.x, c.y, c.z, c.w, d.x};
-    w.win = a.x >= 0;
-    w.len = a.x;
+    const int *bw = s.blockWin + kWinInts * (size_t)(slot / kFastBlock);
+    w.len = bw[0];
+    w.win = w.len >= 0;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        w.dm[q] = off[2 * q] - st[2 * q];
-        w.dw[q] = off[2 * q + 1] - st[2 * q + 1];
+        w.dm[q] = bw[7 + 2 * q] - bw[1 + 2 * q];
+        w.dw[q] = bw[8 + 2 * q] - bw[2 + 2 * q];
     }
     return w;
 }
@@ -498,7 +505,7 @@ __global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int che
     }
     if (valid) {
         s.nbrCount[ns] = k;
-        if (wd.win) atomicMax(&s.blockWin[4 * (size_t)(ns / kFastBlock) + 3].z, ng);
+
         if (ns >= s.nBonded) {
             const int id = s.sPerm[ns];
             pos[ns] = s.sPos[ns];
@@ -511,6 +518,13 @@ __global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int che
             if (s.wallDelta) const_cast<float *>(s.wallDelta)[ns] = __ldg(s.idWallDelta + id);
             if (s.wallSig) const_cast<float *>(s.wallSig)[ns] = __ldg(s.idWallSig + id);
         }
+    }
+    {
+        // the longest list of each step block, one atomic per block a warp touches
+        const int blk = valid ? ns / kFastBlock : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, blk);
+        const int gm = __reduce_max_sync(peers, ng);
+        if (valid && lane == __ffs(peers) - 1) atomicMax(&s.blockWin[kWinInts * (size_t)blk + 19], gm);
     }
     const int kmax = __reduce_max_sync(0xffffffffu, valid ? k : 0);
     const int ksum = __reduce_add_sync(0xffffffffu, valid ? k : 0);
@@ -606,29 +620,42 @@ __device__ __forceinline__ void fpair(const DevSys &s, const PairEntry *tab, con
     }
 }
 
-// Lennard-Jones forces of particle i over its list (cnt entries; its first
-// two 16-byte groups g0, g1 loaded by the caller; the group two ahead in
-// flight while the current one is worked).  WIN: the entries index the
-// block's staged window (wpos, wtyp, wsig); otherwise they are storage slots
-// gathered from pin.  Unused words of the last group name the ghost, so no
-// entry needs a count test.  Energy and virial come back doubled (per
-// ordered pair), as the reference-exact kernel's.
+// Lennard-Jones forces of particle i over its list (cnt entries).  The
+// list's 16-byte groups come from the block's shared copy (slist, one row of
+// kFastBlock groups per group index) or, without one, from global memory with
+// the group two ahead in flight.  WIN: the entries index the block's staged
+// window (wpos, wtyp, wsig); otherwise they are storage slots gathered from
+// pin.  Unused words of the last group name the ghost, so no entry needs a
+// count test.  Energy and virial come back doubled (per ordered pair), as
+// the reference-exact kernel's.
 template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG, bool WIN>
-__device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt, int4 g0,
-                                           int4 g1, const float2 *__restrict__ pin, const float2 *wpos,
+__device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt,
+                                           const int4 *slist, const float2 *__restrict__ pin, const float2 *wpos,
                                            const int *wtyp, const float *wsig, float &fx, float &fy, float &ue2,
                                            float &we2) {
     const int ng = (cnt + 3) >> 2;
     const size_t row = (size_t)s.Ncap;
-    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i + 2 * row;
+    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
     const int ti = MT ? s.typeId[i] : 0;
     const float si = SG ? s.sigma[i] : 0.0f;
     const PairEntry pe0 = tab[0];
     float A = 0.0f, B = 0.0f, n = 0.0f, u2 = 0.0f, w2 = 0.0f;
+    const int4 zero4 = make_int4(0, 0, 0, 0);
+    int4 g1 = zero4, g2 = zero4;
+    if (!slist) {
+        g1 = ng > 0 ? __ldg(lst) : zero4;
+        g2 = ng > 1 ? __ldg(lst + row) : zero4;
+    }
 #pragma unroll 1
     for (int gi = 0; gi < ng; gi++) {
-        const int4 g2 = gi + 2 < ng ? __ldg(lst) : make_int4(0, 0, 0, 0);
-        lst += row;
+        int4 g0;
+        if (slist) {
+            g0 = slist[gi * kFastBlock + threadIdx.x];
+        } else {
+            g0 = g1;
+            g1 = g2;
+            g2 = gi + 2 < ng ? __ldg(lst + (gi + 2) * row) : zero4;
+        }
         int e[4] = {g0.x, g0.y, g0.z, g0.w};
         float2 q[4];
         int tj[4] = {0, 0, 0, 0};
@@ -638,7 +665,7 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
             if (WIN) {
                 // masked to the window: a stray entry can name a wrong
                 // window slot but never one outside the shared arrays
-                e[u] &= kWinMax - 1;
+                e[u] = min((unsigned)e[u], (unsigned)(kWinMax - 1));
                 q[u] = wpos[e[u]];
                 if (MT) tj[u] = wtyp[e[u]];
                 if (SG) sj[u] = wsig[e[u]];
@@ -653,8 +680,6 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
         for (int u = 0; u < 4; u++)
             fpair<MT, SG, SIG1, WX, WY, IMG>(s, tab, pe0, ti, si, pi, q[u].x, q[u].y, tj[u], sj[u], fx, fy, A, B, n,
                                              u2, w2);
-        g0 = g1;
-        g1 = g2;
     }
     if (MT || SG) {
         ue2 += u2;
@@ -736,34 +761,110 @@ __device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, fl
     we_out += we;
 }
 
+// ---- asynchronous bulk copies global -> shared (the untiled TMA form) on an
+// mbarrier.  Both addresses and the size are multiples of 16 bytes.
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// A wait that gives up: false after 'limit' polls (each of which may itself
+// block for a short, hardware-bounded time).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, int limit) {
+    for (int k = 0; k < limit; k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+constexpr int kWaitLimit = 1 << 22;  // polls before a step block reports a stuck copy
+constexpr int kFlagTimeout = 8;      // DevScalars::overflow bit: a bounded wait expired
+
 // Resident blocks per SM the register allocation must allow (kFastBlock
 // threads each).
 #ifndef FEMMD_FAST_MINB
-#define FEMMD_FAST_MINB 10
+#define FEMMD_FAST_MINB 8
 #endif
 constexpr int kFastMinBlocks = FEMMD_FAST_MINB;
 
+// The step kernel of the fast mode, one thread per storage slot.  One thread
+// of each block starts asynchronous bulk copies of the block's list groups
+// (rows > 0: 'rows' rows of kFastBlock groups reserved in shared memory) and,
+// for a windowed block of one particle kind whose cell slots are storage
+// slots, of its window pieces; the other threads meanwhile load their own
+// particle and, where the window was not copied, gather it.  The pair loop
+// then reads shared memory only.
 template <bool MT, bool SG, bool SIG1, bool WX, bool WY>
 __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, int mode, int parity,
-                                                                     cudaGraphConditionalHandle h, int use_h) {
+                                                                     cudaGraphConditionalHandle h, int use_h,
+                                                                     int rows) {
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
     extern __shared__ float4 smem_f4[];
     const int nt = s.numTypes;
     const int ntab = MT ? nt * nt : 1;
-    PairEntry *tab = reinterpret_cast<PairEntry *>(smem_f4);
-    float2 *wpos = reinterpret_cast<float2 *>(tab + ntab);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_f4);
+    PairEntry *tab = reinterpret_cast<PairEntry *>(smem_f4 + 1);
+    int4 *slist = reinterpret_cast<int4 *>(tab + ntab);
+    float2 *wpos = reinterpret_cast<float2 *>(slist + (size_t)rows * kFastBlock);
     int *wtyp = reinterpret_cast<int *>(wpos + kWinMax);
     float *wsig = reinterpret_cast<float *>(wtyp + (MT ? kWinMax : 0));
-    // the particle's own data and its first two list groups, issued first so
-    // that their latency overlaps the staging of the window
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int *bw = s.blockWin + kWinInts * (size_t)blockIdx.x;
+    const int len = bw[0];
+    const int b0 = blockIdx.x * kFastBlock;
+    const bool tmaWin = !MT && !SG && len >= 0 && s.nBonded == 0;
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int G = rows > 0 ? min(bw[19], rows) : 0;
+        const unsigned rowBytes = (unsigned)min(kFastBlock, s.Ncap - b0) * 16u;
+        unsigned total = (unsigned)G * rowBytes;
+        if (tmaWin)
+            for (int p = 0; p < 6; p++) {
+                const int a = bw[1 + p], c = bw[13 + p];
+                if (c > 0) total += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
+            }
+        mbar_expect_tx(bar, total);
+        const int4 *lsrc = reinterpret_cast<const int4 *>(s.nbr) + b0;
+        for (int g = 0; g < G; g++) bulk_copy_g2s(slist + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, bar);
+        if (tmaWin)
+            for (int p = 0; p < 6; p++) {
+                const int a = bw[1 + p], c = bw[13 + p];
+                if (c > 0) {
+                    const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
+                    bulk_copy_g2s(wpos + bw[7 + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u, bar);
+                }
+            }
+    }
+    // the particle's own data meanwhile
+    const int i = b0 + threadIdx.x;
     const bool act = i < s.N;
     const int ic = act ? i : 0;
     const float2 pi = pin[ic];
     const int cnt = act ? min(s.nbrCount[ic], s.nbrCap) : 0;
-    const int4 *lst0 = reinterpret_cast<const int4 *>(s.nbr) + ic;
-    const int4 g0 = __ldg(lst0), g1 = __ldg(lst0 + s.Ncap);
     const float m = s.mass[ic];
     const float2 v = (mode != MODE_FORCES && mode != MODE_INIT) ? s.vel[ic] : make_float2(0.0f, 0.0f);
     if (MT) {
@@ -775,22 +876,17 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
         const int row = s.sc->obsRow;
         if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
     }
-    // the block's window: the current positions (types, sigmas) of the cell
-    // slots of its pieces, and the ghost after them
-    const int4 *bw = s.blockWin + 4 * (size_t)blockIdx.x;
-    const int len = bw[0].x;
     if (len >= 0) {
-        const int4 a = bw[0], b = bw[1], c = bw[2], d = bw[3];
-        const int st[6] = {a.y, a.z, a.w, b.x, b.y, b.z};
-        const int off[7] = {b.w, c.x, c.y, c.z, c.w, d.x, d.y};
-#pragma unroll
-        for (int p = 0; p < 6; p++) {
-            const int n = off[p + 1] - off[p];
-            for (int w = threadIdx.x; w < n; w += kFastBlock) {
-                const int j = __ldg(s.sortedIds + st[p] + w);
-                wpos[off[p] + w] = __ldg(pin + j);
-                if (MT) wtyp[off[p] + w] = s.typeId[j];
-                if (SG) wsig[off[p] + w] = s.sigma[j];
+        if (!tmaWin) {
+            // the window gathered: cell slots are not storage slots
+            for (int p = 0; p < 6; p++) {
+                const int st = bw[1 + p], off = bw[7 + p], c = bw[13 + p];
+                for (int w = threadIdx.x; w < c; w += kFastBlock) {
+                    const int j = __ldg(s.sortedIds + st + w);
+                    wpos[off + w] = __ldg(pin + j);
+                    if (MT) wtyp[off + w] = s.typeId[j];
+                    if (SG) wsig[off + w] = s.sigma[j];
+                }
             }
         }
         if (threadIdx.x == 0) {
@@ -800,6 +896,13 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
         }
     }
     __syncthreads();
+    bool ok = mbar_wait_bounded(bar, 0, kWaitLimit);
+    if (!ok) {
+        // a copy that never completed: report it, give the copies in flight
+        // one more bounded wait before the block leaves, skip the pair terms
+        atomicOr(&s.sc->overflow, kFlagTimeout);
+        mbar_wait_bounded(bar, 0, kWaitLimit);
+    }
     float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
     bool bad = false;
     float fx = 0.0f, fy = 0.0f, ue2 = 0.0f, we2 = 0.0f, utri = 0.0f, uwall = 0.0f;
@@ -807,34 +910,49 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
     const float D = s.imgD;
     const bool near = act && ((WX && (pi.x < D || pi.x > s.Lx - D)) || (WY && (pi.y < D || pi.y > s.Ly - D)));
     const bool img = __any_sync(0xffffffffu, near);
-    if (act) {
+    const int4 *sl = rows > 0 ? slist : nullptr;
+    if (act && ok) {
         if (len >= 0) {
             if (img)
-                fast_pairs<MT, SG, SIG1, WX, WY, true, true>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
-                                                             fy, ue2, we2);
+                fast_pairs<MT, SG, SIG1, WX, WY, true, true>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                                                             ue2, we2);
             else
-                fast_pairs<MT, SG, SIG1, WX, WY, false, true>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
-                                                              fy, ue2, we2);
+                fast_pairs<MT, SG, SIG1, WX, WY, false, true>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                                                              ue2, we2);
         } else {
             if (img)
-                fast_pairs<MT, SG, SIG1, WX, WY, true, false>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig, fx,
-                                                              fy, ue2, we2);
+                fast_pairs<MT, SG, SIG1, WX, WY, true, false>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                                                              ue2, we2);
             else
-                fast_pairs<MT, SG, SIG1, WX, WY, false, false>(s, tab, i, pi, cnt, g0, g1, pin, wpos, wtyp, wsig,
-                                                               fx, fy, ue2, we2);
+                fast_pairs<MT, SG, SIG1, WX, WY, false, false>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx,
+                                                               fy, ue2, we2);
         }
-        fast_finish<WX, WY>(s, i, mode, pi, m, v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke, vvm, bad);
     }
+    if (act) fast_finish<WX, WY>(s, i, mode, pi, m, v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke, vvm, bad);
     step_reduce<kFastBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
 }
+
+// Shared memory of a step block: the mbarrier, the pair table, 'rows' rows
+// of list groups, the window (positions; types and sigmas where needed).
+static size_t fstep_smem(const DevSys &s, bool mt, bool sg, int rows) {
+    return 16 + sizeof(PairEntry) * (size_t)(mt ? s.numTypes * s.numTypes : 1) +
+           (size_t)rows * kFastBlock * sizeof(int4) +
+           (size_t)kWinMax * (sizeof(float2) + (mt ? sizeof(int) : 0) + (sg ? sizeof(float) : 0));
+}
+
+constexpr size_t kFastSmemMax = 200 * 1024;  // the list rows stay in global memory beyond this
 
 template <bool MT, bool SG, bool SIG1, bool WX, bool WY>
 static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                                 int use_h) {
     const dim3 g((s.N + kFastBlock - 1) / kFastBlock), b(kFastBlock);
-    const size_t smt = sizeof(PairEntry) * (size_t)(MT ? s.numTypes * s.numTypes : 1) +
-                       (size_t)kWinMax * (sizeof(float2) + (MT ? sizeof(int) : 0) + (SG ? sizeof(float) : 0));
-    return L.kernel(k_fstep<MT, SG, SIG1, WX, WY>, g, b, smt, s, mode, parity, h, use_h);
+    int rows = s.nbrCap / 4;
+    if (fstep_smem(s, MT, SG, rows) > kFastSmemMax) rows = 0;
+    const size_t smem = fstep_smem(s, MT, SG, rows);
+    cudaError_t e = cudaFuncSetAttribute(k_fstep<MT, SG, SIG1, WX, WY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e) return e;
+    return L.kernel(k_fstep<MT, SG, SIG1, WX, WY>, g, b, smem, s, mode, parity, h, use_h, rows);
 }
 
 template <bool MT, bool SG, bool SIG1>
