@@ -161,14 +161,16 @@ struct DevSys {
     // lists hold window indices instead of storage slots.  blockWin holds
     // kWinInts ints per block: {len, start[6], off[6], count[6], groups, -}:
     // piece p's cell slots start[p] .. start[p] + count[p] - 1 sit at window
-    // entries off[p] ..; len is the ghost's entry (len < 0: the block reads
-    // global slots); groups: 16-byte list groups of the block's longest list.
+    // entries off[p] ..; len: the entries the pieces span (len < 0: the
+    // block reads global slots); groups: 16-byte list groups of the block's
+    // longest list.  The window's last entry, kWinGhost, is the ghost's.
     int *newCell;   // cell of the particle at each storage slot
     int *blockWin;
 };
 
 constexpr int kFastBlock = 128;  // storage slots per block of the fast step kernel
 constexpr int kWinMax = 768;     // window entries per block (the ghost included)
+constexpr int kWinGhost = kWinMax - 1;  // the window entry of the ghost slot
 constexpr int kWinInts = 24;     // ints of window data per block
 
 __device__ __forceinline__ unsigned long long global_ns() {

@@ -32,6 +32,7 @@
 // (nn.cpp:8-62), NeighborList::update (nn.cpp:114-134), the leapfrog of
 // Integrator::doStep (integrator.cpp:8-29, 100-135).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "femmd_internal.h"
 #include "launch.h"
 #include "device_common.cuh"
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
                     if (cnt[p] > 0) acc += ((e[h] + 1) & ~1) - (a[h] & ~1);
                 }
             }
-            ok = acc + 1 <= kWinMax;
+            ok = acc <= kWinMax - 1;  // the last entry is the ghost's
         }
     }
     out[0] = ok ? acc : -1;
@@ -484,7 +485,7 @@ __global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int che
     }
     // the stage to the list: group g of every lane in one store per g; the
     // unused words of the last group name the ghost
-    const int ghost = wd.win ? wd.len : s.N;
+    const int ghost = wd.win ? kWinGhost : s.N;
     const int kk = valid ? min(k, cap) : 0;
     const int ng = (kk + 3) >> 2;
     const int ngs = min(ng, kLStage / 4);
@@ -621,16 +622,18 @@ __device__ __forceinline__ void fpair(const DevSys &s, const PairEntry *tab, con
 }
 
 // Lennard-Jones forces of particle i over its list (cnt entries).  The
-// list's 16-byte groups come from the block's shared copy (slist, one row of
-// kFastBlock groups per group index) or, without one, from global memory with
-// the group two ahead in flight.  WIN: the entries index the block's staged
+// list's 16-byte groups come from the block's shared copy (slist: its first
+// srows groups, one row of kFastBlock groups per group index; the rest from
+// global memory) or, with srows = 0, from global memory with the group two
+// ahead in flight.  WIN: the entries index the block's staged
 // window (wpos, wtyp, wsig); otherwise they are storage slots gathered from
 // pin.  Unused words of the last group name the ghost, so no entry needs a
 // count test.  Energy and virial come back doubled (per ordered pair), as
 // the reference-exact kernel's.
 template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG, bool WIN>
 __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt,
-                                           const int4 *slist, const float2 *__restrict__ pin, const float2 *wpos,
+                                           const int4 *slist, int srows, const float2 *__restrict__ pin,
+                                           const float2 *wpos,
                                            const int *wtyp, const float *wsig, float &fx, float &fy, float &ue2,
                                            float &we2) {
     const int ng = (cnt + 3) >> 2;
@@ -642,15 +645,15 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
     float A = 0.0f, B = 0.0f, n = 0.0f, u2 = 0.0f, w2 = 0.0f;
     const int4 zero4 = make_int4(0, 0, 0, 0);
     int4 g1 = zero4, g2 = zero4;
-    if (!slist) {
+    if (srows == 0) {
         g1 = ng > 0 ? __ldg(lst) : zero4;
         g2 = ng > 1 ? __ldg(lst + row) : zero4;
     }
 #pragma unroll 1
     for (int gi = 0; gi < ng; gi++) {
         int4 g0;
-        if (slist) {
-            g0 = slist[gi * kFastBlock + threadIdx.x];
+        if (srows > 0) {
+            g0 = gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
         } else {
             g0 = g1;
             g1 = g2;
@@ -688,6 +691,59 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
         ue2 += __fmaf_rn(pe0.eps4, A - B, pe0.us * n);
         we2 += pe0.eps48 * __fmaf_rn(-0.5f, B, A);
     }
+}
+
+// The pair loop of the persistent kernel for a warp with no image work (one
+// particle type): the four pairs of a list group are worked two at a time in
+// packed float2 arithmetic (lane x of every float2 is one pair, lane y the
+// other), the x and y differences in separate float2s.  The pairs inside
+// the cutoff are counted as sum ir2 r2 (each term 1 to within the
+// reciprocal's rounding, 0 outside the cutoff), the energy shift's weight.
+template <bool SIG1, bool WIN>
+__device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &pe, int i, float2 pi, int cnt,
+                                              const int4 *slist, int srows, const float2 *__restrict__ pin,
+                                              const float2 *wpos, float &fx, float &fy, float &ue2, float &we2) {
+    const int ng = (cnt + 3) >> 2;
+    const size_t row = (size_t)s.Ncap;
+    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
+    const float rc2 = pe.rcut2;
+    const float2 cv = make_float2(pe.c, pe.c), hcv = make_float2(-0.5f * pe.c, -0.5f * pe.c);
+    const float2 sv = make_float2(pe.sig2, pe.sig2), m1 = make_float2(-1.0f, -1.0f);
+    const float2 xv = make_float2(pi.x, pi.x), yv = make_float2(pi.y, pi.y);
+    const float2 z = make_float2(0.0f, 0.0f);
+    float2 FX = z, FY = z, Av = z, Bv = z, Nv = z;
+#pragma unroll 1
+    for (int gi = 0; gi < ng; gi++) {
+        const int4 g =
+            gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
+        const int e[4] = {g.x, g.y, g.z, g.w};
+        float2 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            q[u] = WIN ? wpos[min((unsigned)e[u], (unsigned)kWinGhost)] : __ldg(pin + e[u]);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 qa = q[2 * h], qb = q[2 * h + 1];
+            const float2 dx = __ffma2_rn(make_float2(qa.x, qb.x), m1, xv);
+            const float2 dy = __ffma2_rn(make_float2(qa.y, qb.y), m1, yv);
+            const float2 r2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+            float2 ir2 = make_float2(r2.x < rc2 ? rcp_approx(r2.x) : 0.0f, r2.y < rc2 ? rcp_approx(r2.y) : 0.0f);
+            if (!SIG1) ir2 = __fmul2_rn(ir2, sv);
+            const float2 ir4 = __fmul2_rn(ir2, ir2), ir6 = __fmul2_rn(ir4, ir2), ir8 = __fmul2_rn(ir4, ir4);
+            const float2 fc = __fmul2_rn(ir8, __ffma2_rn(cv, ir6, hcv));
+            FX = __ffma2_rn(fc, dx, FX);
+            FY = __ffma2_rn(fc, dy, FY);
+            Av = __ffma2_rn(ir6, ir6, Av);
+            Bv = __fadd2_rn(Bv, ir6);
+            Nv = __ffma2_rn(ir2, r2, Nv);
+        }
+    }
+    fx += FX.x + FX.y;
+    fy += FY.x + FY.y;
+    const float A = Av.x + Av.y, B = Bv.x + Bv.y;
+    const float n = SIG1 ? Nv.x + Nv.y : (Nv.x + Nv.y) / pe.sig2;
+    ue2 += __fmaf_rn(pe.eps4, A - B, pe.us * n);
+    we2 += pe.eps48 * __fmaf_rn(-0.5f, B, A);
 }
 
 // x wrapped into [0, L): one box length added or taken away, the reference's
@@ -890,9 +946,9 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
             }
         }
         if (threadIdx.x == 0) {
-            wpos[len] = __ldg(pin + s.N);  // the ghost slot's far position
-            if (MT) wtyp[len] = 0;
-            if (SG) wsig[len] = 1.0f;
+            wpos[kWinGhost] = __ldg(pin + s.N);  // the ghost slot's far position
+            if (MT) wtyp[kWinGhost] = 0;
+            if (SG) wsig[kWinGhost] = 1.0f;
         }
     }
     __syncthreads();
@@ -910,21 +966,21 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
     const float D = s.imgD;
     const bool near = act && ((WX && (pi.x < D || pi.x > s.Lx - D)) || (WY && (pi.y < D || pi.y > s.Ly - D)));
     const bool img = __any_sync(0xffffffffu, near);
-    const int4 *sl = rows > 0 ? slist : nullptr;
+    const int srows = rows > 0 ? rows : 0;
     if (act && ok) {
         if (len >= 0) {
             if (img)
-                fast_pairs<MT, SG, SIG1, WX, WY, true, true>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                fast_pairs<MT, SG, SIG1, WX, WY, true, true>(s, tab, i, pi, cnt, slist, srows, pin, wpos, wtyp, wsig, fx, fy,
                                                              ue2, we2);
             else
-                fast_pairs<MT, SG, SIG1, WX, WY, false, true>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                fast_pairs<MT, SG, SIG1, WX, WY, false, true>(s, tab, i, pi, cnt, slist, srows, pin, wpos, wtyp, wsig, fx, fy,
                                                               ue2, we2);
         } else {
             if (img)
-                fast_pairs<MT, SG, SIG1, WX, WY, true, false>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx, fy,
+                fast_pairs<MT, SG, SIG1, WX, WY, true, false>(s, tab, i, pi, cnt, slist, srows, pin, wpos, wtyp, wsig, fx, fy,
                                                               ue2, we2);
             else
-                fast_pairs<MT, SG, SIG1, WX, WY, false, false>(s, tab, i, pi, cnt, sl, pin, wpos, wtyp, wsig, fx,
+                fast_pairs<MT, SG, SIG1, WX, WY, false, false>(s, tab, i, pi, cnt, slist, srows, pin, wpos, wtyp, wsig, fx,
                                                                fy, ue2, we2);
         }
     }
@@ -955,6 +1011,225 @@ static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity
     return L.kernel(k_fstep<MT, SG, SIG1, WX, WY>, g, b, smem, s, mode, parity, h, use_h, rows);
 }
 
+// ---- the persistent step kernel (one particle kind, no bonded particles).
+// Each block holds kFastBlock consumer threads and one producer warp and
+// works the tiles (step blocks of kFastBlock storage slots) blockIdx.x,
+// blockIdx.x + gridDim.x, ... through two shared-memory stages.  The
+// producer's lane 0 copies a tile's list rows and window pieces into a stage
+// with asynchronous bulk copies while the consumers work the other stage;
+// 'full' barriers carry the copied bytes to the consumers, 'empty' barriers
+// (one arrival per consumer warp) hand a stage back.  The consumers load
+// their next tile's own particle data while they work the current one, and
+// the energies, the largest speed and the finiteness flag are reduced once
+// per block.  Every wait is bounded: a wait that gives up sets kFlagTimeout,
+// the consumers skip the pair terms from then on, and the producer issues no
+// further copy and waits (bounded) for those in flight before it leaves.
+constexpr int kPBlock = kFastBlock + 32;  // consumer threads + the producer warp
+constexpr int kPRows = 8;                 // list rows staged per tile (the rest read from global memory)
+#ifndef FEMMD_FAST_PMINB
+#define FEMMD_FAST_PMINB 5
+#endif
+constexpr int kPMinBlocks = FEMMD_FAST_PMINB;
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Shared memory of a persistent block: full[2], empty[2], the pair table
+// entry, then per stage 'rows' list rows and the window.
+__host__ __device__ constexpr size_t pstage_bytes(int rows) {
+    return (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2);
+}
+__host__ __device__ constexpr size_t pstage_base() { return 32 + sizeof(PairEntry); }
+static size_t pstep_smem(int rows) { return pstage_base() + 2 * pstage_bytes(rows); }
+
+// A consumer's own particle data of one tile, loaded a tile ahead.
+struct PTile {
+    float2 p, v;
+    float m;
+    int cnt, len;
+};
+
+__device__ __forceinline__ PTile ptile_load(const DevSys &s, const float2 *__restrict__ pin, int t, int mode) {
+    PTile r;
+    const int i = t * kFastBlock + (int)threadIdx.x;
+    const bool act = i < s.N;
+    const int ic = act ? i : 0;
+    r.p = __ldg(pin + ic);
+    r.cnt = act ? min(__ldg(s.nbrCount + ic), s.nbrCap) : 0;
+    r.m = __ldg(s.mass + ic);
+    r.v = (mode != MODE_FORCES && mode != MODE_INIT) ? s.vel[ic] : make_float2(0.0f, 0.0f);
+    r.len = __ldg(s.blockWin + kWinInts * (size_t)t);
+    return r;
+}
+
+template <bool SIG1, bool WX, bool WY>
+__global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int mode, int parity,
+                                                                 cudaGraphConditionalHandle h, int use_h, int rows) {
+    const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
+    float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
+    extern __shared__ float4 smem_f4[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(sm);
+    unsigned long long *empty = full + 2;
+    PairEntry *tab = reinterpret_cast<PairEntry *>(sm + 32);
+    const size_t sb = pstage_bytes(rows);
+    int4 *slist[2];
+    float2 *wpos[2];
+    for (int q = 0; q < 2; q++) {
+        slist[q] = reinterpret_cast<int4 *>(sm + pstage_base() + q * sb);
+        wpos[q] = reinterpret_cast<float2 *>(slist[q] + (size_t)rows * kFastBlock);
+    }
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], kFastBlock / 32);
+        mbar_init(&empty[1], kFastBlock / 32);
+        tab[0] = s.pair[0];
+        const float2 g = __ldg(pin + s.N);  // the ghost slot's far position
+        wpos[0][kWinGhost] = g;
+        wpos[1][kWinGhost] = g;
+        if (s.trace && blockIdx.x == 0) {
+            const int row = s.sc->obsRow;
+            if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
+        }
+    }
+    __syncthreads();
+    float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
+    bool bad = false;
+    if (threadIdx.x >= kFastBlock) {
+        // the producer
+        if (threadIdx.x == kFastBlock) {
+            int k = 0;
+            bool live = true;
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
+                const int st = k & 1, use = k >> 1;
+                if (use > 0) {
+                    // the stage's last tile: consumed, and its copies landed
+                    live = mbar_wait_bounded(&empty[st], (use - 1) & 1, kWaitLimit) &&
+                           mbar_wait_bounded(&full[st], (use - 1) & 1, kWaitLimit);
+                    if (!live) {
+                        atomicOr(&s.sc->overflow, kFlagTimeout);
+                        break;
+                    }
+                }
+                const int *bw = s.blockWin + kWinInts * (size_t)t;
+                const int len = bw[0];
+                const int b0 = t * kFastBlock;
+                const int G = min(bw[19], rows);
+                const unsigned rowBytes = (unsigned)min(kFastBlock, s.Ncap - b0) * 16u;
+                unsigned total = (unsigned)G * rowBytes;
+                if (len >= 0)
+                    for (int p = 0; p < 6; p++) {
+                        const int a = bw[1 + p], c = bw[13 + p];
+                        if (c > 0) total += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
+                    }
+                mbar_expect_tx(&full[st], total);
+                const int4 *lsrc = reinterpret_cast<const int4 *>(s.nbr) + b0;
+                for (int g = 0; g < G; g++)
+                    bulk_copy_g2s(slist[st] + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, &full[st]);
+                if (len >= 0)
+                    for (int p = 0; p < 6; p++) {
+                        const int a = bw[1 + p], c = bw[13 + p];
+                        if (c > 0) {
+                            const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
+                            bulk_copy_g2s(wpos[st] + bw[7 + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
+                                          &full[st]);
+                        }
+                    }
+            }
+            if (!live) {
+                // copies of the last two tiles issued may still be in flight:
+                // a bounded wait each
+                for (int kl = k - 2; kl < k; kl++)
+                    if (kl >= 0) mbar_wait_bounded(&full[kl & 1], (kl >> 1) & 1, kWaitLimit);
+            }
+        }
+        __syncwarp();
+    } else {
+        // the consumers
+        const int lane = threadIdx.x & 31;
+        const float D = s.imgD;
+        bool dead = false;
+        int t = blockIdx.x;
+        PTile nx;
+        if (t < ntiles) nx = ptile_load(s, pin, t, mode);
+        for (int k = 0; t < ntiles; k++) {
+            const PTile cur = nx;
+            const int tn = t + gridDim.x;
+            if (tn < ntiles) nx = ptile_load(s, pin, tn, mode);
+            const int st = k & 1;
+            bool ok = false;
+            if (!dead) {
+                ok = mbar_wait_bounded(&full[st], (k >> 1) & 1, kWaitLimit);
+                if (!ok) {
+                    dead = true;
+                    atomicOr(&s.sc->overflow, kFlagTimeout);
+                }
+            }
+            const int i = t * kFastBlock + threadIdx.x;
+            const bool act = i < s.N;
+            float fx = 0.0f, fy = 0.0f, ue2 = 0.0f, we2 = 0.0f, utri = 0.0f, uwall = 0.0f;
+            if (act) bonded_forces<WX, WY, true>(s, i, mode, pin, cur.p, fx, fy, ue2, utri, uwall);
+            const bool near = act && ((WX && (cur.p.x < D || cur.p.x > s.Lx - D)) ||
+                                      (WY && (cur.p.y < D || cur.p.y > s.Ly - D)));
+            const bool img = __any_sync(0xffffffffu, near);
+            if (act && ok) {
+                if (cur.len >= 0) {
+                    if (img)
+                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist[st], rows,
+                                                                           pin, wpos[st], nullptr, nullptr, fx, fy,
+                                                                           ue2, we2);
+                    else
+                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist[st], rows, pin, wpos[st], fx,
+                                                  fy, ue2, we2);
+                } else {
+                    if (img)
+                        fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist[st],
+                                                                            rows, pin, wpos[st], nullptr, nullptr, fx,
+                                                                            fy, ue2, we2);
+                    else
+                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist[st], rows, pin, wpos[st], fx,
+                                                   fy, ue2, we2);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            if (act)
+                fast_finish<WX, WY>(s, i, mode, cur.p, cur.m, cur.v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke,
+                                    vvm, bad);
+            t = tn;
+        }
+    }
+    step_reduce<kPBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
+}
+
+template <bool SIG1, bool WX, bool WY>
+static cudaError_t launch_fstep_p(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                                  int use_h) {
+    const int rows = std::max(1, std::min(s.nbrCap / 4, kPRows));
+    const size_t smem = pstep_smem(rows);
+    auto kern = k_fstep_p<SIG1, WX, WY>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    int dev = 0, sms = 0, per = 0;
+    if ((e = cudaGetDevice(&dev))) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kPBlock, smem))) return e;
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    const int grid = std::max(1, std::min(ntiles, std::max(1, per) * sms));
+    return L.kernel(kern, dim3(grid), dim3(kPBlock), smem, s, mode, parity, h, use_h, rows);
+}
+
+template <bool SIG1>
+static cudaError_t fstep_p_image(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
+                                 int use_h) {
+    if (s.wrapx && s.wrapy) return launch_fstep_p<SIG1, true, true>(L, s, mode, parity, h, use_h);
+    if (s.wrapx) return launch_fstep_p<SIG1, true, false>(L, s, mode, parity, h, use_h);
+    return launch_fstep_p<SIG1, false, false>(L, s, mode, parity, h, use_h);
+}
+
 template <bool MT, bool SG, bool SIG1>
 static cudaError_t fstep_image(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                                int use_h) {
@@ -969,6 +1244,9 @@ cudaError_t enqueue_step_fast(Launch &L, const DevSys &s, int mode, int parity, 
     if (mt) return sg ? fstep_image<true, true, false>(L, s, mode, parity, h, use_h)
                       : fstep_image<true, false, false>(L, s, mode, parity, h, use_h);
     if (sg) return fstep_image<false, true, false>(L, s, mode, parity, h, use_h);
+    if (s.nBonded == 0)
+        return s.sigmaOne ? fstep_p_image<true>(L, s, mode, parity, h, use_h)
+                          : fstep_p_image<false>(L, s, mode, parity, h, use_h);
     return s.sigmaOne ? fstep_image<false, false, true>(L, s, mode, parity, h, use_h)
                       : fstep_image<false, false, false>(L, s, mode, parity, h, use_h);
 }
