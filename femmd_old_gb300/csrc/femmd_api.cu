@@ -2506,9 +2506,10 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     auto fast_entry = [&](int r, int q) -> int {
         const int *b = &bw[kWinInts * (size_t)(r / kFastBlock)];
         const int w = raw[nbr_at(q, r, ctx->Ncap)];
-        if (b[0] < 0) return w & kIdMask;
-        for (int p = 0; p < 6; p++)
-            if (w >= b[7 + p] && w < b[7 + p] + b[13 + p]) return cellIds[b[1 + p] + (w - b[7 + p])];
+        if (b[kWLen] < 0) return w & kIdMask;
+        for (int p = 0; p < kWinPieces; p++)
+            if (w >= b[kWOff + p] && w < b[kWOff + p] + b[kWCount + p])
+                return cellIds[b[kWStart + p] + (w - b[kWOff + p])];
         return -1;  // not an entry of the window: a mismatch the set comparison exposes
     };
     long long k = 0;

@@ -155,15 +155,16 @@ struct DevSys {
     const float *idMass, *idSigma, *idWallDelta, *idWallSig;
     const int *idType;
     // The step kernel's blocks of kFastBlock storage slots: a block of free
-    // particles inside one cell column stages the positions of its stencil
-    // window (up to six cell-slot ranges: per stencil column the rows around
-    // the block, and the row across the y edge) in shared memory, and its
-    // lists hold window indices instead of storage slots.  blockWin holds
-    // kWinInts ints per block: {len, start[6], off[6], count[6], groups, -}:
-    // piece p's cell slots start[p] .. start[p] + count[p] - 1 sit at window
-    // entries off[p] ..; len: the entries the pieces span (len < 0: the
-    // block reads global slots); groups: 16-byte list groups of the block's
-    // longest list.  The window's last entry, kWinGhost, is the ghost's.
+    // particles inside one cell column, or across two neighbouring ones,
+    // stages the positions of its stencil window (up to kWinPieces cell-slot
+    // ranges) in shared memory, and its lists hold window indices instead of
+    // storage slots.  blockWin holds kWinInts ints per block (the kW*
+    // offsets): piece p's cell slots start[p] .. start[p] + count[p] - 1 sit
+    // at window entries off[p] ..; len: the entries the pieces span (len < 0:
+    // the block reads global slots); groups: 16-byte list groups of the
+    // block's longest list; col0, two: the block's first cell column and
+    // whether it reaches into the next.  The window's last entry, kWinGhost,
+    // is the ghost's.
     int *newCell;   // cell of the particle at each storage slot
     int *blockWin;
 };
@@ -171,7 +172,10 @@ struct DevSys {
 constexpr int kFastBlock = 128;  // storage slots per block of the fast step kernel
 constexpr int kWinMax = 768;     // window entries per block (the ghost included)
 constexpr int kWinGhost = kWinMax - 1;  // the window entry of the ghost slot
-constexpr int kWinInts = 24;     // ints of window data per block
+constexpr int kWinPieces = 8;    // cell-slot ranges of a window
+constexpr int kWLen = 0, kWStart = 1, kWOff = kWStart + kWinPieces, kWCount = kWOff + kWinPieces,
+              kWGroups = kWCount + kWinPieces, kWCol0 = kWGroups + 1, kWTwo = kWCol0 + 1;
+constexpr int kWinInts = kWTwo + 1;  // ints of window data per block
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

@@ -8,8 +8,9 @@
 // framework's memory accounting.  femmd_bin_cells_noalloc serves those
 // callers: the caller passes device pointers for the positions and for both
 // outputs, and the working memory the counting sort needs lives in one
-// file-scope __device__ array of fixed size.  Every GPU that loads this
-// library holds that array until the process exits.
+// file-scope __device__ array of fixed size, which only device code names.
+// Every GPU that loads this library holds that array until the process
+// exits.
 //
 // The sort is the same counting sort as the context's rebuild: each particle
 // gets the reference's cell id, the counts are histogrammed with
@@ -18,8 +19,6 @@
 // particle id.  The output order is the reference CPU's order (ascending id
 // inside a cell), so it equals femmd_get_cells after a context build.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "femmd.h"
 #include "femmd_internal.h"
@@ -41,16 +40,19 @@ constexpr size_t kOffBlock = kOffCount + kNaMaxCells;
 constexpr size_t kScratchInts = kOffBlock + kNaMaxScanBlocks;
 
 // The scratch: per-particle cell and rank, per-cell counts, per-block sums.
-// Host code must not pass this name to a kernel (on the host it names a
-// stand-in, not device memory); the device address comes from
-// cudaGetSymbolAddress, once per device.
+// Only device code names it, so every launch uses the array of the module
+// and context it runs in (nothing about it is cached on the host, and a
+// device reset leaves nothing stale behind).
 static __device__ __align__(256) int g_bin_scratch[kScratchInts];
 
-std::mutex g_mu;
-int *g_scratch_addr[64] = {};
+// The counts start at zero; the array keeps the previous call's contents.
+__global__ void __launch_bounds__(kBlock) na_clear(int ncells) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncells) g_bin_scratch[kOffCount + c] = 0;
+}
 
-__global__ void __launch_bounds__(kBlock) na_count(const float2 *pos, int n, int ncx, int ncy, float Lx, float Ly,
-                                                   int *scratch) {
+__global__ void __launch_bounds__(kBlock) na_count(const float2 *pos, int n, int ncx, int ncy, float Lx, float Ly) {
+    int *scratch = g_bin_scratch;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = i < n;
     unsigned active = __ballot_sync(0xffffffffu, act);
@@ -67,7 +69,9 @@ __global__ void __launch_bounds__(kBlock) na_count(const float2 *pos, int n, int
     scratch[kOffRank + i] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(kNaScan) na_block_sums(int ncells, const int *scratch, int *block_sums) {
+__global__ void __launch_bounds__(kNaScan) na_block_sums(int ncells) {
+    const int *scratch = g_bin_scratch;
+    int *block_sums = g_bin_scratch + kOffBlock;
     __shared__ int red[32];
     int c = blockIdx.x * kNaScan + threadIdx.x;
     int v = c < ncells ? scratch[kOffCount + c] : 0;
@@ -80,8 +84,9 @@ __global__ void __launch_bounds__(kNaScan) na_block_sums(int ncells, const int *
     }
 }
 
-__global__ void __launch_bounds__(kNaScan) na_scan(int ncells, int n, const int *scratch, const int *block_sums,
-                                                   int *cell_start) {
+__global__ void __launch_bounds__(kNaScan) na_scan(int ncells, int n, int *cell_start) {
+    const int *scratch = g_bin_scratch;
+    const int *block_sums = g_bin_scratch + kOffBlock;
     __shared__ int wsum[32];
     __shared__ int prefix;
     int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -121,7 +126,8 @@ __global__ void __launch_bounds__(kNaScan) na_scan(int ncells, int n, const int 
     if (blockIdx.x == gridDim.x - 1 && t == 0) cell_start[ncells] = n;
 }
 
-__global__ void __launch_bounds__(kBlock) na_scatter(int n, const int *scratch, const int *cell_start, int *cell_ids) {
+__global__ void __launch_bounds__(kBlock) na_scatter(int n, const int *cell_start, int *cell_ids) {
+    const int *scratch = g_bin_scratch;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int slot = cell_start[scratch[kOffCell + i]] + scratch[kOffRank + i];
@@ -154,28 +160,21 @@ extern "C" femmd_status femmd_bin_cells_noalloc(const float *d_pos, int n, doubl
     long long ncells = (long long)ncx * ncy;
     if (n > kNaMaxParticles || ncells > kNaMaxCells) return FEMMD_CAPACITY_OVERFLOW;
     if (!d_cell_start || (n > 0 && (!d_pos || !d_cell_ids))) return FEMMD_INVALID_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FEMMD_CUDA_ERROR;
-    int *scratch;
-    {
-        // set-up, once per device, with that device current
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_addr[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_bin_scratch) != cudaSuccess || !p) return FEMMD_CUDA_ERROR;
-            g_scratch_addr[dev] = (int *)p;
-        }
-        scratch = g_scratch_addr[dev];
-    }
+    // an error an earlier, unrelated call left pending stays in place for
+    // its owner; only an error this call's launches raise is reported (and
+    // cleared)
+    const cudaError_t prior = cudaPeekAtLastError();
     cudaStream_t s = (cudaStream_t)stream;
     const int nc = (int)ncells;
-    // the counts must start at zero; the array keeps the previous call's contents
-    if (cudaMemsetAsync(scratch + kOffCount, 0, sizeof(int) * (size_t)nc, s) != cudaSuccess) return FEMMD_CUDA_ERROR;
     const int pb = (n + kBlock - 1) / kBlock, sb = (nc + kNaScan - 1) / kNaScan, cb = (nc + kBlock - 1) / kBlock;
-    if (pb > 0) na_count<<<pb, kBlock, 0, s>>>((const float2 *)d_pos, n, ncx, ncy, (float)Lx, (float)Ly, scratch);
-    na_block_sums<<<sb, kNaScan, 0, s>>>(nc, scratch, scratch + kOffBlock);
-    na_scan<<<sb, kNaScan, 0, s>>>(nc, n, scratch, scratch + kOffBlock, d_cell_start);
-    if (pb > 0) na_scatter<<<pb, kBlock, 0, s>>>(n, scratch, d_cell_start, d_cell_ids);
+    na_clear<<<cb, kBlock, 0, s>>>(nc);
+    if (pb > 0) na_count<<<pb, kBlock, 0, s>>>((const float2 *)d_pos, n, ncx, ncy, (float)Lx, (float)Ly);
+    na_block_sums<<<sb, kNaScan, 0, s>>>(nc);
+    na_scan<<<sb, kNaScan, 0, s>>>(nc, n, d_cell_start);
+    if (pb > 0) na_scatter<<<pb, kBlock, 0, s>>>(n, d_cell_start, d_cell_ids);
     na_sort<<<cb, kBlock, 0, s>>>(nc, d_cell_start, d_cell_ids);
-    return cudaGetLastError() == cudaSuccess ? FEMMD_OK : FEMMD_CUDA_ERROR;
+    const cudaError_t now = cudaPeekAtLastError();
+    if (now == cudaSuccess || now == prior) return FEMMD_OK;
+    cudaGetLastError();
+    return FEMMD_CUDA_ERROR;
 }

@@ -142,19 +142,23 @@ __global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int 
 }
 
 // The window of every step-kernel block (one thread per block).  A block of
-// free particles whose first and last slot lie in one cell column (rows r0 ..
-// r1) gets, per stencil column d (dx = d - 1, wrapped as the list walk
-// wraps), the cell-slot range of rows r0 - 1 .. r1 + 1 inside the grid (piece
-// 2d) and, where the block touches a y edge, the row across it (piece 2d + 1).
-// Every candidate the list build walks for the block's particles lies in one
-// of these pieces, so a list entry is the candidate's index in the block's
-// window.  A piece starting at cell slot a takes window entries from an even
-// base, with a & 1 entries before it and its end padded to an even count, so
-// that its positions can be copied straight from the storage array in
-// 16-byte units when cell slots and storage slots coincide.  Other blocks
-// (bonded particles, blocks across two columns, windows too large, grids the
-// fast walk does not cover) keep global storage slots.  The block's longest
-// list (in groups) is gathered by the list build.
+// free particles whose cell slots lie in one cell column (rows r0 .. r1 of
+// column ix) takes, per stencil column ix - 1 .. ix + 1, the rows r0 - 1 ..
+// r1 + 1 (piece 2d) and the row across the y edge when the block touches it
+// (piece 2d + 1).  A block reaching from the lower rows r0 .. of column ix
+// into the upper rows .. r1 of column ix + 1 takes, per column ix - 1 + w
+// (w = 0 .. 3), the upper range (piece 2w + 1: rows r0 - 1 .. ncy - 1, only
+// the last row for w = 3) and the lower range (piece 2w: rows 0 .. r1 + 1,
+// only row 0 for w = 0): the lower column's particles find their stencil
+// rows in the upper ranges and their row across the edge in the lower ones,
+// the upper column's the other way round.  A piece starting at cell slot a
+// takes window entries from an even base, with a & 1 entries before it and
+// its end padded to an even count, so that its positions can be copied
+// straight from the storage array in 16-byte units when cell slots and
+// storage slots coincide.  Other blocks (bonded particles, blocks over more
+// cells, windows too large, grids the fast walk does not cover) keep global
+// storage slots.  The block's longest list (in groups) is gathered by the
+// list build.
 __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -164,51 +168,66 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
     const int f = b * kFastBlock, l = min(f + kFastBlock, s.N) - 1;
     const int ncy = s.ncy, ncx = s.ncx;
     bool ok = f >= s.nBonded && fast_walk_ok(s) && ncy >= 3;
-    int st[6] = {0, 0, 0, 0, 0, 0}, off[6] = {0, 0, 0, 0, 0, 0}, cnt[6] = {0, 0, 0, 0, 0, 0};
-    int acc = 0;
+    int st[kWinPieces], off[kWinPieces], cnt[kWinPieces];
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) st[p] = off[p] = cnt[p] = 0;
+    int acc = 0, ix = 0, two = 0;
     if (ok) {
         const int cf = s.newCell[f], cl = s.newCell[l];
-        const int ix = cf / ncy, r0 = cf - ix * ncy, r1 = cl - ix * ncy;
-        ok = cl / ncy == ix && !(r0 == 0 && r1 == ncy - 1);
-        if (ok) {
+        ix = cf / ncy;
+        const int ixl = cl / ncy, r0 = cf - ix * ncy, r1 = cl - ixl * ncy;
+        // row ranges [ra, rb] per piece and window column (rb < ra: empty)
+        int ra[kWinPieces], rb[kWinPieces];
+#pragma unroll
+        for (int p = 0; p < kWinPieces; p++) ra[p] = 0, rb[p] = -1;
+        if (ixl == ix && !(r0 == 0 && r1 == ncy - 1)) {
             const int lo = max(r0 - 1, 0), hi = min(r1 + 1, ncy - 1);
 #pragma unroll
             for (int d = 0; d < 3; d++) {
-                int nx = ix + d - 1;
-                if (nx < 0) nx = ncx - 1;
-                else if (nx == ncx) nx = 0;
-                const int col = nx * ncy;
-                int a[2], e[2];
-                a[0] = s.cellStart[col + lo];
-                e[0] = s.cellStart[col + hi + 1];
-                a[1] = e[1] = 0;
-                if (r0 == 0) {
-                    a[1] = s.cellStart[col + ncy - 1];
-                    e[1] = s.cellStart[col + ncy];
-                } else if (r1 == ncy - 1) {
-                    a[1] = s.cellStart[col];
-                    e[1] = s.cellStart[col + 1];
-                }
+                ra[2 * d] = lo;
+                rb[2 * d] = hi;
+                if (r0 == 0) ra[2 * d + 1] = rb[2 * d + 1] = ncy - 1;
+                else if (r1 == ncy - 1) ra[2 * d + 1] = rb[2 * d + 1] = 0;
+            }
+        } else if (ixl == ix + 1 && r0 >= 1 && r1 <= ncy - 2) {
+            two = 1;
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const int p = 2 * d + h;
-                    st[p] = a[h];
-                    cnt[p] = e[h] - a[h];
-                    off[p] = acc + (a[h] & 1);
-                    if (cnt[p] > 0) acc += ((e[h] + 1) & ~1) - (a[h] & ~1);
-                }
+            for (int w = 0; w < 4; w++) {
+                ra[2 * w] = 0;
+                rb[2 * w] = w == 0 ? 0 : r1 + 1;
+                ra[2 * w + 1] = w == 3 ? ncy - 1 : r0 - 1;
+                rb[2 * w + 1] = ncy - 1;
+            }
+        } else {
+            ok = false;
+        }
+        if (ok) {
+#pragma unroll
+            for (int p = 0; p < kWinPieces; p++) {
+                if (rb[p] < ra[p]) continue;
+                int nx = ix + (p >> 1) - 1;
+                if (nx < 0) nx += ncx;
+                else if (nx >= ncx) nx -= ncx;
+                const int col = nx * ncy;
+                const int a = s.cellStart[col + ra[p]], e = s.cellStart[col + rb[p] + 1];
+                st[p] = a;
+                cnt[p] = e - a;
+                off[p] = acc + (a & 1);
+                if (cnt[p] > 0) acc += ((e + 1) & ~1) - (a & ~1);
             }
             ok = acc <= kWinMax - 1;  // the last entry is the ghost's
         }
     }
-    out[0] = ok ? acc : -1;
+    out[kWLen] = ok ? acc : -1;
 #pragma unroll
-    for (int p = 0; p < 6; p++) {
-        out[1 + p] = st[p];
-        out[7 + p] = off[p];
-        out[13 + p] = cnt[p];
+    for (int p = 0; p < kWinPieces; p++) {
+        out[kWStart + p] = st[p];
+        out[kWOff + p] = off[p];
+        out[kWCount + p] = cnt[p];
     }
-    out[19] = 0;
+    out[kWGroups] = 0;
+    out[kWCol0] = ix;
+    out[kWTwo] = two;
 }
 
 // The list build of the fast mode.  One thread per cell slot t builds the
@@ -285,7 +304,11 @@ __device__ __forceinline__ void fwalk(const float4 *cand, int qb, int qe, int qb
 }
 
 // The window deltas of a lane: entry = cell slot + dm[d] for the main rows
-// of stencil column d, + dw[d] for the row across the y edge.
+// of stencil column d, + dw[d] for the row across the y edge.  In a block
+// over two columns a lane of the lower column (j = 0) finds its main rows in
+// the upper ranges of window columns d and its edge row in their lower
+// ranges; a lane of the upper column (j = 1) the other way round, in window
+// columns d + 1.
 struct WinDelta {
     bool win;
     int len;
@@ -295,12 +318,16 @@ struct WinDelta {
 __device__ __forceinline__ WinDelta win_delta(const DevSys &s, int slot) {
     WinDelta w;
     const int *bw = s.blockWin + kWinInts * (size_t)(slot / kFastBlock);
-    w.len = bw[0];
+    w.len = bw[kWLen];
     w.win = w.len >= 0;
+    const bool two = bw[kWTwo] != 0;
+    const int j = two && s.newCell[slot] / s.ncy != bw[kWCol0] ? 1 : 0;
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-        w.dm[q] = bw[7 + 2 * q] - bw[1 + 2 * q];
-        w.dw[q] = bw[8 + 2 * q] - bw[2 + 2 * q];
+    for (int d = 0; d < 3; d++) {
+        const int pm = !two ? 2 * d : (j == 0 ? 2 * d + 1 : 2 * d + 2);
+        const int pw = !two ? 2 * d + 1 : (j == 0 ? 2 * d : 2 * d + 3);
+        w.dm[d] = bw[kWOff + pm] - bw[kWStart + pm];
+        w.dw[d] = bw[kWOff + pw] - bw[kWStart + pw];
     }
     return w;
 }
@@ -525,7 +552,7 @@ __global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int che
         const int blk = valid ? ns / kFastBlock : -1;
         const unsigned peers = __match_any_sync(0xffffffffu, blk);
         const int gm = __reduce_max_sync(peers, ng);
-        if (valid && lane == __ffs(peers) - 1) atomicMax(&s.blockWin[kWinInts * (size_t)blk + 19], gm);
+        if (valid && lane == __ffs(peers) - 1) atomicMax(&s.blockWin[kWinInts * (size_t)blk + kWGroups], gm);
     }
     const int kmax = __reduce_max_sync(0xffffffffu, valid ? k : 0);
     const int ksum = __reduce_add_sync(0xffffffffu, valid ? k : 0);
@@ -856,7 +883,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     return false;
 }
 
-constexpr int kWaitLimit = 1 << 22;  // polls before a step block reports a stuck copy
+// A poll that may suspend the thread in hardware until the phase completes,
+// for at most about hint_ns nanoseconds: a waiting thread takes no issue
+// slots from the warps that work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(unsigned long long *bar, unsigned parity, unsigned hint_ns) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar, unsigned parity, int limit,
+                                                unsigned hint_ns) {
+    for (int k = 0; k < limit; k++)
+        if (mbar_try_wait_sleep(bar, parity, hint_ns)) return true;
+    return false;
+}
+
+constexpr int kWaitLimit = 1 << 22;   // polls before a step block reports a stuck copy
+constexpr int kSleepLimit = 1 << 19;  // suspending polls (of at most kSleepNs each) before it does
+constexpr unsigned kSleepNs = 2000;
 constexpr int kFlagTimeout = 8;      // DevScalars::overflow bit: a bounded wait expired
 
 // Resident blocks per SM the register allocation must allow (kFastBlock
@@ -889,29 +938,29 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
     int *wtyp = reinterpret_cast<int *>(wpos + kWinMax);
     float *wsig = reinterpret_cast<float *>(wtyp + (MT ? kWinMax : 0));
     const int *bw = s.blockWin + kWinInts * (size_t)blockIdx.x;
-    const int len = bw[0];
+    const int len = bw[kWLen];
     const int b0 = blockIdx.x * kFastBlock;
     const bool tmaWin = !MT && !SG && len >= 0 && s.nBonded == 0;
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const int G = rows > 0 ? min(bw[19], rows) : 0;
+        const int G = rows > 0 ? min(bw[kWGroups], rows) : 0;
         const unsigned rowBytes = (unsigned)min(kFastBlock, s.Ncap - b0) * 16u;
         unsigned total = (unsigned)G * rowBytes;
         if (tmaWin)
-            for (int p = 0; p < 6; p++) {
-                const int a = bw[1 + p], c = bw[13 + p];
+            for (int p = 0; p < kWinPieces; p++) {
+                const int a = bw[kWStart + p], c = bw[kWCount + p];
                 if (c > 0) total += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
             }
         mbar_expect_tx(bar, total);
         const int4 *lsrc = reinterpret_cast<const int4 *>(s.nbr) + b0;
         for (int g = 0; g < G; g++) bulk_copy_g2s(slist + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, bar);
         if (tmaWin)
-            for (int p = 0; p < 6; p++) {
-                const int a = bw[1 + p], c = bw[13 + p];
+            for (int p = 0; p < kWinPieces; p++) {
+                const int a = bw[kWStart + p], c = bw[kWCount + p];
                 if (c > 0) {
                     const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                    bulk_copy_g2s(wpos + bw[7 + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u, bar);
+                    bulk_copy_g2s(wpos + bw[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u, bar);
                 }
             }
     }
@@ -935,8 +984,8 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
     if (len >= 0) {
         if (!tmaWin) {
             // the window gathered: cell slots are not storage slots
-            for (int p = 0; p < 6; p++) {
-                const int st = bw[1 + p], off = bw[7 + p], c = bw[13 + p];
+            for (int p = 0; p < kWinPieces; p++) {
+                const int st = bw[kWStart + p], off = bw[kWOff + p], c = bw[kWCount + p];
                 for (int w = threadIdx.x; w < c; w += kFastBlock) {
                     const int j = __ldg(s.sortedIds + st + w);
                     wpos[off + w] = __ldg(pin + j);
@@ -1059,7 +1108,7 @@ __device__ __forceinline__ PTile ptile_load(const DevSys &s, const float2 *__res
     r.cnt = act ? min(__ldg(s.nbrCount + ic), s.nbrCap) : 0;
     r.m = __ldg(s.mass + ic);
     r.v = (mode != MODE_FORCES && mode != MODE_INIT) ? s.vel[ic] : make_float2(0.0f, 0.0f);
-    r.len = __ldg(s.blockWin + kWinInts * (size_t)t);
+    r.len = __ldg(s.blockWin + kWinInts * (size_t)t + kWLen);
     return r;
 }
 
@@ -1107,22 +1156,22 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 const int st = k & 1, use = k >> 1;
                 if (use > 0) {
                     // the stage's last tile: consumed, and its copies landed
-                    live = mbar_wait_bounded(&empty[st], (use - 1) & 1, kWaitLimit) &&
-                           mbar_wait_bounded(&full[st], (use - 1) & 1, kWaitLimit);
+                    live = mbar_wait_sleep(&empty[st], (use - 1) & 1, kSleepLimit, kSleepNs) &&
+                           mbar_wait_sleep(&full[st], (use - 1) & 1, kSleepLimit, kSleepNs);
                     if (!live) {
                         atomicOr(&s.sc->overflow, kFlagTimeout);
                         break;
                     }
                 }
                 const int *bw = s.blockWin + kWinInts * (size_t)t;
-                const int len = bw[0];
+                const int len = bw[kWLen];
                 const int b0 = t * kFastBlock;
-                const int G = min(bw[19], rows);
+                const int G = min(bw[kWGroups], rows);
                 const unsigned rowBytes = (unsigned)min(kFastBlock, s.Ncap - b0) * 16u;
                 unsigned total = (unsigned)G * rowBytes;
                 if (len >= 0)
-                    for (int p = 0; p < 6; p++) {
-                        const int a = bw[1 + p], c = bw[13 + p];
+                    for (int p = 0; p < kWinPieces; p++) {
+                        const int a = bw[kWStart + p], c = bw[kWCount + p];
                         if (c > 0) total += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
                     }
                 mbar_expect_tx(&full[st], total);
@@ -1130,11 +1179,11 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 for (int g = 0; g < G; g++)
                     bulk_copy_g2s(slist[st] + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, &full[st]);
                 if (len >= 0)
-                    for (int p = 0; p < 6; p++) {
-                        const int a = bw[1 + p], c = bw[13 + p];
+                    for (int p = 0; p < kWinPieces; p++) {
+                        const int a = bw[kWStart + p], c = bw[kWCount + p];
                         if (c > 0) {
                             const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                            bulk_copy_g2s(wpos[st] + bw[7 + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
+                            bulk_copy_g2s(wpos[st] + bw[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
                                           &full[st]);
                         }
                     }
@@ -1143,7 +1192,7 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 // copies of the last two tiles issued may still be in flight:
                 // a bounded wait each
                 for (int kl = k - 2; kl < k; kl++)
-                    if (kl >= 0) mbar_wait_bounded(&full[kl & 1], (kl >> 1) & 1, kWaitLimit);
+                    if (kl >= 0) mbar_wait_sleep(&full[kl & 1], (kl >> 1) & 1, kSleepLimit, kSleepNs);
             }
         }
         __syncwarp();

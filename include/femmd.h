@@ -401,11 +401,15 @@ femmd_status femmd_adjoint_observable(femmd_ctx *ctx, double *wall_stress, doubl
  * is enqueued on 'stream' (a cudaStream_t; NULL = the default stream) and the
  * call returns without waiting.  n above FEMMD_NOALLOC_MAX_PARTICLES or
  * ncx*ncy above FEMMD_NOALLOC_MAX_CELLS returns FEMMD_CAPACITY_OVERFLOW and
- * does nothing.  The first call on a device looks up the device address of
- * the working array (once per device, with that device current): make that
- * first call before any stream capture.  Every call uses the same working
- * array and leaves its contents behind, so calls that can overlap on the GPU
- * (different streams without ordering between them) race. */
+ * does nothing.  The kernels name the working array in device code, so each
+ * call uses the array of the context it runs in; nothing is cached on the
+ * host, and after cudaDeviceReset the next call simply runs in the new
+ * context.  Make the first call on a device outside stream capture (it may
+ * load the library's kernels).  Every call uses the same working array and
+ * leaves its contents behind, so calls that can overlap on the GPU (different
+ * streams without ordering between them) race.  A CUDA error that an earlier,
+ * unrelated call left pending is left in place; FEMMD_CUDA_ERROR means one of
+ * this call's launches failed. */
 femmd_status femmd_bin_cells_noalloc(const float *d_pos, int n, double Lx, double Ly, int ncx, int ncy,
                                      int *d_cell_start, int *d_cell_ids, void *stream);
 

@@ -76,3 +76,71 @@ def test_noalloc_rejects_sizes_beyond_its_maximum():
     side = int(header_limit("FEMMD_NOALLOC_MAX_CELLS") ** 0.5) + 1
     st = lib.femmd_bin_cells_noalloc(None, 0, 10.0, 10.0, side, side, C.c_void_p(1), None, None)
     assert _lib.STATUS[st] == "CAPACITY_OVERFLOW"
+
+
+def call(lib, d_pos, n, box, grid, d_start, d_ids, stream):
+    return lib.femmd_bin_cells_noalloc(C.c_void_p(d_pos.data_ptr()) if d_pos is not None else None, n, box[0],
+                                       box[1], grid[0], grid[1], C.c_void_p(d_start.data_ptr()),
+                                       C.c_void_p(d_ids.data_ptr()) if d_ids is not None else None,
+                                       C.c_void_p(stream) if stream else None)
+
+
+def test_noalloc_with_no_particles_gives_empty_cells():
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    d_start = torch.full((5 * 4 + 1,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert call(lib, None, 0, (10.0, 8.0), (5, 4), d_start, None, 0) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(d_start.cpu().numpy(), np.zeros(21, np.int32))
+
+
+def test_noalloc_on_a_side_stream():
+    """The work goes to the caller's stream: synchronising that stream alone
+    is enough to read the result."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    pos, box, grid, st, ids = context_cells(S.lj_fluid(n_side=30, seed_pos=11, seed_vel=12))
+    n = pos.shape[0]
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        d_pos = torch.from_numpy(np.ascontiguousarray(pos, np.float32)).cuda()
+        d_start = torch.full((grid[0] * grid[1] + 1,), -7, dtype=torch.int32, device="cuda")
+        d_ids = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+        assert call(lib, d_pos, n, box, grid, d_start, d_ids, side.cuda_stream) == 0
+    side.synchronize()
+    assert np.array_equal(d_start.cpu().numpy(), st)
+    assert np.array_equal(d_ids.cpu().numpy(), ids)
+
+
+def test_noalloc_captured_into_a_graph_and_replayed_on_two_systems():
+    """A warm call, then one call captured into a CUDA graph on a torch
+    stream; the graph is replayed on two systems of the same size and box
+    (positions copied into the captured buffer before each replay), and each
+    replay equals the context's binning of that system."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    a = context_cells(S.lj_fluid(n_side=32, seed_pos=21, seed_vel=22))
+    b = context_cells(S.lj_fluid(n_side=32, seed_pos=23, seed_vel=24))
+    assert a[1] == b[1] and tuple(a[2]) == tuple(b[2])
+    pos, box, grid = a[0], a[1], a[2]
+    n = pos.shape[0]
+    d_pos = torch.from_numpy(np.ascontiguousarray(pos, np.float32)).cuda()
+    d_start = torch.zeros((grid[0] * grid[1] + 1,), dtype=torch.int32, device="cuda")
+    d_ids = torch.zeros((n,), dtype=torch.int32, device="cuda")
+    cap = torch.cuda.Stream()
+    with torch.cuda.stream(cap):
+        assert call(lib, d_pos, n, box, grid, d_start, d_ids, cap.cuda_stream) == 0
+    cap.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=cap):
+        st = call(lib, d_pos, n, box, grid, d_start, d_ids, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    for pos_k, _, _, st_k, ids_k in (b, a, b):
+        d_start.fill_(-7)
+        d_ids.fill_(-7)
+        d_pos.copy_(torch.from_numpy(np.ascontiguousarray(pos_k, np.float32)))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(d_start.cpu().numpy(), st_k)
+        assert np.array_equal(d_ids.cpu().numpy(), ids_k)
