@@ -904,8 +904,8 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar, unsigne
 }
 
 constexpr int kWaitLimit = 1 << 22;   // polls before a step block reports a stuck copy
-constexpr int kSleepLimit = 1 << 19;  // suspending polls (of at most kSleepNs each) before it does
-constexpr unsigned kSleepNs = 2000;
+constexpr int kSleepLimit = 1 << 22;  // suspending polls (of at most kSleepNs each) before it does
+constexpr unsigned kSleepNs = 256;
 constexpr int kFlagTimeout = 8;      // DevScalars::overflow bit: a bounded wait expired
 
 // Resident blocks per SM the register allocation must allow (kFastBlock
@@ -1148,10 +1148,18 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
     float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
     bool bad = false;
     if (threadIdx.x >= kFastBlock) {
-        // the producer
+        // the producer; the window record of its next tile is loaded an
+        // iteration ahead, so its latency passes while the producer waits
+        // for a free stage
         if (threadIdx.x == kFastBlock) {
             int k = 0;
             bool live = true;
+            int wv[kWGroups + 1];
+            if (blockIdx.x < ntiles) {
+                const int *bw = s.blockWin + kWinInts * (size_t)blockIdx.x;
+#pragma unroll
+                for (int q = 0; q <= kWGroups; q++) wv[q] = bw[q];
+            }
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
                 const int st = k & 1, use = k >> 1;
                 if (use > 0) {
@@ -1163,15 +1171,15 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                         break;
                     }
                 }
-                const int *bw = s.blockWin + kWinInts * (size_t)t;
-                const int len = bw[kWLen];
+                const int len = wv[kWLen];
                 const int b0 = t * kFastBlock;
-                const int G = min(bw[kWGroups], rows);
+                const int G = min(wv[kWGroups], rows);
                 const unsigned rowBytes = (unsigned)min(kFastBlock, s.Ncap - b0) * 16u;
                 unsigned total = (unsigned)G * rowBytes;
                 if (len >= 0)
+#pragma unroll
                     for (int p = 0; p < kWinPieces; p++) {
-                        const int a = bw[kWStart + p], c = bw[kWCount + p];
+                        const int a = wv[kWStart + p], c = wv[kWCount + p];
                         if (c > 0) total += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
                     }
                 mbar_expect_tx(&full[st], total);
@@ -1179,14 +1187,21 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 for (int g = 0; g < G; g++)
                     bulk_copy_g2s(slist[st] + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, &full[st]);
                 if (len >= 0)
+#pragma unroll
                     for (int p = 0; p < kWinPieces; p++) {
-                        const int a = bw[kWStart + p], c = bw[kWCount + p];
+                        const int a = wv[kWStart + p], c = wv[kWCount + p];
                         if (c > 0) {
                             const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                            bulk_copy_g2s(wpos[st] + bw[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
+                            bulk_copy_g2s(wpos[st] + wv[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
                                           &full[st]);
                         }
                     }
+                const int tn = t + gridDim.x;
+                if (tn < ntiles) {
+                    const int *bw = s.blockWin + kWinInts * (size_t)tn;
+#pragma unroll
+                    for (int q = 0; q <= kWGroups; q++) wv[q] = bw[q];
+                }
             }
             if (!live) {
                 // copies of the last two tiles issued may still be in flight:
