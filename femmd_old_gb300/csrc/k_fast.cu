@@ -1123,12 +1123,12 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
     unsigned long long *empty = full + 2;
     PairEntry *tab = reinterpret_cast<PairEntry *>(sm + 32);
     const size_t sb = pstage_bytes(rows);
-    int4 *slist[2];
-    float2 *wpos[2];
-    for (int q = 0; q < 2; q++) {
-        slist[q] = reinterpret_cast<int4 *>(sm + pstage_base() + q * sb);
-        wpos[q] = reinterpret_cast<float2 *>(slist[q] + (size_t)rows * kFastBlock);
-    }
+    // stage q's list rows and window (computed, not indexed from an array:
+    // an array indexed by the stage number would live in local memory)
+    auto slist_of = [&](int q) { return reinterpret_cast<int4 *>(sm + pstage_base() + q * sb); };
+    auto wpos_of = [&](int q) {
+        return reinterpret_cast<float2 *>(sm + pstage_base() + q * sb + (size_t)rows * kFastBlock * sizeof(int4));
+    };
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     if (threadIdx.x == 0) {
         mbar_init(&full[0], 1);
@@ -1137,8 +1137,8 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
         mbar_init(&empty[1], kFastBlock / 32);
         tab[0] = s.pair[0];
         const float2 g = __ldg(pin + s.N);  // the ghost slot's far position
-        wpos[0][kWinGhost] = g;
-        wpos[1][kWinGhost] = g;
+        wpos_of(0)[kWinGhost] = g;
+        wpos_of(1)[kWinGhost] = g;
         if (s.trace && blockIdx.x == 0) {
             const int row = s.sc->obsRow;
             if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
@@ -1185,14 +1185,14 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 mbar_expect_tx(&full[st], total);
                 const int4 *lsrc = reinterpret_cast<const int4 *>(s.nbr) + b0;
                 for (int g = 0; g < G; g++)
-                    bulk_copy_g2s(slist[st] + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, &full[st]);
+                    bulk_copy_g2s(slist_of(st) + g * kFastBlock, lsrc + (size_t)g * s.Ncap, rowBytes, &full[st]);
                 if (len >= 0)
 #pragma unroll
                     for (int p = 0; p < kWinPieces; p++) {
                         const int a = wv[kWStart + p], c = wv[kWCount + p];
                         if (c > 0) {
                             const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                            bulk_copy_g2s(wpos[st] + wv[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
+                            bulk_copy_g2s(wpos_of(st) + wv[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
                                           &full[st]);
                         }
                     }
@@ -1242,19 +1242,19 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
             if (act && ok) {
                 if (cur.len >= 0) {
                     if (img)
-                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist[st], rows,
-                                                                           pin, wpos[st], nullptr, nullptr, fx, fy,
+                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st), rows,
+                                                                           pin, wpos_of(st), nullptr, nullptr, fx, fy,
                                                                            ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist[st], rows, pin, wpos[st], fx,
+                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st), fx,
                                                   fy, ue2, we2);
                 } else {
                     if (img)
-                        fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist[st],
-                                                                            rows, pin, wpos[st], nullptr, nullptr, fx,
+                        fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist_of(st),
+                                                                            rows, pin, wpos_of(st), nullptr, nullptr, fx,
                                                                             fy, ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist[st], rows, pin, wpos[st], fx,
+                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st), fx,
                                                    fy, ue2, we2);
                 }
             }
