@@ -75,7 +75,8 @@ def parse():
                          "reference: the reference's float operations and list order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--probe", default=None,
-                    choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras", "lj_1m"],
+                    choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras", "lj_1m",
+                             "lj_1m_rebuild"],
                     help="run one small fixed workload for a profiler capture and exit (no JSON line)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
@@ -617,6 +618,20 @@ def probe(name, mode="fast"):
         torch.cuda.nvtx.range_push("steps")
         s.set_profiling(True)
         s.run(12)
+        s.sync()
+        torch.cuda.nvtx.range_pop()
+    elif name == "lj_1m_rebuild":
+        # three full neighbour rebuilds of the 1M-atom LJ fluid after run(50),
+        # in the force mode of --force-mode, inside the NVTX range "rebuild"
+        s = F.System()
+        s.set_force_mode(FORCE_MODES[mode])
+        S.lj_fluid(n_side=1000).replay(s)
+        s.run(0)
+        s.run(50)
+        s.sync()
+        torch.cuda.nvtx.range_push("rebuild")
+        for _ in range(3):
+            s.build_nn()
         s.sync()
         torch.cuda.nvtx.range_pop()
     elif name == "adjoint":

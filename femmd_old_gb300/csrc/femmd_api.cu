@@ -789,7 +789,10 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
     CK(ctx->dsigma.ensure(ctx->sigmaByType ? 1 : N + 1));  // + the ghost slot
     CK(ctx->cellOf.ensure(N)); CK(ctx->rank.ensure(N)); CK(ctx->sortedIds.ensure(N)); CK(ctx->unsorted.ensure(N));
     CK(ctx->cellSorted.ensure(N)); CK(ctx->nbrCount.ensure(N));
-    CK(ctx->cellCount.ensure(ctx->ncells)); CK(ctx->cellStart.ensure(ctx->ncells + 1));
+    CK(ctx->cellCount.ensure(ctx->ncells));
+    // cellStart: ncells + 1 words, padded: the fast list build copies
+    // cell-start ranges rounded out to 16 bytes
+    CK(ctx->cellStart.ensure(ctx->ncells + 8));
     CK(ctx->blockSums.ensure(scan_blocks(ctx->ncells)));
     CK(ctx->sc.ensure(1));
     cudaStream_t s = ctx->stream;

@@ -163,8 +163,9 @@ struct DevSys {
     // at window entries off[p] ..; len: the entries the pieces span (len < 0:
     // the block reads global slots); groups: 16-byte list groups of the
     // block's longest list; col0, two: the block's first cell column and
-    // whether it reaches into the next.  The window's last entry, kWinGhost,
-    // is the ghost's.
+    // whether it reaches into the next; row0[p], row1[p]: the cell rows piece
+    // p covers (row1 < row0: none).  The window's last entry, kWinGhost, is
+    // the ghost's.
     int *newCell;   // cell of the particle at each storage slot
     int *blockWin;
 };
@@ -174,8 +175,9 @@ constexpr int kWinMax = 768;     // window entries per block (the ghost included
 constexpr int kWinGhost = kWinMax - 1;  // the window entry of the ghost slot
 constexpr int kWinPieces = 8;    // cell-slot ranges of a window
 constexpr int kWLen = 0, kWStart = 1, kWOff = kWStart + kWinPieces, kWCount = kWOff + kWinPieces,
-              kWGroups = kWCount + kWinPieces, kWCol0 = kWGroups + 1, kWTwo = kWCol0 + 1;
-constexpr int kWinInts = kWTwo + 1;  // ints of window data per block
+              kWGroups = kWCount + kWinPieces, kWCol0 = kWGroups + 1, kWTwo = kWCol0 + 1, kWRow0 = kWTwo + 1,
+              kWRow1 = kWRow0 + kWinPieces;
+constexpr int kWinInts = kWRow1 + kWinPieces;  // ints of window data per block
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

@@ -172,6 +172,9 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
 #pragma unroll
     for (int p = 0; p < kWinPieces; p++) st[p] = off[p] = cnt[p] = 0;
     int acc = 0, ix = 0, two = 0;
+    int rs[kWinPieces], re[kWinPieces];
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) rs[p] = 0, re[p] = -1;
     if (ok) {
         const int cf = s.newCell[f], cl = s.newCell[l];
         ix = cf / ncy;
@@ -204,6 +207,8 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
         if (ok) {
 #pragma unroll
             for (int p = 0; p < kWinPieces; p++) {
+                rs[p] = ra[p];
+                re[p] = rb[p];
                 if (rb[p] < ra[p]) continue;
                 int nx = ix + (p >> 1) - 1;
                 if (nx < 0) nx += ncx;
@@ -228,6 +233,11 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
     out[kWGroups] = 0;
     out[kWCol0] = ix;
     out[kWTwo] = two;
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) {
+        out[kWRow0 + p] = ok ? rs[p] : 0;
+        out[kWRow1 + p] = ok ? re[p] : -1;
+    }
 }
 
 // The list build of the fast mode.  One thread per cell slot t builds the
@@ -447,8 +457,11 @@ __device__ __forceinline__ void flist_walk(const DevSys &s, bool fastw, bool sta
 // shared memory first.  The free particles' state then moves from the
 // scratch arrays to their new slots, with the constant arrays gathered from
 // the id-order originals.
-__global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int check) {
+__global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int check, int skip_windowed) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    // skip_windowed: k_flist_p builds the windowed blocks (block = step
+    // block: cell slots are storage slots without bonded particles)
+    if (skip_windowed && s.blockWin[kWinInts * (size_t)blockIdx.x + kWLen] >= 0) return;
     __shared__ float4 win[kLBlock / 32][kLWin];
     __shared__ int stage[kLBlock / 32][kLStage + 1][32];
     float2 *pos = parity ? s.pos1 : s.pos0;
@@ -561,12 +574,14 @@ __global__ void __launch_bounds__(kLBlock) k_flist(DevSys s, int parity, int che
         if (kmax > 0) atomicMax(&s.sc->maxCount, kmax);
         if (kmax > s.nbrCap) atomicOr(&s.sc->overflow, 1);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
+    if (!skip_windowed && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
     if (s.trace && lane == 0) {
         const int row = s.sc->obsRow - 1;
         if (row >= 0 && row < s.obsCap) atomicMax(&s.trace[(size_t)row * kTraceCols + 5], global_ns());
     }
 }
+
+static cudaError_t launch_flist_p(Launch &L, const DevSys &s, int parity, int check);
 
 cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int check) {
     cudaError_t e;
@@ -579,7 +594,13 @@ cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int che
     const int fb = (s.N + kFastBlock - 1) / kFastBlock;
     if ((e = L.kernel(k_fwindows, dim3((fb + kBlock - 1) / kBlock), dim3(kBlock), 0, s, check))) return e;
     const int nb = (s.N + kLBlock - 1) / kLBlock;
-    return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check);
+    if (s.nBonded == 0) {
+        // windowed step blocks through the persistent build, the rest here
+        static_assert(kLBlock == kFastBlock, "a list-build block is a step block");
+        if ((e = launch_flist_p(L, s, parity, check))) return e;
+        return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check, 1);
+    }
+    return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check, 0);
 }
 
 // ============================================================ step kernel
@@ -1292,6 +1313,326 @@ static cudaError_t fstep_p_image(Launch &L, const DevSys &s, int mode, int parit
     if (s.wrapx && s.wrapy) return launch_fstep_p<SIG1, true, true>(L, s, mode, parity, h, use_h);
     if (s.wrapx) return launch_fstep_p<SIG1, true, false>(L, s, mode, parity, h, use_h);
     return launch_fstep_p<SIG1, false, false>(L, s, mode, parity, h, use_h);
+}
+
+// ---- the persistent list build (systems without bonded particles).
+// The windowed step blocks' lists (k_fwindows) are built here, k_flist
+// builds the others.  A block holds kFastBlock consumer threads, one per
+// slot of a tile, and a producer warp; tiles blockIdx.x, blockIdx.x +
+// gridDim.x, ... pass through two shared-memory stages.  The producer's lane
+// 0 copies, with asynchronous bulk copies, a tile's window pieces of
+// cellSorted and the cell starts of the rows those pieces cover into a stage,
+// with a header (tile, window deltas, where each piece's cell starts sit).
+// A consumer finds its own particle in the window, walks its stencil
+// ranges there (the reference's float dr^2 <= (rc + skin)^2, as k_flist),
+// stages its entries (window indices) in its own column of a per-block
+// [entry][slot] array, stores them as 16-byte groups and copies the
+// reordered state of its slot back from the scratch arrays.  Waits are
+// bounded as in k_fstep_p.
+constexpr int kLPMinBlocks = 5;
+constexpr int kLPCs = 512;   // cell-start words per stage
+constexpr int kLPHdr = 32;   // header words per stage
+// header word offsets
+constexpr int kHT = 0, kHLen = 1, kHTwo = 2, kHCol0 = 3, kHCsOk = 4, kHDelta = 5, kHCsb = kHDelta + kWinPieces,
+              kHColp = kHCsb + kWinPieces;
+static_assert(kHColp + kWinPieces <= kLPHdr, "list-build stage header");
+
+__host__ __device__ constexpr size_t lp_stage_bytes() {
+    return (size_t)kLPHdr * 4 + (size_t)kLPCs * 4 + (size_t)kWinMax * sizeof(float4);
+}
+static size_t lp_smem() {
+    return 32 + 2 * lp_stage_bytes() + (size_t)(kLStage + 1) * kFastBlock * sizeof(unsigned short);
+}
+
+// the consumers' entry stage (window indices fit 16 bits): column = the
+// thread's slot in the tile
+struct TileStagePut {
+    unsigned short (*st)[kFastBlock];  // [kLStage + 1][kFastBlock]
+    int col;
+    __device__ __forceinline__ void put(bool hit, int val, int &k) const {
+        if (hit) st[min(k, kLStage)][col] = (unsigned short)val;
+        k += hit ? 1 : 0;
+    }
+};
+
+// Window candidates [wb, we) of a lane at p whose own window entry is self,
+// with the image shift (sx, sy) where SX / SY; the entry is the window
+// index.  The lane's own particle appears once among its ranges (no stencil
+// row of the lane repeats its own row), at entry self.
+template <bool SX, bool SY, class Put>
+__device__ __forceinline__ void lp_walk(const float4 *wc, int wb, int we, float sx, float sy, float2 p, int self,
+                                        float R2, const Put &out, int &k) {
+    wb = min(max(wb, 0), kWinMax);
+    we = min(max(we, wb), kWinMax);
+    auto one = [&](int w) {
+        const float4 e = wc[w];
+        const float dx = SX ? (p.x - e.x) - sx : p.x - e.x;
+        const float dy = SY ? (p.y - e.y) - sy : p.y - e.y;
+        const float dr2 = dx * dx + dy * dy;
+        out.put(dr2 <= R2 && w != self, w, k);
+    };
+    int w = wb;
+#pragma unroll 1
+    for (; w + 1 < we; w += 2) {
+        one(w);
+        one(w + 1);
+    }
+    if (w < we) one(w);
+}
+
+template <class Put>
+__device__ __forceinline__ void lp_range(const float4 *wc, int wb, int we, float sx, float sy, float2 p, int self,
+                                         float R2, const Put &out, int &k) {
+    if (sx == 0.0f && sy == 0.0f) lp_walk<false, false>(wc, wb, we, 0.0f, 0.0f, p, self, R2, out, k);
+    else lp_walk<true, true>(wc, wb, we, sx, sy, p, self, R2, out, k);
+}
+
+// All stencil ranges of a lane (cell (ix, iy), own column j of the tile).
+template <class Put>
+__device__ __forceinline__ void lp_stencil(const DevSys &s, const int *hd, const int *csm, const float4 *wc, int ix,
+                                           int iy, int j, float2 p, int self, const Put &out, int &k) {
+    const int ncx = s.ncx, ncy = s.ncy;
+    const float R2 = s.nnRadiusSq;
+    const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
+    const bool two = hd[kHTwo] != 0, csok = hd[kHCsOk] != 0;
+    // the cell start of row r of piece q's column
+    // (indices clamped to the staged words: a record that disagreed with the
+    // cells could give wrong entries, never an access outside the stage)
+    auto cs = [&](int q, int r) {
+        return csok ? csm[min(max(hd[kHCsb + q] + hd[kHColp + q] + r, 0), kLPCs - 1)]
+                    : __ldg(s.cellStart + hd[kHColp + q] + r);
+    };
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int pm = !two ? 2 * d : (j == 0 ? 2 * d + 1 : 2 * d + 2);
+        const int pw = !two ? 2 * d + 1 : (j == 0 ? 2 * d : 2 * d + 3);
+        const int nx = ix + d - 1;
+        const float sx = nx < 0 ? -Lx : (nx == ncx ? Lx : 0.0f);
+        const int dm = hd[kHDelta + pm], dw = hd[kHDelta + pw];
+        if (iy > 0 && iy < ncy - 1) {
+            lp_range(wc, cs(pm, iy - 1) + dm, cs(pm, iy + 2) + dm, sx, 0.0f, p, self, R2, out, k);
+        } else if (iy == 0) {
+            lp_range(wc, cs(pw, ncy - 1) + dw, cs(pw, ncy) + dw, sx, -Ly, p, self, R2, out, k);
+            lp_range(wc, cs(pm, 0) + dm, cs(pm, 2) + dm, sx, 0.0f, p, self, R2, out, k);
+        } else {
+            lp_range(wc, cs(pm, ncy - 2) + dm, cs(pm, ncy) + dm, sx, 0.0f, p, self, R2, out, k);
+            lp_range(wc, cs(pw, 0) + dw, cs(pw, 1) + dw, sx, Ly, p, self, R2, out, k);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int parity, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    float2 *pos = parity ? s.pos1 : s.pos0;
+    extern __shared__ float4 smem_f4[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(sm);
+    unsigned long long *empty = full + 2;
+    auto hdr_of = [&](int q) { return reinterpret_cast<int *>(sm + 32 + q * lp_stage_bytes()); };
+    auto cs_of = [&](int q) { return reinterpret_cast<int *>(sm + 32 + q * lp_stage_bytes() + kLPHdr * 4); };
+    auto wc_of = [&](int q) {
+        return reinterpret_cast<float4 *>(sm + 32 + q * lp_stage_bytes() + kLPHdr * 4 + kLPCs * 4);
+    };
+    unsigned short(*ost)[kFastBlock] =
+        reinterpret_cast<unsigned short(*)[kFastBlock]>(sm + 32 + 2 * lp_stage_bytes());
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], kFastBlock / 32);
+        mbar_init(&empty[1], kFastBlock / 32);
+        if (blockIdx.x == 0) atomicAdd(&s.sc->builds, 1ull);
+    }
+    __syncthreads();
+    if (threadIdx.x >= kFastBlock) {
+        // the producer
+        if (threadIdx.x == kFastBlock) {
+            const int ncx = s.ncx, ncy = s.ncy;
+            int k = 0;
+            bool live = true;
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
+                const int st = k & 1, use = k >> 1;
+                if (use > 0) {
+                    live = mbar_wait_sleep(&empty[st], (use - 1) & 1, kSleepLimit, kSleepNs) &&
+                           mbar_wait_sleep(&full[st], (use - 1) & 1, kSleepLimit, kSleepNs);
+                    if (!live) {
+                        atomicOr(&s.sc->overflow, kFlagTimeout);
+                        break;
+                    }
+                }
+                const int *bw = s.blockWin + kWinInts * (size_t)t;
+                int *hd = hdr_of(st);
+                const int len = bw[kWLen];
+                hd[kHT] = t;
+                hd[kHLen] = len;
+                if (len < 0) {
+                    mbar_expect_tx(&full[st], 0u);  // a block k_flist builds
+                    continue;
+                }
+                const int col0 = bw[kWCol0];
+                hd[kHTwo] = bw[kWTwo];
+                hd[kHCol0] = col0;
+                // first pass: sizes, where each piece's cell starts go
+                int used = 0;
+                unsigned total = 0;
+                int a0s[kWinPieces], nws[kWinPieces];
+#pragma unroll
+                for (int p = 0; p < kWinPieces; p++) {
+                    int nx = col0 + (p >> 1) - 1;
+                    if (nx < 0) nx += ncx;
+                    else if (nx >= ncx) nx -= ncx;
+                    const int colp = nx * ncy;
+                    const int ra = bw[kWRow0 + p], rb = bw[kWRow1 + p];
+                    hd[kHColp + p] = colp;
+                    hd[kHDelta + p] = bw[kWOff + p] - bw[kWStart + p];
+                    a0s[p] = 0;
+                    nws[p] = 0;
+                    if (rb >= ra) {
+                        const int a0 = (colp + ra) & ~3, e0 = (colp + rb + 2 + 3) & ~3;
+                        a0s[p] = a0;
+                        nws[p] = e0 - a0;
+                        hd[kHCsb + p] = used - a0;
+                        used += e0 - a0;
+                    }
+                    total += (unsigned)bw[kWCount + p] * 16u;
+                }
+                const bool csok = used <= kLPCs;
+                hd[kHCsOk] = csok ? 1 : 0;
+                if (csok) total += (unsigned)used * 4u;
+                mbar_expect_tx(&full[st], total);
+                int *csm = cs_of(st);
+                float4 *wc = wc_of(st);
+#pragma unroll
+                for (int p = 0; p < kWinPieces; p++) {
+                    const int c = bw[kWCount + p];
+                    if (c > 0)
+                        bulk_copy_g2s(wc + bw[kWOff + p], s.cellSorted + bw[kWStart + p], (unsigned)c * 16u,
+                                      &full[st]);
+                    if (csok && nws[p] > 0)
+                        bulk_copy_g2s(csm + (hd[kHCsb + p] + a0s[p]), s.cellStart + a0s[p], (unsigned)nws[p] * 4u,
+                                      &full[st]);
+                }
+            }
+            if (!live) {
+                for (int kl = k - 2; kl < k; kl++)
+                    if (kl >= 0) mbar_wait_sleep(&full[kl & 1], (kl >> 1) & 1, kSleepLimit, kSleepNs);
+            }
+        }
+        __syncwarp();
+        return;
+    }
+    // the consumers
+    const int lane = threadIdx.x & 31;
+    const int cap = s.nbrCap;
+    TileStagePut sp;
+    sp.st = ost;
+    sp.col = threadIdx.x;
+    for (int t = blockIdx.x, k = 0; t < ntiles; t += gridDim.x, k++) {
+        const int st = k & 1;
+        if (!mbar_wait_sleep(&full[st], (k >> 1) & 1, kSleepLimit, kSleepNs)) {
+            atomicOr(&s.sc->overflow, kFlagTimeout);
+            break;
+        }
+        const int *hd = hdr_of(st);
+        if (hd[kHLen] < 0) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            continue;
+        }
+        const int slot = t * kFastBlock + threadIdx.x;
+        const bool valid = slot < s.N;
+        // the reordered state of the slot, back from the scratch arrays
+        // (loaded now, stored at the end)
+        const int sl = valid ? slot : 0;
+        const int id = __ldg(s.sPerm + sl);
+        const float2 np = __ldg(s.sPos + sl), nv = __ldg(s.sVel + sl), na = __ldg(s.sAcc + sl);
+        const int *csm = cs_of(st);
+        const float4 *wc = wc_of(st);
+        const bool two = hd[kHTwo] != 0;
+        // the lane's cell column in the tile: the upper column's slots
+        // start at row 0 of window column 2 (piece 4)
+        int j = 0;
+        if (two) {
+            const int bnd = hd[kHCsOk] ? csm[min(max(hd[kHCsb + 4] + hd[kHColp + 4], 0), kLPCs - 1)]
+                                       : __ldg(s.cellStart + hd[kHColp + 4]);
+            j = slot >= bnd ? 1 : 0;
+        }
+        const int pown = !two ? 2 : (j == 0 ? 3 : 4);
+        int kk = 0;
+        if (valid) {
+            const int self = min(max(slot + hd[kHDelta + pown], 0), kWinMax - 1);
+            const float4 me = wc[self];
+            int ix, iy;
+            cell_xy(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
+            const float2 p = make_float2(me.x, me.y);
+            lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, sp, kk);
+            if (kk > kLStage && cap > kLStage) {
+                DirectPut dp;
+                dp.nbr = s.nbr;
+                dp.slot = slot;
+                dp.cap = cap;
+                dp.Ncap = s.Ncap;
+                int k2 = 0;
+                lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, dp, k2);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+        // the stage to the list: group g of every lane in one store per g
+        const int kc = valid ? min(kk, cap) : 0;
+        const int ng = (kc + 3) >> 2;
+        const int ngs = min(ng, kLStage / 4);
+        const int gmax = __reduce_max_sync(0xffffffffu, ngs);
+        int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
+        for (int g = 0; g < gmax; g++) {
+            if (g < ngs) {
+                int v[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) v[u] = 4 * g + u < kc ? (int)ost[4 * g + u][threadIdx.x] : kWinGhost;
+                out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        if (valid && kc > kLStage && (kc & 3))
+            for (int q = kc; q < 4 * ng; q++) s.nbr[nbr_at(q, slot, s.Ncap)] = kWinGhost;
+        if (valid) {
+            s.nbrCount[slot] = kk;
+            pos[slot] = np;
+            s.vel[slot] = nv;
+            s.acc[slot] = na;
+            s.perm[slot] = id;
+            const_cast<float *>(s.mass)[slot] = __ldg(s.idMass + id);
+            if (s.numTypes > 1) const_cast<int *>(s.typeId)[slot] = __ldg(s.idType + id);
+            if (!s.sigmaByType) const_cast<float *>(s.sigma)[slot] = __ldg(s.idSigma + id);
+            if (s.wallDelta) const_cast<float *>(s.wallDelta)[slot] = __ldg(s.idWallDelta + id);
+            if (s.wallSig) const_cast<float *>(s.wallSig)[slot] = __ldg(s.idWallSig + id);
+        }
+        const int gm = __reduce_max_sync(0xffffffffu, ng);
+        const int kmax = __reduce_max_sync(0xffffffffu, valid ? kk : 0);
+        const int ksum = __reduce_add_sync(0xffffffffu, valid ? kk : 0);
+        if (lane == 0) {
+            atomicMax(&s.blockWin[kWinInts * (size_t)t + kWGroups], gm);
+            if (ksum) atomicAdd(&s.sc->nbrSum, (unsigned long long)ksum);
+            if (kmax > 0) atomicMax(&s.sc->maxCount, kmax);
+            if (kmax > cap) atomicOr(&s.sc->overflow, 1);
+            if (s.trace) {
+                const int row = s.sc->obsRow - 1;
+                if (row >= 0 && row < s.obsCap) atomicMax(&s.trace[(size_t)row * kTraceCols + 5], global_ns());
+            }
+        }
+    }
+}
+
+static cudaError_t launch_flist_p(Launch &L, const DevSys &s, int parity, int check) {
+    const size_t smem = lp_smem();
+    cudaError_t e = cudaFuncSetAttribute(k_flist_p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    int dev = 0, sms = 0, per = 0;
+    if ((e = cudaGetDevice(&dev))) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flist_p, kPBlock, smem))) return e;
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    const int grid = std::max(1, std::min(ntiles, std::max(1, per) * sms));
+    return L.kernel(k_flist_p, dim3(grid), dim3(kPBlock), smem, s, parity, check);
 }
 
 template <bool MT, bool SG, bool SIG1>
