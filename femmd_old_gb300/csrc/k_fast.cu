@@ -159,11 +159,7 @@ __global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int 
 // cells, windows too large, grids the fast walk does not cover) keep global
 // storage slots.  The block's longest list (in groups) is gathered by the
 // list build.
-__global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
-    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nblk = (s.N + kFastBlock - 1) / kFastBlock;
-    if (b >= nblk) return;
+__device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
     int *out = s.blockWin + kWinInts * (size_t)b;
     const int f = b * kFastBlock, l = min(f + kFastBlock, s.N) - 1;
     const int ncy = s.ncy, ncx = s.ncx;
@@ -240,6 +236,12 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
     }
 }
 
+__global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
+    if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < (s.N + kFastBlock - 1) / kFastBlock) fwindow_record(s, b);
+}
+
 // The list build of the fast mode.  One thread per cell slot t builds the
 // list of the particle stored there (storage slot = its tag).  An entry is
 // the neighbour's storage slot, or -- for a particle of a windowed step
@@ -273,6 +275,18 @@ struct DirectPut {
     __device__ __forceinline__ void put(bool hit, int val, int &k) const {
         if (hit) {
             if (k >= kLStage && k < cap) nbr[nbr_at(k, slot, Ncap)] = val;
+            k++;
+        }
+    }
+};
+
+// Every entry written straight to the list (up to the capacity).
+struct ListPut {
+    int *nbr;
+    int slot, cap, Ncap;
+    __device__ __forceinline__ void put(bool hit, int val, int &k) const {
+        if (hit) {
+            if (k < cap) nbr[nbr_at(k, slot, Ncap)] = val;
             k++;
         }
     }
@@ -591,15 +605,12 @@ cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int che
     if ((e = L.kernel(k_fplace, dim3(pb), dim3(kBlock), 0, s, check))) return e;
     if (s.nBonded > 0 && (e = L.kernel(k_ffree_count, dim3(permb), dim3(kPermBlock), 0, s, check))) return e;
     if ((e = L.kernel(k_fperm, dim3(permb), dim3(kPermBlock), 0, s, parity, check))) return e;
+    // without bonded particles the persistent build makes the windows and
+    // every list itself
+    if (s.nBonded == 0) return launch_flist_p(L, s, parity, check);
     const int fb = (s.N + kFastBlock - 1) / kFastBlock;
     if ((e = L.kernel(k_fwindows, dim3((fb + kBlock - 1) / kBlock), dim3(kBlock), 0, s, check))) return e;
     const int nb = (s.N + kLBlock - 1) / kLBlock;
-    if (s.nBonded == 0) {
-        // windowed step blocks through the persistent build, the rest here
-        static_assert(kLBlock == kFastBlock, "a list-build block is a step block");
-        if ((e = launch_flist_p(L, s, parity, check))) return e;
-        return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check, 1);
-    }
     return L.kernel(k_flist, dim3(nb), dim3(kLBlock), 0, s, parity, check, 0);
 }
 
@@ -1447,9 +1458,13 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
     if (threadIdx.x >= kFastBlock) {
         // the producer
         if (threadIdx.x == kFastBlock) {
+            // the window record of a tile is made (fwindow_record) an
+            // iteration before its copies are issued, so its loads pass
+            // while the producer waits for a free stage
             const int ncx = s.ncx, ncy = s.ncy;
             int k = 0;
             bool live = true;
+            if (blockIdx.x < ntiles) fwindow_record(s, blockIdx.x);
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
                 const int st = k & 1, use = k >> 1;
                 if (use > 0) {
@@ -1465,8 +1480,10 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
                 const int len = bw[kWLen];
                 hd[kHT] = t;
                 hd[kHLen] = len;
+                const int tn = t + gridDim.x;
                 if (len < 0) {
-                    mbar_expect_tx(&full[st], 0u);  // a block k_flist builds
+                    mbar_expect_tx(&full[st], 0u);  // a block the consumers walk in global memory
+                    if (tn < ntiles) fwindow_record(s, tn);
                     continue;
                 }
                 const int col0 = bw[kWCol0];
@@ -1512,6 +1529,7 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
                         bulk_copy_g2s(csm + (hd[kHCsb + p] + a0s[p]), s.cellStart + a0s[p], (unsigned)nws[p] * 4u,
                                       &full[st]);
                 }
+                if (tn < ntiles) fwindow_record(s, tn);
             }
             if (!live) {
                 for (int kl = k - 2; kl < k; kl++)
@@ -1534,11 +1552,7 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
             break;
         }
         const int *hd = hdr_of(st);
-        if (hd[kHLen] < 0) {
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[st]);
-            continue;
-        }
+        const bool win = hd[kHLen] >= 0;
         const int slot = t * kFastBlock + threadIdx.x;
         const bool valid = slot < s.N;
         // the reordered state of the slot, back from the scratch arrays
@@ -1548,7 +1562,7 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
         const float2 np = __ldg(s.sPos + sl), nv = __ldg(s.sVel + sl), na = __ldg(s.sAcc + sl);
         const int *csm = cs_of(st);
         const float4 *wc = wc_of(st);
-        const bool two = hd[kHTwo] != 0;
+        const bool two = win && hd[kHTwo] != 0;
         // the lane's cell column in the tile: the upper column's slots
         // start at row 0 of window column 2 (piece 4)
         int j = 0;
@@ -1559,7 +1573,33 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
         }
         const int pown = !two ? 2 : (j == 0 ? 3 : 4);
         int kk = 0;
-        if (valid) {
+        if (!win) {
+            // no window: the lane's stencil straight from global memory,
+            // entries (storage slots) written straight to the list
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            if (valid) {
+                const float4 me = __ldg(s.cellSorted + slot);
+                int ix, iy;
+                cell_xy(me.x, me.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
+                const float2 p = make_float2(me.x, me.y);
+                ListPut lp;
+                lp.nbr = s.nbr;
+                lp.slot = slot;
+                lp.cap = cap;
+                lp.Ncap = s.Ncap;
+                if (fast_walk_ok(s)) {
+                    WinDelta wd;
+                    wd.win = false;
+                    wd.len = -1;
+#pragma unroll
+                    for (int d = 0; d < 3; d++) wd.dm[d] = wd.dw[d] = 0;
+                    flist_columns<false>(s, ix, iy, p, -1, slot, wd, lp, kk);
+                } else {
+                    flist_general(s, ix, iy, p, -1, slot, lp, kk);
+                }
+            }
+        } else if (valid) {
             const int self = min(max(slot + hd[kHDelta + pown], 0), kWinMax - 1);
             const float4 me = wc[self];
             int ix, iy;
@@ -1576,24 +1616,29 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
                 lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, dp, k2);
             }
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[st]);
-        // the stage to the list: group g of every lane in one store per g
         const int kc = valid ? min(kk, cap) : 0;
         const int ng = (kc + 3) >> 2;
-        const int ngs = min(ng, kLStage / 4);
-        const int gmax = __reduce_max_sync(0xffffffffu, ngs);
-        int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
-        for (int g = 0; g < gmax; g++) {
-            if (g < ngs) {
-                int v[4];
+        if (win) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            // the stage to the list: group g of every lane in one store per g
+            const int ngs = min(ng, kLStage / 4);
+            const int gmax = __reduce_max_sync(0xffffffffu, ngs);
+            int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
+            for (int g = 0; g < gmax; g++) {
+                if (g < ngs) {
+                    int v[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) v[u] = 4 * g + u < kc ? (int)ost[4 * g + u][threadIdx.x] : kWinGhost;
-                out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+                    for (int u = 0; u < 4; u++) v[u] = 4 * g + u < kc ? (int)ost[4 * g + u][threadIdx.x] : kWinGhost;
+                    out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+                }
             }
+            if (valid && kc > kLStage && (kc & 3))
+                for (int q = kc; q < 4 * ng; q++) s.nbr[nbr_at(q, slot, s.Ncap)] = kWinGhost;
+        } else if (valid) {
+            // unused words of the last group name the ghost slot
+            for (int q = kc; q < 4 * ng; q++) s.nbr[nbr_at(q, slot, s.Ncap)] = s.N;
         }
-        if (valid && kc > kLStage && (kc & 3))
-            for (int q = kc; q < 4 * ng; q++) s.nbr[nbr_at(q, slot, s.Ncap)] = kWinGhost;
         if (valid) {
             s.nbrCount[slot] = kk;
             pos[slot] = np;
