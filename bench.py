@@ -56,6 +56,17 @@ WORKLOADS = {
               "lattice), rho=0.8, rc=2.5, skin 0.3, dt=0.005, T=1", lambda: S.lj_fluid(n_side=1000)),
 }
 FORCE_MODES = {"fast": 1, "reference": 0}
+# workloads without bonded particles: the fast mode's persistent step and list
+# kernels apply (with bonded particles the reference-exact kernels are faster)
+UNBONDED = ("lj_fluid", "lj_1m")
+AUTO_RULE = "auto: fast mode without bonded particles, reference-exact mode with them"
+
+
+def resolve_mode(workload, mode):
+    """The force mode a workload runs in: 'auto' picks the faster kind."""
+    if mode != "auto":
+        return mode
+    return "fast" if workload in UNBONDED else "reference"
 BATCHED_DESC = ("batched ensemble: 512 independent LJ+elastomer replicas, atom counts log-uniform in [500, 20000] "
                 "(seed 8), density U(0.6, 0.85) and T U(0.1, 1.5) (seed 9), 90 % solvent + hex-ring disks, "
                 "dt=0.005, skin 0.3, one persistent launch per run() under a CUDA graph, autotuned block shape")
@@ -70,9 +81,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mixed", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--md-steps", type=int, default=100)
-    ap.add_argument("--force-mode", default="fast", choices=sorted(FORCE_MODES),
-                    help="fast: same sets, forces within 1e-5 of FP64, cell-ordered storage (default); "
-                         "reference: the reference's float operations and list order")
+    ap.add_argument("--force-mode", default="auto", choices=sorted(FORCE_MODES) + ["auto"],
+                    help="fast: same sets, forces within 1e-5 of FP64, cell-ordered storage; "
+                         "reference: the reference's float operations and list order; "
+                         "auto (default): fast without bonded particles, reference otherwise")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--probe", default=None,
                     choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras", "lj_1m",
@@ -270,8 +282,9 @@ def ours(args, dist):
     sc = make()
     sc.meta["types"] = max([a[0] for nm, a in sc.calls if nm == "set_numTypes"] or [1])
     dev = dist.local
+    mode = resolve_mode(args.workload, args.force_mode)
     s = F.System(dev)
-    s.set_force_mode(FORCE_MODES[args.force_mode])
+    s.set_force_mode(FORCE_MODES[mode])
     sc.replay(s)
     n = s.N
     md = args.md_steps
@@ -351,7 +364,7 @@ def ours(args, dist):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = kbytes / (kms / 1e3) / 1e9
-    fast = args.force_mode == "fast"
+    fast = mode == "fast"
     kname = "k_fstep" if fast else "k_step"
     traffic = load_traffic(kname, args.workload)
     what = ("fast mode: cell-ordered storage, windows in shared memory, fused multiply-adds, hardware "
@@ -377,7 +390,8 @@ def ours(args, dist):
                        "parallelism": "replicas" if dist.world > 1 else "single",
                        "l2": "L2 flushed between timed steps" if flush is not None else
                              "inputs larger than L2 (state + lists > 129 MB)",
-                       "image_mode": "exact", "fea_law": "neo-Hookean", "force_mode": args.force_mode},
+                       "image_mode": "exact", "fea_law": "neo-Hookean", "force_mode": mode,
+                       "force_mode_rule": AUTO_RULE if args.force_mode == "auto" else "requested"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     return line
 
@@ -390,7 +404,8 @@ def batched(args, dist):
     import torch
     dev = dist.local
     torch.cuda.set_device(dev)
-    scenes = S.batched_ensemble()
+    # several ranks split the ensemble (strong scaling: the total is fixed)
+    scenes = ensemble_share(S.batched_ensemble(), dist.world, dist.rank)
     systems = []
     b = F.Batch(dev)
     for sc in scenes:
@@ -419,7 +434,8 @@ def batched(args, dist):
     clocks = clk.stop()
     dist.barrier()
     t_max = dist.max(t_ms)
-    value = natoms * md * args.steps * dist.world / (t_max / 1e3)
+    natoms_all = int(dist.sum(natoms))
+    value = natoms_all * md * args.steps / (t_max / 1e3)
     rebuilds = sum(s.total_updates() for s in systems)
 
     # end to end: every replica's positions and velocities in from pinned host
@@ -438,8 +454,8 @@ def batched(args, dist):
             s.get_state_ptr(hp.data_ptr(), hv.data_ptr())
     torch.cuda.synchronize()
     e2e_s = dist.max(time.perf_counter() - t0)
-    e2e = {"value": natoms * md * args.steps * dist.world / e2e_s, "unit": "atom-steps/s",
-           "h2d_bytes_per_step": 16 * natoms, "d2h_bytes_per_step": 16 * natoms}
+    e2e = {"value": natoms_all * md * args.steps / e2e_s, "unit": "atom-steps/s",
+           "h2d_bytes_per_step": 16 * natoms_all, "d2h_bytes_per_step": 16 * natoms_all}
 
     # the plain form on the same replicas: one System.run per replica
     md_plain = max(1, min(md, 100))
@@ -482,9 +498,10 @@ def batched(args, dist):
     mixed_atoms = mix.N
     del mix
 
-    # opt-in tuning of the rebuild cadence and cell size (changes rounding,
-    # not physics), reported beside the reference-exact figure
-    tuned = b.autotune_lists(20, skins=(0.3, 0.45, 0.6), factors=(1.0,))
+    # the tuner's search over rebuild cadence (skin) and cell size (cell
+    # factor): it changes rounding, not physics, and is reported beside the
+    # reference-exact figure
+    tuned = b.autotune_lists(20, skins=(0.3, 0.45, 0.6), factors=(1.0, 1.2, 1.5))
     for _ in range(2):
         b.run(md)
     tms = []
@@ -504,10 +521,12 @@ def batched(args, dist):
     launches_per_run = 1
     return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched", "description": BATCHED_DESC, "replicas": len(systems),
-                       "atoms": natoms, "md_steps_per_step": md, "launch": launch, "autotune": tune,
-                       "rebuilds_last_run": rebuilds, "parallelism": "replicas" if dist.world > 1 else "single",
+            "higher_is_better": True, "scaling": "strong" if dist.world > 1 else "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched", "description": BATCHED_DESC, "replicas": len(S.batched_ensemble()),
+                       "replicas_this_rank": len(systems), "atoms": natoms_all, "md_steps_per_step": md,
+                       "launch": launch, "autotune": tune, "rebuilds_last_run": rebuilds,
+                       "parallelism": f"replicas split over {dist.world} ranks" if dist.world > 1 else "single",
                        "l2": "inputs larger than L2 (512 replicas' state + lists > 129 MB)"},
             "plain_same_atoms": {"value": plain_value, "unit": "atom-steps/s", "md_steps": md_plain,
                                  "how": "System.run on each replica in turn, wall clock"},
@@ -674,11 +693,36 @@ def probe(name, mode="fast"):
     print("ok", flush=True)
 
 
+def relaunch_cmd(gpus, argv):
+    """The command that runs this bench as one process per GPU (torchrun on
+    the loopback rendezvous with a free port)."""
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+
+
+def ensemble_share(scenes, world, rank):
+    """The replicas of an ensemble one rank advances: the atom counts split
+    over the ranks heaviest first (replicas.partition), the same split on
+    every rank without communication."""
+    from femmd_old_gb300.replicas import partition
+    if world <= 1:
+        return list(scenes)
+    mine = partition([int(sc.meta["N"]) for sc in scenes], world)[rank]
+    return [scenes[i] for i in sorted(mine)]
+
+
 def main():
     args = parse()
     if args.probe:
-        probe(args.probe, args.force_mode)
+        probe(args.probe, "fast" if args.force_mode == "auto" else args.force_mode)
         return
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: launch the ranks here when no launcher did
+        raise SystemExit(subprocess.call(relaunch_cmd(args.gpus, sys.argv[1:])))
     dist = Dist()
     try:
         if args.impl == "reference":
@@ -692,9 +736,11 @@ def main():
                 # the 1M-atom LJ fluid (the solvent class, where the HBM-roofline
                 # target is stated) and the headline system in the other force mode
                 keep = ("value", "unit", "ms_per_step", "roofline", "e2e", "gpu_launches", "clocks")
-                for key, wl, mode in (("lj_1m", "lj_1m", args.force_mode),
-                                      ("other_mode", "large_mixed",
-                                       "reference" if args.force_mode == "fast" else "fast")):
+                main_mode = resolve_mode("large_mixed", args.force_mode)
+                for key, wl, mode in (("lj_1m", "lj_1m", resolve_mode("lj_1m", args.force_mode)),
+                                      ("other_mode", "large_mixed", "reference" if main_mode == "fast" else "fast"),
+                                      ("lj_fluid", "lj_fluid", resolve_mode("lj_fluid", args.force_mode)),
+                                      ("suspension", "suspension", resolve_mode("suspension", args.force_mode))):
                     sub = argparse.Namespace(**vars(args))
                     sub.workload, sub.force_mode = wl, mode
                     sub.steps, sub.warmup, sub.no_cpu_baseline = max(3, min(args.steps, 10)), 3, True
