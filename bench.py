@@ -326,7 +326,13 @@ def ours(args, dist):
 
     # kernel launches inside the timed region
     has_tri = 1 if s.counts()["triangles"] else 0
-    rebuild_kernels = 7  # k_rebuild_begin, count, scan x2, scatter, cell sort, list build
+    bonded = s._vertex_count() > 0
+    if mode != "fast":
+        rebuild_kernels = 7  # k_rebuild_begin, count, scan x2, scatter, cell sort, list build
+    elif not bonded:
+        rebuild_kernels = 8  # k_rebuild_begin, count, scan x2, scatter, k_fplace, k_fperm, k_flist_p
+    else:
+        rebuild_kernels = 10  # + k_ffree_count, k_fwindows, k_flist in place of k_flist_p
     launches = args.steps * (1 + rebuild_kernels + (md + 1) * (1 + has_tri)) + rebuild_kernels * rebuilds
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -365,10 +371,12 @@ def ours(args, dist):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = kbytes / (kms / 1e3) / 1e9
     fast = mode == "fast"
-    kname = "k_fstep" if fast else "k_step"
+    kname = ("k_fstep" if bonded else "k_fstep_p") if fast else "k_step"
     traffic = load_traffic(kname, args.workload)
     what = ("fast mode: cell-ordered storage, windows in shared memory, fused multiply-adds, hardware "
-            "reciprocal" if fast else "reference-exact arithmetic and list order")
+            "reciprocal" + ("" if bonded else "; persistent, a producer warp stages list rows and windows by "
+                            "bulk asynchronous copies, packed float2 pair arithmetic")
+            if fast else "reference-exact arithmetic and list order")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic,
                 "kernel": f"{kname} (fused LJ+bond+triangle gather, leapfrog, fixed-point energy sums; {what})",
