@@ -603,6 +603,7 @@ def probe(name, mode="fast"):
         # one neighbour rebuild of the large mixed system after 200 steps,
         # inside the NVTX range "midrun", then run(12) launched directly
         s = F.System()
+        s.set_force_mode(FORCE_MODES[mode])
         S.large_mixed().replay(s)
         s.run(0)
         s.run(200)

@@ -229,7 +229,8 @@ struct femmd_ctx {
     int forceMode = FEMMD_FORCE_REFERENCE;
     DBuf<int> perm, sPerm, fBlockSums, ckPerm, idType, newCell;
     DBuf<int> blockWin;
-    DBuf<float2> sPos, sVel, sAcc;
+    DBuf<float2> sPos, sVel, sAcc, cpos0, cpos1;
+    DBuf<int> cslot;
     DBuf<float> idMass, idSigma, idWallDelta, idWallSig, xfer1;
     float imgD = 0;
 };
@@ -342,6 +343,7 @@ static void release_device(femmd_ctx *c) {
     c->propsUploaded = false;
     c->perm.release(); c->sPerm.release(); c->fBlockSums.release(); c->ckPerm.release(); c->idType.release();
     c->newCell.release(); c->blockWin.release(); c->sPos.release(); c->sVel.release(); c->sAcc.release();
+    c->cpos0.release(); c->cpos1.release(); c->cslot.release();
     c->idMass.release(); c->idSigma.release(); c->idWallDelta.release(); c->idWallSig.release(); c->xfer1.release();
     auto &a = c->adj;
     a.ckX.release(); a.ckV.release(); a.slots.release(); a.finalX.release(); a.finalV.release(); a.finalA.release();
@@ -523,6 +525,12 @@ static DevSys make_sys(femmd_ctx *c) {
         s.idWallSig = s.wallSig ? c->idWallSig.p : nullptr;
         s.newCell = c->newCell.p;
         s.blockWin = c->blockWin.p;
+        if (c->cslot.p) {
+            s.cpos0 = c->cpos0.p;
+            s.cpos1 = c->cpos1.p;
+            s.cslot = c->cslot.p;
+            s.cposOn = area ? 0 : 1;
+        }
     }
     return s;
 }
@@ -873,6 +881,15 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(ctx->fBlockSums.ensure((N + 1023) / 1024));
         CK(ctx->newCell.ensure(N));
         CK(ctx->blockWin.ensure(kWinInts * (size_t)((N + kFastBlock - 1) / kFastBlock)));
+        if (ctx->nBonded > 0) {
+            // the cell-ordered position mirror (slot N: the ghost)
+            CK(ctx->cpos0.ensure(N + 1)); CK(ctx->cpos1.ensure(N + 1)); CK(ctx->cslot.ensure(N));
+            static const float2 far = make_float2(3.0e15f, 3.0e15f);
+            CK(cudaMemcpyAsync(ctx->cpos0.p + N, &far, sizeof(float2), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(ctx->cpos1.p + N, &far, sizeof(float2), cudaMemcpyHostToDevice, s));
+        } else {
+            ctx->cpos0.release(); ctx->cpos1.release(); ctx->cslot.release();
+        }
         CK(ctx->idMass.ensure(N)); CK(ctx->idType.ensure(N)); CK(ctx->idSigma.ensure(ctx->sigmaByType ? 1 : N));
         CK(cudaMemcpyAsync(ctx->idMass.p, ctx->mass.data(), N * sizeof(float), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->idType.p, ctx->type.data(), N * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1862,6 +1879,7 @@ femmd_status femmd_set_gravity(femmd_ctx *ctx, double g) {
 // springs, otherwise they are disabled (the stored value is kept)
 femmd_status femmd_set_karea(femmd_ctx *ctx, double k) {
     NEED(ctx);
+    const bool was = ctx->areaForces;
     if (k > 0) {
         ctx->kArea = (float)k;
         ctx->areaForces = true;
@@ -1870,6 +1888,15 @@ femmd_status femmd_set_karea(femmd_ctx *ctx, double k) {
     }
     ctx->forcesValid = false;
     release_graphs(ctx);
+    if (was && !ctx->areaForces && fast_mode(ctx) && ctx->cslot.p && ctx->listBuilt && !ctx->topoDirty &&
+        !ctx->stateDirty) {
+        // the mirror was not kept while the springs moved vertices: bring it
+        // up to the current positions
+        DevSys ds = make_sys(ctx);
+        Launch L;
+        L.stream = ctx->stream;
+        CK(enqueue_cpos_refresh(L, ds, ctx->cur));
+    }
     return FEMMD_OK;
 }
 
@@ -2508,8 +2535,8 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     // (a windowed block's entry is an index into its window's cell slots)
     auto fast_entry = [&](int r, int q) -> int {
         const int *b = &bw[kWinInts * (size_t)(r / kFastBlock)];
-        const int w = raw[nbr_at(q, r, ctx->Ncap)];
-        if (b[kWLen] < 0) return w & kIdMask;
+        const int w = raw[nbr_at(q, r, ctx->Ncap)] & kIdMask;  // (the high bits: the neighbour's type)
+        if (b[kWLen] < 0) return w;
         for (int p = 0; p < kWinPieces; p++)
             if (w >= b[kWOff + p] && w < b[kWOff + p] + b[kWCount + p])
                 return cellIds[b[kWStart + p] + (w - b[kWOff + p])];

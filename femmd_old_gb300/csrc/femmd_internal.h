@@ -167,6 +167,14 @@ struct DevSys {
     // p covers (row1 < row0: none).  The window's last entry, kWinGhost, is
     // the ghost's.
     int *newCell;   // cell of the particle at each storage slot
+    // With bonded particles (whose storage slots never move) the storage order
+    // is not the cell order; cpos0/cpos1 mirror pos0/pos1 in cell-slot order
+    // (written by the rebuild and by every drift; cslot: the cell slot of each
+    // storage slot), so that every window is one bulk copy.  cposOn: the
+    // mirror is current (off while area springs move vertices in place).
+    float2 *cpos0, *cpos1;
+    int *cslot;
+    int cposOn;
     int *blockWin;
 };
 
@@ -215,6 +223,7 @@ cudaError_t enqueue_unpermute2(Launch &L, const DevSys &s, const float2 *in, flo
 cudaError_t enqueue_unpermute1(Launch &L, const DevSys &s, const float *in, float *out);
 cudaError_t enqueue_permute2(Launch &L, const DevSys &s, const float2 *in, float2 *out);
 cudaError_t enqueue_perm_identity(Launch &L, const DevSys &s);
+cudaError_t enqueue_cpos_refresh(Launch &L, const DevSys &s, int parity);
 cudaError_t enqueue_perm_consts(Launch &L, const DevSys &s);
 
 // ---- forces + integration (k_force.cu)

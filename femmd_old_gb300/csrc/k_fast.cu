@@ -133,6 +133,11 @@ __global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int 
     s.cellSorted[t] = make_float4(p.x, p.y, __int_as_float(tag), __int_as_float(s.excl[old]));
     s.sortedIds[t] = ns;
     s.newCell[ns] = s.cellOf[old];
+    if (s.cslot) {
+        // the cell-ordered mirror of the positions the next step reads
+        (parity ? s.cpos1 : s.cpos0)[t] = p;
+        s.cslot[ns] = t;
+    }
     if (fr) {
         s.sPos[ns] = p;
         s.sVel[ns] = s.vel[old];
@@ -318,12 +323,13 @@ __device__ __forceinline__ void fwalk(const float4 *cand, int qb, int qe, int qb
 #pragma unroll
         for (int u = 0; u < 4; u++)
             out.put(fhit<EX>(e[u], SX ? sx : 0.0f, sy, p, gi, R2, qbase + q + u, self),
-                    win ? q + u + dv : __float_as_int(e[u].z), k);
+                    win ? ((q + u + dv) | (__float_as_int(e[u].z) & ~kIdMask)) : __float_as_int(e[u].z), k);
     }
 #pragma unroll 1
     for (; q < qe; q++) {
         const float4 e = RO ? __ldg(cand + q) : cand[q];
-        out.put(fhit<EX>(e, SX ? sx : 0.0f, sy, p, gi, R2, qbase + q, self), win ? q + dv : __float_as_int(e.z), k);
+        out.put(fhit<EX>(e, SX ? sx : 0.0f, sy, p, gi, R2, qbase + q, self),
+                win ? ((q + dv) | (__float_as_int(e.z) & ~kIdMask)) : __float_as_int(e.z), k);
     }
 }
 
@@ -607,7 +613,7 @@ cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int che
     if ((e = L.kernel(k_fperm, dim3(permb), dim3(kPermBlock), 0, s, parity, check))) return e;
     // without bonded particles the persistent build makes the windows and
     // every list itself
-    if (s.nBonded == 0) return launch_flist_p(L, s, parity, check);
+    if (s.nBonded == 0 && s.numTypes == 1) return launch_flist_p(L, s, parity, check);
     const int fb = (s.N + kFastBlock - 1) / kFastBlock;
     if ((e = L.kernel(k_fwindows, dim3((fb + kBlock - 1) / kBlock), dim3(kBlock), 0, s, check))) return e;
     const int nb = (s.N + kLBlock - 1) / kLBlock;
@@ -726,11 +732,12 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
         for (int u = 0; u < 4; u++) {
             if (WIN) {
                 // masked to the window: a stray entry can name a wrong
-                // window slot but never one outside the shared arrays
-                e[u] = min((unsigned)e[u], (unsigned)(kWinMax - 1));
-                q[u] = wpos[e[u]];
-                if (MT) tj[u] = wtyp[e[u]];
-                if (SG) sj[u] = wsig[e[u]];
+                // window slot but never one outside the shared arrays; the
+                // type travels in the entry's high bits
+                const int w = (int)min((unsigned)e[u] & (unsigned)kIdMask, (unsigned)(kWinMax - 1));
+                q[u] = wpos[w];
+                if (MT) tj[u] = (unsigned)e[u] >> kIdBits;
+                if (SG) sj[u] = wsig[w];
             } else {
                 const int j = MT ? (e[u] & kIdMask) : e[u];
                 q[u] = __ldg(pin + j);
@@ -820,7 +827,8 @@ __device__ __forceinline__ float fast_wrap(float x, float L) {
 // wrap, and the mass and velocity loaded by the caller.
 template <bool WX, bool WY>
 __device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, float2 pi, float m, float2 v,
-                                            float2 *pout, float fx, float fy, float ue, float we, float utri,
+                                            float2 *pout, float2 *cpout, float fx, float fy, float ue, float we,
+                                            float utri,
                                             float uwall, float &ue_out, float &we_out, float &ke, float &vvm,
                                             bool &bad) {
     ue *= 0.5f;
@@ -869,6 +877,7 @@ __device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, fl
             if (WX) x.x = fast_wrap(x.x, s.Lx);
             if (WY) x.y = fast_wrap(x.y, s.Ly);
             pout[i] = x;
+            if (cpout) cpout[s.cslot[i]] = x;  // the cell-ordered mirror
             s.vel[i] = v;
         }
     }
@@ -960,6 +969,7 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
                                                                      int rows) {
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
+    float2 *cpout = s.cposOn ? (parity ? s.cpos0 : s.cpos1) : nullptr;
     extern __shared__ float4 smem_f4[];
     const int nt = s.numTypes;
     const int ntab = MT ? nt * nt : 1;
@@ -972,7 +982,10 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
     const int *bw = s.blockWin + kWinInts * (size_t)blockIdx.x;
     const int len = bw[kWLen];
     const int b0 = blockIdx.x * kFastBlock;
-    const bool tmaWin = !MT && !SG && len >= 0 && s.nBonded == 0;
+    // the window is copied straight from the positions when cell slots are
+    // storage slots, else from their cell-ordered mirror
+    const bool tmaWin = !SG && len >= 0 && (s.nBonded == 0 || s.cposOn);
+    const float2 *wsrc = s.nBonded == 0 ? pin : (parity ? s.cpos1 : s.cpos0);
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -992,7 +1005,7 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
                 const int a = bw[kWStart + p], c = bw[kWCount + p];
                 if (c > 0) {
                     const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                    bulk_copy_g2s(wpos + bw[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u, bar);
+                    bulk_copy_g2s(wpos + bw[kWOff + p] - (a & 1), wsrc + a0, (unsigned)(e0 - a0) * 8u, bar);
                 }
             }
     }
@@ -1021,14 +1034,12 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
                 for (int w = threadIdx.x; w < c; w += kFastBlock) {
                     const int j = __ldg(s.sortedIds + st + w);
                     wpos[off + w] = __ldg(pin + j);
-                    if (MT) wtyp[off + w] = s.typeId[j];
                     if (SG) wsig[off + w] = s.sigma[j];
                 }
             }
         }
         if (threadIdx.x == 0) {
             wpos[kWinGhost] = __ldg(pin + s.N);  // the ghost slot's far position
-            if (MT) wtyp[kWinGhost] = 0;
             if (SG) wsig[kWinGhost] = 1.0f;
         }
     }
@@ -1065,7 +1076,7 @@ __global__ void __launch_bounds__(kFastBlock, kFastMinBlocks) k_fstep(DevSys s, 
                                                                fy, ue2, we2);
         }
     }
-    if (act) fast_finish<WX, WY>(s, i, mode, pi, m, v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke, vvm, bad);
+    if (act) fast_finish<WX, WY>(s, i, mode, pi, m, v, pout, cpout, fx, fy, ue2, we2, utri, uwall, ue, we, ke, vvm, bad);
     step_reduce<kFastBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
 }
 
@@ -1121,8 +1132,8 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
 __host__ __device__ constexpr size_t pstage_bytes(int rows) {
     return (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2);
 }
-__host__ __device__ constexpr size_t pstage_base() { return 32 + sizeof(PairEntry); }
-static size_t pstep_smem(int rows) { return pstage_base() + 2 * pstage_bytes(rows); }
+__host__ __device__ constexpr size_t pstage_base(int ntab) { return 32 + (size_t)ntab * sizeof(PairEntry); }
+static size_t pstep_smem(int rows, int ntab) { return pstage_base(ntab) + 2 * pstage_bytes(rows); }
 
 // A consumer's own particle data of one tile, loaded a tile ahead.
 struct PTile {
@@ -1144,22 +1155,28 @@ __device__ __forceinline__ PTile ptile_load(const DevSys &s, const float2 *__res
     return r;
 }
 
-template <bool SIG1, bool WX, bool WY>
+template <bool MT, bool SIG1, bool WX, bool WY>
 __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int mode, int parity,
                                                                  cudaGraphConditionalHandle h, int use_h, int rows) {
     const float2 *__restrict__ pin = parity ? s.pos1 : s.pos0;
     float2 *__restrict__ pout = parity ? s.pos0 : s.pos1;
+    float2 *cpout = s.cposOn ? (parity ? s.cpos0 : s.cpos1) : nullptr;
     extern __shared__ float4 smem_f4[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
     unsigned long long *full = reinterpret_cast<unsigned long long *>(sm);
     unsigned long long *empty = full + 2;
     PairEntry *tab = reinterpret_cast<PairEntry *>(sm + 32);
+    const int ntab = MT ? s.numTypes * s.numTypes : 1;
+    // window source: the positions when cell slots are storage slots, else
+    // their cell-ordered mirror
+    const float2 *wsrc = s.nBonded == 0 ? pin : (parity ? s.cpos1 : s.cpos0);
     const size_t sb = pstage_bytes(rows);
     // stage q's list rows and window (computed, not indexed from an array:
     // an array indexed by the stage number would live in local memory)
-    auto slist_of = [&](int q) { return reinterpret_cast<int4 *>(sm + pstage_base() + q * sb); };
+    const size_t base = pstage_base(ntab);
+    auto slist_of = [&](int q) { return reinterpret_cast<int4 *>(sm + base + q * sb); };
     auto wpos_of = [&](int q) {
-        return reinterpret_cast<float2 *>(sm + pstage_base() + q * sb + (size_t)rows * kFastBlock * sizeof(int4));
+        return reinterpret_cast<float2 *>(sm + base + q * sb + (size_t)rows * kFastBlock * sizeof(int4));
     };
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     if (threadIdx.x == 0) {
@@ -1167,7 +1184,7 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
         mbar_init(&full[1], 1);
         mbar_init(&empty[0], kFastBlock / 32);
         mbar_init(&empty[1], kFastBlock / 32);
-        tab[0] = s.pair[0];
+        if (!MT) tab[0] = s.pair[0];
         const float2 g = __ldg(pin + s.N);  // the ghost slot's far position
         wpos_of(0)[kWinGhost] = g;
         wpos_of(1)[kWinGhost] = g;
@@ -1176,6 +1193,8 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
             if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
         }
     }
+    if (MT)
+        for (int q = threadIdx.x; q < ntab; q += blockDim.x) tab[q] = s.pair[q];
     __syncthreads();
     float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
     bool bad = false;
@@ -1224,7 +1243,7 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                         const int a = wv[kWStart + p], c = wv[kWCount + p];
                         if (c > 0) {
                             const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
-                            bulk_copy_g2s(wpos_of(st) + wv[kWOff + p] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u,
+                            bulk_copy_g2s(wpos_of(st) + wv[kWOff + p] - (a & 1), wsrc + a0, (unsigned)(e0 - a0) * 8u,
                                           &full[st]);
                         }
                     }
@@ -1272,28 +1291,50 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                                       (WY && (cur.p.y < D || cur.p.y > s.Ly - D)));
             const bool img = __any_sync(0xffffffffu, near);
             if (act && ok) {
-                if (cur.len >= 0) {
+                if (MT) {
+                    // several types: the scalar loop, each pair's type from its entry
+                    if (cur.len >= 0) {
+                        if (img)
+                            fast_pairs<true, false, false, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st),
+                                                                               rows, pin, wpos_of(st), nullptr,
+                                                                               nullptr, fx, fy, ue2, we2);
+                        else
+                            fast_pairs<true, false, false, WX, WY, false, true>(s, tab, i, cur.p, cur.cnt,
+                                                                                slist_of(st), rows, pin, wpos_of(st),
+                                                                                nullptr, nullptr, fx, fy, ue2, we2);
+                    } else {
+                        if (img)
+                            fast_pairs<true, false, false, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt,
+                                                                                slist_of(st), rows, pin, wpos_of(st),
+                                                                                nullptr, nullptr, fx, fy, ue2, we2);
+                        else
+                            fast_pairs<true, false, false, WX, WY, false, false>(s, tab, i, cur.p, cur.cnt,
+                                                                                 slist_of(st), rows, pin,
+                                                                                 wpos_of(st), nullptr, nullptr, fx, fy,
+                                                                                 ue2, we2);
+                    }
+                } else if (cur.len >= 0) {
                     if (img)
-                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st), rows,
-                                                                           pin, wpos_of(st), nullptr, nullptr, fx, fy,
-                                                                           ue2, we2);
+                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st),
+                                                                           rows, pin, wpos_of(st), nullptr, nullptr,
+                                                                           fx, fy, ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st), fx,
-                                                  fy, ue2, we2);
+                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st),
+                                                  fx, fy, ue2, we2);
                 } else {
                     if (img)
                         fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist_of(st),
-                                                                            rows, pin, wpos_of(st), nullptr, nullptr, fx,
-                                                                            fy, ue2, we2);
+                                                                            rows, pin, wpos_of(st), nullptr, nullptr,
+                                                                            fx, fy, ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st), fx,
-                                                   fy, ue2, we2);
+                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
+                                                   wpos_of(st), fx, fy, ue2, we2);
                 }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);
             if (act)
-                fast_finish<WX, WY>(s, i, mode, cur.p, cur.m, cur.v, pout, fx, fy, ue2, we2, utri, uwall, ue, we, ke,
+                fast_finish<WX, WY>(s, i, mode, cur.p, cur.m, cur.v, pout, cpout, fx, fy, ue2, we2, utri, uwall, ue, we, ke,
                                     vvm, bad);
             t = tn;
         }
@@ -1301,12 +1342,12 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
     step_reduce<kPBlock>(s, mode, ue, we, ke, vvm, bad, h, use_h);
 }
 
-template <bool SIG1, bool WX, bool WY>
+template <bool MT, bool SIG1, bool WX, bool WY>
 static cudaError_t launch_fstep_p(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                                   int use_h) {
     const int rows = std::max(1, std::min(s.nbrCap / 4, kPRows));
-    const size_t smem = pstep_smem(rows);
-    auto kern = k_fstep_p<SIG1, WX, WY>;
+    const size_t smem = pstep_smem(rows, MT ? s.numTypes * s.numTypes : 1);
+    auto kern = k_fstep_p<MT, SIG1, WX, WY>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e) return e;
     int dev = 0, sms = 0, per = 0;
@@ -1318,12 +1359,12 @@ static cudaError_t launch_fstep_p(Launch &L, const DevSys &s, int mode, int pari
     return L.kernel(kern, dim3(grid), dim3(kPBlock), smem, s, mode, parity, h, use_h, rows);
 }
 
-template <bool SIG1>
+template <bool MT, bool SIG1>
 static cudaError_t fstep_p_image(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                                  int use_h) {
-    if (s.wrapx && s.wrapy) return launch_fstep_p<SIG1, true, true>(L, s, mode, parity, h, use_h);
-    if (s.wrapx) return launch_fstep_p<SIG1, true, false>(L, s, mode, parity, h, use_h);
-    return launch_fstep_p<SIG1, false, false>(L, s, mode, parity, h, use_h);
+    if (s.wrapx && s.wrapy) return launch_fstep_p<MT, SIG1, true, true>(L, s, mode, parity, h, use_h);
+    if (s.wrapx) return launch_fstep_p<MT, SIG1, true, false>(L, s, mode, parity, h, use_h);
+    return launch_fstep_p<MT, SIG1, false, false>(L, s, mode, parity, h, use_h);
 }
 
 // ---- the persistent list build (systems without bonded particles).
@@ -1688,15 +1729,21 @@ static cudaError_t fstep_image(Launch &L, const DevSys &s, int mode, int parity,
     return launch_fstep<MT, SG, SIG1, false, false>(L, s, mode, parity, h, use_h);
 }
 
+// The persistent kernel wherever every window can be one bulk copy (no
+// bonded particles, or their cell-ordered mirror current) and sigma comes by
+// type; one block per step block otherwise.
 cudaError_t enqueue_step_fast(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                               int use_h) {
     const bool mt = s.numTypes > 1, sg = !s.sigmaByType;
+    const bool persist = !sg && (s.nBonded == 0 || s.cposOn);
+    if (persist) {
+        if (mt) return fstep_p_image<true, false>(L, s, mode, parity, h, use_h);
+        return s.sigmaOne ? fstep_p_image<false, true>(L, s, mode, parity, h, use_h)
+                          : fstep_p_image<false, false>(L, s, mode, parity, h, use_h);
+    }
     if (mt) return sg ? fstep_image<true, true, false>(L, s, mode, parity, h, use_h)
                       : fstep_image<true, false, false>(L, s, mode, parity, h, use_h);
     if (sg) return fstep_image<false, true, false>(L, s, mode, parity, h, use_h);
-    if (s.nBonded == 0)
-        return s.sigmaOne ? fstep_p_image<true>(L, s, mode, parity, h, use_h)
-                          : fstep_p_image<false>(L, s, mode, parity, h, use_h);
     return s.sigmaOne ? fstep_image<false, false, true>(L, s, mode, parity, h, use_h)
                       : fstep_image<false, false, false>(L, s, mode, parity, h, use_h);
 }
@@ -1720,6 +1767,18 @@ __global__ void __launch_bounds__(kBlock) k_perm2(const int *perm, const float2 
 
 // The constant arrays in storage order from the id-order originals (with
 // ident: the storage order becomes the id order).
+// The cell-ordered mirror brought up to the current positions.
+__global__ void __launch_bounds__(kBlock) k_cpos_refresh(DevSys s, int parity) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.N) return;
+    (parity ? s.cpos1 : s.cpos0)[s.cslot[i]] = (parity ? s.pos1 : s.pos0)[i];
+}
+
+cudaError_t enqueue_cpos_refresh(Launch &L, const DevSys &s, int parity) {
+    if (!s.cslot || s.N == 0) return cudaSuccess;
+    return L.kernel(k_cpos_refresh, dim3((s.N + kBlock - 1) / kBlock), dim3(kBlock), 0, s, parity);
+}
+
 __global__ void __launch_bounds__(kBlock) k_perm_consts(DevSys s, int ident) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.N) return;

@@ -290,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_drift(DevSys s, int parity, int adva
     if (s.wrapx) p.x = wrap_coord(p.x, s.Lx);
     if (s.wrapy) p.y = wrap_coord(p.y, s.Ly);
     pout[i] = p;
+    if (s.cposOn) (parity ? s.cpos0 : s.cpos1)[s.cslot[i]] = p;  // the fast mode's cell-ordered mirror
     s.vel[i] = v;
 }
 
