@@ -525,6 +525,7 @@ static DevSys make_sys(femmd_ctx *c) {
         s.idWallSig = s.wallSig ? c->idWallSig.p : nullptr;
         s.newCell = c->newCell.p;
         s.blockWin = c->blockWin.p;
+        s.win16 = (c->nBonded == 0 && s.numTypes == 1 && s.sigmaByType) ? 1 : 0;
         if (c->cslot.p) {
             s.cpos0 = c->cpos0.p;
             s.cpos1 = c->cpos1.p;
@@ -2533,10 +2534,12 @@ femmd_status femmd_get_neighbors(femmd_ctx *ctx, int *nbr_start, int *nbr_list) 
     }
     // fast mode: entry q of the particle at storage slot r, as a storage slot
     // (a windowed block's entry is an index into its window's cell slots)
+    const bool win16 = fast_mode(ctx) && make_sys(ctx).win16;
+    const unsigned short *raw16 = reinterpret_cast<const unsigned short *>(raw.data());
     auto fast_entry = [&](int r, int q) -> int {
         const int *b = &bw[kWinInts * (size_t)(r / kFastBlock)];
-        const int w = raw[nbr_at(q, r, ctx->Ncap)] & kIdMask;  // (the high bits: the neighbour's type)
-        if (b[kWLen] < 0) return w;
+        if (b[kWLen] < 0) return raw[nbr_at(q, r, ctx->Ncap)] & kIdMask;  // (the high bits: the neighbour's type)
+        const int w = win16 ? (int)raw16[nbr16_at(q, r, ctx->Ncap)] : raw[nbr_at(q, r, ctx->Ncap)] & kIdMask;
         for (int p = 0; p < kWinPieces; p++)
             if (w >= b[kWOff + p] && w < b[kWOff + p] + b[kWCount + p])
                 return cellIds[b[kWStart + p] + (w - b[kWOff + p])];

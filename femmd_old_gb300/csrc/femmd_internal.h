@@ -61,6 +61,12 @@ constexpr int kFixFrac = 24;
 __host__ __device__ __forceinline__ size_t nbr_at(int k, int i, int Ncap) {
     return ((size_t)(k >> 2) * Ncap + i) * 4 + (k & 3);
 }
+// The same storage as 16-bit entries (the fast mode's windowed blocks with
+// win16): entry k of particle i at ((unsigned short *)nbr)[nbr16_at(k, i,
+// Ncap)], eight entries of a particle to one 16-byte group.
+__host__ __device__ __forceinline__ size_t nbr16_at(int k, int i, int Ncap) {
+    return ((size_t)(k >> 3) * Ncap + i) * 8 + (k & 7);
+}
 
 struct DevScalars {
     double U, W, KE, Ufea;          // last force evaluation (FP64 from the fixed-point sums)
@@ -175,6 +181,10 @@ struct DevSys {
     float2 *cpos0, *cpos1;
     int *cslot;
     int cposOn;
+    // win16: the entries of windowed step blocks are 16-bit window indices,
+    // eight to a 16-byte group (nbr16_at); one particle kind, sigma by type,
+    // no bonded particles.  Other blocks keep 32-bit entries (nbr_at).
+    int win16;
     int *blockWin;
 };
 

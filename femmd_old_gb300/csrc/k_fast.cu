@@ -262,7 +262,8 @@ __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
 // no count test per entry.
 constexpr int kLBlock = 128;  // threads per block of the list build
 constexpr int kLWin = 256;    // staged candidates per warp
-constexpr int kLStage = 48;   // list entries per lane staged in shared memory (a multiple of 4)
+constexpr int kLStage = 48;   // list entries per lane staged in shared memory (a multiple of 8)
+static_assert(kLStage % 8 == 0, "whole 16-bit groups in the stage");
 
 struct StagePut {
     int (*st)[32];  // [kLStage + 1][32]; row kLStage takes the misses
@@ -280,6 +281,18 @@ struct DirectPut {
     __device__ __forceinline__ void put(bool hit, int val, int &k) const {
         if (hit) {
             if (k >= kLStage && k < cap) nbr[nbr_at(k, slot, Ncap)] = val;
+            k++;
+        }
+    }
+};
+
+// Entries from kLStage on, straight to a list of 16-bit window entries.
+struct DirectPut16 {
+    unsigned short *nbr16;
+    int slot, cap, Ncap;
+    __device__ __forceinline__ void put(bool hit, int val, int &k) const {
+        if (hit) {
+            if (k >= kLStage && k < cap) nbr16[nbr16_at(k, slot, Ncap)] = (unsigned short)val;
             k++;
         }
     }
@@ -765,11 +778,12 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
 // other), the x and y differences in separate float2s.  The pairs inside
 // the cutoff are counted as sum ir2 r2 (each term 1 to within the
 // reciprocal's rounding, 0 outside the cutoff), the energy shift's weight.
-template <bool SIG1, bool WIN>
+template <bool SIG1, bool WIN, bool W16>
 __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &pe, int i, float2 pi, int cnt,
                                               const int4 *slist, int srows, const float2 *__restrict__ pin,
                                               const float2 *wpos, float &fx, float &fy, float &ue2, float &we2) {
-    const int ng = (cnt + 3) >> 2;
+    // W16: the group holds eight 16-bit window entries, worked as two halves
+    const int ng = W16 ? (cnt + 7) >> 3 : (cnt + 3) >> 2;
     const size_t row = (size_t)s.Ncap;
     const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
     const float rc2 = pe.rcut2;
@@ -778,15 +792,8 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
     const float2 xv = make_float2(pi.x, pi.x), yv = make_float2(pi.y, pi.y);
     const float2 z = make_float2(0.0f, 0.0f);
     float2 FX = z, FY = z, Av = z, Bv = z, Nv = z;
-#pragma unroll 1
-    for (int gi = 0; gi < ng; gi++) {
-        const int4 g =
-            gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
-        const int e[4] = {g.x, g.y, g.z, g.w};
-        float2 q[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-            q[u] = WIN ? wpos[min((unsigned)e[u], (unsigned)kWinGhost)] : __ldg(pin + e[u]);
+    // four neighbours, two pairs at a time
+    auto quad = [&](const float2 *q) {
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const float2 qa = q[2 * h], qb = q[2 * h + 1];
@@ -803,6 +810,30 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
             Bv = __fadd2_rn(Bv, ir6);
             Nv = __ffma2_rn(ir2, r2, Nv);
         }
+    };
+#pragma unroll 1
+    for (int gi = 0; gi < ng; gi++) {
+        const int4 g =
+            gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
+        if (W16) {
+            const unsigned wd[4] = {(unsigned)g.x, (unsigned)g.y, (unsigned)g.z, (unsigned)g.w};
+#pragma unroll
+            for (int hf = 0; hf < 2; hf++) {
+                const unsigned e[4] = {wd[2 * hf] & 0xffffu, wd[2 * hf] >> 16, wd[2 * hf + 1] & 0xffffu,
+                                       wd[2 * hf + 1] >> 16};
+                float2 q[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) q[u] = wpos[min(e[u], (unsigned)kWinGhost)];
+                quad(q);
+            }
+        } else {
+            const int e[4] = {g.x, g.y, g.z, g.w};
+            float2 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                q[u] = WIN ? wpos[min((unsigned)e[u], (unsigned)kWinGhost)] : __ldg(pin + e[u]);
+            quad(q);
+        }
     }
     fx += FX.x + FX.y;
     fy += FY.x + FY.y;
@@ -810,6 +841,34 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
     const float n = SIG1 ? Nv.x + Nv.y : (Nv.x + Nv.y) / pe.sig2;
     ue2 += __fmaf_rn(pe.eps4, A - B, pe.us * n);
     we2 += pe.eps48 * __fmaf_rn(-0.5f, B, A);
+}
+
+// The scalar pair loop over 16-bit window entries (warps at a periodic edge
+// of a win16 system: the exact image per pair).
+template <bool SIG1, bool WX, bool WY>
+__device__ __forceinline__ void fast_pairs16_img(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt,
+                                                 const int4 *slist, int srows, const float2 *wpos, float &fx,
+                                                 float &fy, float &ue2, float &we2) {
+    const int ng = (cnt + 7) >> 3;
+    const size_t row = (size_t)s.Ncap;
+    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
+    const PairEntry pe0 = tab[0];
+    float A = 0.0f, B = 0.0f, n = 0.0f, u2 = 0.0f, w2 = 0.0f;
+#pragma unroll 1
+    for (int gi = 0; gi < ng; gi++) {
+        const int4 g =
+            gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
+        const unsigned wd[4] = {(unsigned)g.x, (unsigned)g.y, (unsigned)g.z, (unsigned)g.w};
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const unsigned e = (u & 1) ? wd[u >> 1] >> 16 : wd[u >> 1] & 0xffffu;
+            const float2 q = wpos[min(e, (unsigned)kWinGhost)];
+            fpair<false, false, SIG1, WX, WY, true>(s, tab, pe0, 0, 0.0f, pi, q.x, q.y, 0, 0.0f, fx, fy, A, B, n, u2,
+                                                    w2);
+        }
+    }
+    ue2 += __fmaf_rn(pe0.eps4, A - B, pe0.us * n);
+    we2 += pe0.eps48 * __fmaf_rn(-0.5f, B, A);
 }
 
 // x wrapped into [0, L): one box length added or taken away, the reference's
@@ -1118,6 +1177,7 @@ static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity
 // further copy and waits (bounded) for those in flight before it leaves.
 constexpr int kPBlock = kFastBlock + 32;  // consumer threads + the producer warp
 constexpr int kPRows = 8;                 // list rows staged per tile (the rest read from global memory)
+constexpr int kPRows16 = 5;               // the same with 16-bit entries (40 entries)
 #ifndef FEMMD_FAST_PMINB
 #define FEMMD_FAST_PMINB 5
 #endif
@@ -1313,22 +1373,29 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                                                                                  wpos_of(st), nullptr, nullptr, fx, fy,
                                                                                  ue2, we2);
                     }
+                } else if (cur.len >= 0 && s.win16) {
+                    if (img)
+                        fast_pairs16_img<SIG1, WX, WY>(s, tab, i, cur.p, cur.cnt, slist_of(st), rows, wpos_of(st), fx,
+                                                       fy, ue2, we2);
+                    else
+                        fast_pairs_x2<SIG1, true, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
+                                                        wpos_of(st), fx, fy, ue2, we2);
                 } else if (cur.len >= 0) {
                     if (img)
                         fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st),
                                                                            rows, pin, wpos_of(st), nullptr, nullptr,
                                                                            fx, fy, ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin, wpos_of(st),
-                                                  fx, fy, ue2, we2);
+                        fast_pairs_x2<SIG1, true, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
+                                                         wpos_of(st), fx, fy, ue2, we2);
                 } else {
                     if (img)
                         fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist_of(st),
                                                                             rows, pin, wpos_of(st), nullptr, nullptr,
                                                                             fx, fy, ue2, we2);
                     else
-                        fast_pairs_x2<SIG1, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
-                                                   wpos_of(st), fx, fy, ue2, we2);
+                        fast_pairs_x2<SIG1, false, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
+                                                          wpos_of(st), fx, fy, ue2, we2);
                 }
             }
             __syncwarp();
@@ -1345,7 +1412,10 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
 template <bool MT, bool SIG1, bool WX, bool WY>
 static cudaError_t launch_fstep_p(Launch &L, const DevSys &s, int mode, int parity, cudaGraphConditionalHandle h,
                                   int use_h) {
-    const int rows = std::max(1, std::min(s.nbrCap / 4, kPRows));
+    // staged list rows: 16-byte groups of eight 16-bit entries (win16) or
+    // four 32-bit ones; longer lists read their last groups from global memory
+    const int rows = s.win16 ? std::max(1, std::min((s.nbrCap + 7) / 8, kPRows16))
+                             : std::max(1, std::min(s.nbrCap / 4, kPRows));
     const size_t smem = pstep_smem(rows, MT ? s.numTypes * s.numTypes : 1);
     auto kern = k_fstep_p<MT, SIG1, WX, WY>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1648,18 +1718,53 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
             const float2 p = make_float2(me.x, me.y);
             lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, sp, kk);
             if (kk > kLStage && cap > kLStage) {
-                DirectPut dp;
-                dp.nbr = s.nbr;
-                dp.slot = slot;
-                dp.cap = cap;
-                dp.Ncap = s.Ncap;
                 int k2 = 0;
-                lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, dp, k2);
+                if (s.win16) {
+                    DirectPut16 dp;
+                    dp.nbr16 = reinterpret_cast<unsigned short *>(s.nbr);
+                    dp.slot = slot;
+                    dp.cap = cap;
+                    dp.Ncap = s.Ncap;
+                    lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, dp, k2);
+                } else {
+                    DirectPut dp;
+                    dp.nbr = s.nbr;
+                    dp.slot = slot;
+                    dp.cap = cap;
+                    dp.Ncap = s.Ncap;
+                    lp_stencil(s, hd, csm, wc, ix, iy, j, p, self, dp, k2);
+                }
             }
         }
         const int kc = valid ? min(kk, cap) : 0;
-        const int ng = (kc + 3) >> 2;
-        if (win) {
+        // groups of the list: eight 16-bit window entries with win16, else
+        // four 32-bit entries
+        const bool w16 = win && s.win16;
+        const int ng = w16 ? (kc + 7) >> 3 : (kc + 3) >> 2;
+        if (w16) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            const int ngs = min(ng, kLStage / 8);
+            const int gmax = __reduce_max_sync(0xffffffffu, ngs);
+            int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
+            for (int g = 0; g < gmax; g++) {
+                if (g < ngs) {
+                    int v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int k0 = 8 * g + 2 * u;
+                        const unsigned lo = k0 < kc ? ost[k0][threadIdx.x] : kWinGhost;
+                        const unsigned hi = k0 + 1 < kc ? ost[k0 + 1][threadIdx.x] : kWinGhost;
+                        v[u] = (int)(lo | hi << 16);
+                    }
+                    out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+                }
+            }
+            if (valid && kc > kLStage && (kc & 7)) {
+                unsigned short *n16 = reinterpret_cast<unsigned short *>(s.nbr);
+                for (int q = kc; q < 8 * ng; q++) n16[nbr16_at(q, slot, s.Ncap)] = (unsigned short)kWinGhost;
+            }
+        } else if (win) {
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);
             // the stage to the list: group g of every lane in one store per g
