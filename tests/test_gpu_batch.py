@@ -179,3 +179,31 @@ def test_large_replicas_on_cta_pairs_match_alone(sizes, launch):
         b.run(41)
         for sc, s in zip(scs, systems):
             assert same(s, alone(sc, [60, 0, 41])), (split, s.N)
+
+
+def test_batched_replicas_match_the_oracle_directly():
+    """Three replicas of the ensemble's kind (LJ solvent plus hex-ring disks,
+    uneven sizes), advanced together by the batched kernel through run(60)
+    then run(41), against the oracle (the reference's CPU path restated, the
+    same exact image mode and log) running each replica alone: positions,
+    velocities, accelerations bit-identical, and the same rebuild count."""
+    from oracle import Oracle
+    scs = replicas(3, seed=2)
+    b = F.Batch(0)
+    systems = []
+    for sc in scs:
+        s = F.System(0)
+        sc.replay(s)
+        systems.append(s)
+        b.add(s)
+    b.run(60)
+    b.run(41)
+    for sc, s in zip(scs, systems):
+        o = Oracle(image_mode=1, log_mode=1)
+        sc.replay(o)
+        o.run(60)
+        o.run(41)
+        for a, c in ((s.positions(), o.positions()), (s.velocities(), o.velocities()),
+                     (s.accelerations(), o.accelerations())):
+            assert np.array_equal(G.bits(a), G.bits(c))
+        assert s.total_updates() == o.total_updates()

@@ -61,6 +61,24 @@ def test_noalloc_binning_matches_context_binning_on_consecutive_calls():
         assert np.array_equal(got_ids, ids)
 
 
+def test_noalloc_binning_matches_the_oracle():
+    """The same binning against the oracle's cells (the reference's CPU
+    updateCellsCPU restated) at the same positions, not only against the
+    context's own GPU binning."""
+    torch = pytest.importorskip("torch")
+    from oracle import Oracle
+    for sc in (S.suspension(n_side=4, rings=4, T=0.3), S.lj_fluid(n_side=40, seed_pos=7, seed_vel=8)):
+        pos, box, grid, _, _ = context_cells(sc)
+        o = Oracle(image_mode=1, log_mode=1)
+        sc.replay(o)
+        o.set_positions_array(pos)
+        o.build_nn()
+        ost, oids = o.cells()
+        got_st, got_ids = noalloc_cells(torch, pos, box, grid)
+        assert np.array_equal(got_st, ost)
+        assert np.array_equal(got_ids, oids)
+
+
 def header_limit(name):
     hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "femmd.h")
     m = re.search(r"#define\s+" + name + r"\s+\(?([0-9]+)\s*<<\s*([0-9]+)\)?", open(hdr).read())
