@@ -115,6 +115,9 @@ class _Solo:
     def max(self, x):
         return x
 
+    def sum(self, x):
+        return x
+
 
 # ------------------------------------------------------------------ clocks
 

@@ -100,3 +100,12 @@ def test_two_gloo_ranks_split_the_ensemble():
     assert total == want
     assert sorted(got[0] + got[1]) == list(range(512))
     assert not set(got[0]) & set(got[1])
+
+
+def test_single_process_stand_in_has_the_group_methods_the_bench_uses():
+    from femmd_old_gb300.replicas import Group
+    solo = bench._Solo()
+    for name in ("barrier", "max", "sum"):
+        assert callable(getattr(solo, name)) and callable(getattr(Group, name))
+    assert solo.sum(3.5) == 3.5 and solo.max(2.0) == 2.0
+    assert (solo.world, solo.rank, solo.local) == (1, 0, 0)
