@@ -202,6 +202,8 @@ struct femmd_ctx {
     DevScalars *hsc = nullptr;  // pinned mirror
     int obsCap = 0, obsRows = 0;
     GraphSet graphs[2][2];      // [parity][0: kGraphUnits units, 1: one unit]
+    GraphSet smallGraph;        // the small-system run's WHILE graph (fast mode)
+    bool smallGraphFailed = false;
     // profiling
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> forceEvents;
@@ -322,6 +324,7 @@ static void mark_topology(femmd_ctx *c) {
 static void release_graphs(femmd_ctx *c) {
     for (auto &p : c->graphs)
         for (auto &g : p) g.release();
+    c->smallGraph.release();
 }
 
 static void release_device(femmd_ctx *c) {
@@ -1139,8 +1142,78 @@ static femmd_status build_graph(femmd_ctx *ctx, GraphSet &gs, int parity, int un
     return FEMMD_OK;
 }
 
+// The run graph of a small fast-mode system: WHILE (steps left) { the
+// cooperative small run; IF (rebuild) { the rebuild on parity 0 } }.
+static femmd_status build_small_graph(femmd_ctx *ctx, const DevSys &s) {
+    GraphSet &gs = ctx->smallGraph;
+    gs.release();
+    CK(cudaGraphCreate(&gs.g, 0));
+    Launch L;
+    L.stream = ctx->stream;
+    L.graph = gs.g;
+    cudaGraphConditionalHandle hw;
+    CK(cudaGraphConditionalHandleCreate(&hw, gs.g, 1, cudaGraphCondAssignDefault));
+    Launch body;
+    CK(L.begin_while(hw, body));
+    cudaGraphConditionalHandle hif;
+    CK(cudaGraphConditionalHandleCreate(&hif, body.graph, 0, cudaGraphCondAssignDefault));
+    CK(enqueue_small_run(body, s, hw, hif));
+    Launch rb;
+    CK(body.begin_if(hif, rb));
+    CK(enqueue_rebuild(rb, s, 0, 1));
+    CK(cudaGraphInstantiate(&gs.x, gs.g, 0));
+    return FEMMD_OK;
+}
+
+// A run's middle steps of a small fast-mode system (small_run_fits): one
+// graph launch whose WHILE loop runs the cooperative small run (each launch
+// up to the step that calls for a rebuild) and the rebuild kernels between
+// them, with no host round trip.  Without that graph (not instantiable here)
+// the host loops over direct cooperative launches, waiting once per launch.
+static femmd_status small_units(femmd_ctx *ctx, const DevSys &s, int units) {
+    DevScalars *d = ctx->sc.p;
+    const size_t N = ctx->pos.size();
+    if (ctx->cur == 1) {
+        // the small run starts and ends on parity 0
+        CK(cudaMemcpyAsync(ctx->dpos0.p, ctx->dpos1.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+        ctx->cur = 0;
+    }
+    ctx->hsc->smallLeft = units;
+    CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(&d->sacc[0][0], 0, sizeof(d->sacc), ctx->stream));
+    CK(cudaMemsetAsync(&d->gbCount, 0, sizeof(unsigned), ctx->stream));
+    if (!ctx->smallGraphFailed && !ctx->smallGraph.x && build_small_graph(ctx, s) != FEMMD_OK) {
+        ctx->smallGraph.release();
+        ctx->smallGraphFailed = true;
+        cudaGetLastError();
+    }
+    if (ctx->smallGraph.x) {
+        CK(cudaGraphLaunch(ctx->smallGraph.x, ctx->stream));
+        return FEMMD_OK;
+    }
+    Launch L;
+    L.stream = ctx->stream;
+    for (int left = units; left > 0;) {
+        CK(launch_small_run(ctx->stream, s));
+        femmd_status st;
+        if ((st = read_scalars(ctx))) return st;
+        const int k = ctx->hsc->smallDone;
+        if (k <= 0 || ctx->hsc->smallLeft <= 0) {
+            if (ctx->hsc->rebuild) CK(enqueue_rebuild(L, s, 0, 1));
+            break;
+        }
+        left = ctx->hsc->smallLeft;
+        if (ctx->hsc->rebuild) CK(enqueue_rebuild(L, s, 0, 1));
+    }
+    return FEMMD_OK;
+}
+
 static femmd_status launch_units(femmd_ctx *ctx, int units, bool use_graphs) {
     if (units <= 0) return FEMMD_OK;
+    if (use_graphs && !ctx->propAvg) {
+        const DevSys s = make_sys(ctx);
+        if (small_run_fits(s)) return small_units(ctx, s, units);
+    }
     if (!use_graphs) {
         DevSys s = make_sys(ctx);
         Launch L;

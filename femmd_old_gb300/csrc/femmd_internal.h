@@ -78,6 +78,12 @@ struct DevScalars {
     unsigned long long nbrSum, builds;
     unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
     unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
+    // the small-system run (k_fsmall): per-step sums in three rotating sets
+    // {U, W, K, max v^2 bits}, the grid barrier's arrival count and
+    // generation, and the steps one launch advanced
+    unsigned long long sacc[3][4];
+    unsigned int gbCount, gbGen;
+    int smallDone, smallLeft;
 };
 
 enum StepMode { MODE_FORCES = 0, MODE_FIRST = 1, MODE_MID = 2, MODE_LAST = 3, MODE_INIT = 4 };
@@ -234,6 +240,14 @@ cudaError_t enqueue_unpermute1(Launch &L, const DevSys &s, const float *in, floa
 cudaError_t enqueue_permute2(Launch &L, const DevSys &s, const float2 *in, float2 *out);
 cudaError_t enqueue_perm_identity(Launch &L, const DevSys &s);
 cudaError_t enqueue_cpos_refresh(Launch &L, const DevSys &s, int parity);
+// The small-system run (k_fsmall): whether a system qualifies (fast mode, one
+// kind, no bonded particles, walls or gravity, XY-periodic, few step blocks,
+// every block resident), and one cooperative launch of up to 'steps' middle
+// steps, ending after a step that calls for a rebuild.
+bool small_run_fits(const DevSys &s);
+cudaError_t launch_small_run(cudaStream_t st, const DevSys &s);
+cudaError_t enqueue_small_run(Launch &L, const DevSys &s, cudaGraphConditionalHandle hw,
+                              cudaGraphConditionalHandle hif);
 cudaError_t enqueue_perm_consts(Launch &L, const DevSys &s);
 
 // ---- forces + integration (k_force.cu)

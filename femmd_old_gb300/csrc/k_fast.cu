@@ -708,7 +708,10 @@ __device__ __forceinline__ void fpair(const DevSys &s, const PairEntry *tab, con
 // pin.  Unused words of the last group name the ghost, so no entry needs a
 // count test.  Energy and virial come back doubled (per ordered pair), as
 // the reference-exact kernel's.
-template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG, bool WIN>
+// NC: the positions stay unchanged for the whole launch, so their gathers
+// may take the non-coherent path; otherwise (the small-system run, where
+// other blocks write them between steps) they are read from L2.
+template <bool MT, bool SG, bool SIG1, bool WX, bool WY, bool IMG, bool WIN, bool NC = true>
 __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt,
                                            const int4 *slist, int srows, const float2 *__restrict__ pin,
                                            const float2 *wpos,
@@ -753,7 +756,7 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
                 if (SG) sj[u] = wsig[w];
             } else {
                 const int j = MT ? (e[u] & kIdMask) : e[u];
-                q[u] = __ldg(pin + j);
+                q[u] = NC ? __ldg(pin + j) : __ldcg(pin + j);
                 if (MT) tj[u] = (unsigned)e[u] >> kIdBits;
                 if (SG) sj[u] = __ldg(s.sigma + j);
             }
@@ -778,7 +781,7 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
 // other), the x and y differences in separate float2s.  The pairs inside
 // the cutoff are counted as sum ir2 r2 (each term 1 to within the
 // reciprocal's rounding, 0 outside the cutoff), the energy shift's weight.
-template <bool SIG1, bool WIN, bool W16>
+template <bool SIG1, bool WIN, bool W16, bool NC = true>
 __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &pe, int i, float2 pi, int cnt,
                                               const int4 *slist, int srows, const float2 *__restrict__ pin,
                                               const float2 *wpos, float &fx, float &fy, float &ue2, float &we2) {
@@ -831,7 +834,8 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
             float2 q[4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
-                q[u] = WIN ? wpos[min((unsigned)e[u], (unsigned)kWinGhost)] : __ldg(pin + e[u]);
+                q[u] = WIN ? wpos[min((unsigned)e[u], (unsigned)kWinGhost)]
+                           : (NC ? __ldg(pin + e[u]) : __ldcg(pin + e[u]));
             quad(q);
         }
     }
@@ -1832,6 +1836,289 @@ static cudaError_t fstep_image(Launch &L, const DevSys &s, int mode, int parity,
     if (s.wrapx && s.wrapy) return launch_fstep<MT, SG, SIG1, true, true>(L, s, mode, parity, h, use_h);
     if (s.wrapx) return launch_fstep<MT, SG, SIG1, true, false>(L, s, mode, parity, h, use_h);
     return launch_fstep<MT, SG, SIG1, false, false>(L, s, mode, parity, h, use_h);
+}
+
+// ---- the small-system run (one particle kind, sigma by type, no bonded
+// particles, walls, gravity or area springs; a few step blocks).  At this
+// size a step kernel lasts a few microseconds and the graph's conditional
+// node and launch cost as much again, so k_fsmall advances a run's middle
+// steps in one cooperative launch: one block per step block, the block's list
+// rows kept in shared memory (no rebuild happens inside a launch), per step
+// the window gathered, the pair terms and the leapfrog of k_fstep_p, the
+// block's energy sums into one of three rotating fixed-point sums, then a
+// bounded grid barrier after which every block takes the same rebuild
+// decision from the same sums.  The launch ends after the step that calls
+// for a rebuild (the host rebuilds and launches again) or after 'steps'
+// steps; the number done goes to DevScalars::smallDone.
+constexpr int kSmallMaxTiles = 128;  // step blocks of the largest system run this way
+constexpr int kGridSpin = 1 << 21;   // polls (about 64 ns each) before a grid barrier gives up
+
+// A bounded grid barrier of nblocks co-resident blocks (generation counter):
+// false on every block that gave up waiting.
+__device__ __forceinline__ bool grid_barrier(DevScalars *sc, unsigned nblocks, int *okflag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &sc->gbGen;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&sc->gbCount, 1u) == nblocks - 1) {
+            sc->gbCount = 0;
+            __threadfence();
+            atomicAdd(&sc->gbGen, 1u);
+        } else {
+            int it = 0;
+            while (*gen == g && it < kGridSpin) {
+                __nanosleep(64);
+                it++;
+            }
+            ok = *gen != g;
+        }
+        __threadfence();
+        *okflag = ok;
+    }
+    __syncthreads();
+    return *okflag != 0;
+}
+
+__host__ __device__ constexpr size_t small_smem(int rows) {
+    return 128 + (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2);
+}
+
+// Steps come from DevScalars::smallLeft; a launch starts and ends with the
+// positions in pos0 (parity 0), so that the rebuild that may follow it has a
+// fixed parity.  use_h: inside the run graph, set its WHILE (steps left) and
+// IF (rebuild) conditions.
+template <bool SIG1, bool WX, bool WY>
+__global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cudaGraphConditionalHandle hw,
+                                                          cudaGraphConditionalHandle hif, int use_h) {
+    extern __shared__ float4 smem_f4[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
+    PairEntry *tab = reinterpret_cast<PairEntry *>(sm);
+    int *flag = reinterpret_cast<int *>(sm + 32);   // [0] barrier ok, [1] rebuild
+    float *dsh = reinterpret_cast<float *>(sm + 40);  // the step's dispHi
+    float *red = reinterpret_cast<float *>(sm + 48);  // [warp][4]
+    int4 *slist = reinterpret_cast<int4 *>(sm + 128);
+    float2 *wpos = reinterpret_cast<float2 *>(sm + 128 + (size_t)rows * kFastBlock * sizeof(int4));
+    DevScalars *sc = s.sc;
+    const int t = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i = t * kFastBlock + threadIdx.x;
+    const bool act = i < s.N;
+    const int ic = act ? i : 0;
+    if (threadIdx.x == 0) tab[0] = s.pair[0];
+    // the block's lists and window record hold for the whole launch
+    const int *bw = s.blockWin + kWinInts * (size_t)t;
+    const int len = bw[kWLen];
+    const int G = min(bw[kWGroups], rows);
+    const int4 *lrow = reinterpret_cast<const int4 *>(s.nbr) + (size_t)t * kFastBlock + threadIdx.x;
+    if (i < s.Ncap)
+        for (int g = 0; g < G; g++) slist[g * kFastBlock + threadIdx.x] = __ldg(lrow + (size_t)g * s.Ncap);
+    const int cnt = act ? min(s.nbrCount[ic], s.nbrCap) : 0;
+    const float m = s.mass[ic];
+    const float D = s.imgD;
+    float dispHi = sc->dispHi;  // every block follows the same recurrence
+    int row = sc->obsRow, stepNow = sc->stepNow;
+    const int steps = sc->smallLeft;
+    int p = 0, k = 0;
+    bool reb = false, failed = false;
+    for (; k < steps;) {
+        const float2 *pin = p ? s.pos1 : s.pos0;
+        float2 *pout = p ? s.pos0 : s.pos1;
+        // the window, read from L2 (other blocks wrote it since the barrier)
+        if (len >= 0) {
+            for (int q = 0; q < kWinPieces; q++) {
+                const int st = bw[kWStart + q], off = bw[kWOff + q], c = bw[kWCount + q];
+                for (int w = threadIdx.x; w < c; w += kFastBlock) wpos[off + w] = __ldcg(pin + st + w);
+            }
+            if (threadIdx.x == 0) wpos[kWinGhost] = pin[s.N];
+        }
+        __syncthreads();
+        const float2 pi = pin[ic];
+        const float2 v = s.vel[ic];
+        float fx = 0.0f, fy = 0.0f, ue2 = 0.0f, we2 = 0.0f;
+        const bool near = act && ((WX && (pi.x < D || pi.x > s.Lx - D)) || (WY && (pi.y < D || pi.y > s.Ly - D)));
+        const bool img = __any_sync(0xffffffffu, near);
+        if (act) {
+            if (len >= 0 && s.win16) {
+                if (img) fast_pairs16_img<SIG1, WX, WY>(s, tab, i, pi, cnt, slist, rows, wpos, fx, fy, ue2, we2);
+                else fast_pairs_x2<SIG1, true, true, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
+                                                            ue2, we2);
+            } else if (len >= 0) {
+                if (img)
+                    fast_pairs<false, false, SIG1, WX, WY, true, true, false>(s, tab, i, pi, cnt, slist, rows, pin,
+                                                                              wpos, nullptr, nullptr, fx, fy, ue2,
+                                                                              we2);
+                else fast_pairs_x2<SIG1, true, false, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
+                                                             ue2, we2);
+            } else {
+                if (img)
+                    fast_pairs<false, false, SIG1, WX, WY, true, false, false>(s, tab, i, pi, cnt, slist, rows, pin,
+                                                                               wpos, nullptr, nullptr, fx, fy, ue2,
+                                                                               we2);
+                else fast_pairs_x2<SIG1, false, false, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
+                                                              ue2, we2);
+            }
+        }
+        float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
+        bool bad = false;
+        if (act)
+            fast_finish<WX, WY>(s, i, MODE_MID, pi, m, v, pout, nullptr, fx, fy, ue2, we2, 0.0f, 0.0f, ue, we, ke,
+                                vvm, bad);
+        // the block's sums into this step's set
+        const float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke), mx = warp_max(vvm);
+        const unsigned anybad = __ballot_sync(0xffffffffu, bad);
+        if (lane == 0) {
+            red[4 * warp + 0] = su;
+            red[4 * warp + 1] = sw;
+            red[4 * warp + 2] = sk;
+            red[4 * warp + 3] = mx;
+            if (anybad) atomicOr(&sc->nonfinite, 1);
+        }
+        __syncthreads();
+        const int set = k % 3;
+        if (threadIdx.x == 0) {
+            float a = 0.0f, b = 0.0f, c = 0.0f, mm = 0.0f;
+            for (int w = 0; w < kFastBlock / 32; w++) {
+                a += red[4 * w];
+                b += red[4 * w + 1];
+                c += red[4 * w + 2];
+                mm = fmaxf(mm, red[4 * w + 3]);
+            }
+            bool ob = false;
+            const unsigned long long qa = to_fixed(a, ob), qb = to_fixed(b, ob), qc = to_fixed(c, ob);
+            if (ob) atomicOr(&sc->nonfinite, 2);
+            if (qa) atomicAdd(&sc->sacc[set][0], qa);
+            if (qb) atomicAdd(&sc->sacc[set][1], qb);
+            if (qc) atomicAdd(&sc->sacc[set][2], qc);
+            if (mm > 0.0f) atomicMax(reinterpret_cast<unsigned *>(&sc->sacc[set][3]), __float_as_uint(mm));
+        }
+        if (!grid_barrier(sc, gridDim.x, flag)) {
+            if (threadIdx.x == 0) atomicOr(&sc->overflow, kFlagTimeout);
+            failed = true;
+            break;
+        }
+        // the step's totals, the same on every block: the rebuild rule of
+        // evalProps / NeighborList::update (md3dsystem.cpp:177, nn.cpp:118)
+        if (threadIdx.x == 0) {
+            const float vm2 = __uint_as_float(*(volatile unsigned *)&sc->sacc[set][3]);
+            const float d = dispHi + sqrtf(vm2) * s.dt;
+            const int r = (double)d > s.halfSkin;
+            flag[1] = r;
+            *dsh = d;
+            if (blockIdx.x == 0) {
+                const double U = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][0]);
+                const double W = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][1]);
+                const double KE = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][2]);
+                sc->U = U;
+                sc->W = W;
+                sc->KE = KE;
+                sc->vvMax = vm2;
+                if (s.obs && row < s.obsCap) {
+                    double *o = s.obs + (size_t)row * kObsCols;
+                    o[0] = U;
+                    o[1] = W;
+                    o[2] = KE;
+                    o[3] = (double)vm2;
+                    o[4] = (double)d;
+                    o[5] = (double)r;
+                }
+                // the set two steps on: every block read it after the last barrier
+                const int nxt = (k + 2) % 3;
+                for (int q = 0; q < 4; q++) sc->sacc[nxt][q] = 0ull;
+            }
+        }
+        __syncthreads();
+        dispHi = *dsh;
+        reb = flag[1] != 0;
+        row++;
+        stepNow++;
+        p ^= 1;
+        k++;
+        if (reb) break;
+    }
+    // back to parity 0 (each thread its own slot), then the sums cleared for
+    // the next launch once every block has read them
+    if (p == 1 && act) s.pos0[i] = s.pos1[i];
+    const bool fin = grid_barrier(sc, gridDim.x, flag);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!fin) atomicOr(&sc->overflow, kFlagTimeout);
+        for (int q = 0; q < 3; q++)
+            for (int c = 0; c < 4; c++) sc->sacc[q][c] = 0ull;
+        // a barrier that gave up ends the run's loop (FEMMD_TIMEOUT)
+        const int left = (k > 0 && fin && !failed) ? steps - k : 0;
+        sc->dispHi = dispHi;
+        sc->rebuild = reb ? 1 : 0;
+        sc->obsRow = row;
+        sc->stepNow = stepNow;
+        sc->smallDone = k;
+        sc->smallLeft = left;
+        if (use_h) {
+            cudaGraphSetConditional(hif, reb ? 1u : 0u);
+            cudaGraphSetConditional(hw, left > 0 ? 1u : 0u);
+        }
+    }
+}
+
+// Launch of the small-system run (cooperative: every block resident); the
+// caller has checked small_run_fits.
+template <bool SIG1, bool WX, bool WY>
+static cudaError_t launch_fsmall_t(cudaStream_t st, const DevSys &s, int rows) {
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    const size_t smem = small_smem(rows);
+    auto kern = k_fsmall<SIG1, WX, WY>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    DevSys a = s;
+    int ra = rows, ua = 0;
+    cudaGraphConditionalHandle h0 = 0, h1 = 0;
+    void *args[] = {&a, &ra, &h0, &h1, &ua};
+    return cudaLaunchCooperativeKernel((const void *)kern, dim3(ntiles), dim3(kFastBlock), args, smem, st);
+}
+
+bool small_run_fits(const DevSys &s) {
+    if (!s.fast || !s.win16 || s.nBonded != 0 || s.wallOn || s.gravity > 0.0f || s.refWalls || s.areaUnits > 0 ||
+        s.trace || s.N <= 0)
+        return false;
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    if (ntiles > kSmallMaxTiles) return false;
+    const int rows = std::max(1, (s.nbrCap + 7) / 8);
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) return false;
+    auto kern = s.sigmaOne ? (s.wrapx && s.wrapy ? k_fsmall<true, true, true> : nullptr)
+                           : (s.wrapx && s.wrapy ? k_fsmall<false, true, true> : nullptr);
+    if (!kern) return false;  // the small run is built for XY-periodic boxes
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem(rows)) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kFastBlock, small_smem(rows)))
+        return false;
+    return per * sms >= ntiles;
+}
+
+cudaError_t launch_small_run(cudaStream_t st, const DevSys &s) {
+    const int rows = std::max(1, (s.nbrCap + 7) / 8);
+    return s.sigmaOne ? launch_fsmall_t<true, true, true>(st, s, rows) : launch_fsmall_t<false, true, true>(st, s, rows);
+}
+
+// The small-system run as a graph node (cooperative), with the WHILE and IF
+// handles it sets.
+cudaError_t enqueue_small_run(Launch &L, const DevSys &s, cudaGraphConditionalHandle hw,
+                              cudaGraphConditionalHandle hif) {
+    const int rows = std::max(1, (s.nbrCap + 7) / 8);
+    const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
+    const size_t smem = small_smem(rows);
+    cudaError_t e;
+    if (s.sigmaOne) {
+        if ((e = cudaFuncSetAttribute(k_fsmall<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem)))
+            return e;
+        e = L.kernel(k_fsmall<true, true, true>, dim3(ntiles), dim3(kFastBlock), smem, s, rows, hw, hif, 1);
+    } else {
+        if ((e = cudaFuncSetAttribute(k_fsmall<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem)))
+            return e;
+        e = L.kernel(k_fsmall<false, true, true>, dim3(ntiles), dim3(kFastBlock), smem, s, rows, hw, hif, 1);
+    }
+    if (e) return e;
+    return L.cooperative_last();
 }
 
 // The persistent kernel wherever every window can be one bulk copy (no

@@ -78,6 +78,32 @@ struct Launch {
         return cudaSuccess;
     }
 
+    // Open a WHILE node (the body runs while the condition, set on the
+    // device, is nonzero); 'body' receives the body graph.  Graph mode only.
+    cudaError_t begin_while(cudaGraphConditionalHandle h, Launch &body) {
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t n;
+        cudaError_t e = cudaGraphAddNode(&n, graph, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &p);
+        if (e != cudaSuccess) return e;
+        deps.assign(1, n);
+        body.stream = stream;
+        body.graph = p.conditional.phGraph_out[0];
+        body.deps.clear();
+        return cudaSuccess;
+    }
+
+    // Mark the last kernel node cooperative (all its blocks co-resident).
+    cudaError_t cooperative_last() {
+        if (!graph || deps.empty()) return cudaErrorInvalidValue;
+        cudaLaunchAttributeValue v = {};
+        v.cooperative = 1;
+        return cudaGraphKernelNodeSetAttribute(deps.back(), cudaLaunchAttributeCooperative, &v);
+    }
+
   private:
     template <typename Tup, size_t... I>
     static void fill(void **ptrs, Tup &t, std::index_sequence<I...>) {
