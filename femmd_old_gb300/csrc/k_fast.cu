@@ -781,7 +781,28 @@ __device__ __forceinline__ void fast_pairs(const DevSys &s, const PairEntry *tab
 // other), the x and y differences in separate float2s.  The pairs inside
 // the cutoff are counted as sum ir2 r2 (each term 1 to within the
 // reciprocal's rounding, 0 outside the cutoff), the energy shift's weight.
-template <bool SIG1, bool WIN, bool W16, bool NC = true>
+// The exact minimum image of two packed differences d = a - q (one axis, box
+// length L): a lane whose |d| exceeds L/2 moves by one box length, rounded
+// once from its exact value, (d -+ L) + the TwoSum error of a - q (the
+// scalar fdiff's arithmetic, operation for operation); other lanes keep d.
+__device__ __forceinline__ float2 img2(float2 d, float2 q, float2 a, float L) {
+    const float h = 0.5f * L;
+    const bool cx = fabsf(d.x) > h, cy = fabsf(d.y) > h;
+    if (!(cx || cy)) return d;
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 bb = __ffma2_rn(a, m1, d);     // d - a
+    const float2 t = __ffma2_rn(bb, m1, d);     // d - bb
+    const float2 e1 = __ffma2_rn(t, m1, a);     // a - t
+    const float2 e2n = __fadd2_rn(q, bb);       // -((-q) - bb)
+    const float2 err = __ffma2_rn(e2n, m1, e1); // (a - t) + ((-q) - bb)
+    float2 r = d;
+    if (cx) r.x = (d.x - (d.x > 0.0f ? L : -L)) + err.x;
+    if (cy) r.y = (d.y - (d.y > 0.0f ? L : -L)) + err.y;
+    return r;
+}
+
+// IMG: a warp at a periodic edge (WX, WY): the packed exact image per pair.
+template <bool SIG1, bool WIN, bool W16, bool NC = true, bool IMG = false, bool WX = false, bool WY = false>
 __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &pe, int i, float2 pi, int cnt,
                                               const int4 *slist, int srows, const float2 *__restrict__ pin,
                                               const float2 *wpos, float &fx, float &fy, float &ue2, float &we2) {
@@ -800,8 +821,11 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const float2 qa = q[2 * h], qb = q[2 * h + 1];
-            const float2 dx = __ffma2_rn(make_float2(qa.x, qb.x), m1, xv);
-            const float2 dy = __ffma2_rn(make_float2(qa.y, qb.y), m1, yv);
+            const float2 qx = make_float2(qa.x, qb.x), qy = make_float2(qa.y, qb.y);
+            float2 dx = __ffma2_rn(qx, m1, xv);
+            float2 dy = __ffma2_rn(qy, m1, yv);
+            if (IMG && WX) dx = img2(dx, qx, xv, s.Lx);
+            if (IMG && WY) dy = img2(dy, qy, yv, s.Ly);
             const float2 r2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
             float2 ir2 = make_float2(r2.x < rc2 ? rcp_approx(r2.x) : 0.0f, r2.y < rc2 ? rcp_approx(r2.y) : 0.0f);
             if (!SIG1) ir2 = __fmul2_rn(ir2, sv);
@@ -845,34 +869,6 @@ __device__ __forceinline__ void fast_pairs_x2(const DevSys &s, const PairEntry &
     const float n = SIG1 ? Nv.x + Nv.y : (Nv.x + Nv.y) / pe.sig2;
     ue2 += __fmaf_rn(pe.eps4, A - B, pe.us * n);
     we2 += pe.eps48 * __fmaf_rn(-0.5f, B, A);
-}
-
-// The scalar pair loop over 16-bit window entries (warps at a periodic edge
-// of a win16 system: the exact image per pair).
-template <bool SIG1, bool WX, bool WY>
-__device__ __forceinline__ void fast_pairs16_img(const DevSys &s, const PairEntry *tab, int i, float2 pi, int cnt,
-                                                 const int4 *slist, int srows, const float2 *wpos, float &fx,
-                                                 float &fy, float &ue2, float &we2) {
-    const int ng = (cnt + 7) >> 3;
-    const size_t row = (size_t)s.Ncap;
-    const int4 *__restrict__ lst = reinterpret_cast<const int4 *>(s.nbr) + i;
-    const PairEntry pe0 = tab[0];
-    float A = 0.0f, B = 0.0f, n = 0.0f, u2 = 0.0f, w2 = 0.0f;
-#pragma unroll 1
-    for (int gi = 0; gi < ng; gi++) {
-        const int4 g =
-            gi < srows ? slist[gi * kFastBlock + (threadIdx.x & (kFastBlock - 1))] : __ldg(lst + gi * row);
-        const unsigned wd[4] = {(unsigned)g.x, (unsigned)g.y, (unsigned)g.z, (unsigned)g.w};
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const unsigned e = (u & 1) ? wd[u >> 1] >> 16 : wd[u >> 1] & 0xffffu;
-            const float2 q = wpos[min(e, (unsigned)kWinGhost)];
-            fpair<false, false, SIG1, WX, WY, true>(s, tab, pe0, 0, 0.0f, pi, q.x, q.y, 0, 0.0f, fx, fy, A, B, n, u2,
-                                                    w2);
-        }
-    }
-    ue2 += __fmaf_rn(pe0.eps4, A - B, pe0.us * n);
-    we2 += pe0.eps48 * __fmaf_rn(-0.5f, B, A);
 }
 
 // x wrapped into [0, L): one box length added or taken away, the reference's
@@ -1379,24 +1375,25 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                     }
                 } else if (cur.len >= 0 && s.win16) {
                     if (img)
-                        fast_pairs16_img<SIG1, WX, WY>(s, tab, i, cur.p, cur.cnt, slist_of(st), rows, wpos_of(st), fx,
-                                                       fy, ue2, we2);
+                        fast_pairs_x2<SIG1, true, true, true, true, WX, WY>(s, tab[0], i, cur.p, cur.cnt,
+                                                                            slist_of(st), rows, pin, wpos_of(st), fx,
+                                                                            fy, ue2, we2);
                     else
                         fast_pairs_x2<SIG1, true, true>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
                                                         wpos_of(st), fx, fy, ue2, we2);
                 } else if (cur.len >= 0) {
                     if (img)
-                        fast_pairs<false, false, SIG1, WX, WY, true, true>(s, tab, i, cur.p, cur.cnt, slist_of(st),
-                                                                           rows, pin, wpos_of(st), nullptr, nullptr,
-                                                                           fx, fy, ue2, we2);
+                        fast_pairs_x2<SIG1, true, false, true, true, WX, WY>(s, tab[0], i, cur.p, cur.cnt,
+                                                                             slist_of(st), rows, pin, wpos_of(st), fx,
+                                                                             fy, ue2, we2);
                     else
                         fast_pairs_x2<SIG1, true, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
                                                          wpos_of(st), fx, fy, ue2, we2);
                 } else {
                     if (img)
-                        fast_pairs<false, false, SIG1, WX, WY, true, false>(s, tab, i, cur.p, cur.cnt, slist_of(st),
-                                                                            rows, pin, wpos_of(st), nullptr, nullptr,
-                                                                            fx, fy, ue2, we2);
+                        fast_pairs_x2<SIG1, false, false, true, true, WX, WY>(s, tab[0], i, cur.p, cur.cnt,
+                                                                              slist_of(st), rows, pin, wpos_of(st),
+                                                                              fx, fy, ue2, we2);
                     else
                         fast_pairs_x2<SIG1, false, false>(s, tab[0], i, cur.p, cur.cnt, slist_of(st), rows, pin,
                                                           wpos_of(st), fx, fy, ue2, we2);
@@ -1940,21 +1937,18 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         const bool img = __any_sync(0xffffffffu, near);
         if (act) {
             if (len >= 0 && s.win16) {
-                if (img) fast_pairs16_img<SIG1, WX, WY>(s, tab, i, pi, cnt, slist, rows, wpos, fx, fy, ue2, we2);
+                if (img) fast_pairs_x2<SIG1, true, true, false, true, WX, WY>(s, tab[0], i, pi, cnt, slist, rows, pin,
+                                                                            wpos, fx, fy, ue2, we2);
                 else fast_pairs_x2<SIG1, true, true, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
                                                             ue2, we2);
             } else if (len >= 0) {
-                if (img)
-                    fast_pairs<false, false, SIG1, WX, WY, true, true, false>(s, tab, i, pi, cnt, slist, rows, pin,
-                                                                              wpos, nullptr, nullptr, fx, fy, ue2,
-                                                                              we2);
+                if (img) fast_pairs_x2<SIG1, true, false, false, true, WX, WY>(s, tab[0], i, pi, cnt, slist, rows, pin,
+                                                                             wpos, fx, fy, ue2, we2);
                 else fast_pairs_x2<SIG1, true, false, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
                                                              ue2, we2);
             } else {
-                if (img)
-                    fast_pairs<false, false, SIG1, WX, WY, true, false, false>(s, tab, i, pi, cnt, slist, rows, pin,
-                                                                               wpos, nullptr, nullptr, fx, fy, ue2,
-                                                                               we2);
+                if (img) fast_pairs_x2<SIG1, false, false, false, true, WX, WY>(s, tab[0], i, pi, cnt, slist, rows,
+                                                                              pin, wpos, fx, fy, ue2, we2);
                 else fast_pairs_x2<SIG1, false, false, false>(s, tab[0], i, pi, cnt, slist, rows, pin, wpos, fx, fy,
                                                               ue2, we2);
             }
