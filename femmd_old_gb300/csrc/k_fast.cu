@@ -49,7 +49,7 @@ constexpr int kPermBlock = 1024;  // cell slots per block of the storage reorder
 // atomics gave arbitrary ranks): sortedIds[t] = old slot.  The new storage
 // order is then a function of the positions and ids alone -- the reference's
 // cell order -- whatever order the particles were stored in before.
-__global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int check) {
+__global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int parity, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.N) return;
@@ -61,6 +61,21 @@ __global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int check) {
     const int slot = b + r;
     if (slot >= e) {  // inconsistent cell contents: never write outside the cell
         atomicOr(&s.sc->overflow, 2);
+        return;
+    }
+    if (s.nBonded == 0) {
+        // no bonded particles: the new storage slot is the cell slot, so the
+        // reorder (k_fperm's work) is written from here, reads by particle
+        const float2 *pos = parity ? s.pos1 : s.pos0;
+        const float2 pp = pos[i];
+        const int tag = slot | (s.numTypes > 1 ? (s.typeId[i] << kIdBits) : 0);
+        s.cellSorted[slot] = make_float4(pp.x, pp.y, __int_as_float(tag), __int_as_float(s.excl[i]));
+        s.sortedIds[slot] = slot;
+        s.newCell[slot] = c;
+        s.sPos[slot] = pp;
+        s.sVel[slot] = s.vel[i];
+        s.sAcc[slot] = s.acc[i];
+        s.sPerm[slot] = id;
         return;
     }
     s.sortedIds[slot] = i;
@@ -621,9 +636,11 @@ cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int che
     if ((e = enqueue_bin(L, s, parity, check))) return e;
     const int pb = (s.N + kBlock - 1) / kBlock;
     const int permb = (s.N + kPermBlock - 1) / kPermBlock;
-    if ((e = L.kernel(k_fplace, dim3(pb), dim3(kBlock), 0, s, check))) return e;
-    if (s.nBonded > 0 && (e = L.kernel(k_ffree_count, dim3(permb), dim3(kPermBlock), 0, s, check))) return e;
-    if ((e = L.kernel(k_fperm, dim3(permb), dim3(kPermBlock), 0, s, parity, check))) return e;
+    if ((e = L.kernel(k_fplace, dim3(pb), dim3(kBlock), 0, s, parity, check))) return e;
+    if (s.nBonded > 0) {
+        if ((e = L.kernel(k_ffree_count, dim3(permb), dim3(kPermBlock), 0, s, check))) return e;
+        if ((e = L.kernel(k_fperm, dim3(permb), dim3(kPermBlock), 0, s, parity, check))) return e;
+    }
     // without bonded particles the persistent build makes the windows and
     // every list itself
     if (s.nBonded == 0 && s.numTypes == 1) return launch_flist_p(L, s, parity, check);
