@@ -231,6 +231,7 @@ struct femmd_ctx {
     int forceMode = FEMMD_FORCE_REFERENCE;
     DBuf<int> perm, sPerm, fBlockSums, ckPerm, idType, newCell;
     DBuf<int> blockWin;
+    DBuf<unsigned long long> smallRec;
     DBuf<float2> sPos, sVel, sAcc, cpos0, cpos1;
     DBuf<int> cslot;
     DBuf<float> idMass, idSigma, idWallDelta, idWallSig, xfer1;
@@ -345,7 +346,7 @@ static void release_device(femmd_ctx *c) {
     c->props.release(); c->propsCk.release(); c->propPart.release(); c->centroid.release();
     c->propsUploaded = false;
     c->perm.release(); c->sPerm.release(); c->fBlockSums.release(); c->ckPerm.release(); c->idType.release();
-    c->newCell.release(); c->blockWin.release(); c->sPos.release(); c->sVel.release(); c->sAcc.release();
+    c->newCell.release(); c->blockWin.release(); c->smallRec.release(); c->sPos.release(); c->sVel.release(); c->sAcc.release();
     c->cpos0.release(); c->cpos1.release(); c->cslot.release();
     c->idMass.release(); c->idSigma.release(); c->idWallDelta.release(); c->idWallSig.release(); c->xfer1.release();
     auto &a = c->adj;
@@ -528,6 +529,7 @@ static DevSys make_sys(femmd_ctx *c) {
         s.idWallSig = s.wallSig ? c->idWallSig.p : nullptr;
         s.newCell = c->newCell.p;
         s.blockWin = c->blockWin.p;
+        s.smallRec = c->smallRec.p;
         s.win16 = (c->nBonded == 0 && s.numTypes == 1 && s.sigmaByType) ? 1 : 0;
         if (c->cslot.p) {
             s.cpos0 = c->cpos0.p;
@@ -885,6 +887,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(ctx->fBlockSums.ensure((N + 1023) / 1024));
         CK(ctx->newCell.ensure(N));
         CK(ctx->blockWin.ensure(kWinInts * (size_t)((N + kFastBlock - 1) / kFastBlock)));
+        CK(ctx->smallRec.ensure(3 * 4 * (size_t)kSmallMaxTiles));
         if (ctx->nBonded > 0) {
             // the cell-ordered position mirror (slot N: the ghost)
             CK(ctx->cpos0.ensure(N + 1)); CK(ctx->cpos1.ensure(N + 1)); CK(ctx->cslot.ensure(N));
@@ -1180,8 +1183,8 @@ static femmd_status small_units(femmd_ctx *ctx, const DevSys &s, int units) {
     }
     ctx->hsc->smallLeft = units;
     CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(&d->sacc[0][0], 0, sizeof(d->sacc), ctx->stream));
-    CK(cudaMemsetAsync(&d->gbCount, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->smallRec.p, 0, ctx->smallRec.n * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(&d->gbTag, 0, sizeof(unsigned), ctx->stream));
     if (!ctx->smallGraphFailed && !ctx->smallGraph.x && build_small_graph(ctx, s) != FEMMD_OK) {
         ctx->smallGraph.release();
         ctx->smallGraphFailed = true;

@@ -78,11 +78,9 @@ struct DevScalars {
     unsigned long long nbrSum, builds;
     unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
     unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
-    // the small-system run (k_fsmall): per-step sums in three rotating sets
-    // {U, W, K, max v^2 bits}, the grid barrier's arrival count and
-    // generation, and the steps one launch advanced
-    unsigned long long sacc[3][4];
-    unsigned int gbCount, gbGen;
+    // the small-system run (k_fsmall): the tag base of its next launch's
+    // exchanges, the steps one launch advanced and the steps left
+    unsigned int gbTag, pad2;
     int smallDone, smallLeft;
 };
 
@@ -192,7 +190,12 @@ struct DevSys {
     // no bonded particles.  Other blocks keep 32-bit entries (nbr_at).
     int win16;
     int *blockWin;
+    // the small-system run's exchange records: three sets of kSmallMaxTiles
+    // records {tag << 32 | max v^2 bits, U, W, K fixed point}
+    unsigned long long *smallRec;
 };
+
+constexpr int kSmallMaxTiles = 128;  // step blocks of the largest system the small-system run takes
 
 constexpr int kFastBlock = 128;  // storage slots per block of the fast step kernel
 constexpr int kWinMax = 768;     // window entries per block (the ghost included)

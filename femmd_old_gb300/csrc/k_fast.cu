@@ -81,6 +81,131 @@ __global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int parity, int che
     s.sortedIds[slot] = i;
 }
 
+// The binning and in-cell placement of a small system without bonded
+// particles and with one particle kind, in one block: what k_rebuild_begin,
+// k_cells_count, k_scan_blocks, k_scan_apply, k_scatter and k_fplace do as
+// six launches, with the cell counts, their exclusive scan and the ids of
+// each cell's particles in shared memory.  The outputs are theirs (cellStart,
+// the cell-ordered candidate copy, sortedIds, newCell and the state in the
+// new order in the scratch arrays); the placement inside a cell is by id, so
+// the order of the counting atomics leaves no trace.
+constexpr int kSmallBinThreads = 1024;
+constexpr int kSmallBinMaxN = kSmallMaxTiles * kFastBlock;
+constexpr size_t kSmallBinMaxSmem = 200 * 1024;
+
+static size_t small_bin_smem(const DevSys &s) { return (size_t)(s.ncells + 1 + 3 * (size_t)s.N + 8) * sizeof(int); }
+
+static bool small_bin_fits(const DevSys &s) {
+    return s.nBonded == 0 && s.numTypes == 1 && !s.trace && s.N > 0 && s.N <= kSmallBinMaxN &&
+           small_bin_smem(s) <= kSmallBinMaxSmem;
+}
+
+__global__ void __launch_bounds__(kSmallBinThreads, 1) k_fbin_small(DevSys s, int parity, int check) {
+    extern __shared__ int ism[];
+    __shared__ int wsum[kSmallBinThreads / 32];
+    __shared__ int skip;
+    DevScalars *sc = s.sc;
+    if (check && !sc->rebuild) return;
+    int *start = ism;                  // counts, then cell starts (ncells + 1)
+    int *cof = start + s.ncells + 1;   // cell of each slot
+    int *rk = cof + s.N;               // rank among the cell's particles (atomic order)
+    int *ids = rk + s.N;               // ids in cell-slot order, unsorted inside a cell
+    const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        // the placement is skipped after a non-finite position or inconsistent counts
+        skip = (sc->nonfinite || (sc->overflow & 2)) ? 1 : 0;
+        if (check) {  // k_rebuild_begin: the taken branch of NeighborList::update
+            sc->totalUpdates += 1;
+            sc->dispHi = 0.0f;
+        }
+    }
+    for (int c = tid; c < s.ncells; c += T) start[c] = 0;
+    __syncthreads();
+    const float2 *pos = parity ? s.pos1 : s.pos0;
+    bool bad = false;
+    for (int i = tid; i < s.N; i += T) {
+        const float2 p = pos[i];
+        if (!(isfinite(p.x) && isfinite(p.y))) {
+            atomicOr(&sc->nonfinite, 1);
+            bad = true;
+        }
+        if (outside_box(s, p)) atomicOr(&sc->outside, 1);
+        const int c = cell_col(p.x, p.y, s.ncx, s.ncy, s.Lx, s.Ly);
+        cof[i] = c;
+        rk[i] = atomicAdd(&start[c], 1);
+    }
+    if (bad) skip = 1;
+    __syncthreads();
+    // exclusive scan of the counts: a contiguous run of cells per thread
+    const int per = (s.ncells + T - 1) / T;
+    const int c0 = min(tid * per, s.ncells), c1 = min(c0 + per, s.ncells);
+    int tot = 0;
+    for (int c = c0; c < c1; c++) tot += start[c];
+    int x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = lane < T / 32 ? wsum[lane] : 0;
+        int z = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
+        }
+        if (lane < T / 32) wsum[lane] = z - w;
+    }
+    __syncthreads();
+    int run = wsum[warp] + x - tot;
+    for (int c = c0; c < c1; c++) {
+        const int v = start[c];
+        start[c] = run;
+        run += v;
+    }
+    if (tid == 0) {
+        start[s.ncells] = s.N;
+        sc->nbrSum = 0ull;
+        sc->maxCount = 0;
+    }
+    __syncthreads();
+    for (int c = tid; c <= s.ncells; c += T) s.cellStart[c] = start[c];
+    for (int i = tid; i < s.N; i += T) {
+        const int slot = start[cof[i]] + rk[i];
+        if (slot >= 0 && slot < s.N) {
+            ids[slot] = s.perm[i];
+        } else {  // inconsistent counts: never write outside the array
+            atomicOr(&sc->overflow, 2);
+            skip = 1;
+        }
+    }
+    __syncthreads();
+    if (skip) return;
+    for (int i = tid; i < s.N; i += T) {
+        const int c = cof[i];
+        const int b = start[c], e = start[c + 1];
+        const int id = s.perm[i];
+        int r = 0;
+        for (int q = b; q < e; q++) r += ids[q] < id;
+        const int slot = b + r;
+        if (slot >= e) {  // inconsistent cell contents: never write outside the cell
+            atomicOr(&sc->overflow, 2);
+            continue;
+        }
+        const float2 pp = pos[i];
+        s.cellSorted[slot] = make_float4(pp.x, pp.y, __int_as_float(slot), __int_as_float(s.excl[i]));
+        s.sortedIds[slot] = slot;
+        s.newCell[slot] = c;
+        s.sPos[slot] = pp;
+        s.sVel[slot] = s.vel[i];
+        s.sAcc[slot] = s.acc[i];
+        s.sPerm[slot] = id;
+    }
+}
+
 // Free particles among each block's cell slots (only with bonded particles).
 __global__ void __launch_bounds__(kPermBlock) k_ffree_count(DevSys s, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
@@ -179,11 +304,14 @@ __global__ void __launch_bounds__(kPermBlock) k_fperm(DevSys s, int parity, int 
 // cells, windows too large, grids the fast walk does not cover) keep global
 // storage slots.  The block's longest list (in groups) is gathered by the
 // list build.
-__device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
+// (walk_ok: fast_walk_ok; cs(c): the start of cell c; nc(q): the cell of
+// cell slot q.)
+template <class CS, class NC>
+__device__ __forceinline__ void fwindow_record_t(const DevSys &s, int b, bool walk_ok, CS cs, NC nc) {
     int *out = s.blockWin + kWinInts * (size_t)b;
     const int f = b * kFastBlock, l = min(f + kFastBlock, s.N) - 1;
     const int ncy = s.ncy, ncx = s.ncx;
-    bool ok = f >= s.nBonded && fast_walk_ok(s) && ncy >= 3;
+    bool ok = f >= s.nBonded && walk_ok && ncy >= 3;
     int st[kWinPieces], off[kWinPieces], cnt[kWinPieces];
 #pragma unroll
     for (int p = 0; p < kWinPieces; p++) st[p] = off[p] = cnt[p] = 0;
@@ -192,7 +320,7 @@ __device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
 #pragma unroll
     for (int p = 0; p < kWinPieces; p++) rs[p] = 0, re[p] = -1;
     if (ok) {
-        const int cf = s.newCell[f], cl = s.newCell[l];
+        const int cf = nc(f), cl = nc(l);
         ix = cf / ncy;
         const int ixl = cl / ncy, r0 = cf - ix * ncy, r1 = cl - ixl * ncy;
         // row ranges [ra, rb] per piece and window column (rb < ra: empty)
@@ -230,7 +358,7 @@ __device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
                 if (nx < 0) nx += ncx;
                 else if (nx >= ncx) nx -= ncx;
                 const int col = nx * ncy;
-                const int a = s.cellStart[col + ra[p]], e = s.cellStart[col + rb[p] + 1];
+                const int a = cs(col + ra[p]), e = cs(col + rb[p] + 1);
                 st[p] = a;
                 cnt[p] = e - a;
                 off[p] = acc + (a & 1);
@@ -254,6 +382,11 @@ __device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
         out[kWRow0 + p] = ok ? rs[p] : 0;
         out[kWRow1 + p] = ok ? re[p] : -1;
     }
+}
+
+__device__ __forceinline__ void fwindow_record(const DevSys &s, int b) {
+    fwindow_record_t(s, b, fast_walk_ok(s), [&](int c) { return s.cellStart[c]; },
+                     [&](int q) { return s.newCell[q]; });
 }
 
 __global__ void __launch_bounds__(kBlock) k_fwindows(DevSys s, int check) {
@@ -633,6 +766,14 @@ static cudaError_t launch_flist_p(Launch &L, const DevSys &s, int parity, int ch
 
 cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int check) {
     cudaError_t e;
+    if (small_bin_fits(s)) {
+        // a small system: binning and placement in one block, then the lists
+        const size_t smem = small_bin_smem(s);
+        if ((e = cudaFuncSetAttribute(k_fbin_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        if ((e = L.kernel(k_fbin_small, dim3(1), dim3(kSmallBinThreads), smem, s, parity, check))) return e;
+        return launch_flist_p(L, s, parity, check);
+    }
     if ((e = enqueue_bin(L, s, parity, check))) return e;
     const int pb = (s.N + kBlock - 1) / kBlock;
     const int permb = (s.N + kPermBlock - 1) / kPermBlock;
@@ -906,7 +1047,7 @@ __device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, fl
                                             float2 *pout, float2 *cpout, float fx, float fy, float ue, float we,
                                             float utri,
                                             float uwall, float &ue_out, float &we_out, float &ke, float &vvm,
-                                            bool &bad) {
+                                            bool &bad, float2 *xo = nullptr, float2 *vo = nullptr) {
     ue *= 0.5f;
     we *= 0.5f;
     ue += uwall;
@@ -955,6 +1096,8 @@ __device__ __forceinline__ void fast_finish(const DevSys &s, int i, int mode, fl
             pout[i] = x;
             if (cpout) cpout[s.cslot[i]] = x;  // the cell-ordered mirror
             s.vel[i] = v;
+            if (xo) *xo = x;
+            if (vo) *vo = v;
         }
     }
     ue_out += ue;
@@ -1561,6 +1704,70 @@ __device__ __forceinline__ void lp_stencil(const DevSys &s, const int *hd, const
     }
 }
 
+// The cell-start words a windowed tile's stage takes (window record bw): a
+// stage holds them when they are at most kLPCs.
+__device__ __forceinline__ int lp_cs_words(const DevSys &s, const int *bw) {
+    int used = 0;
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) {
+        const int ra = bw[kWRow0 + p], rb = bw[kWRow1 + p];
+        if (rb >= ra) {
+            int nx = bw[kWCol0] + (p >> 1) - 1;
+            if (nx < 0) nx += s.ncx;
+            else if (nx >= s.ncx) nx -= s.ncx;
+            const int colp = nx * s.ncy;
+            used += ((colp + rb + 2 + 3) & ~3) - ((colp + ra) & ~3);
+        }
+    }
+    return used;
+}
+
+// The stage of a windowed tile (window record bw, len >= 0): the header
+// rest (the caller wrote kHT and kHLen), then, on bar, bulk copies of the
+// window pieces of cellSorted and of the cell starts of the rows they cover.
+__device__ __forceinline__ void lp_issue(const DevSys &s, const int *bw, int *hd, int *csm, float4 *wc,
+                                         unsigned long long *bar) {
+    const int ncx = s.ncx, ncy = s.ncy;
+    const int col0 = bw[kWCol0];
+    hd[kHTwo] = bw[kWTwo];
+    hd[kHCol0] = col0;
+    // first pass: sizes, where each piece's cell starts go
+    int used = 0;
+    unsigned total = 0;
+    int a0s[kWinPieces], nws[kWinPieces];
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) {
+        int nx = col0 + (p >> 1) - 1;
+        if (nx < 0) nx += ncx;
+        else if (nx >= ncx) nx -= ncx;
+        const int colp = nx * ncy;
+        const int ra = bw[kWRow0 + p], rb = bw[kWRow1 + p];
+        hd[kHColp + p] = colp;
+        hd[kHDelta + p] = bw[kWOff + p] - bw[kWStart + p];
+        a0s[p] = 0;
+        nws[p] = 0;
+        if (rb >= ra) {
+            const int a0 = (colp + ra) & ~3, e0 = (colp + rb + 2 + 3) & ~3;
+            a0s[p] = a0;
+            nws[p] = e0 - a0;
+            hd[kHCsb + p] = used - a0;
+            used += e0 - a0;
+        }
+        total += (unsigned)bw[kWCount + p] * 16u;
+    }
+    const bool csok = used <= kLPCs;
+    hd[kHCsOk] = csok ? 1 : 0;
+    if (csok) total += (unsigned)used * 4u;
+    mbar_expect_tx(bar, total);
+#pragma unroll
+    for (int p = 0; p < kWinPieces; p++) {
+        const int c = bw[kWCount + p];
+        if (c > 0) bulk_copy_g2s(wc + bw[kWOff + p], s.cellSorted + bw[kWStart + p], (unsigned)c * 16u, bar);
+        if (csok && nws[p] > 0)
+            bulk_copy_g2s(csm + (hd[kHCsb + p] + a0s[p]), s.cellStart + a0s[p], (unsigned)nws[p] * 4u, bar);
+    }
+}
+
 __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int parity, int check) {
     if ((check && !s.sc->rebuild) || s.sc->nonfinite || (s.sc->overflow & 2)) return;
     float2 *pos = parity ? s.pos1 : s.pos0;
@@ -1590,7 +1797,6 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
             // the window record of a tile is made (fwindow_record) an
             // iteration before its copies are issued, so its loads pass
             // while the producer waits for a free stage
-            const int ncx = s.ncx, ncy = s.ncy;
             int k = 0;
             bool live = true;
             if (blockIdx.x < ntiles) fwindow_record(s, blockIdx.x);
@@ -1615,49 +1821,7 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
                     if (tn < ntiles) fwindow_record(s, tn);
                     continue;
                 }
-                const int col0 = bw[kWCol0];
-                hd[kHTwo] = bw[kWTwo];
-                hd[kHCol0] = col0;
-                // first pass: sizes, where each piece's cell starts go
-                int used = 0;
-                unsigned total = 0;
-                int a0s[kWinPieces], nws[kWinPieces];
-#pragma unroll
-                for (int p = 0; p < kWinPieces; p++) {
-                    int nx = col0 + (p >> 1) - 1;
-                    if (nx < 0) nx += ncx;
-                    else if (nx >= ncx) nx -= ncx;
-                    const int colp = nx * ncy;
-                    const int ra = bw[kWRow0 + p], rb = bw[kWRow1 + p];
-                    hd[kHColp + p] = colp;
-                    hd[kHDelta + p] = bw[kWOff + p] - bw[kWStart + p];
-                    a0s[p] = 0;
-                    nws[p] = 0;
-                    if (rb >= ra) {
-                        const int a0 = (colp + ra) & ~3, e0 = (colp + rb + 2 + 3) & ~3;
-                        a0s[p] = a0;
-                        nws[p] = e0 - a0;
-                        hd[kHCsb + p] = used - a0;
-                        used += e0 - a0;
-                    }
-                    total += (unsigned)bw[kWCount + p] * 16u;
-                }
-                const bool csok = used <= kLPCs;
-                hd[kHCsOk] = csok ? 1 : 0;
-                if (csok) total += (unsigned)used * 4u;
-                mbar_expect_tx(&full[st], total);
-                int *csm = cs_of(st);
-                float4 *wc = wc_of(st);
-#pragma unroll
-                for (int p = 0; p < kWinPieces; p++) {
-                    const int c = bw[kWCount + p];
-                    if (c > 0)
-                        bulk_copy_g2s(wc + bw[kWOff + p], s.cellSorted + bw[kWStart + p], (unsigned)c * 16u,
-                                      &full[st]);
-                    if (csok && nws[p] > 0)
-                        bulk_copy_g2s(csm + (hd[kHCsb + p] + a0s[p]), s.cellStart + a0s[p], (unsigned)nws[p] * 4u,
-                                      &full[st]);
-                }
+                lp_issue(s, bw, hd, cs_of(st), wc_of(st), &full[st]);
                 if (tn < ntiles) fwindow_record(s, tn);
             }
             if (!live) {
@@ -1854,101 +2018,517 @@ static cudaError_t fstep_image(Launch &L, const DevSys &s, int mode, int parity,
 
 // ---- the small-system run (one particle kind, sigma by type, no bonded
 // particles, walls, gravity or area springs; a few step blocks).  At this
-// size a step kernel lasts a few microseconds and the graph's conditional
-// node and launch cost as much again, so k_fsmall advances a run's middle
-// steps in one cooperative launch: one block per step block, the block's list
-// rows kept in shared memory (no rebuild happens inside a launch), per step
-// the window gathered, the pair terms and the leapfrog of k_fstep_p, the
-// block's energy sums into one of three rotating fixed-point sums, then a
-// bounded grid barrier after which every block takes the same rebuild
-// decision from the same sums.  The launch ends after the step that calls
-// for a rebuild (the host rebuilds and launches again) or after 'steps'
-// steps; the number done goes to DevScalars::smallDone.
-constexpr int kSmallMaxTiles = 128;  // step blocks of the largest system run this way
-constexpr int kGridSpin = 1 << 21;   // polls (about 64 ns each) before a grid barrier gives up
+// size a step kernel lasts a few microseconds and a graph node or a launch
+// costs as much again, so k_fsmall advances a run's middle steps in one
+// cooperative launch: one block per step block (tile), the tile's list rows
+// kept in shared memory, per step the window copied in, the pair terms and
+// the leapfrog of k_fstep_p, then a bounded grid-wide exchange after which
+// every block takes the same rebuild decision from the same maximum.  A
+// rebuild happens inside the launch too (small_rebuild: the binning, the
+// in-cell placement, the window records and the lists of k_fbin_small and
+// k_flist_p, in four exchanges).  Where that cannot be done (a tile without
+// a window, or one whose cell starts overflow a stage) the launch ends with
+// the rebuild pending and the rebuild kernels run; a neighbour-list overflow
+// or a non-finite position ends it too (the run is then repeated or fails).
+// The number of steps done goes to DevScalars::smallDone.
+//
+// The exchange: each block writes a record {tag << 32 | word, U, W, K} (word:
+// its max v^2 bits after a step, flag bits during a rebuild; U, W, K: its
+// fixed-point energy sums) into one of three record sets, the tag word last
+// with release semantics, and warp 0 of every block waits until all tag
+// words carry the exchange's tag (acquire), taking the largest word as a
+// float and the OR of the words.  Block 0 sums a step's fixed-point records
+// (exact integer sums: the same totals as the step kernels' atomics) during
+// the next exchange, while it waits.  Set j is written again at exchange
+// j + 3, which no block reaches before block 0 has published exchange j + 2,
+// after those sums.  Tags grow by one per exchange (DevScalars::gbTag holds
+// the next launch's base).
+constexpr int kGridSpin = 1 << 20;  // polls of one record (about 0.5 us each) before an exchange gives up
 
-// A bounded grid barrier of nblocks co-resident blocks (generation counter):
-// false on every block that gave up waiting.
-__device__ __forceinline__ bool grid_barrier(DevScalars *sc, unsigned nblocks, int *okflag) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = &sc->gbGen;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(&sc->gbCount, 1u) == nblocks - 1) {
-            sc->gbCount = 0;
-            __threadfence();
-            atomicAdd(&sc->gbGen, 1u);
-        } else {
-            int it = 0;
-            while (*gen == g && it < kGridSpin) {
-                __nanosleep(64);
-                it++;
-            }
-            ok = *gen != g;
-        }
-        __threadfence();
-        *okflag = ok;
-    }
-    __syncthreads();
-    return *okflag != 0;
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
 }
 
-__host__ __device__ constexpr size_t small_smem(int rows) {
-    return 128 + (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2);
+// This block's record of exchange 'tag' (record set par), then the wait of
+// warp 0 for every block's: xsh[0] = 1 (0 when a wait gave up), xsh[1] = the
+// OR of the words, xsh[2] = their maximum as a float.  Call after a
+// __syncthreads that follows the block's stores.
+__device__ __forceinline__ void small_exchange(const DevSys &s, unsigned tag, int par, unsigned long long qu,
+                                               unsigned long long qw, unsigned long long qk, unsigned word,
+                                               unsigned *xsh) {
+    unsigned long long *set = s.smallRec + (size_t)par * kSmallMaxTiles * 4;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        unsigned long long *r = set + 4 * (size_t)blockIdx.x;
+        r[1] = qu;
+        r[2] = qw;
+        r[3] = qk;
+        st_release_u64(r, ((unsigned long long)tag << 32) | word);
+    }
+    if (threadIdx.x < 32) {
+        float m = 0.0f;
+        unsigned orw = 0u;
+        int ok = 1;
+        for (int b = lane; b < (int)gridDim.x && ok; b += 32) {
+            const unsigned long long *w = set + 4 * (size_t)b;
+            unsigned long long x = ld_acquire_u64(w);
+            int it = 0;
+            while ((unsigned)(x >> 32) != tag) {
+                if (++it > kGridSpin) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+                x = ld_acquire_u64(w);
+            }
+            if (ok) {
+                m = fmaxf(m, __uint_as_float((unsigned)x));
+                orw |= (unsigned)x;
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        m = warp_max(m);
+        orw = __reduce_or_sync(0xffffffffu, orw);
+        if (lane == 0) {
+            xsh[0] = (unsigned)ok;
+            xsh[1] = orw;
+            xsh[2] = __float_as_uint(m);
+        }
+    }
+}
+
+// Block 0, warp 1: the totals of an earlier step's records (set par), into
+// the scalars and the observable row of that step.
+__device__ __forceinline__ void small_totals(const DevSys &s, int par, float vm2, float d, int r, int row) {
+    const unsigned long long *set = s.smallRec + (size_t)par * kSmallMaxTiles * 4;
+    const int lane = threadIdx.x & 31;
+    unsigned long long su = 0ull, sw = 0ull, sk = 0ull;
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+        su += __ldcg(set + 4 * (size_t)b + 1);
+        sw += __ldcg(set + 4 * (size_t)b + 2);
+        sk += __ldcg(set + 4 * (size_t)b + 3);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        su += __shfl_down_sync(0xffffffffu, su, o);
+        sw += __shfl_down_sync(0xffffffffu, sw, o);
+        sk += __shfl_down_sync(0xffffffffu, sk, o);
+    }
+    if (lane == 0) {
+        DevScalars *sc = s.sc;
+        const double U = from_fixed(su), W = from_fixed(sw), KE = from_fixed(sk);
+        sc->U = U;
+        sc->W = W;
+        sc->KE = KE;
+        sc->vvMax = vm2;
+        if (s.obs && row < s.obsCap) {
+            double *o = s.obs + (size_t)row * kObsCols;
+            o[0] = U;
+            o[1] = W;
+            o[2] = KE;
+            o[3] = (double)vm2;
+            o[4] = (double)d;
+            o[5] = (double)r;
+        }
+    }
+}
+
+// Shared memory of k_fsmall: scalars, the list rows, the step window, the
+// list build's stage (header, cell starts, window of cellSorted, entry
+// stage) and the cell starts of the binning.
+constexpr size_t kSmHdr = 512;
+__host__ __device__ constexpr size_t small_smem(int rows, int ncells) {
+    return kSmHdr + (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2) +
+           lp_stage_bytes() + (size_t)(kLStage + 1) * kFastBlock * sizeof(unsigned short) +
+           (((size_t)ncells + 1 + 3) & ~(size_t)3) * sizeof(int);
+}
+
+// Rebuild outcomes inside the small run
+constexpr int kSmallRebuilt = 0, kSmallStop = 1, kSmallPending = 2;
+
+// The state a thread of k_fsmall carries between steps and rebuilds.
+struct SmallSlot {
+    float2 pi, v;   // position and velocity of the thread's storage slot
+    float m;        // its mass
+    int id, excl;   // its particle id and exclusion group
+    int cnt;        // its list length
+};
+
+// The tile's list rows and window record (from the global list and
+// blockWin; the L2 copy, since this launch may have written them).
+__device__ __forceinline__ void small_load_tile(const DevSys &s, int rows, int4 *slist, int *wrec, int &G) {
+    const int t = blockIdx.x;
+    const int *bw = s.blockWin + kWinInts * (size_t)t;
+    for (int q = threadIdx.x; q < kWinInts; q += blockDim.x) wrec[q] = __ldcg(bw + q);
+    __syncthreads();
+    G = min(wrec[kWGroups], rows);
+    const int i = t * kFastBlock + threadIdx.x;
+    const int4 *lrow = reinterpret_cast<const int4 *>(s.nbr) + (size_t)t * kFastBlock + threadIdx.x;
+    if (i < s.Ncap)
+        for (int g = 0; g < G; g++) slist[g * kFastBlock + threadIdx.x] = __ldcg(lrow + (size_t)g * s.Ncap);
+}
+
+// Window bytes a step copies (16-byte spans of the record's pieces).
+__device__ __forceinline__ unsigned small_win_bytes(const int *wrec) {
+    unsigned b = 0;
+    if (wrec[kWLen] >= 0)
+        for (int q = 0; q < kWinPieces; q++) {
+            const int a = wrec[kWStart + q], c = wrec[kWCount + q];
+            if (c > 0) b += (unsigned)(((a + c + 1) & ~1) - (a & ~1)) * 8u;
+        }
+    return b;
 }
 
 // Steps come from DevScalars::smallLeft; a launch starts and ends with the
-// positions in pos0 (parity 0), so that the rebuild that may follow it has a
+// positions in pos0 (parity 0), so that a rebuild that may follow it has a
 // fixed parity.  use_h: inside the run graph, set its WHILE (steps left) and
-// IF (rebuild) conditions.
+// IF (rebuild pending) conditions.
 template <bool SIG1, bool WX, bool WY>
 __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cudaGraphConditionalHandle hw,
                                                           cudaGraphConditionalHandle hif, int use_h) {
     extern __shared__ float4 smem_f4[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
     PairEntry *tab = reinterpret_cast<PairEntry *>(sm);
-    int *flag = reinterpret_cast<int *>(sm + 32);   // [0] barrier ok, [1] rebuild
-    float *dsh = reinterpret_cast<float *>(sm + 40);  // the step's dispHi
-    float *red = reinterpret_cast<float *>(sm + 48);  // [warp][4]
-    int4 *slist = reinterpret_cast<int4 *>(sm + 128);
-    float2 *wpos = reinterpret_cast<float2 *>(sm + 128 + (size_t)rows * kFastBlock * sizeof(int4));
+    unsigned *xsh = reinterpret_cast<unsigned *>(sm + 32);  // the exchange's ok, OR, max
+    int *bsh = reinterpret_cast<int *>(sm + 44);             // [0] block flags, [1] block max groups
+    float *red = reinterpret_cast<float *>(sm + 52);         // [warp][4]
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(sm + 120);  // the window copies
+    unsigned long long *lbar = bar + 1;                                          // the list build's copies
+    int *wrec = reinterpret_cast<int *>(sm + 136);                               // the tile's window record
+    int *hd = wrec + kWinInts;                                                   // the list build's header
+    int4 *slist = reinterpret_cast<int4 *>(sm + kSmHdr);
+    float2 *wpos = reinterpret_cast<float2 *>(slist + (size_t)rows * kFastBlock);
+    int *csm = reinterpret_cast<int *>(wpos + kWinMax);
+    float4 *wc = reinterpret_cast<float4 *>(csm + kLPCs);
+    unsigned short(*ost)[kFastBlock] = reinterpret_cast<unsigned short(*)[kFastBlock]>(wc + kWinMax);
+    int *cst = reinterpret_cast<int *>(ost + (kLStage + 1));
+    static_assert(136 + (kWinInts + kLPHdr) * 4 <= kSmHdr, "small-run shared header");
     DevScalars *sc = s.sc;
     const int t = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i = t * kFastBlock + threadIdx.x;
     const bool act = i < s.N;
     const int ic = act ? i : 0;
-    if (threadIdx.x == 0) tab[0] = s.pair[0];
-    // the block's lists and window record hold for the whole launch
-    const int *bw = s.blockWin + kWinInts * (size_t)t;
-    const int len = bw[kWLen];
-    const int G = min(bw[kWGroups], rows);
-    const int4 *lrow = reinterpret_cast<const int4 *>(s.nbr) + (size_t)t * kFastBlock + threadIdx.x;
-    if (i < s.Ncap)
-        for (int g = 0; g < G; g++) slist[g * kFastBlock + threadIdx.x] = __ldg(lrow + (size_t)g * s.Ncap);
-    const int cnt = act ? min(s.nbrCount[ic], s.nbrCap) : 0;
-    const float m = s.mass[ic];
+    if (threadIdx.x == 0) {
+        tab[0] = s.pair[0];
+        mbar_init(bar, 1);
+        mbar_init(lbar, 1);
+        wpos[kWinGhost] = s.pos0[s.N];  // the ghost slot's far position, never moved
+    }
+    int G = 0;
+    small_load_tile(s, rows, slist, wrec, G);
+    unsigned wbytes = small_win_bytes(wrec);
+    SmallSlot me;
+    me.pi = s.pos0[ic];
+    me.v = s.vel[ic];
+    me.m = s.mass[ic];
+    me.id = s.perm[ic];
+    me.excl = s.excl[ic];
+    me.cnt = act ? min(s.nbrCount[ic], s.nbrCap) : 0;
     const float D = s.imgD;
+    const bool outside0 = sc->outside != 0;
     float dispHi = sc->dispHi;  // every block follows the same recurrence
     int row = sc->obsRow, stepNow = sc->stepNow;
     const int steps = sc->smallLeft;
+    const unsigned base = sc->gbTag;
+    unsigned xi = 0, wuse = 0, luse = 0;  // exchanges, window copies and list-build copies so far
+    // a step's totals that block 0 has still to sum (record set pset)
+    int pset = -1, prow = 0, pr = 0;
+    float pvm = 0.0f, pd = 0.0f;
     int p = 0, k = 0;
-    bool reb = false, failed = false;
+    bool pending = false, stop = false, failed = false;
+    __syncthreads();
+    // one exchange: true unless a wait gave up
+    auto xchg = [&](unsigned long long qa, unsigned long long qb, unsigned long long qc, unsigned word) {
+        small_exchange(s, base + xi + 1u, (int)(xi % 3u), qa, qb, qc, word, xsh);
+        if (blockIdx.x == 0 && warp == 1 && pset >= 0) small_totals(s, pset, pvm, pd, pr, prow);
+        __syncthreads();
+        pset = -1;
+        xi++;
+        if (xsh[0]) return true;
+        if (threadIdx.x == 0) atomicOr(&sc->overflow, kFlagTimeout);
+        failed = true;
+        return false;
+    };
+    // a bounded wait for a copy phase, the same verdict on every thread; a
+    // copy that never completed is reported and given one more bounded wait
+    auto copies_done = [&](unsigned long long *b, unsigned par) {
+        const bool ok = mbar_wait_bounded(b, par, kWaitLimit);
+        if (!__syncthreads_or(!ok)) return true;
+        if (threadIdx.x == 0) atomicOr(&sc->overflow, kFlagTimeout);
+        mbar_wait_bounded(b, par, kWaitLimit);
+        failed = true;
+        return false;
+    };
+    // block 0 clears the cell counts for the next binning (every block has
+    // added to them or read them)
+    auto clear_counts = [&]() {
+        if (blockIdx.x == 0)
+            for (int q = threadIdx.x; q < s.ncells; q += kFastBlock) s.cellCount[q] = 0;
+    };
+    // the rebuild of the positions in pos (parity p), inside the launch
+    auto small_rebuild = [&](float2 *pos) -> int {
+        // 1: cells and ranks among the cell's particles (counting atomics)
+        int c = 0, rk = 0;
+        unsigned fl = 0;
+        if (act) {
+            if (!(isfinite(me.pi.x) && isfinite(me.pi.y))) {
+                atomicOr(&sc->nonfinite, 1);
+                fl |= 1u;
+            }
+            if (outside_box(s, me.pi)) {
+                atomicOr(&sc->outside, 1);
+                fl |= 2u;
+            }
+            c = cell_col(me.pi.x, me.pi.y, s.ncx, s.ncy, s.Lx, s.Ly);
+            rk = atomicAdd(&s.cellCount[c], 1);
+        }
+        fl = (__syncthreads_or(fl & 1u) ? 1u : 0u) | (__syncthreads_or(fl & 2u) ? 2u : 0u);
+        if (!xchg(0ull, 0ull, 0ull, fl)) return kSmallStop;
+        const unsigned f1 = xsh[1];
+        if (f1 & 1u) {  // a non-finite position: the run fails
+            clear_counts();
+            return kSmallStop;
+        }
+        const bool walk_ok = (s.wrapx ? s.ncx >= 5 : s.ncx >= 3) && (s.wrapy ? s.ncy >= 5 : s.ncy >= 3) &&
+                             !outside0 && !(f1 & 2u);
+        // 2: every block scans the counts into cell starts (block 0 also
+        // writes them out), then the ids go to their cells
+        const int nc = s.ncells;
+        for (int q = threadIdx.x; q < nc; q += kFastBlock) cst[q] = __ldcg(s.cellCount + q);
+        __syncthreads();
+        {
+            const int per = (nc + kFastBlock - 1) / kFastBlock;
+            const int c0 = min((int)threadIdx.x * per, nc), c1 = min(c0 + per, nc);
+            int tot = 0;
+            for (int q = c0; q < c1; q++) tot += cst[q];
+            int x = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            int *ws = reinterpret_cast<int *>(red);  // 4 warp totals
+            if (lane == 31) ws[warp] = x;
+            __syncthreads();
+            int before = 0;
+            for (int w = 0; w < warp; w++) before += ws[w];
+            int run = before + x - tot;
+            for (int q = c0; q < c1; q++) {
+                const int v = cst[q];
+                cst[q] = run;
+                run += v;
+            }
+            if (threadIdx.x == 0) cst[nc] = s.N;
+        }
+        __syncthreads();
+        if (blockIdx.x == 0) {
+            for (int q = threadIdx.x; q <= nc; q += kFastBlock) s.cellStart[q] = cst[q];
+            if (threadIdx.x == 0) {
+                sc->nbrSum = 0ull;
+                sc->maxCount = 0;
+            }
+        }
+        unsigned f2 = 0;
+        if (act) {
+            const int slot0 = cst[c] + rk;
+            if (slot0 >= 0 && slot0 < s.N) s.unsorted[slot0] = me.id;
+            else f2 = 1u;  // inconsistent counts: never write outside the array
+        }
+        f2 = __syncthreads_or(f2) ? 1u : 0u;
+        if (f2 && threadIdx.x == 0) atomicOr(&sc->overflow, 2);
+        if (!xchg(0ull, 0ull, 0ull, f2)) return kSmallStop;
+        clear_counts();
+        if (xsh[1]) return kSmallStop;
+        // 3: the placement inside the cell by id (k_fplace), and the tile's
+        // window record from the cell starts here
+        unsigned f3 = 0;
+        if (act) {
+            const int b = cst[c], e = cst[c + 1];
+            int r = 0;
+            for (int q = b; q < e; q++) r += __ldcg(s.unsorted + q) < me.id;
+            const int ns = b + r;
+            if (ns < e) {
+                s.cellSorted[ns] = make_float4(me.pi.x, me.pi.y, __int_as_float(ns), __int_as_float(me.excl));
+                s.sortedIds[ns] = ns;
+                s.newCell[ns] = c;
+                s.sPos[ns] = me.pi;
+                s.sVel[ns] = me.v;
+                s.sAcc[ns] = s.acc[i];
+                s.sPerm[ns] = me.id;
+            } else {
+                f3 |= 1u;
+            }
+        }
+        if (threadIdx.x == 0) {
+            auto cell_of = [&](int q) {
+                int lo = 0, hi = nc - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (cst[mid] <= q) lo = mid;
+                    else hi = mid - 1;
+                }
+                return lo;
+            };
+            fwindow_record_t(s, t, walk_ok, [&](int q) { return cst[q]; }, cell_of);
+            bsh[0] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // the record just written (this thread's own stores)
+            const int *bw = s.blockWin + kWinInts * (size_t)t;
+            for (int q = 0; q < kWinInts; q++) wrec[q] = bw[q];
+            if (wrec[kWLen] < 0 || lp_cs_words(s, wrec) > kLPCs) bsh[0] = 2;  // no stage for this tile
+        }
+        __syncthreads();
+        f3 = (__syncthreads_or(f3) ? 1u : 0u) | (unsigned)bsh[0];
+        if ((f3 & 1u) && threadIdx.x == 0) atomicOr(&sc->overflow, 2);
+        if (!xchg(0ull, 0ull, 0ull, f3)) return kSmallStop;
+        if (xsh[1] & 1u) return kSmallStop;
+        if (xsh[1] & 2u) return kSmallPending;  // a tile without a stage: the rebuild kernels
+        // 4: the tile's lists (k_flist_p's walk), then the slot's new
+        // particle from the scratch arrays
+        if (threadIdx.x == 0) {
+            if (blockIdx.x == 0) {
+                sc->totalUpdates += 1;  // k_rebuild_begin
+                atomicAdd(&sc->builds, 1ull);
+            }
+            hd[kHT] = t;
+            hd[kHLen] = wrec[kWLen];
+            asm volatile("fence.proxy.async.global;" ::: "memory");
+            lp_issue(s, wrec, hd, csm, wc, lbar);
+        }
+        __syncthreads();
+        if (!copies_done(lbar, luse & 1u)) return kSmallStop;
+        luse++;
+        const int cap = s.nbrCap;
+        const int slot = i;
+        int kk = 0;
+        if (act) {
+            const bool two = hd[kHTwo] != 0;
+            int j = 0;
+            if (two) {
+                const int bnd = csm[min(max(hd[kHCsb + 4] + hd[kHColp + 4], 0), kLPCs - 1)];
+                j = slot >= bnd ? 1 : 0;
+            }
+            const int pown = !two ? 2 : (j == 0 ? 3 : 4);
+            const int self = min(max(slot + hd[kHDelta + pown], 0), kWinMax - 1);
+            const float4 e = wc[self];
+            int ix, iy;
+            cell_xy(e.x, e.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
+            const float2 q = make_float2(e.x, e.y);
+            TileStagePut sp;
+            sp.st = ost;
+            sp.col = threadIdx.x;
+            lp_stencil(s, hd, csm, wc, ix, iy, j, q, self, sp, kk);
+            if (kk > kLStage && cap > kLStage) {
+                int k2 = 0;
+                DirectPut16 dp;
+                dp.nbr16 = reinterpret_cast<unsigned short *>(s.nbr);
+                dp.slot = slot;
+                dp.cap = cap;
+                dp.Ncap = s.Ncap;
+                lp_stencil(s, hd, csm, wc, ix, iy, j, q, self, dp, k2);
+            }
+        }
+        const int kc = act ? min(kk, cap) : 0;
+        const int ng = (kc + 7) >> 3;
+        {
+            const int ngs = min(ng, kLStage / 8);
+            const int gmax = __reduce_max_sync(0xffffffffu, ngs);
+            int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
+            for (int g = 0; g < gmax; g++) {
+                if (g < ngs) {
+                    int v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int k0 = 8 * g + 2 * u;
+                        const unsigned lo = k0 < kc ? ost[k0][threadIdx.x] : kWinGhost;
+                        const unsigned hi = k0 + 1 < kc ? ost[k0 + 1][threadIdx.x] : kWinGhost;
+                        v[u] = (int)(lo | hi << 16);
+                    }
+                    out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
+                }
+            }
+            if (act && kc > kLStage && (kc & 7)) {
+                unsigned short *n16 = reinterpret_cast<unsigned short *>(s.nbr);
+                for (int q = kc; q < 8 * ng; q++) n16[nbr16_at(q, slot, s.Ncap)] = (unsigned short)kWinGhost;
+            }
+        }
+        if (act) {
+            const int id = __ldcg(s.sPerm + slot);
+            me.pi = __ldcg(s.sPos + slot);
+            me.v = __ldcg(s.sVel + slot);
+            const float2 na = __ldcg(s.sAcc + slot);
+            me.id = id;
+            me.m = __ldg(s.idMass + id);
+            me.cnt = kc;
+            s.nbrCount[slot] = kk;
+            pos[slot] = me.pi;
+            s.vel[slot] = me.v;
+            s.acc[slot] = na;
+            s.perm[slot] = id;
+            const_cast<float *>(s.mass)[slot] = me.m;
+        }
+        const int gm = __reduce_max_sync(0xffffffffu, ng);
+        const int kmax = __reduce_max_sync(0xffffffffu, act ? kk : 0);
+        const int ksum = __reduce_add_sync(0xffffffffu, act ? kk : 0);
+        if (threadIdx.x == 0) bsh[1] = 0;
+        __syncthreads();
+        unsigned f4 = 0;
+        if (lane == 0) {
+            atomicMax(&bsh[1], gm);
+            if (ksum) atomicAdd(&sc->nbrSum, (unsigned long long)ksum);
+            if (kmax > 0) atomicMax(&sc->maxCount, kmax);
+            if (kmax > cap) {
+                atomicOr(&sc->overflow, 1);
+                f4 = 1u;
+            }
+        }
+        f4 = __syncthreads_or(f4) ? 1u : 0u;
+        if (threadIdx.x == 0) {
+            s.blockWin[kWinInts * (size_t)t + kWGroups] = bsh[1];
+            wrec[kWGroups] = bsh[1];
+        }
+        __syncthreads();
+        // the tile's rows into shared memory (this block wrote them)
+        G = min(wrec[kWGroups], rows);
+        for (int g = 0; g < G; g++)
+            if (i < s.Ncap)
+                slist[g * kFastBlock + threadIdx.x] =
+                    __ldcg(reinterpret_cast<const int4 *>(s.nbr) + (size_t)g * s.Ncap + i);
+        wbytes = small_win_bytes(wrec);
+        if (!xchg(0ull, 0ull, 0ull, f4)) return kSmallStop;
+        if (xsh[1]) return kSmallStop;  // a list overflow: the run is repeated with longer lists
+        return kSmallRebuilt;
+    };
     for (; k < steps;) {
         const float2 *pin = p ? s.pos1 : s.pos0;
         float2 *pout = p ? s.pos0 : s.pos1;
-        // the window, read from L2 (other blocks wrote it since the barrier)
+        const int len = wrec[kWLen];
+        // the window by bulk copies (other blocks wrote it before the last
+        // exchange; the proxy fence orders their release before the copies)
         if (len >= 0) {
-            for (int q = 0; q < kWinPieces; q++) {
-                const int st = bw[kWStart + q], off = bw[kWOff + q], c = bw[kWCount + q];
-                for (int w = threadIdx.x; w < c; w += kFastBlock) wpos[off + w] = __ldcg(pin + st + w);
+            if (threadIdx.x == 0) {
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                mbar_expect_tx(bar, wbytes);
+                for (int q = 0; q < kWinPieces; q++) {
+                    const int a = wrec[kWStart + q], c = wrec[kWCount + q];
+                    if (c > 0) {
+                        const int a0 = a & ~1, e0 = (a + c + 1) & ~1;
+                        bulk_copy_g2s(wpos + wrec[kWOff + q] - (a & 1), pin + a0, (unsigned)(e0 - a0) * 8u, bar);
+                    }
+                }
             }
-            if (threadIdx.x == 0) wpos[kWinGhost] = pin[s.N];
+            if (!copies_done(bar, wuse & 1u)) break;
+            wuse++;
         }
-        __syncthreads();
-        const float2 pi = pin[ic];
-        const float2 v = s.vel[ic];
+        const float2 pi = me.pi;
+        const int cnt = me.cnt;
         float fx = 0.0f, fy = 0.0f, ue2 = 0.0f, we2 = 0.0f;
         const bool near = act && ((WX && (pi.x < D || pi.x > s.Lx - D)) || (WY && (pi.y < D || pi.y > s.Ly - D)));
         const bool img = __any_sync(0xffffffffu, near);
@@ -1973,9 +2553,9 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         float ue = 0.0f, we = 0.0f, ke = 0.0f, vvm = 0.0f;
         bool bad = false;
         if (act)
-            fast_finish<WX, WY>(s, i, MODE_MID, pi, m, v, pout, nullptr, fx, fy, ue2, we2, 0.0f, 0.0f, ue, we, ke,
-                                vvm, bad);
-        // the block's sums into this step's set
+            fast_finish<WX, WY>(s, i, MODE_MID, pi, me.m, me.v, pout, nullptr, fx, fy, ue2, we2, 0.0f, 0.0f, ue, we,
+                                ke, vvm, bad, &me.pi, &me.v);
+        // the block's sums
         const float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke), mx = warp_max(vvm);
         const unsigned anybad = __ballot_sync(0xffffffffu, bad);
         if (lane == 0) {
@@ -1986,9 +2566,10 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
             if (anybad) atomicOr(&sc->nonfinite, 1);
         }
         __syncthreads();
-        const int set = k % 3;
+        unsigned long long qa = 0ull, qb = 0ull, qc = 0ull;
+        float mm = 0.0f;
         if (threadIdx.x == 0) {
-            float a = 0.0f, b = 0.0f, c = 0.0f, mm = 0.0f;
+            float a = 0.0f, b = 0.0f, c = 0.0f;
             for (int w = 0; w < kFastBlock / 32; w++) {
                 a += red[4 * w];
                 b += red[4 * w + 1];
@@ -1996,75 +2577,60 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
                 mm = fmaxf(mm, red[4 * w + 3]);
             }
             bool ob = false;
-            const unsigned long long qa = to_fixed(a, ob), qb = to_fixed(b, ob), qc = to_fixed(c, ob);
+            qa = to_fixed(a, ob);
+            qb = to_fixed(b, ob);
+            qc = to_fixed(c, ob);
             if (ob) atomicOr(&sc->nonfinite, 2);
-            if (qa) atomicAdd(&sc->sacc[set][0], qa);
-            if (qb) atomicAdd(&sc->sacc[set][1], qb);
-            if (qc) atomicAdd(&sc->sacc[set][2], qc);
-            if (mm > 0.0f) atomicMax(reinterpret_cast<unsigned *>(&sc->sacc[set][3]), __float_as_uint(mm));
         }
-        if (!grid_barrier(sc, gridDim.x, flag)) {
-            if (threadIdx.x == 0) atomicOr(&sc->overflow, kFlagTimeout);
-            failed = true;
-            break;
-        }
+        const int stepSet = (int)(xi % 3u);
+        if (!xchg(qa, qb, qc, __float_as_uint(mm))) break;
         // the step's totals, the same on every block: the rebuild rule of
         // evalProps / NeighborList::update (md3dsystem.cpp:177, nn.cpp:118)
-        if (threadIdx.x == 0) {
-            const float vm2 = __uint_as_float(*(volatile unsigned *)&sc->sacc[set][3]);
-            const float d = dispHi + sqrtf(vm2) * s.dt;
-            const int r = (double)d > s.halfSkin;
-            flag[1] = r;
-            *dsh = d;
-            if (blockIdx.x == 0) {
-                const double U = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][0]);
-                const double W = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][1]);
-                const double KE = from_fixed(*(volatile unsigned long long *)&sc->sacc[set][2]);
-                sc->U = U;
-                sc->W = W;
-                sc->KE = KE;
-                sc->vvMax = vm2;
-                if (s.obs && row < s.obsCap) {
-                    double *o = s.obs + (size_t)row * kObsCols;
-                    o[0] = U;
-                    o[1] = W;
-                    o[2] = KE;
-                    o[3] = (double)vm2;
-                    o[4] = (double)d;
-                    o[5] = (double)r;
-                }
-                // the set two steps on: every block read it after the last barrier
-                const int nxt = (k + 2) % 3;
-                for (int q = 0; q < 4; q++) sc->sacc[nxt][q] = 0ull;
-            }
-        }
-        __syncthreads();
-        dispHi = *dsh;
-        reb = flag[1] != 0;
+        const float vm2 = __uint_as_float(xsh[2]);
+        const float d = dispHi + sqrtf(vm2) * s.dt;
+        const int r = (double)d > s.halfSkin;
+        pset = stepSet;
+        pvm = vm2;
+        pd = d;
+        pr = r;
+        prow = row;
+        dispHi = d;
         row++;
         stepNow++;
         p ^= 1;
         k++;
-        if (reb) break;
+        if (r) {
+            const int o = small_rebuild(p ? s.pos1 : s.pos0);
+            if (o == kSmallRebuilt) {
+                dispHi = 0.0f;  // k_rebuild_begin
+                continue;
+            }
+            if (o == kSmallPending) pending = true;
+            else stop = true;
+            break;
+        }
     }
-    // back to parity 0 (each thread its own slot), then the sums cleared for
-    // the next launch once every block has read them
-    if (p == 1 && act) s.pos0[i] = s.pos1[i];
-    const bool fin = grid_barrier(sc, gridDim.x, flag);
+    // back to parity 0 (each thread its own slot), then one more exchange so
+    // that every block has finished before the rebuild kernels or the next
+    // launch read the positions
+    if (p == 1 && act) s.pos0[i] = me.pi;
+    __syncthreads();
+    bool fin = false;
+    if (!failed) fin = xchg(0ull, 0ull, 0ull, 0u);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!fin) atomicOr(&sc->overflow, kFlagTimeout);
-        for (int q = 0; q < 3; q++)
-            for (int c = 0; c < 4; c++) sc->sacc[q][c] = 0ull;
-        // a barrier that gave up ends the run's loop (FEMMD_TIMEOUT)
-        const int left = (k > 0 && fin && !failed) ? steps - k : 0;
+        // an exchange that gave up, a non-finite position or a list
+        // overflow ends the run's loop
+        const int left = (k > 0 && fin && !stop) ? steps - k : 0;
         sc->dispHi = dispHi;
-        sc->rebuild = reb ? 1 : 0;
+        sc->rebuild = pending ? 1 : 0;
         sc->obsRow = row;
         sc->stepNow = stepNow;
         sc->smallDone = k;
         sc->smallLeft = left;
+        sc->gbTag = base + xi;
         if (use_h) {
-            cudaGraphSetConditional(hif, reb ? 1u : 0u);
+            cudaGraphSetConditional(hif, pending ? 1u : 0u);
             cudaGraphSetConditional(hw, left > 0 ? 1u : 0u);
         }
     }
@@ -2075,7 +2641,7 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
 template <bool SIG1, bool WX, bool WY>
 static cudaError_t launch_fsmall_t(cudaStream_t st, const DevSys &s, int rows) {
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
-    const size_t smem = small_smem(rows);
+    const size_t smem = small_smem(rows, s.ncells);
     auto kern = k_fsmall<SIG1, WX, WY>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e) return e;
@@ -2086,20 +2652,24 @@ static cudaError_t launch_fsmall_t(cudaStream_t st, const DevSys &s, int rows) {
     return cudaLaunchCooperativeKernel((const void *)kern, dim3(ntiles), dim3(kFastBlock), args, smem, st);
 }
 
+constexpr size_t kSmallMaxSmem = 200 * 1024;
+
 bool small_run_fits(const DevSys &s) {
-    if (!s.fast || !s.win16 || s.nBonded != 0 || s.wallOn || s.gravity > 0.0f || s.refWalls || s.areaUnits > 0 ||
-        s.trace || s.N <= 0)
+    if (!s.fast || !s.win16 || !s.smallRec || s.nBonded != 0 || s.wallOn || s.gravity > 0.0f || s.refWalls ||
+        s.areaUnits > 0 || s.trace || s.N <= 0)
         return false;
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     if (ntiles > kSmallMaxTiles) return false;
     const int rows = std::max(1, (s.nbrCap + 7) / 8);
+    const size_t smem = small_smem(rows, s.ncells);
+    if (smem > kSmallMaxSmem) return false;
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) return false;
     auto kern = s.sigmaOne ? (s.wrapx && s.wrapy ? k_fsmall<true, true, true> : nullptr)
                            : (s.wrapx && s.wrapy ? k_fsmall<false, true, true> : nullptr);
     if (!kern) return false;  // the small run is built for XY-periodic boxes
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem(rows)) ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kFastBlock, small_smem(rows)))
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kFastBlock, smem))
         return false;
     return per * sms >= ntiles;
 }
@@ -2115,7 +2685,7 @@ cudaError_t enqueue_small_run(Launch &L, const DevSys &s, cudaGraphConditionalHa
                               cudaGraphConditionalHandle hif) {
     const int rows = std::max(1, (s.nbrCap + 7) / 8);
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
-    const size_t smem = small_smem(rows);
+    const size_t smem = small_smem(rows, s.ncells);
     cudaError_t e;
     if (s.sigmaOne) {
         if ((e = cudaFuncSetAttribute(k_fsmall<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -17,7 +17,10 @@ Tolerances (stated here, used below):
     and the FP64 gradients along the two trajectories differ by as much, so
     no float forward can be closer;
   * GPU adjoint against central differences of the GPU forward in log sigma
-    (h = 1e-3): relative 1e-2 (FP32 forward noise);
+    (h = 1e-3): relative 1e-2 (FP32 forward noise); along one random
+    direction of each other input (log eps, E, nu, initial positions and
+    velocities): 1e-2 of the directional derivative plus 4e-6 |J|, the
+    spread of two FP32 forward runs of the dense compression;
   * the torch.autograd.Function wrapper gives the same gradients as the C ABI.
 """
 import numpy as np
@@ -171,6 +174,62 @@ def test_adjoint_vs_gpu_finite_differences():
     h = 1e-3
     fd = (J(h) - J(-h)) / (2 * h)
     assert abs(fd - g["log_sigma"]) <= 1e-2 * abs(g["log_sigma"]), (fd, g["log_sigma"])
+
+
+@pytest.mark.parametrize("key", ["log_eps", "E", "nu", "x0", "v0"])
+def test_adjoint_directional_finite_differences(key):
+    # the dense compression, where the disks press on each other: central
+    # differences of the GPU forward along one random direction of each input
+    # against the adjoint's directional derivative. E moves by exp(+-h d) per
+    # disk, nu and the initial state by +-h d; the initial state is rounded to
+    # float before the run, so the prediction uses the rounded difference.
+    # h per input keeps the FP64 run's own central-difference error below
+    # 4e-3 of the derivative (E 2e-4, nu 1e-4, x0 2e-3, v0 4e-3, log eps 3e-4)
+    # while the step's change of J is large against the FP32 forward's noise:
+    # two float runs of these stiff contacts land a few 1e-6 of J apart
+    # (J ~ 2e3), which bounds the check from below by 4e-6 |J|.
+    sc = S.compression(n_side=4, steps=100, phi=0.62, strain=0.05, center_jitter=0.3, T=0.02)
+    E0 = np.asarray(sc.meta["E"], np.float64)
+    nu0 = np.asarray(sc.meta["nu"], np.float64)
+    b = build(sc, E0, nu0, 0.0, 0.0)
+    x0, v0 = b.positions(), b.velocities()
+
+    def run(E=E0, nu=nu0, le=0.0, x=x0, v=v0):
+        s = build(sc, E, nu, le, 0.0)
+        s.set_positions_array(x)
+        s.set_velocities_array(v)
+        s.adjoint_forward(100, 20)
+        return s
+
+    def J(**kw):
+        ws, fe = run(**kw).adjoint_observable()
+        return ws + fe
+
+    s0 = run()
+    ws0, fe0 = s0.adjoint_observable()
+    g = s0.adjoint_backward()
+    rng = np.random.default_rng(11)
+    h = {"log_eps": 3e-2, "E": 1e-2, "nu": 1e-3, "x0": 1e-3, "v0": 3e-2}[key]
+    if key == "log_eps":
+        d = J(le=h) - J(le=-h)
+        pred = g["log_eps"] * 2 * h
+    elif key == "E":
+        u = rng.choice([-1.0, 1.0], size=E0.shape)
+        d = J(E=E0 * np.exp(h * u)) - J(E=E0 * np.exp(-h * u))
+        pred = float(np.dot(g["E"], E0 * (np.exp(h * u) - np.exp(-h * u))))
+    elif key == "nu":
+        u = rng.choice([-1.0, 1.0], size=nu0.shape)
+        d = J(nu=nu0 + h * u) - J(nu=nu0 - h * u)
+        pred = float(np.dot(g["nu"], 2 * h * u))
+    else:
+        z = x0 if key == "x0" else v0
+        u = rng.normal(size=z.shape)
+        zp = (z + h * u).astype(np.float32)
+        zm = (z - h * u).astype(np.float32)
+        d = J(**{key[0]: zp}) - J(**{key[0]: zm})
+        pred = float((np.asarray(g[key], np.float64) * (zp.astype(np.float64) - zm)).sum())
+    assert abs(pred) > 25 * 4e-6 * abs(ws0 + fe0), (key, pred)
+    assert abs(d - pred) <= 1e-2 * abs(pred) + 4e-6 * abs(ws0 + fe0), (key, d, pred)
 
 
 def test_torch_autograd_function():
