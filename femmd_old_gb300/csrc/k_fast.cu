@@ -1670,10 +1670,12 @@ __device__ __forceinline__ void lp_range(const float4 *wc, int wb, int we, float
     else lp_walk<true, true>(wc, wb, we, sx, sy, p, self, R2, out, k);
 }
 
-// All stencil ranges of a lane (cell (ix, iy), own column j of the tile).
+// The ranges of stencil column d (cell column ix + d - 1) of a lane (cell
+// (ix, iy), own column j of the tile).
 template <class Put>
-__device__ __forceinline__ void lp_stencil(const DevSys &s, const int *hd, const int *csm, const float4 *wc, int ix,
-                                           int iy, int j, float2 p, int self, const Put &out, int &k) {
+__device__ __forceinline__ void lp_stencil_col(const DevSys &s, const int *hd, const int *csm, const float4 *wc,
+                                               int ix, int iy, int j, float2 p, int self, int d, const Put &out,
+                                               int &k) {
     const int ncx = s.ncx, ncy = s.ncy;
     const float R2 = s.nnRadiusSq;
     const float Lx = s.wrapx ? s.Lx : 0.0f, Ly = s.wrapy ? s.Ly : 0.0f;
@@ -1685,23 +1687,28 @@ __device__ __forceinline__ void lp_stencil(const DevSys &s, const int *hd, const
         return csok ? csm[min(max(hd[kHCsb + q] + hd[kHColp + q] + r, 0), kLPCs - 1)]
                     : __ldg(s.cellStart + hd[kHColp + q] + r);
     };
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const int pm = !two ? 2 * d : (j == 0 ? 2 * d + 1 : 2 * d + 2);
-        const int pw = !two ? 2 * d + 1 : (j == 0 ? 2 * d : 2 * d + 3);
-        const int nx = ix + d - 1;
-        const float sx = nx < 0 ? -Lx : (nx == ncx ? Lx : 0.0f);
-        const int dm = hd[kHDelta + pm], dw = hd[kHDelta + pw];
-        if (iy > 0 && iy < ncy - 1) {
-            lp_range(wc, cs(pm, iy - 1) + dm, cs(pm, iy + 2) + dm, sx, 0.0f, p, self, R2, out, k);
-        } else if (iy == 0) {
-            lp_range(wc, cs(pw, ncy - 1) + dw, cs(pw, ncy) + dw, sx, -Ly, p, self, R2, out, k);
-            lp_range(wc, cs(pm, 0) + dm, cs(pm, 2) + dm, sx, 0.0f, p, self, R2, out, k);
-        } else {
-            lp_range(wc, cs(pm, ncy - 2) + dm, cs(pm, ncy) + dm, sx, 0.0f, p, self, R2, out, k);
-            lp_range(wc, cs(pw, 0) + dw, cs(pw, 1) + dw, sx, Ly, p, self, R2, out, k);
-        }
+    const int pm = !two ? 2 * d : (j == 0 ? 2 * d + 1 : 2 * d + 2);
+    const int pw = !two ? 2 * d + 1 : (j == 0 ? 2 * d : 2 * d + 3);
+    const int nx = ix + d - 1;
+    const float sx = nx < 0 ? -Lx : (nx == ncx ? Lx : 0.0f);
+    const int dm = hd[kHDelta + pm], dw = hd[kHDelta + pw];
+    if (iy > 0 && iy < ncy - 1) {
+        lp_range(wc, cs(pm, iy - 1) + dm, cs(pm, iy + 2) + dm, sx, 0.0f, p, self, R2, out, k);
+    } else if (iy == 0) {
+        lp_range(wc, cs(pw, ncy - 1) + dw, cs(pw, ncy) + dw, sx, -Ly, p, self, R2, out, k);
+        lp_range(wc, cs(pm, 0) + dm, cs(pm, 2) + dm, sx, 0.0f, p, self, R2, out, k);
+    } else {
+        lp_range(wc, cs(pm, ncy - 2) + dm, cs(pm, ncy) + dm, sx, 0.0f, p, self, R2, out, k);
+        lp_range(wc, cs(pw, 0) + dw, cs(pw, 1) + dw, sx, Ly, p, self, R2, out, k);
     }
+}
+
+// All stencil ranges of a lane, column by column.
+template <class Put>
+__device__ __forceinline__ void lp_stencil(const DevSys &s, const int *hd, const int *csm, const float4 *wc, int ix,
+                                           int iy, int j, float2 p, int self, const Put &out, int &k) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) lp_stencil_col(s, hd, csm, wc, ix, iy, j, p, self, d, out, k);
 }
 
 // The cell-start words a windowed tile's stage takes (window record bw): a
@@ -2138,14 +2145,18 @@ __device__ __forceinline__ void small_totals(const DevSys &s, int par, float vm2
     }
 }
 
+// k_fsmall's threads: one per storage slot of the tile for the steps; three
+// per slot (one per stencil column) for the list walk of a rebuild
+constexpr int kSmallThreads = 3 * kFastBlock;
+
 // Shared memory of k_fsmall: scalars, the list rows, the step window, the
-// list build's stage (header, cell starts, window of cellSorted, entry
-// stage) and the cell starts of the binning.
+// list build's stage (header, cell starts, window of cellSorted), an entry
+// stage and a count per stencil column, and the cell starts of the binning.
 constexpr size_t kSmHdr = 512;
 __host__ __device__ constexpr size_t small_smem(int rows, int ncells) {
     return kSmHdr + (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2) +
-           lp_stage_bytes() + (size_t)(kLStage + 1) * kFastBlock * sizeof(unsigned short) +
-           (((size_t)ncells + 1 + 3) & ~(size_t)3) * sizeof(int);
+           lp_stage_bytes() + 3 * (size_t)(kLStage + 1) * kFastBlock * sizeof(unsigned short) +
+           3 * (size_t)kFastBlock * sizeof(int) + (((size_t)ncells + 1 + 3) & ~(size_t)3) * sizeof(int);
 }
 
 // Rebuild outcomes inside the small run
@@ -2169,7 +2180,7 @@ __device__ __forceinline__ void small_load_tile(const DevSys &s, int rows, int4 
     G = min(wrec[kWGroups], rows);
     const int i = t * kFastBlock + threadIdx.x;
     const int4 *lrow = reinterpret_cast<const int4 *>(s.nbr) + (size_t)t * kFastBlock + threadIdx.x;
-    if (i < s.Ncap)
+    if (threadIdx.x < kFastBlock && i < s.Ncap)
         for (int g = 0; g < G; g++) slist[g * kFastBlock + threadIdx.x] = __ldcg(lrow + (size_t)g * s.Ncap);
 }
 
@@ -2189,8 +2200,8 @@ __device__ __forceinline__ unsigned small_win_bytes(const int *wrec) {
 // fixed parity.  use_h: inside the run graph, set its WHILE (steps left) and
 // IF (rebuild pending) conditions.
 template <bool SIG1, bool WX, bool WY>
-__global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cudaGraphConditionalHandle hw,
-                                                          cudaGraphConditionalHandle hif, int use_h) {
+__global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows, cudaGraphConditionalHandle hw,
+                                                             cudaGraphConditionalHandle hif, int use_h) {
     extern __shared__ float4 smem_f4[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
     PairEntry *tab = reinterpret_cast<PairEntry *>(sm);
@@ -2206,12 +2217,15 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
     int *csm = reinterpret_cast<int *>(wpos + kWinMax);
     float4 *wc = reinterpret_cast<float4 *>(csm + kLPCs);
     unsigned short(*ost)[kFastBlock] = reinterpret_cast<unsigned short(*)[kFastBlock]>(wc + kWinMax);
-    int *cst = reinterpret_cast<int *>(ost + (kLStage + 1));
+    int *kcol = reinterpret_cast<int *>(ost + 3 * (kLStage + 1));  // [stencil column][slot] entry counts
+    int *cst = kcol + 3 * kFastBlock;
     static_assert(136 + (kWinInts + kLPHdr) * 4 <= kSmHdr, "small-run shared header");
     DevScalars *sc = s.sc;
     const int t = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i = t * kFastBlock + threadIdx.x;
-    const bool act = i < s.N;
+    // threads below kFastBlock own the tile's storage slots
+    const bool worker = threadIdx.x < kFastBlock;
+    const int i = t * kFastBlock + (threadIdx.x & (kFastBlock - 1));
+    const bool act = worker && i < s.N;
     const int ic = act ? i : 0;
     if (threadIdx.x == 0) {
         tab[0] = s.pair[0];
@@ -2268,7 +2282,7 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
     // added to them or read them)
     auto clear_counts = [&]() {
         if (blockIdx.x == 0)
-            for (int q = threadIdx.x; q < s.ncells; q += kFastBlock) s.cellCount[q] = 0;
+            for (int q = threadIdx.x; q < s.ncells; q += kSmallThreads) s.cellCount[q] = 0;
     };
     // the rebuild of the positions in pos (parity p), inside the launch
     auto small_rebuild = [&](float2 *pos) -> int {
@@ -2299,11 +2313,13 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         // 2: every block scans the counts into cell starts (block 0 also
         // writes them out), then the ids go to their cells
         const int nc = s.ncells;
-        for (int q = threadIdx.x; q < nc; q += kFastBlock) cst[q] = __ldcg(s.cellCount + q);
+        for (int q = threadIdx.x; q < nc; q += kSmallThreads) cst[q] = __ldcg(s.cellCount + q);
         __syncthreads();
         {
+            // a run of cells per slot thread: its total, the scan of the
+            // totals (warps, then the kFastBlock / 32 warp sums), its run
             const int per = (nc + kFastBlock - 1) / kFastBlock;
-            const int c0 = min((int)threadIdx.x * per, nc), c1 = min(c0 + per, nc);
+            const int c0 = worker ? min((int)threadIdx.x * per, nc) : nc, c1 = min(c0 + per, nc);
             int tot = 0;
             for (int q = c0; q < c1; q++) tot += cst[q];
             int x = tot;
@@ -2312,11 +2328,12 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
                 const int y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
-            int *ws = reinterpret_cast<int *>(red);  // 4 warp totals
-            if (lane == 31) ws[warp] = x;
+            int *ws = reinterpret_cast<int *>(red);  // the slot warps' totals
+            if (worker && lane == 31) ws[warp] = x;
             __syncthreads();
             int before = 0;
-            for (int w = 0; w < warp; w++) before += ws[w];
+            if (worker)
+                for (int w = 0; w < warp; w++) before += ws[w];
             int run = before + x - tot;
             for (int q = c0; q < c1; q++) {
                 const int v = cst[q];
@@ -2327,7 +2344,7 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         }
         __syncthreads();
         if (blockIdx.x == 0) {
-            for (int q = threadIdx.x; q <= nc; q += kFastBlock) s.cellStart[q] = cst[q];
+            for (int q = threadIdx.x; q <= nc; q += kSmallThreads) s.cellStart[q] = cst[q];
             if (threadIdx.x == 0) {
                 sc->nbrSum = 0ull;
                 sc->maxCount = 0;
@@ -2407,25 +2424,37 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         luse++;
         const int cap = s.nbrCap;
         const int slot = i;
-        int kk = 0;
-        if (act) {
+        // three threads per slot walk the three stencil columns, each into
+        // its own entry stage; the slot's thread then joins them in column
+        // order (the order of k_flist_p's walk)
+        const int sub = threadIdx.x / kFastBlock;
+        int kd = 0, ix = 0, iy = 0, j = 0, self = 0;
+        float2 q = make_float2(0.0f, 0.0f);
+        if (slot < s.N) {
             const bool two = hd[kHTwo] != 0;
-            int j = 0;
             if (two) {
                 const int bnd = csm[min(max(hd[kHCsb + 4] + hd[kHColp + 4], 0), kLPCs - 1)];
                 j = slot >= bnd ? 1 : 0;
             }
             const int pown = !two ? 2 : (j == 0 ? 3 : 4);
-            const int self = min(max(slot + hd[kHDelta + pown], 0), kWinMax - 1);
+            self = min(max(slot + hd[kHDelta + pown], 0), kWinMax - 1);
             const float4 e = wc[self];
-            int ix, iy;
             cell_xy(e.x, e.y, s.ncx, s.ncy, s.Lx, s.Ly, ix, iy);
-            const float2 q = make_float2(e.x, e.y);
+            q = make_float2(e.x, e.y);
             TileStagePut sp;
-            sp.st = ost;
-            sp.col = threadIdx.x;
-            lp_stencil(s, hd, csm, wc, ix, iy, j, q, self, sp, kk);
+            sp.st = ost + sub * (kLStage + 1);
+            sp.col = threadIdx.x & (kFastBlock - 1);
+            lp_stencil_col(s, hd, csm, wc, ix, iy, j, q, self, sub, sp, kd);
+        }
+        kcol[threadIdx.x] = kd;
+        __syncthreads();
+        int k0 = 0, k1 = 0, kk = 0;
+        if (act) {
+            k0 = kcol[threadIdx.x];
+            k1 = kcol[kFastBlock + threadIdx.x];
+            kk = k0 + k1 + kcol[2 * kFastBlock + threadIdx.x];
             if (kk > kLStage && cap > kLStage) {
+                // entries past the stage: the whole walk again, straight to the list
                 int k2 = 0;
                 DirectPut16 dp;
                 dp.nbr16 = reinterpret_cast<unsigned short *>(s.nbr);
@@ -2435,9 +2464,15 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
                 lp_stencil(s, hd, csm, wc, ix, iy, j, q, self, dp, k2);
             }
         }
+        // entry k of the joined list (k < kLStage: every column's first kLStage entries are staged)
+        auto entry = [&](int k) -> unsigned {
+            const int d = k < k0 ? 0 : (k < k0 + k1 ? 1 : 2);
+            const int r = k - (d == 0 ? 0 : (d == 1 ? k0 : k0 + k1));
+            return ost[d * (kLStage + 1) + r][threadIdx.x];
+        };
         const int kc = act ? min(kk, cap) : 0;
         const int ng = (kc + 7) >> 3;
-        {
+        if (worker) {
             const int ngs = min(ng, kLStage / 8);
             const int gmax = __reduce_max_sync(0xffffffffu, ngs);
             int4 *out = reinterpret_cast<int4 *>(s.nbr) + slot;
@@ -2446,9 +2481,9 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
                     int v[4];
 #pragma unroll
                     for (int u = 0; u < 4; u++) {
-                        const int k0 = 8 * g + 2 * u;
-                        const unsigned lo = k0 < kc ? ost[k0][threadIdx.x] : kWinGhost;
-                        const unsigned hi = k0 + 1 < kc ? ost[k0 + 1][threadIdx.x] : kWinGhost;
+                        const int e0 = 8 * g + 2 * u;
+                        const unsigned lo = e0 < kc ? entry(e0) : kWinGhost;
+                        const unsigned hi = e0 + 1 < kc ? entry(e0 + 1) : kWinGhost;
                         v[u] = (int)(lo | hi << 16);
                     }
                     out[(size_t)g * s.Ncap] = make_int4(v[0], v[1], v[2], v[3]);
@@ -2497,8 +2532,8 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         __syncthreads();
         // the tile's rows into shared memory (this block wrote them)
         G = min(wrec[kWGroups], rows);
-        for (int g = 0; g < G; g++)
-            if (i < s.Ncap)
+        if (worker && i < s.Ncap)
+            for (int g = 0; g < G; g++)
                 slist[g * kFastBlock + threadIdx.x] =
                     __ldcg(reinterpret_cast<const int4 *>(s.nbr) + (size_t)g * s.Ncap + i);
         wbytes = small_win_bytes(wrec);
@@ -2558,7 +2593,7 @@ __global__ void __launch_bounds__(kFastBlock, 1) k_fsmall(DevSys s, int rows, cu
         // the block's sums
         const float su = warp_sum_f(ue), sw = warp_sum_f(we), sk = warp_sum_f(ke), mx = warp_max(vvm);
         const unsigned anybad = __ballot_sync(0xffffffffu, bad);
-        if (lane == 0) {
+        if (worker && lane == 0) {
             red[4 * warp + 0] = su;
             red[4 * warp + 1] = sw;
             red[4 * warp + 2] = sk;
@@ -2649,7 +2684,7 @@ static cudaError_t launch_fsmall_t(cudaStream_t st, const DevSys &s, int rows) {
     int ra = rows, ua = 0;
     cudaGraphConditionalHandle h0 = 0, h1 = 0;
     void *args[] = {&a, &ra, &h0, &h1, &ua};
-    return cudaLaunchCooperativeKernel((const void *)kern, dim3(ntiles), dim3(kFastBlock), args, smem, st);
+    return cudaLaunchCooperativeKernel((const void *)kern, dim3(ntiles), dim3(kSmallThreads), args, smem, st);
 }
 
 constexpr size_t kSmallMaxSmem = 200 * 1024;
@@ -2669,7 +2704,7 @@ bool small_run_fits(const DevSys &s) {
                            : (s.wrapx && s.wrapy ? k_fsmall<false, true, true> : nullptr);
     if (!kern) return false;  // the small run is built for XY-periodic boxes
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kFastBlock, smem))
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kSmallThreads, smem))
         return false;
     return per * sms >= ntiles;
 }
@@ -2691,12 +2726,12 @@ cudaError_t enqueue_small_run(Launch &L, const DevSys &s, cudaGraphConditionalHa
         if ((e = cudaFuncSetAttribute(k_fsmall<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem)))
             return e;
-        e = L.kernel(k_fsmall<true, true, true>, dim3(ntiles), dim3(kFastBlock), smem, s, rows, hw, hif, 1);
+        e = L.kernel(k_fsmall<true, true, true>, dim3(ntiles), dim3(kSmallThreads), smem, s, rows, hw, hif, 1);
     } else {
         if ((e = cudaFuncSetAttribute(k_fsmall<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem)))
             return e;
-        e = L.kernel(k_fsmall<false, true, true>, dim3(ntiles), dim3(kFastBlock), smem, s, rows, hw, hif, 1);
+        e = L.kernel(k_fsmall<false, true, true>, dim3(ntiles), dim3(kSmallThreads), smem, s, rows, hw, hif, 1);
     }
     if (e) return e;
     return L.cooperative_last();
