@@ -204,6 +204,9 @@ struct femmd_ctx {
     GraphSet graphs[2][2];      // [parity][0: kGraphUnits units, 1: one unit]
     GraphSet smallGraph;        // the small-system run's WHILE graph (fast mode)
     bool smallGraphFailed = false;
+    // the small run's exchange records and tag base are zero (set again after
+    // a wait that gave up, which can leave records ahead of the tag base)
+    bool smallClean = false;
     // profiling
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> forceEvents;
@@ -888,6 +891,7 @@ static femmd_status upload_topology(femmd_ctx *ctx) {
         CK(ctx->newCell.ensure(N));
         CK(ctx->blockWin.ensure(kWinInts * (size_t)((N + kFastBlock - 1) / kFastBlock)));
         CK(ctx->smallRec.ensure(3 * 4 * (size_t)kSmallMaxTiles));
+        ctx->smallClean = false;
         if (ctx->nBonded > 0) {
             // the cell-ordered position mirror (slot N: the ghost)
             CK(ctx->cpos0.ensure(N + 1)); CK(ctx->cpos1.ensure(N + 1)); CK(ctx->cslot.ensure(N));
@@ -1175,16 +1179,17 @@ static femmd_status build_small_graph(femmd_ctx *ctx, const DevSys &s) {
 // the host loops over direct cooperative launches, waiting once per launch.
 static femmd_status small_units(femmd_ctx *ctx, const DevSys &s, int units) {
     DevScalars *d = ctx->sc.p;
-    const size_t N = ctx->pos.size();
-    if (ctx->cur == 1) {
-        // the small run starts and ends on parity 0
-        CK(cudaMemcpyAsync(ctx->dpos0.p, ctx->dpos1.p, N * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
-        ctx->cur = 0;
-    }
+    // the small run starts from the current parity and ends on parity 0
     ctx->hsc->smallLeft = units;
-    CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(ctx->smallRec.p, 0, ctx->smallRec.n * sizeof(unsigned long long), ctx->stream));
-    CK(cudaMemsetAsync(&d->gbTag, 0, sizeof(unsigned), ctx->stream));
+    ctx->hsc->smallPar = ctx->cur;
+    static_assert(offsetof(DevScalars, smallPar) == offsetof(DevScalars, smallLeft) + sizeof(int), "small-run scalars");
+    CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->cur = 0;
+    if (!ctx->smallClean) {
+        CK(cudaMemsetAsync(ctx->smallRec.p, 0, ctx->smallRec.n * sizeof(unsigned long long), ctx->stream));
+        CK(cudaMemsetAsync(&d->gbTag, 0, sizeof(unsigned), ctx->stream));
+        ctx->smallClean = true;
+    }
     if (!ctx->smallGraphFailed && !ctx->smallGraph.x && build_small_graph(ctx, s) != FEMMD_OK) {
         ctx->smallGraph.release();
         ctx->smallGraphFailed = true;
@@ -2292,8 +2297,10 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         if ((st = collect_profile(ctx))) return st;
         if ((st = read_scalars(ctx))) return st;
         if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
-        if (ctx->hsc->overflow & 8)
+        if (ctx->hsc->overflow & 8) {
+            ctx->smallClean = false;
             return fail(ctx, FEMMD_TIMEOUT, "a step block's copy to shared memory did not complete in time");
+        }
         if (!ctx->hsc->overflow && !aborted) {
             traj_commit(ctx->traj);
             ctx->steps += steps;

@@ -79,9 +79,10 @@ struct DevScalars {
     unsigned long long accU, accW, accK;  // fixed-point accumulators (two's complement)
     unsigned int vvMaxBits, pad1;         // max v^2 as float bits (v^2 >= 0)
     // the small-system run (k_fsmall): the tag base of its next launch's
-    // exchanges, the steps one launch advanced and the steps left
+    // exchanges, the steps one launch advanced, the steps left and the
+    // position parity the next launch starts from (it ends on parity 0)
     unsigned int gbTag, pad2;
-    int smallDone, smallLeft;
+    int smallDone, smallLeft, smallPar, pad3;
 };
 
 enum StepMode { MODE_FORCES = 0, MODE_FIRST = 1, MODE_MID = 2, MODE_LAST = 3, MODE_INIT = 4 };

@@ -33,6 +33,8 @@
 // Integrator::doStep (integrator.cpp:8-29, 100-135).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <mutex>
+#include <vector>
 #include "femmd_internal.h"
 #include "launch.h"
 #include "device_common.cuh"
@@ -42,6 +44,53 @@
 namespace femmd {
 
 constexpr int kPermBlock = 1024;  // cell slots per block of the storage reorder
+
+// A kernel's dynamic shared-memory limit raised to at least 'smem', and the
+// blocks of 'threads' threads it keeps resident on the whole GPU at that
+// size, queried once per device, kernel, block size and size: the attribute
+// call and the occupancy query would cost host time at every launch
+// otherwise.  The limit only grows (it is one value per kernel, and launches
+// of one kernel take different sizes).
+static cudaError_t kernel_setup(const void *fn, int threads, size_t smem, int *resident) {
+    struct Occ {
+        int dev;
+        const void *fn;
+        int threads;
+        size_t smem;
+        int resident;
+    };
+    struct Limit {
+        int dev;
+        const void *fn;
+        size_t smem;
+    };
+    static std::mutex mu;
+    static std::vector<Occ> occ;
+    static std::vector<Limit> limits;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    std::lock_guard<std::mutex> g(mu);
+    Limit *lim = nullptr;
+    for (Limit &l : limits)
+        if (l.dev == dev && l.fn == fn) lim = &l;
+    if (!lim || lim->smem < smem) {
+        if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+        if (lim) lim->smem = smem;
+        else limits.push_back(Limit{dev, fn, smem});
+    }
+    for (const Occ &c : occ)
+        if (c.dev == dev && c.fn == fn && c.threads == threads && c.smem == smem) {
+            *resident = c.resident;
+            return cudaSuccess;
+        }
+    int sms = 0, per = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem))) return e;
+    *resident = per * sms;
+    occ.push_back(Occ{dev, fn, threads, smem, *resident});
+    return cudaSuccess;
+}
 
 // ================================================================ rebuild
 
@@ -769,8 +818,8 @@ cudaError_t enqueue_rebuild_fast(Launch &L, const DevSys &s, int parity, int che
     if (small_bin_fits(s)) {
         // a small system: binning and placement in one block, then the lists
         const size_t smem = small_bin_smem(s);
-        if ((e = cudaFuncSetAttribute(k_fbin_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
+        int resident = 0;
+        if ((e = kernel_setup((const void *)k_fbin_small, kSmallBinThreads, smem, &resident))) return e;
         if ((e = L.kernel(k_fbin_small, dim3(1), dim3(kSmallBinThreads), smem, s, parity, check))) return e;
         return launch_flist_p(L, s, parity, check);
     }
@@ -1316,8 +1365,8 @@ static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity
     int rows = s.nbrCap / 4;
     if (fstep_smem(s, MT, SG, rows) > kFastSmemMax) rows = 0;
     const size_t smem = fstep_smem(s, MT, SG, rows);
-    cudaError_t e = cudaFuncSetAttribute(k_fstep<MT, SG, SIG1, WX, WY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    int resident = 0;
+    cudaError_t e = kernel_setup((const void *)k_fstep<MT, SG, SIG1, WX, WY>, kFastBlock, smem, &resident);
     if (e) return e;
     return L.kernel(k_fstep<MT, SG, SIG1, WX, WY>, g, b, smem, s, mode, parity, h, use_h, rows);
 }
@@ -1579,14 +1628,11 @@ static cudaError_t launch_fstep_p(Launch &L, const DevSys &s, int mode, int pari
                              : std::max(1, std::min(s.nbrCap / 4, kPRows));
     const size_t smem = pstep_smem(rows, MT ? s.numTypes * s.numTypes : 1);
     auto kern = k_fstep_p<MT, SIG1, WX, WY>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int resident = 0;
+    cudaError_t e = kernel_setup((const void *)kern, kPBlock, smem, &resident);
     if (e) return e;
-    int dev = 0, sms = 0, per = 0;
-    if ((e = cudaGetDevice(&dev))) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kPBlock, smem))) return e;
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
-    const int grid = std::max(1, std::min(ntiles, std::max(1, per) * sms));
+    const int grid = std::max(1, std::min(ntiles, std::max(1, resident)));
     return L.kernel(kern, dim3(grid), dim3(kPBlock), smem, s, mode, parity, h, use_h, rows);
 }
 
@@ -2004,14 +2050,11 @@ __global__ void __launch_bounds__(kPBlock, kLPMinBlocks) k_flist_p(DevSys s, int
 
 static cudaError_t launch_flist_p(Launch &L, const DevSys &s, int parity, int check) {
     const size_t smem = lp_smem();
-    cudaError_t e = cudaFuncSetAttribute(k_flist_p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int resident = 0;
+    cudaError_t e = kernel_setup((const void *)k_flist_p, kPBlock, smem, &resident);
     if (e) return e;
-    int dev = 0, sms = 0, per = 0;
-    if ((e = cudaGetDevice(&dev))) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_flist_p, kPBlock, smem))) return e;
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
-    const int grid = std::max(1, std::min(ntiles, std::max(1, per) * sms));
+    const int grid = std::max(1, std::min(ntiles, std::max(1, resident)));
     return L.kernel(k_flist_p, dim3(grid), dim3(kPBlock), smem, s, parity, check);
 }
 
@@ -2195,9 +2238,9 @@ __device__ __forceinline__ unsigned small_win_bytes(const int *wrec) {
     return b;
 }
 
-// Steps come from DevScalars::smallLeft; a launch starts and ends with the
-// positions in pos0 (parity 0), so that a rebuild that may follow it has a
-// fixed parity.  use_h: inside the run graph, set its WHILE (steps left) and
+// Steps come from DevScalars::smallLeft and the start parity from
+// DevScalars::smallPar; a launch ends with the positions in pos0 (parity 0),
+// so that a rebuild that may follow it has a fixed parity.  use_h: inside the run graph, set its WHILE (steps left) and
 // IF (rebuild pending) conditions.
 template <bool SIG1, bool WX, bool WY>
 __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows, cudaGraphConditionalHandle hw,
@@ -2236,8 +2279,9 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
     int G = 0;
     small_load_tile(s, rows, slist, wrec, G);
     unsigned wbytes = small_win_bytes(wrec);
+    int p = sc->smallPar;  // the parity of the current positions
     SmallSlot me;
-    me.pi = s.pos0[ic];
+    me.pi = (p ? s.pos1 : s.pos0)[ic];
     me.v = s.vel[ic];
     me.m = s.mass[ic];
     me.id = s.perm[ic];
@@ -2253,7 +2297,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
     // a step's totals that block 0 has still to sum (record set pset)
     int pset = -1, prow = 0, pr = 0;
     float pvm = 0.0f, pd = 0.0f;
-    int p = 0, k = 0;
+    int k = 0;
     bool pending = false, stop = false, failed = false;
     __syncthreads();
     // one exchange: true unless a wait gave up
@@ -2663,6 +2707,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
         sc->stepNow = stepNow;
         sc->smallDone = k;
         sc->smallLeft = left;
+        sc->smallPar = 0;
         sc->gbTag = base + xi;
         if (use_h) {
             cudaGraphSetConditional(hif, pending ? 1u : 0u);
@@ -2678,7 +2723,8 @@ static cudaError_t launch_fsmall_t(cudaStream_t st, const DevSys &s, int rows) {
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     const size_t smem = small_smem(rows, s.ncells);
     auto kern = k_fsmall<SIG1, WX, WY>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int resident = 0;
+    cudaError_t e = kernel_setup((const void *)kern, kSmallThreads, smem, &resident);
     if (e) return e;
     DevSys a = s;
     int ra = rows, ua = 0;
@@ -2698,15 +2744,12 @@ bool small_run_fits(const DevSys &s) {
     const int rows = std::max(1, (s.nbrCap + 7) / 8);
     const size_t smem = small_smem(rows, s.ncells);
     if (smem > kSmallMaxSmem) return false;
-    int dev = 0, sms = 0, per = 0;
-    if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) return false;
     auto kern = s.sigmaOne ? (s.wrapx && s.wrapy ? k_fsmall<true, true, true> : nullptr)
                            : (s.wrapx && s.wrapy ? k_fsmall<false, true, true> : nullptr);
     if (!kern) return false;  // the small run is built for XY-periodic boxes
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kSmallThreads, smem))
-        return false;
-    return per * sms >= ntiles;
+    int resident = 0;
+    if (kernel_setup((const void *)kern, kSmallThreads, smem, &resident)) return false;
+    return resident >= ntiles;
 }
 
 cudaError_t launch_small_run(cudaStream_t st, const DevSys &s) {
@@ -2722,15 +2765,12 @@ cudaError_t enqueue_small_run(Launch &L, const DevSys &s, cudaGraphConditionalHa
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     const size_t smem = small_smem(rows, s.ncells);
     cudaError_t e;
+    int resident = 0;
     if (s.sigmaOne) {
-        if ((e = cudaFuncSetAttribute(k_fsmall<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem)))
-            return e;
+        if ((e = kernel_setup((const void *)k_fsmall<true, true, true>, kSmallThreads, smem, &resident))) return e;
         e = L.kernel(k_fsmall<true, true, true>, dim3(ntiles), dim3(kSmallThreads), smem, s, rows, hw, hif, 1);
     } else {
-        if ((e = cudaFuncSetAttribute(k_fsmall<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem)))
-            return e;
+        if ((e = kernel_setup((const void *)k_fsmall<false, true, true>, kSmallThreads, smem, &resident))) return e;
         e = L.kernel(k_fsmall<false, true, true>, dim3(ntiles), dim3(kSmallThreads), smem, s, rows, hw, hif, 1);
     }
     if (e) return e;

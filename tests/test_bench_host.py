@@ -2,7 +2,8 @@
 workload, --gpus N without a launcher becomes a torchrun command on the
 loopback rendezvous, and several ranks split the batched ensemble so that
 every replica is advanced by exactly one rank (the same split on every rank,
-without communication)."""
+without communication), and which workloads take the cooperative
+small-system run."""
 import os
 import sys
 
@@ -109,3 +110,17 @@ def test_single_process_stand_in_has_the_group_methods_the_bench_uses():
         assert callable(getattr(solo, name)) and callable(getattr(Group, name))
     assert solo.sum(3.5) == 3.5 and solo.max(2.0) == 2.0
     assert (solo.world, solo.rank, solo.local) == (1, 0, 0)
+
+
+def test_small_run_path_follows_the_library_rule():
+    # the cooperative small-system run: fast mode, one kind, no bonded
+    # particles, walls, gravity or area springs, XY-periodic, <= 128 blocks
+    lj = S.lj_fluid()
+    lj.meta["types"] = 1
+    assert bench.small_run_path(lj, 4096, False)
+    assert not bench.small_run_path(lj, 4096, True)
+    assert not bench.small_run_path(lj, bench.SMALL_RUN_MAX_ATOMS + 1, False)
+    walled = S.lj_fluid()
+    walled.meta["types"] = 1
+    walled.add("set_gravity", 0.1)
+    assert not bench.small_run_path(walled, 4096, False)
