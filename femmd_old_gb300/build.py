@@ -66,5 +66,38 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
+FRONTEND = os.path.join(PKG, "frontend", "md_js.cpp")
+FRONTEND_BIN = os.path.join(OUT, "md_js")
+
+
+def build_frontend(duktape_dir: str) -> str:
+    """The script front end (frontend/md_js.cpp) linked against libfemmd.so,
+    with the Duktape engine compiled from duktape_dir (duktape.cpp,
+    duktape.h, duk_config.h: third-party sources this repository does not
+    carry).  Returns the binary's path."""
+    for f in ("duktape.cpp", "duktape.h", "duk_config.h"):
+        if not os.path.exists(os.path.join(duktape_dir, f)):
+            raise FileNotFoundError(os.path.join(duktape_dir, f))
+    os.makedirs(OUT, exist_ok=True)
+    engine = os.path.join(OUT, "duktape.o")
+    cxx = os.environ.get("CXX", "g++")
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("front end build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+    if _stale(engine, [os.path.join(duktape_dir, "duktape.cpp")]):
+        run([cxx, "-O2", "-w", "-c", os.path.join(duktape_dir, "duktape.cpp"), "-I" + duktape_dir, "-o", engine])
+    if _stale(FRONTEND_BIN, [FRONTEND, engine, LIB, os.path.join(ROOT, "include", "femmd.h")]):
+        run([cxx, "-O2", "-std=c++17", "-Wall", FRONTEND, engine, "-I" + duktape_dir,
+             "-I" + os.path.join(ROOT, "include"), "-L" + PKG, "-lfemmd", "-Wl,-rpath," + PKG, "-lm",
+             "-o", FRONTEND_BIN])
+    # where the engine came from (scripts shipped beside it are the tests' inputs)
+    with open(FRONTEND_BIN + ".src", "w") as f:
+        f.write(os.path.abspath(duktape_dir) + "\n")
+    return FRONTEND_BIN
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
