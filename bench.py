@@ -88,7 +88,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--probe", default=None,
                     choices=["midrun_rebuild", "batch_run10", "batch_run10_single", "adjoint", "extras", "lj_1m",
-                             "lj_1m_rebuild"],
+                             "lj_1m_rebuild", "lj_small_rebuild"],
                     help="run one small fixed workload for a profiler capture and exit (no JSON line)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
@@ -703,6 +703,21 @@ def probe(name, mode="fast"):
         S.lj_fluid(n_side=1000).replay(s)
         s.run(0)
         s.run(50)
+        s.sync()
+        torch.cuda.nvtx.range_push("rebuild")
+        for _ in range(3):
+            s.build_nn()
+        s.sync()
+        torch.cuda.nvtx.range_pop()
+    elif name == "lj_small_rebuild":
+        # three full neighbour rebuilds of config 1 (4096 LJ atoms) after
+        # run(200), in the force mode of --force-mode, inside the NVTX range
+        # "rebuild" (the fast mode's one-block binning and list build)
+        s = F.System()
+        s.set_force_mode(FORCE_MODES[mode])
+        S.lj_fluid().replay(s)
+        s.run(0)
+        s.run(200)
         s.sync()
         torch.cuda.nvtx.range_push("rebuild")
         for _ in range(3):
