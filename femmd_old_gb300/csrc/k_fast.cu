@@ -1386,23 +1386,34 @@ static cudaError_t launch_fstep(Launch &L, const DevSys &s, int mode, int parity
 // further copy and waits (bounded) for those in flight before it leaves.
 constexpr int kPBlock = kFastBlock + 32;  // consumer threads + the producer warp
 constexpr int kPRows = 8;                 // list rows staged per tile (the rest read from global memory)
-constexpr int kPRows16 = 5;               // the same with 16-bit entries (40 entries)
+#ifndef FEMMD_FAST_PROWS16
+#define FEMMD_FAST_PROWS16 5
+#endif
+constexpr int kPRows16 = FEMMD_FAST_PROWS16;  // the same with 16-bit entries (8 per row)
 #ifndef FEMMD_FAST_PMINB
 #define FEMMD_FAST_PMINB 5
 #endif
 constexpr int kPMinBlocks = FEMMD_FAST_PMINB;
+#ifndef FEMMD_FAST_PSTAGES
+#define FEMMD_FAST_PSTAGES 2
+#endif
+constexpr int kPStages = FEMMD_FAST_PSTAGES;  // stages per block: tiles copied ahead of the one worked + 1
+static_assert(kPStages >= 2 && kPStages <= 4, "persistent step stages");
 
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// Shared memory of a persistent block: full[2], empty[2], the pair table
-// entry, then per stage 'rows' list rows and the window.
+// Shared memory of a persistent block: full[kPStages], empty[kPStages], the
+// pair table entry, then per stage 'rows' list rows and the window.
 __host__ __device__ constexpr size_t pstage_bytes(int rows) {
     return (size_t)rows * kFastBlock * sizeof(int4) + (size_t)kWinMax * sizeof(float2);
 }
-__host__ __device__ constexpr size_t pstage_base(int ntab) { return 32 + (size_t)ntab * sizeof(PairEntry); }
-static size_t pstep_smem(int rows, int ntab) { return pstage_base(ntab) + 2 * pstage_bytes(rows); }
+constexpr size_t kPBarBytes = 2 * kPStages * sizeof(unsigned long long);
+__host__ __device__ constexpr size_t pstage_base(int ntab) {
+    return ((kPBarBytes + 31) & ~(size_t)31) + (size_t)ntab * sizeof(PairEntry);
+}
+static size_t pstep_smem(int rows, int ntab) { return pstage_base(ntab) + kPStages * pstage_bytes(rows); }
 
 // A consumer's own particle data of one tile, loaded a tile ahead.
 struct PTile {
@@ -1433,8 +1444,8 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
     extern __shared__ float4 smem_f4[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(smem_f4);
     unsigned long long *full = reinterpret_cast<unsigned long long *>(sm);
-    unsigned long long *empty = full + 2;
-    PairEntry *tab = reinterpret_cast<PairEntry *>(sm + 32);
+    unsigned long long *empty = full + kPStages;
+    PairEntry *tab = reinterpret_cast<PairEntry *>(sm + ((kPBarBytes + 31) & ~(size_t)31));
     const int ntab = MT ? s.numTypes * s.numTypes : 1;
     // window source: the positions when cell slots are storage slots, else
     // their cell-ordered mirror
@@ -1449,14 +1460,13 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
     };
     const int ntiles = (s.N + kFastBlock - 1) / kFastBlock;
     if (threadIdx.x == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
-        mbar_init(&empty[0], kFastBlock / 32);
-        mbar_init(&empty[1], kFastBlock / 32);
-        if (!MT) tab[0] = s.pair[0];
         const float2 g = __ldg(pin + s.N);  // the ghost slot's far position
-        wpos_of(0)[kWinGhost] = g;
-        wpos_of(1)[kWinGhost] = g;
+        for (int q = 0; q < kPStages; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], kFastBlock / 32);
+            wpos_of(q)[kWinGhost] = g;
+        }
+        if (!MT) tab[0] = s.pair[0];
         if (s.trace && blockIdx.x == 0) {
             const int row = s.sc->obsRow;
             if (row < s.obsCap) s.trace[(size_t)row * kTraceCols + 2] = global_ns();
@@ -1481,7 +1491,7 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 for (int q = 0; q <= kWGroups; q++) wv[q] = bw[q];
             }
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
-                const int st = k & 1, use = k >> 1;
+                const int st = k % kPStages, use = k / kPStages;
                 if (use > 0) {
                     // the stage's last tile: consumed, and its copies landed
                     live = mbar_wait_sleep(&empty[st], (use - 1) & 1, kSleepLimit, kSleepNs) &&
@@ -1524,10 +1534,11 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
                 }
             }
             if (!live) {
-                // copies of the last two tiles issued may still be in flight:
-                // a bounded wait each
-                for (int kl = k - 2; kl < k; kl++)
-                    if (kl >= 0) mbar_wait_sleep(&full[kl & 1], (kl >> 1) & 1, kSleepLimit, kSleepNs);
+                // copies of the last kPStages tiles issued may still be in
+                // flight: a bounded wait each
+                for (int kl = k - kPStages; kl < k; kl++)
+                    if (kl >= 0)
+                        mbar_wait_sleep(&full[kl % kPStages], (kl / kPStages) & 1, kSleepLimit, kSleepNs);
             }
         }
         __syncwarp();
@@ -1543,10 +1554,10 @@ __global__ void __launch_bounds__(kPBlock, kPMinBlocks) k_fstep_p(DevSys s, int 
             const PTile cur = nx;
             const int tn = t + gridDim.x;
             if (tn < ntiles) nx = ptile_load(s, pin, tn, mode);
-            const int st = k & 1;
+            const int st = k % kPStages;
             bool ok = false;
             if (!dead) {
-                ok = mbar_wait_bounded(&full[st], (k >> 1) & 1, kWaitLimit);
+                ok = mbar_wait_bounded(&full[st], (k / kPStages) & 1, kWaitLimit);
                 if (!ok) {
                     dead = true;
                     atomicOr(&s.sc->overflow, kFlagTimeout);
