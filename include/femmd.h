@@ -36,7 +36,8 @@ typedef enum {
     FEMMD_CAPACITY_OVERFLOW = 2,  /* a capacity could not be grown */
     FEMMD_NONFINITE = 3,          /* a force or energy became NaN/inf */
     FEMMD_CUDA_ERROR = 4,         /* a CUDA call failed (no GPU, OOM, ...) */
-    FEMMD_TIMEOUT = 5,            /* a bounded device wait expired (the fast step's copies) */
+    FEMMD_TIMEOUT = 5,            /* a bounded device wait expired (the fast step's copies, the small-system
+                                     run's grid-wide exchanges) */
     FEMMD_NOT_READY = 6,          /* call order: e.g. run before init_neighbor_list */
     FEMMD_UNSUPPORTED = 7         /* feature of the reference outside this path */
 } femmd_status;
