@@ -258,14 +258,18 @@ def test_fast_lj_1m_full_size_sets_and_forces():
     assert np.abs(p1 - p0).max() < 1e-2
 
 
-def test_small_system_run_matches_the_step_kernels():
-    """Config 1 (4096 LJ atoms) in the fast mode advances a run's middle steps
-    in one cooperative launch per rebuild (k_fsmall).  The same run with every
+@pytest.mark.parametrize("n_side", [64, 120, 10])
+def test_small_system_run_matches_the_step_kernels(n_side):
+    """Small fast-mode systems advance a run's steps and rebuilds in one
+    cooperative launch (k_fsmall): config 1 (64^2 = 4096 LJ atoms), 120^2 =
+    14,400 atoms (113 step blocks, near the 128 the run takes), and 10^2 atoms
+    in a box of 3 x 3 cells, where no step block has a window and every
+    rebuild is handed back to the rebuild kernels.  The same run with every
     kernel launched on its own (profiling mode: k_fstep_p and the rebuild
     kernels) gives bit-identical positions, velocities and accelerations and
     the same rebuilds; the per-step energies agree within 1e-9 of |U| (exact
     fixed-point sums of per-block float partial sums that differ)."""
-    sc = S.lj_fluid()
+    sc = S.lj_fluid(n_side=n_side)
     a = fast_system()
     sc.replay(a)
     a.run(0)
