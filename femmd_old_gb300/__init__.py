@@ -359,6 +359,11 @@ class System:
     def set_profiling(self, on):
         self._call("femmd_set_profiling", int(bool(on)))
 
+    def test_expire_next_exchange(self):
+        """Tests of the failure path: the next small-system run's first
+        grid-wide exchange is left to time out (run() raises FEMMD_TIMEOUT)."""
+        self._call("femmd_test_expire_next_exchange")
+
     def counts(self):
         return dict(bonds=self._L.femmd_get_num_bonds(self._h), triangles=self._L.femmd_get_num_triangles(self._h),
                     elastomers=self._L.femmd_get_num_elastomers(self._h))

@@ -110,6 +110,7 @@ SIGNATURES = {
     "femmd_event_record": (i_, [P, i_]),
     "femmd_event_elapsed": (i_, [P, i_, i_, fp]),
     "femmd_set_profiling": (i_, [P, i_]),
+    "femmd_test_expire_next_exchange": (i_, [P]),
     "femmd_get_profile": (i_, [P, dp, llp, dp, llp, llp]),
     "femmd_bin_cells_noalloc": (i_, [P, i_, d_, d_, i_, i_, P, P, P]),
     "femmd_batch_create": (i_, [i_, C.POINTER(P)]),

@@ -207,6 +207,7 @@ struct femmd_ctx {
     // the small run's exchange records and tag base are zero (set again after
     // a wait that gave up, which can leave records ahead of the tag base)
     bool smallClean = false;
+    bool testExpire = false;  // femmd_test_expire_next_exchange
     // profiling
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> forceEvents;
@@ -1182,8 +1183,12 @@ static femmd_status small_units(femmd_ctx *ctx, const DevSys &s, int units) {
     // the small run starts from the current parity and ends on parity 0
     ctx->hsc->smallLeft = units;
     ctx->hsc->smallPar = ctx->cur;
-    static_assert(offsetof(DevScalars, smallPar) == offsetof(DevScalars, smallLeft) + sizeof(int), "small-run scalars");
-    CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->hsc->testWithhold = ctx->testExpire ? 1 : 0;
+    ctx->testExpire = false;
+    static_assert(offsetof(DevScalars, smallPar) == offsetof(DevScalars, smallLeft) + sizeof(int) &&
+                      offsetof(DevScalars, testWithhold) == offsetof(DevScalars, smallLeft) + 2 * sizeof(int),
+                  "small-run scalars");
+    CK(cudaMemcpyAsync(&d->smallLeft, &ctx->hsc->smallLeft, 3 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     ctx->cur = 0;
     if (!ctx->smallClean) {
         CK(cudaMemsetAsync(ctx->smallRec.p, 0, ctx->smallRec.n * sizeof(unsigned long long), ctx->stream));
@@ -2299,7 +2304,8 @@ femmd_status femmd_run(femmd_ctx *ctx, int steps) {
         if (ctx->hsc->overflow & 2) return fail(ctx, FEMMD_CAPACITY_OVERFLOW, "inconsistent cell counts");
         if (ctx->hsc->overflow & 8) {
             ctx->smallClean = false;
-            return fail(ctx, FEMMD_TIMEOUT, "a step block's copy to shared memory did not complete in time");
+            return fail(ctx, FEMMD_TIMEOUT,
+                        "a bounded device wait expired (a copy to shared memory or a grid-wide exchange)");
         }
         if (!ctx->hsc->overflow && !aborted) {
             traj_commit(ctx->traj);
@@ -2783,6 +2789,12 @@ femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile) {
     ctx->profiling = profile != 0;
     ctx->profForceMs = ctx->profRebuildMs = 0;
     ctx->profForceLaunches = ctx->profRebuilds = ctx->profKernels = 0;
+    return FEMMD_OK;
+}
+
+femmd_status femmd_test_expire_next_exchange(femmd_ctx *ctx) {
+    NEED(ctx);
+    ctx->testExpire = true;
     return FEMMD_OK;
 }
 

@@ -82,7 +82,8 @@ struct DevScalars {
     // exchanges, the steps one launch advanced, the steps left and the
     // position parity the next launch starts from (it ends on parity 0)
     unsigned int gbTag, pad2;
-    int smallDone, smallLeft, smallPar, pad3;
+    int smallDone, smallLeft, smallPar;
+    int testWithhold;  // the next small run's block 0 withholds its first exchange record (a test of the timeout)
 };
 
 enum StepMode { MODE_FORCES = 0, MODE_FIRST = 1, MODE_MID = 2, MODE_LAST = 3, MODE_INIT = 4 };

@@ -2117,14 +2117,15 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 
 // This block's record of exchange 'tag' (record set par), then the wait of
 // warp 0 for every block's: xsh[0] = 1 (0 when a wait gave up), xsh[1] = the
-// OR of the words, xsh[2] = their maximum as a float.  Call after a
-// __syncthreads that follows the block's stores.
+// OR of the words, xsh[2] = their maximum as a float.  withhold: the record
+// is not written (femmd_test_expire_next_exchange: every wait gives up).
+// Call after a __syncthreads that follows the block's stores.
 __device__ __forceinline__ void small_exchange(const DevSys &s, unsigned tag, int par, unsigned long long qu,
                                                unsigned long long qw, unsigned long long qk, unsigned word,
-                                               unsigned *xsh) {
+                                               unsigned *xsh, bool withhold) {
     unsigned long long *set = s.smallRec + (size_t)par * kSmallMaxTiles * 4;
     const int lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !withhold) {
         unsigned long long *r = set + 4 * (size_t)blockIdx.x;
         r[1] = qu;
         r[2] = qw;
@@ -2304,6 +2305,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
     int row = sc->obsRow, stepNow = sc->stepNow;
     const int steps = sc->smallLeft;
     const unsigned base = sc->gbTag;
+    const bool withhold = sc->testWithhold != 0;
     unsigned xi = 0, wuse = 0, luse = 0;  // exchanges, window copies and list-build copies so far
     // a step's totals that block 0 has still to sum (record set pset)
     int pset = -1, prow = 0, pr = 0;
@@ -2313,7 +2315,8 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
     __syncthreads();
     // one exchange: true unless a wait gave up
     auto xchg = [&](unsigned long long qa, unsigned long long qb, unsigned long long qc, unsigned word) {
-        small_exchange(s, base + xi + 1u, (int)(xi % 3u), qa, qb, qc, word, xsh);
+        small_exchange(s, base + xi + 1u, (int)(xi % 3u), qa, qb, qc, word, xsh,
+                       withhold && xi == 0 && blockIdx.x == 0);
         if (blockIdx.x == 0 && warp == 1 && pset >= 0) small_totals(s, pset, pvm, pd, pr, prow);
         __syncthreads();
         pset = -1;
@@ -2719,6 +2722,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_fsmall(DevSys s, int rows,
         sc->smallDone = k;
         sc->smallLeft = left;
         sc->smallPar = 0;
+        sc->testWithhold = 0;
         sc->gbTag = base + xi;
         if (use_h) {
             cudaGraphSetConditional(hif, pending ? 1u : 0u);

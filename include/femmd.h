@@ -248,6 +248,12 @@ femmd_status femmd_event_elapsed(femmd_ctx *ctx, int slot_a, int slot_b, float *
 femmd_status femmd_set_profiling(femmd_ctx *ctx, int profile);
 femmd_status femmd_get_profile(femmd_ctx *ctx, double *force_kernel_ms, long long *force_kernel_launches,
                                double *rebuild_ms, long long *rebuilds, long long *kernel_launches);
+/* For tests of the failure path: in the next run that takes the small-system
+ * run (the fast mode's cooperative launch), block 0 withholds its record of
+ * the first grid-wide exchange, so every block's bounded wait gives up
+ * (about a second) and femmd_run returns FEMMD_TIMEOUT with the context
+ * still usable.  No GPU fault, trap or endless wait is involved. */
+femmd_status femmd_test_expire_next_exchange(femmd_ctx *ctx);
 
 /* ------------------------------------------------------- batched replicas */
 /* Many independent systems advanced in one persistent launch: each replica

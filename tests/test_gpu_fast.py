@@ -287,3 +287,29 @@ def test_small_system_run_matches_the_step_kernels(n_side):
     assert oa.shape == ob.shape == (300, 6)
     assert np.array_equal(oa[:, 3:], ob[:, 3:])  # max v^2, dispHi, rebuilt: exact
     assert np.abs(oa[:, :3] - ob[:, :3]).max() <= 1e-9 * np.abs(oa[:, 0]).max()
+
+
+def test_small_run_exchange_timeout_is_reported_and_recovered():
+    """A grid-wide exchange of the small-system run that never completes (block
+    0 withholds its first record: femmd_test_expire_next_exchange) gives up
+    after its bounded wait; run() returns FEMMD_TIMEOUT, and the context stays
+    usable: the same run from the same state then matches a fresh system bit
+    for bit."""
+    sc = S.lj_fluid(n_side=24)
+    s = fast_system()
+    sc.replay(s)
+    s.run(0)
+    p0, v0, _ = s.get_state()
+    s.test_expire_next_exchange()
+    with pytest.raises(F.FemmdError) as err:
+        s.run(50)
+    assert err.value.status == 5  # FEMMD_TIMEOUT
+    s.set_state(p0, v0)
+    s.run(50)
+    t = fast_system()
+    sc.replay(t)
+    t.run(0)
+    t.set_state(p0, v0)
+    t.run(50)
+    assert np.array_equal(G.bits(s.positions()), G.bits(t.positions()))
+    assert np.array_equal(G.bits(s.velocities()), G.bits(t.velocities()))
