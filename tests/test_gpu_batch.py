@@ -154,6 +154,36 @@ def test_batch_autotune_lists_applies_the_choice():
         assert same(s, a)
 
 
+def test_tuned_lists_keep_the_trajectory():
+    """The tuner's other skin and cell size change only the rounding: the
+    lists still hold every pair inside the cutoff, so a replica run with skin
+    0.5 and cells 1.25x larger (another list order, so other roundings of the
+    force sums) stays within 1e-3 sigma of the default run after 30 steps
+    (before the chaos of the dense disks amplifies the rounding) and its
+    total energy within 1e-4 of |E|."""
+    sc = replicas(1, seed=5)[0]
+    runs = []
+    for skin, factor in ((None, None), (0.5, 1.25)):
+        s = F.System(0)
+        sc.replay(s)
+        if skin is not None:
+            s.set_skin(skin)
+            s.set_cell_factor(factor)
+            s.init_neighbor_list()
+        s.run(0)
+        s.run(30)
+        runs.append(s)
+    a, t = runs
+    box = a.get_box()
+    L = np.array([box["x"], box["y"]])
+    d = a.positions().astype(np.float64) - t.positions().astype(np.float64)
+    d -= L * np.round(d / L)
+    assert np.abs(d).max() <= 1e-3
+    ea, et = a.energies(), t.energies()
+    tot_a, tot_t = ea[0] + 0.5 * ea[2], et[0] + 0.5 * et[2]
+    assert abs(tot_a - tot_t) <= 1e-4 * abs(tot_a)
+
+
 @pytest.mark.parametrize("sizes,launch", [((8000, 600, 900, 1200, 700, 500), (1024, 1)),
                                           ((6000, 5000, 700, 800), (512, 2)),
                                           ((7000, 6500, 6000, 900, 400, 300), (256, 4))])
