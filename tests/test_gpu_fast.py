@@ -258,7 +258,16 @@ def test_fast_lj_1m_full_size_sets_and_forces():
     assert np.abs(p1 - p0).max() < 1e-2
 
 
-@pytest.mark.parametrize("n_side", [64, 120, 10])
+def lj_fluid_sigma(n_side, sigma, density):
+    """The LJ fluid scene with every particle's sigma set to 'sigma' (one
+    kind: sigma by type, not 1, so the pair loops scale 1/r^2 by sigma^2)."""
+    sc = S.lj_fluid(n_side=n_side, density=density)
+    sc.calls = [(n, a[:5] + (np.full_like(a[5], sigma),) + a[6:]) if n == "add_particles" else (n, a)
+                for n, a in sc.calls]
+    return sc
+
+
+@pytest.mark.parametrize("n_side", [64, 120, 10, "sigma"])
 def test_small_system_run_matches_the_step_kernels(n_side):
     """Small fast-mode systems advance a run's steps and rebuilds in one
     cooperative launch (k_fsmall): config 1 (64^2 = 4096 LJ atoms), 120^2 =
@@ -268,8 +277,10 @@ def test_small_system_run_matches_the_step_kernels(n_side):
     kernel launched on its own (profiling mode: k_fstep_p and the rebuild
     kernels) gives bit-identical positions, velocities and accelerations and
     the same rebuilds; the per-step energies agree within 1e-9 of |U| (exact
-    fixed-point sums of per-block float partial sums that differ)."""
-    sc = S.lj_fluid(n_side=n_side)
+    fixed-point sums of per-block float partial sums that differ).  "sigma":
+    48^2 atoms of sigma 1.2 at the same packing (the kernels' sigma != 1
+    form)."""
+    sc = lj_fluid_sigma(48, 1.2, 0.8 / 1.44) if n_side == "sigma" else S.lj_fluid(n_side=n_side)
     a = fast_system()
     sc.replay(a)
     a.run(0)
