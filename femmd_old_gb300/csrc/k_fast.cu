@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(kBlock) k_fplace(DevSys s, int parity, int che
 // the order of the counting atomics leaves no trace.
 constexpr int kSmallBinThreads = 1024;
 constexpr int kSmallBinMaxN = kSmallMaxTiles * kFastBlock;
+constexpr int kSmallBinPer = kSmallBinMaxN / kSmallBinThreads;  // particles per thread at most
 constexpr size_t kSmallBinMaxSmem = 200 * 1024;
 
 static size_t small_bin_smem(const DevSys &s) { return (size_t)(s.ncells + 1 + 3 * (size_t)s.N + 8) * sizeof(int); }
@@ -172,8 +173,19 @@ __global__ void __launch_bounds__(kSmallBinThreads, 1) k_fbin_small(DevSys s, in
     __syncthreads();
     const float2 *pos = parity ? s.pos1 : s.pos0;
     bool bad = false;
-    for (int i = tid; i < s.N; i += T) {
-        const float2 p = pos[i];
+    // the thread's particles i = tid + u T (at most kSmallBinPer): every
+    // position loaded before the first is binned, so the loads overlap
+    float2 pp[kSmallBinPer];
+#pragma unroll
+    for (int u = 0; u < kSmallBinPer; u++) {
+        const int i = tid + u * T;
+        if (i < s.N) pp[u] = pos[i];
+    }
+#pragma unroll
+    for (int u = 0; u < kSmallBinPer; u++) {
+        const int i = tid + u * T;
+        if (i >= s.N) break;
+        const float2 p = pp[u];
         if (!(isfinite(p.x) && isfinite(p.y))) {
             atomicOr(&sc->nonfinite, 1);
             bad = true;
@@ -222,10 +234,20 @@ __global__ void __launch_bounds__(kSmallBinThreads, 1) k_fbin_small(DevSys s, in
     }
     __syncthreads();
     for (int c = tid; c <= s.ncells; c += T) s.cellStart[c] = start[c];
-    for (int i = tid; i < s.N; i += T) {
+    int pid[kSmallBinPer];
+#pragma unroll
+    for (int u = 0; u < kSmallBinPer; u++) {
+        const int i = tid + u * T;
+        pid[u] = i < s.N ? __ldg(s.perm + i) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSmallBinPer; u++) {
+        const int i = tid + u * T;
+        if (i >= s.N) break;
         const int slot = start[cof[i]] + rk[i];
+        rk[i] = pid[u];  // the rank is spent: the slot's id from here on
         if (slot >= 0 && slot < s.N) {
-            ids[slot] = s.perm[i];
+            ids[slot] = pid[u];
         } else {  // inconsistent counts: never write outside the array
             atomicOr(&sc->overflow, 2);
             skip = 1;
@@ -233,10 +255,11 @@ __global__ void __launch_bounds__(kSmallBinThreads, 1) k_fbin_small(DevSys s, in
     }
     __syncthreads();
     if (skip) return;
+#pragma unroll 4
     for (int i = tid; i < s.N; i += T) {
         const int c = cof[i];
         const int b = start[c], e = start[c + 1];
-        const int id = s.perm[i];
+        const int id = rk[i];
         int r = 0;
         for (int q = b; q < e; q++) r += ids[q] < id;
         const int slot = b + r;
@@ -244,13 +267,13 @@ __global__ void __launch_bounds__(kSmallBinThreads, 1) k_fbin_small(DevSys s, in
             atomicOr(&sc->overflow, 2);
             continue;
         }
-        const float2 pp = pos[i];
-        s.cellSorted[slot] = make_float4(pp.x, pp.y, __int_as_float(slot), __int_as_float(s.excl[i]));
+        const float2 x = __ldg(pos + i);
+        s.cellSorted[slot] = make_float4(x.x, x.y, __int_as_float(slot), __int_as_float(__ldg(s.excl + i)));
         s.sortedIds[slot] = slot;
         s.newCell[slot] = c;
-        s.sPos[slot] = pp;
-        s.sVel[slot] = s.vel[i];
-        s.sAcc[slot] = s.acc[i];
+        s.sPos[slot] = x;
+        s.sVel[slot] = __ldg(s.vel + i);
+        s.sAcc[slot] = __ldg(s.acc + i);
         s.sPerm[slot] = id;
     }
 }
